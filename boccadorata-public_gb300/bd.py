@@ -1,0 +1,336 @@
+"""ctypes binding of the C ABI (include/bd_gb300.h) and a host-side mirror of the
+reference's call boundaries.
+
+``Context`` wraps one ``bd_ctx``.  ``WideSelfEnergy`` and ``dyson_matrix`` mirror,
+name for name, the three calls of the reference's per-channel loop
+(source/BcDor-Main.cpp:241-391):
+
+* ``WideSelfEnergy.Build_Dynamic_SlfEn_2ndOrder``  (source/BcDor-Self_energy_ext_Op_c.cpp:323)
+* ``WideSelfEnergy.Reduce_SelfEn_Lncz``            (source/BcDor-Self_energy_ext_Op_e.cpp:55)
+* ``dyson_matrix``                                 (source/BcDor-DysonMatrix.cpp:123)
+
+There is no CPU fallback: importing this module raises when the CUDA library has
+not been built, and every call goes through the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbd_gb300.so")
+
+BD_OK, BD_ERR_ARG, BD_ERR_CUDA, BD_ERR_CAPACITY, BD_ERR_STATE, BD_ERR_NUMERIC, BD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
+BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL = 1, 2, 4
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+
+class _ModSpace(C.Structure):
+    _fields_ = [("nsubsh", C.c_int), ("norb", C.c_int), ("l", _ip), ("j2", _ip), ("ip", _ip), ("ch", _ip),
+                ("no", _ip), ("orb_sh", _ip), ("orb_xe", _dp)]
+
+
+class _Propagator(C.Structure):
+    _fields_ = [("nspb", C.c_int), ("np", _ip), ("nh", _ip), ("ep", _dp), ("eh", _dp), ("fqp", _dp), ("fqh", _dp)]
+
+
+class _Interaction(C.Structure):
+    _fields_ = [("n_me", C.c_int), ("iabJ", _ip), ("icdJ", _ip), ("V", _dp)]
+
+
+class _Pivots(C.Structure):
+    _fields_ = [("npvt", _ip), ("n_itr_fw", _ip), ("n_itr_bk", _ip), ("vec", _dp)]
+
+
+class BDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"bd error {code}: {msg}")
+        self.code = code
+
+
+EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload_problem", "bd_upload_pivots",
+            "bd_count_poles", "bd_ehf", "bd_sigma2_build", "bd_lanczos_reduce", "bd_dyson_solve", "bd_run_all",
+            "bd_sync", "bd_result_counts", "bd_result_fetch", "bd_result_koltun_all", "bd_last_timings",
+            "bd_dyson_rows", "bd_lanczos_vectors"]
+
+
+def load_library(path: str = LIB_PATH):
+    if not os.path.exists(path):
+        raise ImportError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.bd_create.argtypes = [C.POINTER(vp), C.c_int]
+    lib.bd_destroy.argtypes = [vp]; lib.bd_destroy.restype = None
+    lib.bd_last_error.argtypes = [vp]; lib.bd_last_error.restype = C.c_char_p
+    lib.bd_upload_problem.argtypes = [vp, C.POINTER(_ModSpace), C.POINTER(_Interaction), C.POINTER(_Propagator)]
+    lib.bd_upload_pivots.argtypes = [vp, C.POINTER(_Pivots)]
+    lib.bd_count_poles.argtypes = [vp, C.c_int, _ip, _ip]
+    lib.bd_ehf.argtypes = [vp, C.c_int, _dp]
+    lib.bd_sigma2_build.argtypes = [vp, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int, _ip]
+    lib.bd_lanczos_reduce.argtypes = [vp, C.c_int, C.c_int, _dp, _ip, _ip, _dp, C.c_int, _ip, _ip,
+                                      _dp, C.c_int, _ip, _ip, C.c_int]
+    lib.bd_dyson_solve.argtypes = [vp, C.c_int, _dp, _dp, C.c_double, _dp, C.c_int, _ip, _dp, C.c_int, _ip, _dp]
+    lib.bd_dyson_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _ip, C.c_int, _dp, _ip, _dp, _dp, C.c_double,
+                                  _dp, C.c_int, _ip, _dp, C.c_int, _ip, _dp]
+    lib.bd_lanczos_vectors.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, C.c_longlong]
+    lib.bd_run_all.argtypes = [vp, C.c_int]
+    lib.bd_sync.argtypes = [vp]
+    lib.bd_result_counts.argtypes = [vp, C.c_int, _ip, _ip]
+    lib.bd_result_fetch.argtypes = [vp, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
+    lib.bd_result_koltun_all.argtypes = [vp, _dp]
+    lib.bd_last_timings.argtypes = [vp, _dp]
+    lib.bd_diag_two_pass.argtypes = [vp]
+    lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+    return lib
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = load_library()
+    return _LIB
+
+
+def _i(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+def _d(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def _pi(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def _pd(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+class Context:
+    """One device context with the problem resident in HBM."""
+
+    def __init__(self, device: int = 0):
+        self.lib = lib()
+        h = C.c_void_p()
+        rc = self.lib.bd_create(C.byref(h), device)
+        if rc != BD_OK:
+            raise BDError(rc, "bd_create failed (no usable CUDA device?)")
+        self.h = h
+        self._keep = []
+        self.prob = None
+
+    def close(self):
+        if self.h:
+            self.lib.bd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != BD_OK:
+            raise BDError(rc, self.lib.bd_last_error(self.h).decode())
+        return rc
+
+    # ---------------------------------------------------------------- inputs
+    def upload(self, prob, with_pivots: bool = True):
+        ms, pr, vp = prob.ms, prob.prop, prob.vpp
+        arrs = dict(l=_i(ms.l), j2=_i(ms.j2), ip=_i(ms.ip), ch=_i(ms.ch), no=_i(ms.no), orb_sh=_i(ms.orb_sh),
+                    orb_xe=_d(ms.orb_xe), np=_i(pr.np_), nh=_i(pr.nh),
+                    ep=_d(pr.ep if len(pr.ep) else np.zeros(1)), eh=_d(pr.eh if len(pr.eh) else np.zeros(1)),
+                    fqp=_d(pr.fqp.reshape(-1) if len(pr.ep) else np.zeros(pr.nspb)),
+                    fqh=_d(pr.fqh.reshape(-1) if len(pr.eh) else np.zeros(pr.nspb)),
+                    iabJ=_i(vp.iabJ), icdJ=_i(vp.icdJ), V=_d(vp.V))
+        m = _ModSpace(ms.nsubsh, ms.norb, _pi(arrs["l"]), _pi(arrs["j2"]), _pi(arrs["ip"]), _pi(arrs["ch"]),
+                      _pi(arrs["no"]), _pi(arrs["orb_sh"]), _pd(arrs["orb_xe"]))
+        p = _Propagator(pr.nspb, _pi(arrs["np"]), _pi(arrs["nh"]), _pd(arrs["ep"]), _pd(arrs["eh"]),
+                        _pd(arrs["fqp"]), _pd(arrs["fqh"]))
+        v = _Interaction(vp.n, _pi(arrs["iabJ"]), _pi(arrs["icdJ"]), _pd(arrs["V"]))
+        self._chk(self.lib.bd_upload_problem(self.h, C.byref(m), C.byref(v), C.byref(p)))
+        self.prob = prob
+        if with_pivots and prob.piv is not None:
+            self.upload_pivots(prob.piv)
+        return self
+
+    def upload_pivots(self, piv):
+        npvt = _i([len(v) for v in piv.vec])
+        nfw = _i(np.concatenate([np.asarray(x, np.int32) for x in piv.n_fw]) if len(piv.n_fw) else [])
+        nbk = _i(np.concatenate([np.asarray(x, np.int32) for x in piv.n_bk]) if len(piv.n_bk) else [])
+        vec = _d(np.concatenate([np.asarray(x, np.float64).reshape(-1) for x in piv.vec]))
+        pv = _Pivots(_pi(npvt), _pi(nfw), _pi(nbk), _pd(vec))
+        self._chk(self.lib.bd_upload_pivots(self.h, C.byref(pv)))
+
+    def set_tuning(self, lz_cluster=8, dy_cluster=8, eta=0.70710678118654752):
+        self._chk(self.lib.bd_set_tuning(self.h, lz_cluster, dy_cluster, eta))
+
+    # ---------------------------------------------------------------- per channel
+    def D(self, ish):
+        return int(self.prob.ms.no[ish])
+
+    def count_poles(self, ish):
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_count_poles(self.h, ish, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def ehf(self, ish):
+        D = self.D(ish)
+        U = np.zeros(D * D)
+        self._chk(self.lib.bd_ehf(self.h, ish, _pd(U)))
+        return U.reshape(D, D)
+
+    def sigma2_build(self, ish, copy: bool = True):
+        nfw, nbk = self.count_poles(ish)
+        D = self.D(ish)
+        fw = np.zeros((max(nfw, 1), 2 + D)) if copy else None
+        bk = np.zeros((max(nbk, 1), 2 + D)) if copy else None
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_sigma2_build(self.h, ish, _pd(fw), max(nfw, 1), C.byref(a), _pd(bk), max(nbk, 1),
+                                           C.byref(b)))
+        if not copy:
+            return None, None
+        return fw[:a.value], bk[:b.value]
+
+    def lanczos_reduce(self, ish, pivots, nitr_fw, nitr_bk, mixed: bool = False):
+        D = self.D(ish)
+        piv = _d(np.array(pivots, np.float64).reshape(-1, D)).copy()
+        nf, nb = _i(nitr_fw).copy(), _i(nitr_bk).copy()
+        npv = len(piv)
+        nfw, nbk = self.count_poles(ish)
+        capf, capb = max(1, min(int(nf[nf > 0].sum()), nfw)), max(1, min(int(nb[nb > 0].sum()), nbk))
+        nt = npv + 1 + D
+        lf, lb = np.zeros((capf, nt)), np.zeros((capb, nt))
+        ipf, ipb = np.zeros(nt, np.int32), np.zeros(nt, np.int32)
+        Lf, Lb = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_lanczos_reduce(self.h, ish, npv, _pd(piv), _pi(nf), _pi(nb), _pd(lf), capf, C.byref(Lf),
+                                             _pi(ipf), _pd(lb), capb, C.byref(Lb), _pi(ipb),
+                                             BD_RUN_MIXED if mixed else 0))
+        return dict(lz_fw=lf[:Lf.value], lz_bk=lb[:Lb.value], ipiv_fw=ipf, ipiv_bk=ipb, NDEN=npv + 1,
+                    n_piv_fw=int(ipf[0]) if Lf.value else 0, n_piv_bk=int(ipb[0]) if Lb.value else 0,
+                    pivots=piv, nitr_fw=nf, nitr_bk=nb)
+
+    def dyson_solve(self, ish, sig1b=None, sighf=None, efermi=float("nan")):
+        D = self.D(ish)
+        nfw, nbk = self.count_poles(ish)
+        cap = D + nfw + nbk + 8
+        qp, qh = np.zeros((cap, 2 + D)), np.zeros((cap, 2 + D))
+        a, b = C.c_int(), C.c_int()
+        kol = np.zeros(3)
+        s1 = _d(sig1b) if sig1b is not None else None
+        sh = _d(sighf) if sighf is not None else None
+        self._chk(self.lib.bd_dyson_solve(self.h, ish, _pd(s1), _pd(sh), efermi, _pd(qp), cap, C.byref(a), _pd(qh), cap,
+                                          C.byref(b), _pd(kol)))
+        return dict(qp=qp[:a.value], qh=qh[:b.value], koltun=kol)
+
+    def lanczos_vectors(self, ish, dir, L, N, fp32=False):
+        out = np.zeros((max(L, 1), max(N, 1)))
+        self._chk(self.lib.bd_lanczos_vectors(self.h, ish, dir, 1 if fp32 else 0, _pd(out), out.size))
+        return out[:L, :N]
+
+    def dyson_rows(self, ish, nden, fw, bk, ipiv_fw=None, ipiv_bk=None, sig1b=None, sighf=None, efermi=float("nan")):
+        """DysonMatrix on caller-supplied self-energy rows (plain if ipiv_* is None)."""
+        D = self.D(ish)
+        fw = _d(np.asarray(fw).reshape(-1, nden + D)); bk = _d(np.asarray(bk).reshape(-1, nden + D))
+        n = D + len(fw) + len(bk)
+        qp, qh = np.zeros((n, 2 + D)), np.zeros((n, 2 + D))
+        a, b = C.c_int(), C.c_int()
+        kol = np.zeros(3)
+        ipf = _i(ipiv_fw) if ipiv_fw is not None else None
+        ipb = _i(ipiv_bk) if ipiv_bk is not None else None
+        s1 = _d(sig1b) if sig1b is not None else None
+        sh = _d(sighf) if sighf is not None else None
+        self._chk(self.lib.bd_dyson_rows(self.h, ish, nden, len(fw), _pd(fw) if len(fw) else None, _pi(ipf), len(bk),
+                                         _pd(bk) if len(bk) else None, _pi(ipb), _pd(s1), _pd(sh), efermi,
+                                         _pd(qp), n, C.byref(a), _pd(qh), n, C.byref(b), _pd(kol)))
+        return dict(qp=qp[:a.value], qh=qh[:b.value], koltun=kol)
+
+    # ---------------------------------------------------------------- all channels
+    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True):
+        flags = (BD_RUN_LANCZOS if lanczos else 0) | (BD_RUN_MIXED if mixed else 0) | (BD_RUN_PER_CHANNEL if per_channel else 0)
+        self._chk(self.lib.bd_run_all(self.h, flags))
+        if sync:
+            self.sync()
+
+    def sync(self):
+        self._chk(self.lib.bd_sync(self.h))
+
+    def timings(self):
+        t = np.zeros(5)
+        self._chk(self.lib.bd_last_timings(self.h, _pd(t)))
+        return dict(sigma2=t[0], sort=t[1], lanczos=t[2], dyson=t[3], total=t[4])
+
+    def two_pass_steps(self):
+        return int(self.lib.bd_diag_two_pass(self.h))
+
+    def koltun_all(self):
+        k = np.zeros(3 * self.prob.ms.nsubsh)
+        self._chk(self.lib.bd_result_koltun_all(self.h, _pd(k)))
+        return k.reshape(-1, 3)
+
+    def result(self, ish):
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_result_counts(self.h, ish, C.byref(a), C.byref(b)))
+        D = self.D(ish)
+        qp, qh, kol = np.zeros((max(a.value, 1), 2 + D)), np.zeros((max(b.value, 1), 2 + D)), np.zeros(3)
+        self._chk(self.lib.bd_result_fetch(self.h, ish, _pd(qp), max(a.value, 1), _pd(qh), max(b.value, 1), _pd(kol)))
+        return dict(qp=qp[:a.value], qh=qh[:b.value], koltun=kol)
+
+
+def koltun_totals(kol_per_channel, ch):
+    """Koltun totals as Run_itrs forms them (source/BcDor-Main.cpp:387-417): per charge
+    U1 = sum x1, E = sum (x1 + x2)/2, A = sum x3."""
+    out = {}
+    k = np.asarray(kol_per_channel)
+    for c in (0, 1):
+        m = np.asarray(ch) == c
+        out[c] = dict(U1=float(k[m, 0].sum()), E=float(((k[m, 0] + k[m, 1]) / 2.0).sum()), A=float(k[m, 2].sum()))
+    out["E_tot"] = out[0]["E"] + out[1]["E"]
+    out["A_tot"] = out[0]["A"] + out[1]["A"]
+    return out
+
+
+# ------------------------------------------------------------------------------------------
+# mirror of the reference's per-channel interface
+# ------------------------------------------------------------------------------------------
+class WideSelfEnergy:
+    """Per-channel self-energy with the reference's method names (Wide_self_energy_t,
+    source/BcDor-SlfEn_classes.hh:16-111).  State lives on the device."""
+
+    def __init__(self, ctx: Context, ish: int):
+        self.ctx, self.I_SH = ctx, ish
+        self.NTOT_ORB = ctx.D(ish)
+        self.Sig_dyn_fw = self.Sig_dyn_bk = None
+        self.N_PLS_fw = self.N_PLS_bk = 0
+        self.lanczos = None
+
+    def Count_2p1h_2h1p_poles(self):
+        return self.ctx.count_poles(self.I_SH)
+
+    def Build_ExtendedHartreeFock(self):
+        self.Sig_HF = self.ctx.ehf(self.I_SH)
+        return self.Sig_HF
+
+    def Build_Dynamic_SlfEn_2ndOrder(self):
+        self.Sig_dyn_fw, self.Sig_dyn_bk = self.ctx.sigma2_build(self.I_SH)
+        self.N_PLS_fw, self.N_PLS_bk = len(self.Sig_dyn_fw), len(self.Sig_dyn_bk)
+        return self.N_PLS_fw, self.N_PLS_bk
+
+    def Reduce_SelfEn_Lncz(self, pivots, n_itr_fw, n_itr_bk, mixed=False):
+        self.lanczos = self.ctx.lanczos_reduce(self.I_SH, pivots, n_itr_fw, n_itr_bk, mixed=mixed)
+        return self.lanczos
+
+
+def dyson_matrix(sfv: WideSelfEnergy, sig1b, sighf=None, efermi=float("nan")):
+    """DysonMatrix: returns dict(qp=rows, qh=rows, koltun=[x1, x2, x3])."""
+    return sfv.ctx.dyson_solve(sfv.I_SH, sig1b, sighf, efermi)

@@ -1,0 +1,1188 @@
+// bd_api.cu -- host orchestration and the extern "C" entry points of include/bd_gb300.h.
+//
+// The context keeps every input resident on the device and pre-computes, once
+// per upload, the integer plan of the chain: the (Jab, ia, ib, ig) blocks of
+// every channel in the reference's loop order (source/BcDor-Self_energy_ext_Op_c.cpp:
+// 380-394), the pole offsets, and the buffer layout.  Both call patterns share the
+// kernels:
+//   * per channel (bd_sigma2_build / bd_lanczos_reduce / bd_dyson_solve), the
+//     drop-in for the reference's three calls, one channel per launch;
+//   * all channels at once (bd_run_all), one launch per phase over every channel.
+#include <cub/cub.cuh>
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/bd_gb300.h"
+#include "bd_common.cuh"
+#include "bd_kernels.h"
+
+using namespace bd;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+enum ChanState { ST_NONE = 0, ST_SIGMA = 1, ST_LANCZOS = 2 };
+
+struct ChainPlan {     // one Lanczos direction of one channel
+    int N = 0, L = 0, n_used = 0, nden_out = 0, n_pvt = 0;
+    std::vector<int> nitr;         // rescaled, per pivot (all pivots)
+    std::vector<int> start, last;  // per used pivot (+ sentinel in start)
+    std::vector<double> piv;       // used pivots, normalised
+    std::vector<int> used;         // indices of the pivots that start a chain
+    std::vector<int> ipiv;         // [n_used, 1, last+1 ...] padded to nden_out + D with -100
+};
+
+struct Chan {
+    int D = 0, j2 = 0, ch = 0;
+    int nfw = 0, nbk = 0;
+    long long fw_off = 0, bk_off = 0, mfw_off = 0, mbk_off = 0;
+    int blk_first = 0, nblk = 0;
+    long long vp_first = 0, nvp = 0;
+    double efermi = 0.0;
+    ChainPlan lz[2];
+    // resident results of the per-channel API
+    int state = ST_NONE;
+};
+
+}  // namespace
+
+struct bd_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string err;
+    bool uploaded = false, have_pivots = false;
+    int lz_cluster = 8, dy_cluster = 8;
+    double eta = 0.70710678118654752;
+    // host copies of the inputs
+    int nsubsh = 0, norb = 0, jmax = 0, nspb = 0;
+    std::vector<int> l, j2, ip, ch, no, orb_start, orb_sh, np, nh, p_start, h_start;
+    std::vector<double> orb_xe, ep, eh;
+    std::vector<int> piv_npvt, piv_nfw, piv_nbk, piv_first;
+    std::vector<double> piv_vec;
+    // plan
+    std::vector<Chan> chans;
+    std::vector<S2Block> blocks;
+    std::vector<long long> blk_fw_first, blk_bk_first, blk_vp_first;
+    long long tot_fw = 0, tot_bk = 0, tot_mfw = 0, tot_mbk = 0, tot_vp = 0;
+    // device
+    std::vector<DevBuf> bufs;
+    DevProblem dp{};
+    S2Block *d_blocks = nullptr;
+    long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr, *d_blk_vp_first = nullptr;
+    ChanSig *d_cs = nullptr;
+    double *d_vp = nullptr;
+    double *d_Efw = nullptr, *d_S2fw = nullptr, *d_Mfw = nullptr, *d_Ebk = nullptr, *d_S2bk = nullptr, *d_Mbk = nullptr;
+    double *d_Efw_s = nullptr, *d_Mfw_s = nullptr, *d_Ebk_s = nullptr, *d_Mbk_s = nullptr;  // sorted copies
+    int *d_seg_fw = nullptr, *d_seg_bk = nullptr, *d_idx_fw = nullptr, *d_idx_bk = nullptr, *d_perm_fw = nullptr,
+        *d_perm_bk = nullptr;
+    double *d_keys_tmp = nullptr;
+    int *d_segoff_fw = nullptr, *d_segoff_bk = nullptr;
+    void *d_cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    double *d_sighf = nullptr, *d_sig1b = nullptr;  // per channel D*D at chan_dd_off
+    std::vector<long long> chan_dd_off;
+    long long *d_dd_off = nullptr;
+    int3 *d_ehf_entries = nullptr;
+    int n_ehf_entries = 0;
+    // Lanczos
+    std::vector<long long> lz_v_off[2], lz_out_off[2];
+    char *d_lzV = nullptr;
+    double *d_lzout = nullptr;
+    int *d_lzint = nullptr;      // start / last / ipiv blocks
+    double *d_lzpiv = nullptr;
+    int *d_lzstat = nullptr;
+    size_t lzV_bytes = 0;
+    long long lzout_total = 0;
+    std::vector<long long> lz_int_off[2], lz_piv_off[2];
+    LzChain *d_chains = nullptr;
+    int lz_two_pass = 0;
+    // Dyson
+    std::vector<long long> dy_A_off, dy_vec_off, dy_sol_off, dy_R_off, dy_work_off;
+    double *d_dyA = nullptr, *d_dyvec = nullptr, *d_dysol = nullptr, *d_dykol = nullptr, *d_dyR = nullptr,
+           *d_dywork = nullptr;
+    long long *d_work_first = nullptr;
+    size_t dyR_cap = 0, dywork_cap = 0;
+    int *d_dynq = nullptr, *d_dystat = nullptr;
+    DyJob *d_jobs = nullptr;
+    long long *d_row_first = nullptr;
+    size_t dyA_cap = 0, dyvec_cap = 0, dysol_cap = 0;
+    int last_lanczos_flags = 0;
+    bool results_valid = false;
+    std::vector<int> res_nq;  // after run_all: 2 per channel
+    double timings[5] = {0, 0, 0, 0, 0};
+};
+
+namespace {
+
+int fail(bd_ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(ctx, BD_ERR_CUDA, "%s: %s (%s:%d)", #call,              \
+                                           cudaGetErrorString(e_), __FILE__, __LINE__);            \
+    } while (0)
+
+template <typename T>
+int dalloc(bd_ctx *ctx, T **p, size_t count) {
+    *p = nullptr;
+    size_t bytes = sizeof(T) * (count > 0 ? count : 1);
+    void *q = nullptr;
+    CU(cudaMalloc(&q, bytes));
+    ctx->bufs.push_back({q, bytes});
+    *p = reinterpret_cast<T *>(q);
+    return BD_OK;
+}
+
+template <typename T>
+int dupload(bd_ctx *ctx, T **p, const std::vector<T> &h) {
+    int rc = dalloc(ctx, p, h.size());
+    if (rc) return rc;
+    if (!h.empty()) CU(cudaMemcpyAsync(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    return BD_OK;
+}
+
+void free_all(bd_ctx *ctx) {
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (auto &b : ctx->bufs) cudaFree(b.p);
+    ctx->bufs.clear();
+}
+
+// Seek_EFermi on the input propagator (source/BcDor-DysonMatrix.cpp:619-635).
+double seek_efermi(const bd_ctx *c, int I) {
+    const int chI = c->ch[I];
+    double x1 = (c->ep.empty() ? 0.0 : c->ep[0]) + 100., x2 = (c->eh.empty() ? 0.0 : c->eh[0]) - 100.;
+    for (int s = 0; s < c->nsubsh; ++s) {
+        if (c->ch[s] != chI) continue;
+        for (int k = 0; k < c->np[s]; ++k) if (c->ep[c->p_start[s] + k] < x1) x1 = c->ep[c->p_start[s] + k];
+        for (int k = 0; k < c->nh[s]; ++k) if (c->eh[c->h_start[s] + k] > x2) x2 = c->eh[c->h_start[s] + k];
+    }
+    return (x1 + x2) / 2.0;
+}
+
+// Block enumeration in the loop order of Build_Dynamic_SlfEn_2ndOrder and the
+// all-poles counts of Count_2p1h_2h1p_poles (source/BcDor-Self_energy_ext_Op_c.cpp:47-111,380-394).
+void build_plan(bd_ctx *c) {
+    c->chans.assign(c->nsubsh, Chan());
+    c->blocks.clear();
+    c->blk_fw_first.clear(); c->blk_bk_first.clear(); c->blk_vp_first.clear();
+    long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
+    const int ns = c->nsubsh;
+    // triangle-valid (ia, ib) per Jab, and valid ig per (I, Jab)
+    for (int I = 0; I < ns; ++I) {
+        Chan &C = c->chans[I];
+        C.D = c->no[I]; C.j2 = c->j2[I]; C.ch = c->ch[I];
+        C.fw_off = fw; C.bk_off = bk; C.mfw_off = mfw; C.mbk_off = mbk;
+        C.blk_first = (int)c->blocks.size(); C.vp_first = vp;
+        int nfw = 0, nbk = 0;
+        for (int Jab = 0; Jab <= c->jmax; ++Jab) {
+            std::vector<int> gl;
+            for (int ig = 0; ig < ns; ++ig) if (!tri_fail(c->j2[ig], c->j2[I], 2 * Jab)) gl.push_back(ig);
+            if (gl.empty()) continue;
+            for (int ia = 0; ia < ns; ++ia)
+                for (int ib = ia; ib < ns; ++ib) {
+                    if (tri_fail(c->j2[ia], c->j2[ib], 2 * Jab)) continue;
+                    const int nJab = std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2;
+                    for (int ig : gl) {
+                        if (c->ch[ia] + c->ch[ib] - c->ch[ig] != c->ch[I]) continue;
+                        if ((c->ip[ia] + c->ip[ib] + c->ip[ig] + c->ip[I]) % 2 != 0) continue;
+                        S2Block B{};
+                        B.ch = I; B.Jab = Jab; B.ia = ia; B.ib = ib; B.ig = ig;
+                        B.nJab = nJab;
+                        B.nJgd = std::abs((c->j2[ig] + c->j2[I]) / 2 - Jab + 1) % 2;
+                        int na = c->np[ia], nb = c->np[ib], ng = c->nh[ig], s = na * nb * ng;
+                        if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
+                        B.nfw = s;
+                        na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; s = na * nb * ng;
+                        if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
+                        B.nbk = s;
+                        B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
+                        B.vp_first = vp;
+                        B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
+                        c->blk_fw_first.push_back(fw + nfw);
+                        c->blk_bk_first.push_back(bk + nbk);
+                        c->blk_vp_first.push_back(vp);
+                        nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
+                        c->blocks.push_back(B);
+                    }
+                }
+        }
+        C.nfw = nfw; C.nbk = nbk;
+        C.nblk = (int)c->blocks.size() - C.blk_first;
+        C.nvp = vp - C.vp_first;
+        fw += nfw; bk += nbk; mfw += (long long)nfw * C.D; mbk += (long long)nbk * C.D;
+        C.efermi = seek_efermi(c, I);
+    }
+    c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
+}
+
+// Lanczos sizes and pivot schedule of one direction (Reduce_SelfEn_Lncz
+// source/BcDor-Self_energy_ext_Op_e.cpp:161-226 and Reduce_Mtx_Lncz source/BcDor-Lanczos.cpp:59-135,236-241).
+// The pivots of the used chains are normalised in place in `piv` (the caller's
+// working copy), as Reduce_Mtx_Lncz does (source/BcDor-Lanczos.cpp:129-132); the
+// backward pass sees the vectors the forward pass already normalised.
+void plan_chain(ChainPlan &P, int N, int D, int npvt, const int *nitr_in, double *piv) {
+    P = ChainPlan();
+    P.N = N; P.n_pvt = npvt; P.nden_out = npvt + 1;
+    P.nitr.assign(nitr_in, nitr_in + npvt);
+    P.ipiv.assign(P.nden_out + D, -100);
+    long long tot = 0;
+    for (int v : P.nitr) if (v > 0) tot += v;
+    if (N < 1 || tot < 1) { P.L = 0; P.start.push_back(0); return; }
+    if (tot > N) {
+        const double x1 = (double)N / (double)tot;
+        for (auto &v : P.nitr) v = (int)(x1 * v + 1.0);
+    }
+    long long nL = 0;
+    for (int v : P.nitr) if (v > 0) nL += v;
+    P.L = (int)std::min<long long>(nL, N);
+    int jn = 0;
+    for (int p = 0; p < npvt && jn < P.L; ++p) {
+        if (P.nitr[p] < 1) continue;
+        double x1 = 0.0;
+        for (int i = 0; i < D; ++i) x1 += piv[(size_t)p * D + i] * piv[(size_t)p * D + i];
+        x1 = std::sqrt(x1);
+        for (int i = 0; i < D; ++i) piv[(size_t)p * D + i] /= x1;
+        P.used.push_back(p);
+        P.start.push_back(jn);
+        jn += P.nitr[p];
+        P.last.push_back(jn - 1);
+        for (int i = 0; i < D; ++i) P.piv.push_back(piv[(size_t)p * D + i]);
+    }
+    P.n_used = (int)P.used.size();
+    P.start.push_back(P.L);
+    P.ipiv[0] = P.n_used;
+    P.ipiv[1] = 1;
+    for (int i = 0; i < P.n_used && 2 + i < (int)P.ipiv.size(); ++i) P.ipiv[2 + i] = P.last[i] + 1;
+}
+
+int check_chan(bd_ctx *ctx, int ish) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+    if (ish < 0 || ish >= ctx->nsubsh) return fail(ctx, BD_ERR_ARG, "channel %d out of range", ish);
+    return BD_OK;
+}
+
+// ---------------------------------------------------------------- Sigma(2)
+int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
+    const Chan &A = ctx->chans[ch_lo], &Z = ctx->chans[ch_hi - 1];
+    const int b0 = A.blk_first, nb = Z.blk_first + Z.nblk - b0;
+    if (nb <= 0) return BD_OK;
+    const long long vp0 = A.vp_first, nvp = Z.vp_first + Z.nvp - vp0;
+    if (nvp > 0) {
+        k_vgather<<<(unsigned)((nvp + 255) / 256), 256, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
+                                                                        ctx->d_blk_vp_first + b0, nb, vp0, nvp,
+                                                                        ctx->d_vp);
+        CU(cudaGetLastError());
+    }
+    const long long f0 = A.fw_off, nf = Z.fw_off + Z.nfw - f0;
+    if (nf > 0) {
+        k_poles<<<(unsigned)((nf + 127) / 128), 128, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
+                                                                     ctx->d_blk_fw_first + b0, nb, f0, nf, ctx->d_cs,
+                                                                     0, ctx->d_vp, ctx->d_Efw, ctx->d_S2fw, ctx->d_Mfw);
+        CU(cudaGetLastError());
+    }
+    const long long k0 = A.bk_off, nk = Z.bk_off + Z.nbk - k0;
+    if (nk > 0) {
+        k_poles<<<(unsigned)((nk + 127) / 128), 128, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
+                                                                     ctx->d_blk_bk_first + b0, nb, k0, nk, ctx->d_cs,
+                                                                     1, ctx->d_vp, ctx->d_Ebk, ctx->d_S2bk, ctx->d_Mbk);
+        CU(cudaGetLastError());
+    }
+    return BD_OK;
+}
+
+int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
+    // entries of channels [ch_lo, ch_hi) are contiguous in d_ehf_entries
+    int e0 = 0, e1 = 0, acc = 0;
+    for (int I = 0; I < ctx->nsubsh; ++I) {
+        const int cnt = ctx->no[I] * (ctx->no[I] + 1) / 2;
+        if (I == ch_lo) e0 = acc;
+        acc += cnt;
+        if (I == ch_hi - 1) e1 = acc;
+    }
+    if (e1 > e0) {
+        k_ehf<<<e1 - e0, 128, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries + e0, e1 - e0, ctx->d_dd_off, ctx->d_sighf);
+        CU(cudaGetLastError());
+    }
+    return BD_OK;
+}
+
+// Stable sort of each channel's poles by energy: forward ascending, backward descending
+// (the orders Reduce_SelfEn_Lncz establishes, source/BcDor-Self_energy_ext_Op_e.cpp:119-130),
+// then gather E and M into the sorted copies.
+int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
+    for (int dir = 0; dir < 2; ++dir) {
+        const Chan &A = ctx->chans[ch_lo], &Z = ctx->chans[ch_hi - 1];
+        const long long n0 = dir == 0 ? A.fw_off : A.bk_off;
+        const long long n = (dir == 0 ? Z.fw_off + Z.nfw : Z.bk_off + Z.nbk) - n0;
+        if (n <= 0) continue;
+        std::vector<int> rel(ch_hi - ch_lo + 1);
+        for (int I = ch_lo; I < ch_hi; ++I)
+            rel[I - ch_lo] = (int)((dir == 0 ? ctx->chans[I].fw_off : ctx->chans[I].bk_off) - n0);
+        rel[ch_hi - ch_lo] = (int)n;
+        int *d_off = dir == 0 ? ctx->d_segoff_fw : ctx->d_segoff_bk;
+        CU(cudaMemcpyAsync(d_off, rel.data(), sizeof(int) * rel.size(), cudaMemcpyHostToDevice, ctx->st));
+        double *E = dir == 0 ? ctx->d_Efw : ctx->d_Ebk;
+        int *idx = dir == 0 ? ctx->d_idx_fw : ctx->d_idx_bk;
+        int *perm = dir == 0 ? ctx->d_perm_fw : ctx->d_perm_bk;
+        size_t bytes = ctx->cub_bytes;
+        const int nseg = ch_hi - ch_lo;
+        cudaError_t e;
+        if (dir == 0)
+            e = cub::DeviceSegmentedRadixSort::SortPairs(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp, idx + n0,
+                                                         perm + n0, (int)n, nseg, d_off, d_off + 1, 0, 64, ctx->st);
+        else
+            e = cub::DeviceSegmentedRadixSort::SortPairsDescending(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp,
+                                                                   idx + n0, perm + n0, (int)n, nseg, d_off,
+                                                                   d_off + 1, 0, 64, ctx->st);
+        CU(e);
+        k_permute_soa<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(
+            perm, n0, n, dir == 0 ? ctx->d_seg_fw : ctx->d_seg_bk, ctx->d_cs, dir, E, dir == 0 ? ctx->d_Mfw : ctx->d_Mbk,
+            dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s, dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s);
+        CU(cudaGetLastError());
+    }
+    return BD_OK;
+}
+
+// Lanczos chains of channels [ch_lo, ch_hi), both directions.
+int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
+    std::vector<LzChain> ch;
+    int Smax = 1, rmax = 1;
+    for (int I = ch_lo; I < ch_hi; ++I) {
+        Chan &C = ctx->chans[I];
+        for (int dir = 0; dir < 2; ++dir) {
+            ChainPlan &P = C.lz[dir];
+            if (P.L <= 0) continue;
+            LzChain z{};
+            z.N = P.N; z.D = C.D; z.L = P.L; z.n_used = P.n_used; z.nden_out = P.nden_out;
+            z.ld = (P.N + 31) / 32 * 32;
+            z.E = (dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s) + (dir == 0 ? C.fw_off : C.bk_off);
+            z.M = (dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s) + (dir == 0 ? C.mfw_off : C.mbk_off);
+            z.piv = ctx->d_lzpiv + ctx->lz_piv_off[dir][I];
+            z.start = ctx->d_lzint + ctx->lz_int_off[dir][I];
+            z.last = z.start + (P.n_used + 1);
+            z.V = ctx->d_lzV + ctx->lz_v_off[dir][I];
+            z.out = ctx->d_lzout + ctx->lz_out_off[dir][I];
+            z.stat = ctx->d_lzstat;
+            ch.push_back(z);
+            Smax = std::max(Smax, (P.N + ctx->lz_cluster - 1) / ctx->lz_cluster);
+            rmax = std::max(rmax, P.L + 1);
+        }
+    }
+    if (ch.empty()) return BD_OK;
+    if (2 + 7 + 7 > 32) return fail(ctx, BD_ERR_ARG, "too many scalars");
+    // largest chains first so the long ones start early
+    std::sort(ch.begin(), ch.end(), [](const LzChain &a, const LzChain &b) {
+        return (double)a.N * a.L * a.L > (double)b.N * b.L * b.L;
+    });
+    // zero the output rows (the reference clears them, source/BcDor-Lanczos.cpp:88)
+    for (int I = ch_lo; I < ch_hi; ++I)
+        for (int dir = 0; dir < 2; ++dir) {
+            const ChainPlan &P = ctx->chans[I].lz[dir];
+            if (P.L > 0)
+                CU(cudaMemsetAsync(ctx->d_lzout + ctx->lz_out_off[dir][I], 0,
+                                   sizeof(double) * (size_t)P.L * (P.nden_out + ctx->chans[I].D), ctx->st));
+        }
+    // chain descriptors live in a small device array (one slot per chain of the range)
+    LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
+    CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
+    CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, ctx->lz_cluster, ctx->eta, ctx->st));
+    return BD_OK;
+}
+
+int dyson_order(const bd_ctx *ctx, int I, bool lanczos) {
+    const Chan &C = ctx->chans[I];
+    return lanczos ? C.D + C.lz[0].L + C.lz[1].L : C.D + C.nfw + C.nbk;
+}
+
+// Scratch of every channel's Dyson problem at fixed offsets (no overlap between channels).
+int ensure_dyson(bd_ctx *ctx, bool lanczos) {
+    const int ns = ctx->nsubsh;
+    ctx->dy_A_off.assign(ns, 0); ctx->dy_vec_off.assign(ns, 0); ctx->dy_sol_off.assign(ns, 0);
+    ctx->dy_R_off.assign(ns, 0); ctx->dy_work_off.assign(ns, 0);
+    size_t a = 0, v = 0, s = 0, r = 0, w = 0;
+    for (int I = 0; I < ns; ++I) {
+        const size_t n = (size_t)dyson_order(ctx, I, lanczos), D = ctx->chans[I].D;
+        ctx->dy_A_off[I] = (long long)a; a += n * n;
+        ctx->dy_vec_off[I] = (long long)v; v += 3 * n;
+        ctx->dy_sol_off[I] = (long long)s; s += n * (2 + D);
+        ctx->dy_R_off[I] = (long long)r; r += D * n + n * (2 + D);
+        ctx->dy_work_off[I] = (long long)w; w += 5 * n * n;
+    }
+    if (a > (size_t)2 << 30) return fail(ctx, BD_ERR_CAPACITY, "Dyson matrices need %.1f GB", a * 8.0 / 1e9);
+    if (a > ctx->dyA_cap || v > ctx->dyvec_cap || s > ctx->dysol_cap || r > ctx->dyR_cap || w > ctx->dywork_cap) {
+        CU(cudaStreamSynchronize(ctx->st));
+        if (r > ctx->dyR_cap) {
+            if (ctx->d_dyR) cudaFree(ctx->d_dyR);
+            ctx->d_dyR = nullptr; ctx->dyR_cap = 0;
+            CU(cudaMalloc(&ctx->d_dyR, sizeof(double) * r));
+            ctx->dyR_cap = r;
+        }
+        if (w > ctx->dywork_cap) {
+            if (ctx->d_dywork) cudaFree(ctx->d_dywork);
+            ctx->d_dywork = nullptr; ctx->dywork_cap = 0;
+            CU(cudaMalloc(&ctx->d_dywork, sizeof(double) * w));
+            ctx->dywork_cap = w;
+        }
+        if (a > ctx->dyA_cap) {
+            if (ctx->d_dyA) cudaFree(ctx->d_dyA);
+            ctx->d_dyA = nullptr; ctx->dyA_cap = 0;
+            CU(cudaMalloc(&ctx->d_dyA, sizeof(double) * a));
+            ctx->dyA_cap = a;
+        }
+        if (v > ctx->dyvec_cap) {
+            if (ctx->d_dyvec) cudaFree(ctx->d_dyvec);
+            ctx->d_dyvec = nullptr; ctx->dyvec_cap = 0;
+            CU(cudaMalloc(&ctx->d_dyvec, sizeof(double) * v));
+            ctx->dyvec_cap = v;
+        }
+        if (s > ctx->dysol_cap) {
+            if (ctx->d_dysol) cudaFree(ctx->d_dysol);
+            ctx->d_dysol = nullptr; ctx->dysol_cap = 0;
+            CU(cudaMalloc(&ctx->d_dysol, sizeof(double) * s));
+            ctx->dysol_cap = s;
+        }
+    }
+    return BD_OK;
+}
+
+// Dyson jobs of channels [ch_lo, ch_hi); ensure_dyson must have run for this mode.
+int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
+    std::vector<DyJob> jobs;
+    std::vector<long long> row_first;
+    long long rows = 0;
+    int nmax = 1, Dmax = 1;
+    for (int I = ch_lo; I < ch_hi; ++I) {
+        Chan &C = ctx->chans[I];
+        DyJob J{};
+        J.ch = I; J.D = C.D; J.j2 = C.j2;
+        if (lanczos) {
+            const ChainPlan &F = C.lz[0], &B = C.lz[1];
+            J.nfw = F.L; J.nbk = B.L; J.nden = F.nden_out;
+            J.lanczos_fw = F.L > 0; J.lanczos_bk = B.L > 0;
+            J.fw_rows = ctx->d_lzout + ctx->lz_out_off[0][I];
+            J.bk_rows = ctx->d_lzout + ctx->lz_out_off[1][I];
+            J.ipiv_fw = ctx->d_lzint + ctx->lz_int_off[0][I] + 2 * (F.n_used + 1);
+            J.ipiv_bk = ctx->d_lzint + ctx->lz_int_off[1][I] + 2 * (B.n_used + 1);
+        } else {
+            J.nfw = C.nfw; J.nbk = C.nbk; J.nden = 2;
+            J.E_fw = ctx->d_Efw + C.fw_off; J.M_fw = ctx->d_Mfw + C.mfw_off;
+            J.E_bk = ctx->d_Ebk + C.bk_off; J.M_bk = ctx->d_Mbk + C.mbk_off;
+        }
+        J.n = C.D + J.nfw + J.nbk;
+        if (J.n != dyson_order(ctx, I, lanczos)) return fail(ctx, BD_ERR_STATE, "Dyson layout mismatch");
+        J.sighf = ctx->d_sighf + ctx->chan_dd_off[I];
+        J.sig1b = ctx->d_sig1b + ctx->chan_dd_off[I];
+        J.efermi = C.efermi;
+        J.A = ctx->d_dyA + ctx->dy_A_off[I];
+        J.d = ctx->d_dyvec + ctx->dy_vec_off[I]; J.e = J.d + J.n; J.tau = J.e + J.n;
+        J.R = ctx->d_dyR + ctx->dy_R_off[I];
+        J.sol = ctx->d_dysol + ctx->dy_sol_off[I];
+        J.nq = ctx->d_dynq + 2 * I;
+        J.koltun = ctx->d_dykol + 3 * I;
+        J.stat = ctx->d_dystat + I;
+        jobs.push_back(J);
+        row_first.push_back(rows);
+        rows += J.n;
+        nmax = std::max(nmax, J.n);
+        Dmax = std::max(Dmax, J.D);
+    }
+    if (Dmax > 8) return fail(ctx, BD_ERR_CAPACITY, "more than 8 orbitals in a channel");
+    // descriptors at the channel's slot so per-channel launches never overwrite queued ones
+    CU(cudaMemcpyAsync(ctx->d_jobs + ch_lo, jobs.data(), sizeof(DyJob) * jobs.size(), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_row_first + ch_lo, row_first.data(), sizeof(long long) * row_first.size(),
+                       cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(ctx->d_work_first + ch_lo, ctx->dy_work_off.data() + ch_lo, sizeof(long long) * jobs.size(),
+                       cudaMemcpyHostToDevice, ctx->st));
+    CU(launch_dyson(ctx->d_jobs + ch_lo, (int)jobs.size(), ctx->d_row_first + ch_lo, rows, nmax, Dmax,
+                    ctx->dy_cluster, ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
+    return BD_OK;
+}
+
+int alloc_lanczos(bd_ctx *ctx) {
+    // descriptors, vectors, rows for every channel x direction
+    size_t vbytes = 0;
+    long long out = 0, ints = 0, pv = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+        ctx->lz_v_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_out_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_int_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_piv_off[dir].assign(ctx->nsubsh, 0);
+    }
+    std::vector<int> hints;
+    std::vector<double> hpiv;
+    for (int I = 0; I < ctx->nsubsh; ++I)
+        for (int dir = 0; dir < 2; ++dir) {
+            ChainPlan &P = ctx->chans[I].lz[dir];
+            const int D = ctx->chans[I].D;
+            ctx->lz_v_off[dir][I] = (long long)vbytes;
+            vbytes += sizeof(double) * (size_t)std::max(P.L, 0) * ((P.N + 31) / 32 * 32);
+            vbytes = (vbytes + 255) / 256 * 256;
+            ctx->lz_out_off[dir][I] = out;
+            out += (long long)std::max(P.L, 0) * (P.nden_out + D);
+            ctx->lz_int_off[dir][I] = ints;
+            // start[n_used+1] | last[n_used+1] | ipiv[nden_out + D]
+            std::vector<int> st = P.start, la = P.last;
+            la.push_back(0);
+            hints.insert(hints.end(), st.begin(), st.end());
+            hints.insert(hints.end(), la.begin(), la.end());
+            hints.insert(hints.end(), P.ipiv.begin(), P.ipiv.end());
+            ints = (long long)hints.size();
+            ctx->lz_piv_off[dir][I] = pv;
+            hpiv.insert(hpiv.end(), P.piv.begin(), P.piv.end());
+            pv = (long long)hpiv.size();
+        }
+    if (vbytes) {
+        void *p = nullptr;
+        CU(cudaMalloc(&p, vbytes));
+        ctx->bufs.push_back({p, vbytes});
+        ctx->d_lzV = reinterpret_cast<char *>(p);
+    }
+    ctx->lzV_bytes = vbytes;
+    ctx->lzout_total = out;
+    int rc;
+    if ((rc = dalloc(ctx, &ctx->d_lzout, (size_t)out))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_lzint, hints))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_lzpiv, hpiv))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_lzstat, 4))) return rc;
+    CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
+    if ((rc = dalloc(ctx, &ctx->d_chains, (size_t)2 * ctx->nsubsh))) return rc;
+    return BD_OK;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+int bd_version(void) { return 1; }
+
+int bd_create(bd_ctx **out, int device) {
+    if (!out) return BD_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return BD_ERR_CUDA;
+    bd_ctx *ctx = new bd_ctx();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return BD_ERR_CUDA;
+    }
+    for (auto &e : ctx->ev) cudaEventCreate(&e);
+    *out = ctx;
+    return BD_OK;
+}
+
+void bd_destroy(bd_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    free_all(ctx);
+    if (ctx->d_dyA) cudaFree(ctx->d_dyA);
+    if (ctx->d_dyvec) cudaFree(ctx->d_dyvec);
+    if (ctx->d_dysol) cudaFree(ctx->d_dysol);
+    if (ctx->d_dyR) cudaFree(ctx->d_dyR);
+    if (ctx->d_dywork) cudaFree(ctx->d_dywork);
+    for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+const char *bd_last_error(const bd_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp, const bd_propagator *prop) {
+    if (!ctx || !ms || !vpp || !prop) return BD_ERR_ARG;
+    if (ms->nsubsh < 1 || ms->norb < 1 || prop->nspb < 1 || vpp->n_me < 0) return fail(ctx, BD_ERR_ARG, "empty problem");
+    CU(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false;
+    const int ns = ms->nsubsh;
+    ctx->nsubsh = ns; ctx->norb = ms->norb; ctx->nspb = prop->nspb;
+    ctx->l.assign(ms->l, ms->l + ns); ctx->j2.assign(ms->j2, ms->j2 + ns); ctx->ip.assign(ms->ip, ms->ip + ns);
+    ctx->ch.assign(ms->ch, ms->ch + ns); ctx->no.assign(ms->no, ms->no + ns);
+    ctx->orb_sh.assign(ms->orb_sh, ms->orb_sh + ms->norb);
+    ctx->orb_xe.assign(ms->orb_xe, ms->orb_xe + ms->norb);
+    ctx->jmax = 0;
+    for (int s = 0; s < ns; ++s) {
+        ctx->jmax = std::max(ctx->jmax, ctx->j2[s]);  // Calculate_Jch_bounds: Jmax = max 2j
+        if (ctx->no[s] < 1 || ctx->no[s] > prop->nspb || ctx->no[s] > 8)
+            return fail(ctx, BD_ERR_ARG, "subshell %d: %d orbits (1..min(nspb,8) supported)", s, ctx->no[s]);
+        if (ctx->j2[s] < 1 || ctx->j2[s] % 2 != 1) return fail(ctx, BD_ERR_ARG, "subshell %d: 2j = %d", s, ctx->j2[s]);
+    }
+    if (ctx->jmax >= kJMult) return fail(ctx, BD_ERR_ARG, "2j too large");
+    ctx->orb_start.assign(ns, 0);
+    {
+        int acc = 0;
+        for (int s = 0; s < ns; ++s) { ctx->orb_start[s] = acc; acc += ctx->no[s]; }
+        if (acc != ms->norb) return fail(ctx, BD_ERR_ARG, "sum of orbits %d != norb %d", acc, ms->norb);
+        for (int o = 0; o < ms->norb; ++o)
+            if (ctx->orb_sh[o] < 0 || ctx->orb_sh[o] >= ns) return fail(ctx, BD_ERR_ARG, "orbit %d: bad subshell", o);
+    }
+    ctx->np.assign(prop->np, prop->np + ns); ctx->nh.assign(prop->nh, prop->nh + ns);
+    ctx->p_start.assign(ns, 0); ctx->h_start.assign(ns, 0);
+    int nqp = 0, nqh = 0;
+    for (int s = 0; s < ns; ++s) {
+        if (ctx->np[s] < 0 || ctx->nh[s] < 0) return fail(ctx, BD_ERR_ARG, "negative fragment count");
+        ctx->p_start[s] = nqp; ctx->h_start[s] = nqh; nqp += ctx->np[s]; nqh += ctx->nh[s];
+    }
+    ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
+    std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
+    std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
+    // segment table of the sorted interaction (prepare_for_reading, source/BcDor-Vpp_potential.cpp:478-496)
+    std::vector<int> seg_str(kSegTable, -10), seg_end(kSegTable, -10);
+    {
+        int prev = -1;
+        for (int i = 0; i < vpp->n_me; ++i) {
+            const int k = vpp->iabJ[i], J = k % kJMult, ab = k / kJMult, a = ab / kABMult, b = ab % kABMult;
+            if (a < 0 || b < 0 || a >= ms->norb || b >= ms->norb) return fail(ctx, BD_ERR_ARG, "element %d: orbit out of range", i);
+            const int cs = ctx->ch[ctx->orb_sh[a]] + ctx->ch[ctx->orb_sh[b]];
+            const int ps = (ctx->ip[ctx->orb_sh[a]] + ctx->ip[ctx->orb_sh[b]]) % 2;
+            const int key = ind_chipJ(cs, ps, J);
+            if (key < 0 || key >= kSegTable) return fail(ctx, BD_ERR_ARG, "element %d: bad channel key", i);
+            if (key != prev) {
+                if (prev >= 0) seg_end[prev] = i - 1;
+                if (seg_str[key] >= 0) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
+                seg_str[key] = i; prev = key;
+            }
+        }
+        if (prev >= 0) seg_end[prev] = vpp->n_me - 1;
+    }
+    build_plan(ctx);
+    int rc;
+    DevProblem &P = ctx->dp;
+    P.nsubsh = ns; P.norb = ctx->norb; P.jmax = ctx->jmax; P.nspb = ctx->nspb; P.n_me = vpp->n_me;
+    int *t;
+    double *td;
+    if ((rc = dupload(ctx, &t, ctx->l))) return rc; P.l = t;
+    if ((rc = dupload(ctx, &t, ctx->j2))) return rc; P.j2 = t;
+    if ((rc = dupload(ctx, &t, ctx->ip))) return rc; P.ip = t;
+    if ((rc = dupload(ctx, &t, ctx->ch))) return rc; P.ch = t;
+    if ((rc = dupload(ctx, &t, ctx->no))) return rc; P.no = t;
+    if ((rc = dupload(ctx, &t, ctx->orb_start))) return rc; P.orb_start = t;
+    if ((rc = dupload(ctx, &t, ctx->orb_sh))) return rc; P.orb_sh = t;
+    if ((rc = dupload(ctx, &td, ctx->orb_xe))) return rc; P.orb_xe = td;
+    if ((rc = dupload(ctx, &t, ctx->np))) return rc; P.np = t;
+    if ((rc = dupload(ctx, &t, ctx->nh))) return rc; P.nh = t;
+    if ((rc = dupload(ctx, &t, ctx->p_start))) return rc; P.p_start = t;
+    if ((rc = dupload(ctx, &t, ctx->h_start))) return rc; P.h_start = t;
+    if ((rc = dupload(ctx, &td, ctx->ep))) return rc; P.ep = td;
+    if ((rc = dupload(ctx, &td, ctx->eh))) return rc; P.eh = td;
+    if ((rc = dupload(ctx, &td, fqp))) return rc; P.fqp = td;
+    if ((rc = dupload(ctx, &td, fqh))) return rc; P.fqh = td;
+    {
+        int *a, *b;
+        double *v;
+        if ((rc = dalloc(ctx, &a, vpp->n_me))) return rc;
+        if ((rc = dalloc(ctx, &b, vpp->n_me))) return rc;
+        if ((rc = dalloc(ctx, &v, vpp->n_me))) return rc;
+        if (vpp->n_me > 0) {
+            CU(cudaMemcpyAsync(a, vpp->iabJ, sizeof(int) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
+            CU(cudaMemcpyAsync(b, vpp->icdJ, sizeof(int) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
+            CU(cudaMemcpyAsync(v, vpp->V, sizeof(double) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
+        }
+        P.iabJ = a; P.icdJ = b; P.V = v;
+    }
+    if ((rc = dupload(ctx, &t, seg_str))) return rc; P.seg_str = t;
+    if ((rc = dupload(ctx, &t, seg_end))) return rc; P.seg_end = t;
+    // plan arrays
+    if ((rc = dupload(ctx, &ctx->d_blocks, ctx->blocks))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_blk_vp_first, ctx->blk_vp_first))) return rc;
+    std::vector<ChanSig> cs(ns);
+    std::vector<int> seg_fw(ctx->tot_fw), seg_bk(ctx->tot_bk), segoff_fw(ns + 1), segoff_bk(ns + 1);
+    std::vector<int> idx_fw(ctx->tot_fw), idx_bk(ctx->tot_bk);
+    for (int I = 0; I < ns; ++I) {
+        const Chan &C = ctx->chans[I];
+        cs[I] = ChanSig{C.D, C.nfw, C.nbk, (int)C.fw_off, (int)C.bk_off, C.mfw_off, C.mbk_off};
+        for (int k = 0; k < C.nfw; ++k) { seg_fw[C.fw_off + k] = I; idx_fw[C.fw_off + k] = (int)(C.fw_off + k); }
+        for (int k = 0; k < C.nbk; ++k) { seg_bk[C.bk_off + k] = I; idx_bk[C.bk_off + k] = (int)(C.bk_off + k); }
+        segoff_fw[I] = (int)C.fw_off; segoff_bk[I] = (int)C.bk_off;
+    }
+    segoff_fw[ns] = (int)ctx->tot_fw; segoff_bk[ns] = (int)ctx->tot_bk;  // scratch for per-range relative offsets
+    if ((rc = dupload(ctx, &ctx->d_cs, cs))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_seg_fw, seg_fw))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_seg_bk, seg_bk))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_idx_fw, idx_fw))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_idx_bk, idx_bk))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_segoff_fw, segoff_fw))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_segoff_bk, segoff_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_perm_fw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_perm_bk, ctx->tot_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_keys_tmp, std::max(ctx->tot_fw, ctx->tot_bk)))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_vp, ctx->tot_vp))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Efw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_S2fw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mfw, ctx->tot_mfw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Ebk, ctx->tot_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_S2bk, ctx->tot_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mbk, ctx->tot_mbk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Efw_s, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mfw_s, ctx->tot_mfw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Ebk_s, ctx->tot_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mbk_s, ctx->tot_mbk))) return rc;
+    {   // CUB scratch for the largest segmented sort
+        size_t b1 = 0, b2 = 0;
+        const int nmax = (int)std::max<long long>(1, std::max(ctx->tot_fw, ctx->tot_bk));
+        CU(cub::DeviceSegmentedRadixSort::SortPairs(nullptr, b1, ctx->d_Efw, ctx->d_keys_tmp, ctx->d_idx_fw,
+                                                    ctx->d_perm_fw, nmax, ns, ctx->d_segoff_fw, ctx->d_segoff_fw + 1,
+                                                    0, 64, ctx->st));
+        CU(cub::DeviceSegmentedRadixSort::SortPairsDescending(nullptr, b2, ctx->d_Efw, ctx->d_keys_tmp,
+                                                              ctx->d_idx_fw, ctx->d_perm_fw, nmax, ns,
+                                                              ctx->d_segoff_fw, ctx->d_segoff_fw + 1, 0, 64, ctx->st));
+        ctx->cub_bytes = std::max(b1, b2);
+        if ((rc = dalloc(ctx, reinterpret_cast<char **>(&ctx->d_cub_tmp), ctx->cub_bytes))) return rc;
+    }
+    // one-body (diag xe, Trel=7 ExtU1=1) and static self-energy, per channel D x D
+    ctx->chan_dd_off.assign(ns, 0);
+    std::vector<double> s1b;
+    std::vector<int3> ent;
+    for (int I = 0; I < ns; ++I) {
+        const int D = ctx->no[I];
+        ctx->chan_dd_off[I] = (long long)s1b.size();
+        for (int r = 0; r < D; ++r)
+            for (int c = 0; c < D; ++c) s1b.push_back(r == c ? ctx->orb_xe[ctx->orb_start[I] + r] : 0.0);
+        for (int nc = 0; nc < D; ++nc)
+            for (int nr = nc; nr < D; ++nr) ent.push_back(make_int3(I, nr, nc));
+    }
+    if ((rc = dupload(ctx, &ctx->d_sig1b, s1b))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_sighf, s1b.size()))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_dd_off, ctx->chan_dd_off))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_ehf_entries, ent))) return rc;
+    ctx->n_ehf_entries = (int)ent.size();
+    // Dyson per-channel small outputs
+    if ((rc = dalloc(ctx, &ctx->d_dynq, (size_t)2 * ns))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_dykol, (size_t)3 * ns))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_dystat, (size_t)ns))) return rc;
+    CU(cudaMemsetAsync(ctx->d_dystat, 0, sizeof(int) * ns, ctx->st));
+    if ((rc = dalloc(ctx, &ctx->d_jobs, (size_t)ns))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_row_first, (size_t)ns))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_work_first, (size_t)ns))) return rc;
+    ctx->dy_sol_off.assign(ns, 0);
+    ctx->res_nq.assign(2 * ns, 0);
+    CU(cudaStreamSynchronize(ctx->st));
+    ctx->uploaded = true;
+    return BD_OK;
+}
+
+int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv) {
+    if (!ctx || !piv) return BD_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+    CU(cudaSetDevice(ctx->device));
+    ctx->piv_npvt.assign(piv->npvt, piv->npvt + ctx->nsubsh);
+    ctx->piv_first.assign(ctx->nsubsh + 1, 0);
+    int tot = 0;
+    size_t vtot = 0;
+    for (int s = 0; s < ctx->nsubsh; ++s) {
+        if (ctx->piv_npvt[s] < 0 || ctx->piv_npvt[s] + 1 + 2 + ctx->no[s] > 32)
+            return fail(ctx, BD_ERR_ARG, "subshell %d: %d pivots", s, ctx->piv_npvt[s]);
+        ctx->piv_first[s] = tot; tot += ctx->piv_npvt[s]; vtot += (size_t)ctx->piv_npvt[s] * ctx->no[s];
+    }
+    ctx->piv_first[ctx->nsubsh] = tot;
+    ctx->piv_nfw.assign(piv->n_itr_fw, piv->n_itr_fw + tot);
+    ctx->piv_nbk.assign(piv->n_itr_bk, piv->n_itr_bk + tot);
+    ctx->piv_vec.assign(piv->vec, piv->vec + vtot);
+    size_t vo = 0;
+    for (int I = 0; I < ctx->nsubsh; ++I) {
+        const int D = ctx->no[I], npv = ctx->piv_npvt[I], p0 = ctx->piv_first[I];
+        Chan &C = ctx->chans[I];
+        std::vector<double> work(ctx->piv_vec.begin() + vo, ctx->piv_vec.begin() + vo + (size_t)npv * D);
+        plan_chain(C.lz[0], C.nfw, D, npv, ctx->piv_nfw.data() + p0, work.data());
+        plan_chain(C.lz[1], C.nbk, D, npv, ctx->piv_nbk.data() + p0, work.data());
+        vo += (size_t)npv * D;
+    }
+    int rc = alloc_lanczos(ctx);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(ctx->st));
+    ctx->have_pivots = true;
+    return BD_OK;
+}
+
+int bd_count_poles(bd_ctx *ctx, int ish, int *n_fw, int *n_bk) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    if (n_fw) *n_fw = ctx->chans[ish].nfw;
+    if (n_bk) *n_bk = ctx->chans[ish].nbk;
+    return BD_OK;
+}
+
+int bd_ehf(bd_ctx *ctx, int ish, double *sig_hf) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    if ((rc = launch_ehf(ctx, ish, ish + 1))) return rc;
+    const int D = ctx->chans[ish].D;
+    if (sig_hf)
+        CU(cudaMemcpyAsync(sig_hf, ctx->d_sighf + ctx->chan_dd_off[ish], sizeof(double) * D * D,
+                           cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    return BD_OK;
+}
+
+int bd_sigma2_build(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, int *n_fw, double *sig_bk, int cap_bk,
+                    int *n_bk) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    Chan &C = ctx->chans[ish];
+    if (n_fw) *n_fw = C.nfw;
+    if (n_bk) *n_bk = C.nbk;
+    if (sig_fw && cap_fw < C.nfw) return fail(ctx, BD_ERR_CAPACITY, "sig_fw holds %d rows, %d needed", cap_fw, C.nfw);
+    if (sig_bk && cap_bk < C.nbk) return fail(ctx, BD_ERR_CAPACITY, "sig_bk holds %d rows, %d needed", cap_bk, C.nbk);
+    if ((rc = launch_sigma2(ctx, ish, ish + 1))) return rc;
+    for (int dir = 0; dir < 2; ++dir) {
+        double *host = dir == 0 ? sig_fw : sig_bk;
+        const int N = dir == 0 ? C.nfw : C.nbk;
+        if (!host || N == 0) continue;
+        double *tmp = nullptr;  // AoS staging in the reference's row layout
+        CU(cudaMallocAsync(&tmp, sizeof(double) * (size_t)N * (2 + C.D), ctx->st));
+        k_rows_aos<<<(N + 255) / 256, 256, 0, ctx->st>>>(
+            (dir == 0 ? ctx->d_Efw + C.fw_off : ctx->d_Ebk + C.bk_off),
+            (dir == 0 ? ctx->d_S2fw + C.fw_off : ctx->d_S2bk + C.bk_off),
+            (dir == 0 ? ctx->d_Mfw + C.mfw_off : ctx->d_Mbk + C.mbk_off), N, C.D, tmp);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(host, tmp, sizeof(double) * (size_t)N * (2 + C.D), cudaMemcpyDeviceToHost, ctx->st));
+        CU(cudaFreeAsync(tmp, ctx->st));
+    }
+    CU(cudaStreamSynchronize(ctx->st));
+    C.state = ST_SIGMA;
+    return BD_OK;
+}
+
+int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_itr_fw, int *n_itr_bk,
+                      double *lz_fw, int cap_fw, int *L_fw, int *ipiv_fw,
+                      double *lz_bk, int cap_bk, int *L_bk, int *ipiv_bk, int flags) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    Chan &C = ctx->chans[ish];
+    if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no Sigma(2) built", ish);
+    if (n_pvt < 0 || (n_pvt > 0 && (!pivots || !n_itr_fw || !n_itr_bk))) return fail(ctx, BD_ERR_ARG, "pivots");
+    if (n_pvt + 1 + 2 + C.D > 32) return fail(ctx, BD_ERR_ARG, "too many pivots (%d)", n_pvt);
+    // (re)plan this channel with the caller's pivots; same side effects as the reference:
+    // started pivots normalised in place, iteration counts rescaled in place
+    ChainPlan F, B;
+    plan_chain(F, C.nfw, C.D, n_pvt, n_itr_fw, pivots);
+    plan_chain(B, C.nbk, C.D, n_pvt, n_itr_bk, pivots);
+    if (F.L > 0) for (int p = 0; p < n_pvt; ++p) n_itr_fw[p] = F.nitr[p];
+    if (B.L > 0) for (int p = 0; p < n_pvt; ++p) n_itr_bk[p] = B.nitr[p];
+    if (L_fw) *L_fw = F.L;
+    if (L_bk) *L_bk = B.L;
+    if (lz_fw && cap_fw < F.L) return fail(ctx, BD_ERR_CAPACITY, "lz_fw holds %d rows, %d needed", cap_fw, F.L);
+    if (lz_bk && cap_bk < B.L) return fail(ctx, BD_ERR_CAPACITY, "lz_bk holds %d rows, %d needed", cap_bk, B.L);
+    // the resident layout was sized from the uploaded pivots; a different layout needs a fresh plan
+    if (!ctx->have_pivots || C.lz[0].L != F.L || C.lz[1].L != B.L || C.lz[0].nden_out != F.nden_out ||
+        C.lz[0].n_used != F.n_used || C.lz[1].n_used != B.n_used)
+        return fail(ctx, BD_ERR_STATE, "channel %d: pivots differ in shape from the uploaded ones", ish);
+    C.lz[0] = F; C.lz[1] = B;
+    // refresh this channel's schedule / pivots on the device
+    for (int dir = 0; dir < 2; ++dir) {
+        const ChainPlan &P = C.lz[dir];
+        std::vector<int> ints = P.start, la = P.last;
+        la.push_back(0);
+        ints.insert(ints.end(), la.begin(), la.end());
+        ints.insert(ints.end(), P.ipiv.begin(), P.ipiv.end());
+        CU(cudaMemcpyAsync(ctx->d_lzint + ctx->lz_int_off[dir][ish], ints.data(), sizeof(int) * ints.size(),
+                           cudaMemcpyHostToDevice, ctx->st));
+        if (!P.piv.empty())
+            CU(cudaMemcpyAsync(ctx->d_lzpiv + ctx->lz_piv_off[dir][ish], P.piv.data(), sizeof(double) * P.piv.size(),
+                               cudaMemcpyHostToDevice, ctx->st));
+    }
+    if ((rc = launch_sort(ctx, ish, ish + 1))) return rc;
+    if ((rc = launch_lanczos_range(ctx, ish, ish + 1, (flags & BD_RUN_MIXED) != 0))) return rc;
+    for (int dir = 0; dir < 2; ++dir) {
+        const ChainPlan &P = C.lz[dir];
+        double *host = dir == 0 ? lz_fw : lz_bk;
+        int *ip = dir == 0 ? ipiv_fw : ipiv_bk;
+        if (host && P.L > 0)
+            CU(cudaMemcpyAsync(host, ctx->d_lzout + ctx->lz_out_off[dir][ish],
+                               sizeof(double) * (size_t)P.L * (P.nden_out + C.D), cudaMemcpyDeviceToHost, ctx->st));
+        if (ip) std::memcpy(ip, P.ipiv.data(), sizeof(int) * P.ipiv.size());
+    }
+    CU(cudaStreamSynchronize(ctx->st));
+    C.state = ST_LANCZOS;
+    return BD_OK;
+}
+
+int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_hf, double e_fermi, double *sol_qp,
+                   int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh, double *koltun) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    Chan &C = ctx->chans[ish];
+    if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no self-energy", ish);
+    const int D = C.D;
+    if (sig1b)
+        CU(cudaMemcpyAsync(ctx->d_sig1b + ctx->chan_dd_off[ish], sig1b, sizeof(double) * D * D, cudaMemcpyHostToDevice,
+                           ctx->st));
+    if (sig_hf)
+        CU(cudaMemcpyAsync(ctx->d_sighf + ctx->chan_dd_off[ish], sig_hf, sizeof(double) * D * D, cudaMemcpyHostToDevice,
+                           ctx->st));
+    else if ((rc = launch_ehf(ctx, ish, ish + 1)))
+        return rc;
+    const double saved_ef = C.efermi;
+    if (!std::isnan(e_fermi)) C.efermi = e_fermi;
+    rc = ensure_dyson(ctx, C.state == ST_LANCZOS);
+    if (!rc) rc = launch_dyson_range(ctx, ish, ish + 1, C.state == ST_LANCZOS);
+    C.efermi = saved_ef;
+    if (rc) return rc;
+    int nq[2] = {0, 0}, st = 0;
+    CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaMemcpyAsync(&st, ctx->d_dystat + ish, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    double kol[3];
+    CU(cudaMemcpyAsync(kol, ctx->d_dykol + 3 * ish, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    if (st) {
+        CU(cudaMemsetAsync(ctx->d_dystat + ish, 0, sizeof(int), ctx->st));
+        return fail(ctx, BD_ERR_NUMERIC, "channel %d: the eigensolver did not converge", ish);
+    }
+    if (n_qp) *n_qp = nq[0];
+    if (n_qh) *n_qh = nq[1];
+    if (koltun) std::memcpy(koltun, kol, sizeof kol);
+    if ((sol_qp && cap_qp < nq[0]) || (sol_qh && cap_qh < nq[1]))
+        return fail(ctx, BD_ERR_CAPACITY, "solution buffers too small (%d, %d needed)", nq[0], nq[1]);
+    const double *dsol = ctx->d_dysol + ctx->dy_sol_off[ish];
+    if (sol_qp && nq[0])
+        CU(cudaMemcpyAsync(sol_qp, dsol, sizeof(double) * (size_t)nq[0] * (2 + D), cudaMemcpyDeviceToHost, ctx->st));
+    if (sol_qh && nq[1])
+        CU(cudaMemcpyAsync(sol_qh, dsol + (size_t)nq[0] * (2 + D), sizeof(double) * (size_t)nq[1] * (2 + D),
+                           cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    return BD_OK;
+}
+
+int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_rows, const int *ipiv_fw, int n_bk,
+                  const double *bk_rows, const int *ipiv_bk, const double *sig1b, const double *sig_hf, double e_fermi,
+                  double *sol_qp, int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh, double *koltun) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    Chan &C = ctx->chans[ish];
+    const int D = C.D, NT = nden + D;
+    if (nden < 2 || n_fw < 0 || n_bk < 0 || (n_fw > 0 && !fw_rows) || (n_bk > 0 && !bk_rows))
+        return fail(ctx, BD_ERR_ARG, "self-energy rows");
+    const int n = D + n_fw + n_bk;
+    const size_t nip = (size_t)nden + D;
+    double *dfw = nullptr, *dbk = nullptr, *dA = nullptr, *dv = nullptr, *dR = nullptr, *dsol = nullptr, *dwork = nullptr;
+    int *dipf = nullptr, *dipb = nullptr;
+    long long *dwf = nullptr, *drf = nullptr;
+    DyJob *dj = nullptr;
+    CU(cudaMallocAsync(&dfw, sizeof(double) * ((size_t)n_fw * NT + 1), ctx->st));
+    CU(cudaMallocAsync(&dbk, sizeof(double) * ((size_t)n_bk * NT + 1), ctx->st));
+    CU(cudaMallocAsync(&dipf, sizeof(int) * nip, ctx->st));
+    CU(cudaMallocAsync(&dipb, sizeof(int) * nip, ctx->st));
+    CU(cudaMallocAsync(&dA, sizeof(double) * (size_t)n * n, ctx->st));
+    CU(cudaMallocAsync(&dv, sizeof(double) * 3 * (size_t)n, ctx->st));
+    CU(cudaMallocAsync(&dR, sizeof(double) * ((size_t)D * n + (size_t)n * (2 + D)), ctx->st));
+    CU(cudaMallocAsync(&dsol, sizeof(double) * (size_t)n * (2 + D), ctx->st));
+    CU(cudaMallocAsync(&dwork, sizeof(double) * 5 * (size_t)n * n, ctx->st));
+    CU(cudaMallocAsync(&dwf, sizeof(long long) * 2, ctx->st));
+    CU(cudaMallocAsync(&drf, sizeof(long long) * 2, ctx->st));
+    CU(cudaMallocAsync(&dj, sizeof(DyJob), ctx->st));
+    if (n_fw) CU(cudaMemcpyAsync(dfw, fw_rows, sizeof(double) * (size_t)n_fw * NT, cudaMemcpyHostToDevice, ctx->st));
+    if (n_bk) CU(cudaMemcpyAsync(dbk, bk_rows, sizeof(double) * (size_t)n_bk * NT, cudaMemcpyHostToDevice, ctx->st));
+    if (ipiv_fw) CU(cudaMemcpyAsync(dipf, ipiv_fw, sizeof(int) * nip, cudaMemcpyHostToDevice, ctx->st));
+    if (ipiv_bk) CU(cudaMemcpyAsync(dipb, ipiv_bk, sizeof(int) * nip, cudaMemcpyHostToDevice, ctx->st));
+    if (sig1b) CU(cudaMemcpyAsync(ctx->d_sig1b + ctx->chan_dd_off[ish], sig1b, sizeof(double) * D * D, cudaMemcpyHostToDevice, ctx->st));
+    if (sig_hf) CU(cudaMemcpyAsync(ctx->d_sighf + ctx->chan_dd_off[ish], sig_hf, sizeof(double) * D * D, cudaMemcpyHostToDevice, ctx->st));
+    else if ((rc = launch_ehf(ctx, ish, ish + 1))) return rc;
+    DyJob J{};
+    J.ch = ish; J.D = D; J.j2 = C.j2; J.n = n; J.nfw = n_fw; J.nbk = n_bk; J.nden = nden;
+    J.lanczos_fw = (ipiv_fw != nullptr) && n_fw > 0 && ipiv_fw[0] > 0;
+    J.lanczos_bk = (ipiv_bk != nullptr) && n_bk > 0 && ipiv_bk[0] > 0;
+    J.fw_rows = dfw; J.bk_rows = dbk; J.ipiv_fw = dipf; J.ipiv_bk = dipb;
+    J.sighf = ctx->d_sighf + ctx->chan_dd_off[ish];
+    J.sig1b = ctx->d_sig1b + ctx->chan_dd_off[ish];
+    J.efermi = std::isnan(e_fermi) ? C.efermi : e_fermi;
+    J.A = dA; J.d = dv; J.e = dv + n; J.tau = dv + 2 * n; J.R = dR; J.sol = dsol;
+    J.nq = ctx->d_dynq + 2 * ish; J.koltun = ctx->d_dykol + 3 * ish; J.stat = ctx->d_dystat + ish;
+    long long zero[2] = {0, 0};
+    CU(cudaMemcpyAsync(dj, &J, sizeof(DyJob), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(dwf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaMemcpyAsync(drf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
+    CU(launch_dyson(dj, 1, drf, n, n, D, ctx->dy_cluster, dwork, dwf, ctx->st));
+    int nq[2] = {0, 0};
+    double kol[3];
+    CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof nq, cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaMemcpyAsync(kol, ctx->d_dykol + 3 * ish, sizeof kol, cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    if (n_qp) *n_qp = nq[0];
+    if (n_qh) *n_qh = nq[1];
+    if (koltun) std::memcpy(koltun, kol, sizeof kol);
+    rc = BD_OK;
+    if ((sol_qp && cap_qp < nq[0]) || (sol_qh && cap_qh < nq[1]))
+        rc = fail(ctx, BD_ERR_CAPACITY, "solution buffers too small (%d, %d needed)", nq[0], nq[1]);
+    else {
+        if (sol_qp && nq[0]) CU(cudaMemcpyAsync(sol_qp, dsol, sizeof(double) * (size_t)nq[0] * (2 + D), cudaMemcpyDeviceToHost, ctx->st));
+        if (sol_qh && nq[1])
+            CU(cudaMemcpyAsync(sol_qh, dsol + (size_t)nq[0] * (2 + D), sizeof(double) * (size_t)nq[1] * (2 + D),
+                               cudaMemcpyDeviceToHost, ctx->st));
+    }
+    for (void *q : {(void *)dfw, (void *)dbk, (void *)dipf, (void *)dipb, (void *)dA, (void *)dv, (void *)dR,
+                    (void *)dsol, (void *)dwork, (void *)dwf, (void *)drf, (void *)dj})
+        CU(cudaFreeAsync(q, ctx->st));
+    CU(cudaStreamSynchronize(ctx->st));
+    return rc;
+}
+
+int bd_lanczos_vectors(bd_ctx *ctx, int ish, int dir, int fp32, double *out, long long cap) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    if (dir != 0 && dir != 1) return fail(ctx, BD_ERR_ARG, "direction");
+    CU(cudaSetDevice(ctx->device));
+    const ChainPlan &P = ctx->chans[ish].lz[dir];
+    const long long need = (long long)P.L * P.N;
+    if (!out || cap < need) return fail(ctx, BD_ERR_CAPACITY, "need %lld doubles", need);
+    const int ld = (P.N + 31) / 32 * 32;
+    const char *base = ctx->d_lzV + ctx->lz_v_off[dir][ish];
+    CU(cudaStreamSynchronize(ctx->st));
+    if (fp32) {
+        std::vector<float> tmp((size_t)P.L * ld);
+        CU(cudaMemcpy(tmp.data(), base, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost));
+        for (int j = 0; j < P.L; ++j) for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = tmp[(size_t)j * ld + i];
+    } else {
+        std::vector<double> tmp((size_t)P.L * ld);
+        CU(cudaMemcpy(tmp.data(), base, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost));
+        for (int j = 0; j < P.L; ++j) for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = tmp[(size_t)j * ld + i];
+    }
+    return BD_OK;
+}
+
+int bd_run_all(bd_ctx *ctx, int flags) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+    const bool lanczos = (flags & BD_RUN_LANCZOS) != 0, fp32 = (flags & BD_RUN_MIXED) != 0;
+    if (lanczos && !ctx->have_pivots) return fail(ctx, BD_ERR_STATE, "no pivots uploaded");
+    CU(cudaSetDevice(ctx->device));
+    const int ns = ctx->nsubsh;
+    int rc;
+    ctx->results_valid = false;
+    if ((rc = ensure_dyson(ctx, lanczos))) return rc;
+    if (ctx->d_lzstat) CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
+    CU(cudaEventRecord(ctx->ev[0], ctx->st));
+    if (flags & BD_RUN_PER_CHANNEL) {
+        // the drop-in call pattern: every phase launched channel by channel
+        for (int I = 0; I < ns; ++I) {
+            if ((rc = launch_ehf(ctx, I, I + 1))) return rc;
+            if ((rc = launch_sigma2(ctx, I, I + 1))) return rc;
+        }
+        CU(cudaEventRecord(ctx->ev[1], ctx->st));
+        if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_sort(ctx, I, I + 1))) return rc;
+        CU(cudaEventRecord(ctx->ev[2], ctx->st));
+        if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_lanczos_range(ctx, I, I + 1, fp32))) return rc;
+        CU(cudaEventRecord(ctx->ev[3], ctx->st));
+        for (int I = 0; I < ns; ++I) if ((rc = launch_dyson_range(ctx, I, I + 1, lanczos))) return rc;
+    } else {
+        if ((rc = launch_ehf(ctx, 0, ns))) return rc;
+        if ((rc = launch_sigma2(ctx, 0, ns))) return rc;
+        CU(cudaEventRecord(ctx->ev[1], ctx->st));
+        if (lanczos && (rc = launch_sort(ctx, 0, ns))) return rc;
+        CU(cudaEventRecord(ctx->ev[2], ctx->st));
+        if (lanczos && (rc = launch_lanczos_range(ctx, 0, ns, fp32))) return rc;
+        CU(cudaEventRecord(ctx->ev[3], ctx->st));
+        if ((rc = launch_dyson_range(ctx, 0, ns, lanczos))) return rc;
+    }
+    CU(cudaEventRecord(ctx->ev[4], ctx->st));
+    for (int I = 0; I < ns; ++I) ctx->chans[I].state = lanczos ? ST_LANCZOS : ST_SIGMA;
+    ctx->last_lanczos_flags = flags;
+    ctx->results_valid = true;
+    return BD_OK;
+}
+
+int bd_sync(bd_ctx *ctx) {
+    if (!ctx) return BD_ERR_ARG;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->st));
+    if (ctx->results_valid) {
+        std::vector<int> st(ctx->nsubsh, 0);
+        CU(cudaMemcpy(ctx->res_nq.data(), ctx->d_dynq, sizeof(int) * 2 * ctx->nsubsh, cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(st.data(), ctx->d_dystat, sizeof(int) * ctx->nsubsh, cudaMemcpyDeviceToHost));
+        float ms[4];
+        for (int q = 0; q < 4; ++q) CU(cudaEventElapsedTime(&ms[q], ctx->ev[q], ctx->ev[q + 1]));
+        for (int q = 0; q < 4; ++q) ctx->timings[q] = ms[q];
+        ctx->timings[4] = ms[0] + ms[1] + ms[2] + ms[3];
+        ctx->lz_two_pass = 0;
+        if (ctx->d_lzstat) CU(cudaMemcpy(&ctx->lz_two_pass, ctx->d_lzstat, sizeof(int), cudaMemcpyDeviceToHost));
+        for (int I = 0; I < ctx->nsubsh; ++I)
+            if (st[I]) {
+                ctx->results_valid = false;
+                CU(cudaMemset(ctx->d_dystat, 0, sizeof(int) * ctx->nsubsh));
+                return fail(ctx, BD_ERR_NUMERIC, "channel %d: the eigensolver did not converge", I);
+            }
+    }
+    return BD_OK;
+}
+
+int bd_result_counts(bd_ctx *ctx, int ish, int *n_qp, int *n_qh) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
+    if (n_qp) *n_qp = ctx->res_nq[2 * ish];
+    if (n_qh) *n_qh = ctx->res_nq[2 * ish + 1];
+    return BD_OK;
+}
+
+int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *sol_qh, int cap_qh, double *koltun) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
+    CU(cudaSetDevice(ctx->device));
+    const int nqp = ctx->res_nq[2 * ish], nqh = ctx->res_nq[2 * ish + 1], D = ctx->chans[ish].D;
+    if ((sol_qp && cap_qp < nqp) || (sol_qh && cap_qh < nqh)) return fail(ctx, BD_ERR_CAPACITY, "solution buffers");
+    const double *dsol = ctx->d_dysol + ctx->dy_sol_off[ish];
+    if (sol_qp && nqp) CU(cudaMemcpy(sol_qp, dsol, sizeof(double) * (size_t)nqp * (2 + D), cudaMemcpyDeviceToHost));
+    if (sol_qh && nqh)
+        CU(cudaMemcpy(sol_qh, dsol + (size_t)nqp * (2 + D), sizeof(double) * (size_t)nqh * (2 + D),
+                      cudaMemcpyDeviceToHost));
+    if (koltun) CU(cudaMemcpy(koltun, ctx->d_dykol + 3 * ish, sizeof(double) * 3, cudaMemcpyDeviceToHost));
+    return BD_OK;
+}
+
+int bd_result_koltun_all(bd_ctx *ctx, double *koltun) {
+    if (!ctx || !koltun) return BD_ERR_ARG;
+    if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaMemcpy(koltun, ctx->d_dykol, sizeof(double) * 3 * ctx->nsubsh, cudaMemcpyDeviceToHost));
+    return BD_OK;
+}
+
+int bd_last_timings(bd_ctx *ctx, double *ms5) {
+    if (!ctx || !ms5) return BD_ERR_ARG;
+    for (int q = 0; q < 5; ++q) ms5[q] = ctx->timings[q];
+    return BD_OK;
+}
+
+/* Not part of the public header: number of Lanczos steps that took a second
+ * reorthogonalisation sweep in the last bd_run_all, and tuning knobs. */
+int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
+int bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta) {
+    if (!ctx) return BD_ERR_ARG;
+    if (lz_cluster != 1 && lz_cluster != 2 && lz_cluster != 4 && lz_cluster != 8 && lz_cluster != 16)
+        return fail(ctx, BD_ERR_ARG, "cluster size");
+    if (dy_cluster != 1 && dy_cluster != 2 && dy_cluster != 4 && dy_cluster != 8 && dy_cluster != 16)
+        return fail(ctx, BD_ERR_ARG, "cluster size");
+    if (!(eta > 0.0 && eta < 1.0)) return fail(ctx, BD_ERR_ARG, "eta");
+    ctx->lz_cluster = lz_cluster; ctx->dy_cluster = dy_cluster; ctx->eta = eta;
+    return BD_OK;
+}
+
+}  // extern "C"

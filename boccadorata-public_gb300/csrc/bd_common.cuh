@@ -1,0 +1,126 @@
+// bd_common.cuh -- device-side data structures shared by the kernels of the
+// Sigma(2) -> Lanczos -> Dyson chain (sm_103a).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bd {
+
+constexpr double kSqr2 = 1.4142135623730950488016887;
+constexpr int kChOff = -2, kJMult = 128, kABMult = 1024, kChMult = 5;
+constexpr int kSegTable = kChMult * kJMult * 2;
+
+// Device-resident problem: model space, propagator and interaction
+// (ModSpace_t / SpProp_t / VppInt_t).  Plain pointers into device memory.
+struct DevProblem {
+    int nsubsh, norb, jmax, nspb;
+    const int *l, *j2, *ip, *ch, *no, *orb_start, *orb_sh;
+    const double *orb_xe;
+    const int *np, *nh, *p_start, *h_start;
+    const double *ep, *eh, *fqp, *fqh;
+    int n_me;
+    const int *iabJ, *icdJ;
+    const double *V;
+    const int *seg_str, *seg_end;
+};
+
+// One (Jab, ia, ib, ig) block of the Sigma(2) build of one channel.  Its poles
+// occupy [fw_first, fw_first + nfw) of the channel's forward rows (same for bk);
+// its V' coefficients occupy vp_first .. vp_first + D*na*nb*ng (dense,
+// [d][alpha][beta][gamma], entries the reference skips are left unused).
+struct S2Block {
+    int ch;              // channel (subshell I)
+    int Jab, ia, ib, ig;
+    int nJab, nJgd;
+    int fw_first, nfw;   // global pole index of the block's first fw pole
+    int bk_first, nbk;
+    long long vp_first;  // offset into the V' scratch
+    int nvp;             // D * no[ia] * no[ib] * no[ig]
+};
+
+// Per-channel layout of the structure-of-arrays Sigma(2) on the device:
+// E[k], S2[k] at pole offset + k, M[d][k] at moff + d*N + k.
+struct ChanSig {
+    int D, nfw, nbk;
+    int fw_off, bk_off;          // pole offsets (global)
+    long long mfw_off, mbk_off;  // offsets into the M arrays
+};
+
+// One Lanczos chain set (channel x direction), processed by one thread-block cluster.
+struct LzChain {
+    int N, D, L;            // poles, orbitals, Lanczos vectors to compute
+    int n_used;             // pivots actually iterated (n_itr > 0)
+    int nden_out;           // leading doubles per output row (= n_pvt + 1)
+    int ld;                 // leading dimension of the vector store (>= N, multiple of 32)
+    const double *E;        // [N]   sorted energies
+    const double *M;        // [D][N] sorted couplings
+    const double *piv;      // [n_used][D] normalised pivots in use order
+    const int *start;       // [n_used + 1] first Lanczos index of each pivot chain
+    const int *last;        // [n_used] last index of each chain (may exceed L-1)
+    void *V;                // [L][ld] Lanczos vectors (double or float)
+    double *out;            // [L][nden_out + D] rows
+    int *stat;              // [2]: number of two-pass steps, error flag
+};
+
+// One Dyson eigenproblem.
+struct DyJob {
+    int ch, D, n, j2;
+    int nfw, nbk;            // pole-block sizes in the matrix
+    int nden;                // leading doubles of the self-energy rows
+    int lanczos_fw, lanczos_bk;  // whether the fw / bk parts are Lanczos rows
+    const double *fw_rows;   // [nfw][nden + D] (Lanczos) or nullptr (plain: SoA below)
+    const double *bk_rows;
+    const int *ipiv_fw, *ipiv_bk;  // [2 + n_used] start indices of the g branches
+    const double *E_fw, *M_fw;     // plain Sigma(2), SoA (M: [D][nfw])
+    const double *E_bk, *M_bk;
+    const double *sighf;     // [D][D] static self-energy
+    const double *sig1b;     // [D][D]
+    double efermi;
+    double *A;               // [n][n] scratch (row-major)
+    double *d, *e, *tau;     // [n] tridiagonal diagonal, off-diagonal, reflector scalars
+    double *R;               // [D][n] first D rows of Q, then n staged rows of 2 + D
+    double *sol;             // [n][2 + D] output rows (qp first, then qh)
+    int *nq;                 // [2] n_qp, n_qh
+    double *koltun;          // [3]
+    int *stat;               // [1] error flag
+};
+
+__host__ __device__ inline int tri_fail(int a, int b, int c) { return (a + b < c) || (b + c < a) || (c + a < b); }
+__host__ __device__ inline int ind_chipJ(int ch, int ip, int J) { return ((ch - kChOff) * 2 + ip) * kJMult + J; }
+__host__ __device__ inline int ind_i1i2J(int i1, int i2, int J) { return (i1 * kABMult + i2) * kJMult + J; }
+
+// VppInt_t::get (source/BcDor-Vpp_potential.cpp:557-607): exchange phase, ordering
+// of the two pair keys, binary search inside the (charge, parity, J) segment.
+__device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int id, int J) {
+    int isha = P.orb_sh[ia], ishb = P.orb_sh[ib];
+    int ip = (P.ip[isha] + P.ip[ishb]) % 2;
+    int ch = P.ch[isha] + P.ch[ishb];
+    int iph = 0, iab, icd;
+    if (ia <= ib) iab = ind_i1i2J(ia, ib, J);
+    else { iab = ind_i1i2J(ib, ia, J); iph += (P.j2[isha] + P.j2[ishb]) / 2 - J + 1; }
+    if (ic <= id) icd = ind_i1i2J(ic, id, J);
+    else {
+        int ishc = P.orb_sh[ic], ishd = P.orb_sh[id];
+        icd = ind_i1i2J(id, ic, J); iph += (P.j2[ishc] + P.j2[ishd]) / 2 - J + 1;
+    }
+    double xph = (double)(1 - 2 * (abs(iph) % 2));
+    if (icd < iab) { int t = iab; iab = icd; icd = t; }
+    int key = ind_chipJ(ch, ip, J);
+    int lo = P.seg_str[key], hi = P.seg_end[key];
+    if (lo < 0 || hi < 0) return 0.0;
+    for (int it = 0; it < 100; ++it) {   // the reference's bounded search
+        int mid = (hi + lo) / 2;
+        int am = P.iabJ[mid];
+        int test = (iab < am);
+        if (am == iab) {
+            int cm = P.icdJ[mid];
+            if (cm == icd) return __dmul_rn(P.V[mid], xph);
+            test = (icd < cm);
+        }
+        if (test) hi = mid;
+        else { lo = mid; if (lo < hi) lo++; }
+    }
+    return 0.0;
+}
+
+}  // namespace bd

@@ -1,0 +1,209 @@
+// k_dyson.cu -- K3-K5: Dyson matrix assembly, batched FP64 symmetric
+// eigensolve, quasiparticle / quasihole split and Koltun partial sums.
+//
+// Restates DysonMatrix (source/BcDor-DysonMatrix.cpp:123-532) and Calc_En
+// (:542-594).  The reference calls LAPACK dsyevd for all eigenvectors but only
+// uses the first D components of each (:448-470).  Here:
+//   K3 k_dyson_assemble   fills the dense matrix row by row (:269-390),
+//   K4a k_tridiag         Householder reduction A = Q T Q^T, one thread-block
+//                         cluster per matrix (rows split across the CTAs),
+//   K4b..K5 (k_eig.cu)    eigenvalues and the first D eigenvector components of T,
+//                         back-transformed, split by E_F, Koltun sums.
+#include <cooperative_groups.h>
+#include "bd_common.cuh"
+#include "bd_kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace bd {
+
+// ---------------------------------------------------------------- K3 assembly
+// One thread per matrix row.  Row order: D one-body rows, nfw forward poles,
+// nbk backward poles.
+__global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *row_first, long long total_rows) {
+    long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= total_rows) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DyJob J = jobs[lo];
+    const int r = (int)(g - row_first[lo]);
+    const int n = J.n, D = J.D, nfw = J.nfw, nbk = J.nbk;
+    double *Ar = J.A + (size_t)r * n;
+    for (int c = 0; c < n; ++c) Ar[c] = 0.0;
+    // couplings of pole i of part (0 fw, 1 bk) to orbital d: from self-energy rows
+    // [E/alpha, *, .., M_0 ..] when given, else from the structure-of-arrays Sigma(2)
+    const int NT = J.nden + D;
+    auto mcoup = [&](int part, int i, int d) -> double {
+        if (part == 0) return J.fw_rows ? J.fw_rows[(size_t)i * NT + J.nden + d] : J.M_fw[(size_t)d * nfw + i];
+        return J.bk_rows ? J.bk_rows[(size_t)i * NT + J.nden + d] : J.M_bk[(size_t)d * nbk + i];
+    };
+    if (r < D) {
+        for (int c = 0; c < D; ++c) Ar[c] = J.sig1b[r * D + c] + J.sighf[r * D + c];
+        for (int i = 0; i < nfw; ++i) Ar[D + i] = mcoup(0, i, r);
+        for (int i = 0; i < nbk; ++i) Ar[D + nfw + i] = mcoup(1, i, r);
+        return;
+    }
+    const int part = (r < D + nfw) ? 0 : 1;
+    const int off = part == 0 ? D : D + nfw;
+    const int np = part == 0 ? nfw : nbk;
+    const int i = r - off;
+    const bool lz = part == 0 ? J.lanczos_fw : J.lanczos_bk;
+    const double *rowsp = part == 0 ? J.fw_rows : J.bk_rows;
+    for (int d = 0; d < D; ++d) Ar[d] = mcoup(part, i, d);
+    if (!lz) {
+        Ar[r] = rowsp ? rowsp[(size_t)i * NT] : (part == 0 ? J.E_fw[i] : J.E_bk[i]);
+        return;
+    }
+    const double *rows = rowsp;
+    const int *ipiv = part == 0 ? J.ipiv_fw : J.ipiv_bk;
+    const int nbr = ipiv[0];  // branches (pivots used)
+    Ar[r] = rows[(size_t)i * NT + 0];
+    if (i >= 1) Ar[r - 1] = rows[(size_t)i * NT + 1];
+    if (i + 1 < np) Ar[r + 1] = rows[(size_t)(i + 1) * NT + 1];
+    // fishbone (:303-333): branch nc (1 .. nbr-1) starts at s = ipiv[nc+1];
+    // row s-1 couples to every later row nr >= s with row_nr[1 + nc]
+    for (int nc = 1; nc < nbr; ++nc) {
+        const int s = ipiv[nc + 1];
+        if (s < 1 || s >= np) continue;
+        if (i == s - 1)
+            for (int nr = s; nr < np; ++nr) Ar[off + nr] = rows[(size_t)nr * NT + 1 + nc];
+        if (i >= s) Ar[off + s - 1] = rows[(size_t)i * NT + 1 + nc];
+    }
+}
+
+// ---------------------------------------------------------------- K4a Householder
+constexpr int kTdThreads = 256;
+
+__device__ inline double block_sum(double v, double *scratch) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += scratch[q];
+    return s;
+}
+
+// Shared layout (doubles): v[nmax] | wfull[nmax] | wpart[RS] | part[4] | scratch[32]
+__global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int njobs, int nmax) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CL = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int jid = blockIdx.x / CL;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.n;
+    const int RS = (nmax + CL - 1) / CL;   // rows per CTA (upper bound for smem)
+    const int rs = (n + CL - 1) / CL;
+    const int r0 = rank * rs, r1 = min(n, r0 + rs);
+    extern __shared__ double sm[];
+    double *v = sm;
+    double *wfull = v + nmax;
+    double *wpart = wfull + nmax;
+    double *part = wpart + RS;
+    double *scratch = part + 4;
+    double *A = J.A;
+    const int tid = threadIdx.x;
+    for (int k = 0; k + 2 < n; ++k) {
+        const int b0 = k + 1, m = n - b0;
+        // reflector from column k (= row k by symmetry), computed identically by every CTA
+        double sig = 0.0;
+        for (int t = 1 + tid; t < m; t += kTdThreads) { double x = __ldcg(A + (size_t)k * n + b0 + t); sig += x * x; }
+        sig = block_sum(sig, scratch);
+        const double alpha = __ldcg(A + (size_t)k * n + b0);
+        double tau = 0.0, beta = alpha;
+        if (sig != 0.0) {
+            beta = -copysign(sqrt(alpha * alpha + sig), alpha);
+            tau = (beta - alpha) / beta;
+            const double scal = 1.0 / (alpha - beta);
+            for (int t = tid; t < m; t += kTdThreads) v[t] = (t == 0) ? 1.0 : __ldcg(A + (size_t)k * n + b0 + t) * scal;
+        }
+        __syncthreads();
+        if (rank == 0 && tid == 0) { J.e[k] = beta; J.tau[k] = tau; J.d[k] = __ldcg(A + (size_t)k * n + k); }
+        if (sig != 0.0) {
+            // p_i = tau * sum_j A_ij v_j for own rows i >= b0; partial p.v
+            const int ra = max(r0, b0);
+            const int warp = tid >> 5, lane = tid & 31;
+            double pv = 0.0;
+            for (int i = ra + warp; i < r1; i += kTdThreads / 32) {
+                const double *Ai = A + (size_t)i * n + b0;
+                double s = 0.0;
+                for (int t = lane; t < m; t += 32) s += Ai[t] * v[t];
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                const double p = tau * s;
+                if (lane == 0) { wpart[i - r0] = p; pv += p * v[i - b0]; }
+            }
+            pv = block_sum(pv, scratch);
+            if (tid == 0) part[0] = pv;
+            cluster.sync();
+            double K = 0.0;
+            for (int q = 0; q < CL; ++q) K += cluster.map_shared_rank(part, q)[0];
+            // w_i = p_i - (tau/2) K v_i for own rows
+            for (int i = ra + tid; i < r1; i += kTdThreads) wpart[i - r0] -= 0.5 * tau * K * v[i - b0];
+            cluster.sync();
+            // all-gather w over the trailing index range
+            for (int t = tid; t < m; t += kTdThreads) {
+                const int i = b0 + t, owner = i / rs;
+                wfull[t] = cluster.map_shared_rank(wpart, owner)[i - owner * rs];
+            }
+            __syncthreads();
+            // A_ij -= v_i w_j + w_i v_j on own rows
+            for (int i = ra; i < r1; ++i) {
+                const double vi = v[i - b0], wi = wfull[i - b0];
+                double *Ai = A + (size_t)i * n + b0;
+                for (int t = tid; t < m; t += kTdThreads) Ai[t] -= vi * wfull[t] + wi * v[t];
+            }
+            // keep the reflector in row k (columns > k) for the back-transformation
+            if (rank == 0)
+                for (int t = tid; t < m; t += kTdThreads) A[(size_t)k * n + b0 + t] = v[t];
+        }
+        cluster.sync();
+    }
+    if (rank == 0 && tid == 0) {
+        if (n >= 2) {
+            J.d[n - 2] = __ldcg(A + (size_t)(n - 2) * n + (n - 2));
+            J.e[n - 2] = __ldcg(A + (size_t)(n - 1) * n + (n - 2));
+            J.tau[n - 2] = 0.0;
+        }
+        J.d[n - 1] = __ldcg(A + (size_t)(n - 1) * n + (n - 1));
+        J.e[n - 1] = 0.0;
+        J.tau[n - 1] = 0.0;
+    }
+    cluster.sync();
+}
+
+size_t tridiag_smem_bytes(int nmax, int cluster) {
+    const int RS = (nmax + cluster - 1) / cluster;
+    return sizeof(double) * ((size_t)2 * nmax + RS + 4 + 32);
+}
+
+cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
+                         int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st) {
+    if (njobs <= 0) return cudaSuccess;
+    k_dyson_assemble<<<(unsigned)((total_rows + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    size_t smem = tridiag_smem_bytes(nmax, cluster);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(njobs * cluster, 1, 1);
+    cfg.blockDim = dim3(kTdThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    e = cudaLaunchKernelEx(&cfg, k_tridiag, d_jobs, njobs, nmax);
+    if (e != cudaSuccess) return e;
+    (void)Dmax;
+    return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);
+}
+
+}  // namespace bd

@@ -1,0 +1,359 @@
+// k_eig.cu -- K4b..K5: eigen-decomposition of the tridiagonal T = Q^T A Q left by
+// k_tridiag, for many matrices at once, returning only what DysonMatrix uses
+// (source/BcDor-DysonMatrix.cpp:442-488): every eigenvalue W_k and the first D
+// components x_k[0:D] of the corresponding eigenvector of A.
+//
+//   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows)
+//   k_bisect  W_k by bisection on Sturm counts, one thread per eigenvalue
+//   k_invit   y_k by inverse iteration on T - W_k I (tridiagonal LU with partial
+//             pivoting), one thread per eigenvalue, each from its own start vector
+//   k_cluster_orth  eigenvalues closer than 1e-6 |T| form a cluster (the Dyson
+//             spectra hold exactly degenerate groups of tens to hundreds of
+//             zero-strength solutions); its vectors are orthonormalised together
+//   k_post    x_k[0:D] = R y_k, Z_k = sum_d x_k[d]^2, quasiparticle / quasihole split
+//             by E_F with both lists by descending W, Koltun partial sums (Calc_En,
+//             source/BcDor-DysonMatrix.cpp:542-594)
+#include "bd_common.cuh"
+#include "bd_kernels.h"
+
+namespace bd {
+
+constexpr int kEigThreads = 256;
+
+// ------------------------------------------------------------------ K4b
+__global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.n, D = J.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ double red[kEigThreads / 32][8];
+    __shared__ double sums[8];
+    double *R = J.R;
+    for (int q = tid; q < D * n; q += kEigThreads) R[q] = ((q % n) == (q / n)) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int k = 0; k + 2 < n; ++k) {
+        const double tau = J.tau[k];
+        if (tau == 0.0) continue;
+        const int b0 = k + 1, m = n - b0;
+        const double *v = J.A + (size_t)k * n + b0;
+        double s[8];
+#pragma unroll
+        for (int d = 0; d < 8; ++d) s[d] = 0.0;
+        for (int t = tid; t < m; t += kEigThreads) {
+            const double vt = v[t];
+#pragma unroll
+            for (int d = 0; d < 8; ++d) if (d < D) s[d] += R[(size_t)d * n + b0 + t] * vt;
+        }
+#pragma unroll
+        for (int d = 0; d < 8; ++d) {
+            double x = s[d];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[warp][d] = x;
+        }
+        __syncthreads();
+        if (tid < D) {
+            double x = 0.0;
+            for (int q = 0; q < kEigThreads / 32; ++q) x += red[q][tid];
+            sums[tid] = tau * x;
+        }
+        __syncthreads();
+        for (int t = tid; t < m; t += kEigThreads) {
+            const double vt = v[t];
+            for (int d = 0; d < D; ++d) R[(size_t)d * n + b0 + t] -= sums[d] * vt;
+        }
+        __syncthreads();
+    }
+}
+
+// number of eigenvalues of T strictly below x (negative pivots of the LDL^T of T - x I)
+__device__ inline int sturm_count(const double *d, const double *e2, int n, double x, double pivmin) {
+    int c = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    c += (q < 0.0);
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - e2[i - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        c += (q < 0.0);
+    }
+    return c;
+}
+
+// ------------------------------------------------------------------ K4c
+// One thread per eigenvalue index of every matrix; row_first maps a global index
+// to its matrix.  e2 (squared off-diagonals) is formed by the first thread of each
+// matrix into the tau array's slot, which k_qrows has consumed.
+__global__ void k_bisect_prep(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) J.tau[i] = (i + 1 < J.n) ? J.e[i] * J.e[i] : 0.0;
+}
+
+__global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DyJob J = jobs[lo];
+    const int k = (int)(g - row_first[lo]), n = J.n;
+    const double *d = J.d, *e = J.e, *e2 = J.tau;
+    // Gershgorin interval
+    double glo = d[0] - fabs(e[0]), ghi = d[0] + fabs(e[0]), tnorm = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+        glo = fmin(glo, d[i] - r); ghi = fmax(ghi, d[i] + r);
+    }
+    tnorm = fmax(fabs(glo), fabs(ghi));
+    const double eps = 2.220446049250313e-16;
+    const double pivmin = fmax(tnorm * 1e-300, 1e-290);
+    double a = glo - 2.0 * eps * tnorm - 1e-300, b = ghi + 2.0 * eps * tnorm + 1e-300;
+    // W_k is the unique x with count(x) <= k < count(x + 0)
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (a + b);
+        if (b - a <= 2.0 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid == a || mid == b) break;
+        if (sturm_count(d, e2, n, mid, pivmin) > k) b = mid; else a = mid;
+    }
+    J.sol[(size_t)k * (2 + J.D)] = 0.5 * (a + b);   // eigenvalue parked in the W slot, ascending
+}
+
+// ------------------------------------------------------------------ K4d
+// Inverse iteration, one thread per eigenvalue.  Eigenvalues closer than
+// ortol = 1e-6 |T| to their predecessor belong to the same cluster; inside a
+// cluster the shifts are kept at least pertol apart (the shift rule of LAPACK's
+// dstein) and every member starts from its own pseudo-random vector, so the
+// members span the cluster's invariant subspace; k_cluster_orth then makes them
+// orthonormal.  Y (the n x n region of A, column k at stride n) receives y_k; the
+// LU factors live in the job's work buffer, columns at stride n.
+__device__ inline unsigned hash32(unsigned x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+struct EigTol { double onenrm, ortol, pertol; };
+
+__device__ inline EigTol eig_tol(const double *d, const double *e, int n) {
+    double onenrm = 0.0;
+    for (int i = 0; i < n; ++i)
+        onenrm = fmax(onenrm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
+    EigTol t;
+    t.onenrm = onenrm;
+    t.ortol = 1e-6 * onenrm;
+    t.pertol = 10.0 * 2.220446049250313e-16 * fmax(onenrm, 1e-300);
+    return t;
+}
+
+__global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first, long long total, double *work,
+                        const long long *work_first) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DyJob J = jobs[lo];
+    const int k = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D;
+    const double *d = J.d, *e = J.e;
+    const EigTol tl = eig_tol(d, e, n);
+    auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
+    // shift: walk to the start of the cluster, then apply the separation rule forward
+    int k0 = k;
+    while (k0 > 0 && W(k0) - W(k0 - 1) <= tl.ortol) --k0;
+    double x = W(k0);
+    for (int q = k0 + 1; q <= k; ++q) x = fmax(W(q), x + tl.pertol);
+    double *Y = J.A;
+    double *wk = work + work_first[lo];   // 5 arrays of n*n: super, super-super, diagonal, multipliers, interchanges
+    double *U1 = wk, *U2 = wk + (size_t)n * n, *DD = wk + 2 * (size_t)n * n, *LL = wk + 3 * (size_t)n * n,
+           *PV = wk + 4 * (size_t)n * n;
+    // LU with partial pivoting of T - x I; rows i and i+1 may swap (PV = 1)
+    for (int i = 0; i < n; ++i) {
+        DD[(size_t)i * n + k] = d[i] - x;
+        U1[(size_t)i * n + k] = (i + 1 < n) ? e[i] : 0.0;
+        LL[(size_t)i * n + k] = (i + 1 < n) ? e[i] : 0.0;
+        U2[(size_t)i * n + k] = 0.0;
+    }
+    for (int i = 0; i + 1 < n; ++i) {
+        const double di = DD[(size_t)i * n + k], li = LL[(size_t)i * n + k];
+        if (fabs(di) >= fabs(li)) {
+            PV[(size_t)i * n + k] = 0.0;
+            const double f = (di != 0.0) ? li / di : 0.0;
+            LL[(size_t)i * n + k] = f;
+            DD[(size_t)(i + 1) * n + k] -= f * U1[(size_t)i * n + k];
+        } else {
+            PV[(size_t)i * n + k] = 1.0;
+            const double f = di / li;
+            DD[(size_t)i * n + k] = li;
+            LL[(size_t)i * n + k] = f;
+            const double t = U1[(size_t)i * n + k];
+            U1[(size_t)i * n + k] = DD[(size_t)(i + 1) * n + k];
+            DD[(size_t)(i + 1) * n + k] = t - f * DD[(size_t)(i + 1) * n + k];
+            if (i + 2 < n) {
+                U2[(size_t)i * n + k] = U1[(size_t)(i + 1) * n + k];
+                U1[(size_t)(i + 1) * n + k] = -f * U1[(size_t)(i + 1) * n + k];
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        if (fabs(DD[(size_t)i * n + k]) < tl.pertol) DD[(size_t)i * n + k] = (DD[(size_t)i * n + k] < 0 ? -tl.pertol : tl.pertol);
+    for (int i = 0; i < n; ++i)
+        Y[(size_t)i * n + k] = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
+    for (int it = 0; it < 3; ++it) {
+        for (int i = 0; i + 1 < n; ++i) {   // L^-1 with the interchanges
+            double bi = Y[(size_t)i * n + k], bi1 = Y[(size_t)(i + 1) * n + k];
+            const double f = LL[(size_t)i * n + k];
+            if (PV[(size_t)i * n + k] == 0.0) bi1 -= f * bi;
+            else { const double t = bi; bi = bi1; bi1 = t - f * bi1; }
+            Y[(size_t)i * n + k] = bi; Y[(size_t)(i + 1) * n + k] = bi1;
+        }
+        double y1 = 0.0, y2 = 0.0, nrm = 0.0;
+        for (int i = n - 1; i >= 0; --i) {   // U y = b, two superdiagonals
+            double v = Y[(size_t)i * n + k];
+            if (i + 1 < n) v -= U1[(size_t)i * n + k] * y1;
+            if (i + 2 < n) v -= U2[(size_t)i * n + k] * y2;
+            v /= DD[(size_t)i * n + k];
+            Y[(size_t)i * n + k] = v;
+            y2 = y1; y1 = v;
+            nrm = fmax(nrm, fabs(v));
+        }
+        const double sc = (nrm > 0.0) ? 1.0 / nrm : 1.0;
+        double s2 = 0.0;
+        for (int i = 0; i < n; ++i) { const double v = Y[(size_t)i * n + k] * sc; Y[(size_t)i * n + k] = v; s2 += v * v; }
+        const double inv = (s2 > 0.0) ? 1.0 / sqrt(s2) : 0.0;
+        for (int i = 0; i < n; ++i) Y[(size_t)i * n + k] *= inv;
+    }
+}
+
+// One CTA per eigenvalue index; the CTA of a cluster's first member (cluster of
+// two or more) orthonormalises the members with two classical Gram-Schmidt sweeps.
+__global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs, int njobs, const long long *row_first,
+                                                               long long total) {
+    const long long g = blockIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DyJob J = jobs[lo];
+    const int k0 = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31,
+              warp = tid >> 5;
+    __shared__ EigTol tl;
+    __shared__ double cbuf[1024];
+    __shared__ double red[kEigThreads / 32];
+    if (tid == 0) tl = eig_tol(J.d, J.e, n);
+    __syncthreads();
+    auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
+    if (k0 > 0 && W(k0) - W(k0 - 1) <= tl.ortol) return;
+    int k1 = k0 + 1;
+    while (k1 < n && W(k1) - W(k1 - 1) <= tl.ortol) ++k1;
+    if (k1 - k0 < 2) return;
+    double *Y = J.A;
+    for (int q = k0; q < k1; ++q) {
+        for (int sweep = 0; sweep < 2; ++sweep) {
+            // c_p = <y_p, y_q> for the earlier members, blocks of 1024
+            for (int p0 = k0; p0 < q; p0 += 1024) {
+                const int p1 = min(q, p0 + 1024);
+                for (int p = p0 + warp; p < p1; p += kEigThreads / 32) {
+                    double s = 0.0;
+                    for (int i = lane; i < n; i += 32) s += Y[(size_t)i * n + p] * Y[(size_t)i * n + q];
+                    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                    if (lane == 0) cbuf[p - p0] = s;
+                }
+                __syncthreads();
+                for (int i = tid; i < n; i += kEigThreads) {
+                    double acc = 0.0;
+                    for (int p = p0; p < p1; ++p) acc += cbuf[p - p0] * Y[(size_t)i * n + p];
+                    Y[(size_t)i * n + q] -= acc;
+                }
+                __syncthreads();
+            }
+        }
+        double s = 0.0;
+        for (int i = tid; i < n; i += kEigThreads) s += Y[(size_t)i * n + q] * Y[(size_t)i * n + q];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[warp] = s;
+        __syncthreads();
+        double tot = 0.0;
+        for (int w = 0; w < kEigThreads / 32; ++w) tot += red[w];
+        const double inv = (tot > 0.0) ? 1.0 / sqrt(tot) : 0.0;
+        for (int i = tid; i < n; i += kEigThreads) Y[(size_t)i * n + q] *= inv;
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ K5
+__global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first, long long total) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const DyJob J = jobs[lo];
+    const int k = (int)(g - row_first[lo]), n = J.n, D = J.D, NS = 2 + D;
+    double x[8];
+#pragma unroll
+    for (int dd = 0; dd < 8; ++dd) x[dd] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double y = J.A[(size_t)i * n + k];
+#pragma unroll
+        for (int dd = 0; dd < 8; ++dd) if (dd < D) x[dd] += J.R[(size_t)dd * n + i] * y;
+    }
+    // rows [W, Z, x] staged behind R in ascending W; k_place orders them
+    double z = 0.0;
+    for (int dd = 0; dd < D; ++dd) z += x[dd] * x[dd];
+    double *st = J.R + (size_t)D * n + (size_t)k * NS;
+    st[0] = J.sol[(size_t)k * NS];
+    st[1] = z;
+    for (int dd = 0; dd < D; ++dd) st[2 + dd] = x[dd];
+}
+
+// Places the staged rows: quasiparticles (W > E_F) then quasiholes, each by
+// descending W, and forms the Koltun partial sums.  One CTA per matrix.
+__global__ void k_place(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.n, D = J.D, NS = 2 + D;
+    const double *st = J.R + (size_t)D * n;
+    __shared__ int nbelow;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int k = 0; k < n; ++k) c += !(st[(size_t)k * NS] > J.efermi);
+        nbelow = c;
+    }
+    __syncthreads();
+    const int nqh = nbelow, nqp = n - nbelow;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int row = (k >= nqh) ? (n - 1 - k) : (nqp + (nqh - 1 - k));
+        for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        J.nq[0] = nqp; J.nq[1] = nqh;
+        double a1 = 0, a2 = 0, a3 = 0, b1 = 0, b2 = 0, b3 = 0, c1 = 0, c2 = 0, c3 = 0;
+        for (int ne = nqh - 1; ne >= 0; --ne) {
+            const double *p1 = J.sol + (size_t)(nqp + ne) * NS, *x = p1 + 2;
+            double x1 = 0.0, x2 = 0.0;
+            for (int r = 0; r < D; ++r) {
+                x1 += x[r] * x[r];
+                for (int c = 0; c < D; ++c) x2 += J.sig1b[r * D + c] * x[r] * x[c];
+            }
+            if (x1 > 0.01) { a1 += x2; b1 += x1 * p1[0]; c1 += x1; }
+            else if (x1 > 1.e-5) { a2 += x2; b2 += x1 * p1[0]; c2 += x1; }
+            else { a3 += x2; b3 += x1 * p1[0]; c3 += x1; }
+        }
+        const double xj = (double)J.j2 + 1.0;
+        J.koltun[0] = (a1 + a2 + a3) * xj;
+        J.koltun[1] = (b1 + b2 + b3) * xj;
+        J.koltun[2] = (c1 + c2 + c3) * xj;
+    }
+}
+
+cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
+                       double *work, const long long *d_work_first, cudaStream_t st) {
+    k_qrows<<<njobs, kEigThreads, 0, st>>>(d_jobs, njobs);
+    k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs);
+    const unsigned nb = (unsigned)((total_rows + 127) / 128);
+    k_bisect<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_invit<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
+    k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_post<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_place<<<njobs, 256, 0, st>>>(d_jobs, njobs);
+    return cudaGetLastError();
+}
+
+}  // namespace bd

@@ -1,0 +1,198 @@
+// k_sigma2.cu -- K0/K1: V' gather and 2p1h / 2h1p coupling build of the
+// second-order self-energy, plus the static (extended Hartree-Fock) term.
+//
+// Restates Wide_self_energy_t::Build_Dynamic_SlfEn_2ndOrder
+// (source/BcDor-Self_energy_ext_Op_c.cpp:323-561) and
+// SpProp_t::ExtendedHartreeFock_Pot (source/BcDor-Sp_Propagator_a.cpp:39-130).
+// Every floating-point operation uses an explicit round-to-nearest intrinsic in
+// the reference's order, so no multiply-add is contracted and the rows are
+// bit-identical to the reference's x86-64 build.
+#include "bd_common.cuh"
+#include "bd_kernels.h"
+
+namespace bd {
+
+__device__ inline int find_block(const long long *first, int nblk, long long g) {
+    int lo = 0, hi = nblk - 1;
+    while (lo < hi) {  // largest b with first[b] <= g
+        int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// K0: V'[d][alpha][beta][gamma] = sqrt((2Jab+1)/(2j_I+1)) * V^Jab_{ab,dg} (* sqrt2 if g == d),
+// source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One thread per coefficient.
+__global__ void k_vgather(DevProblem P, const S2Block *blk, const long long *vp_first, int nblk,
+                          long long g0, long long total, double *vp) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long g = g0 + idx;
+    int b = find_block(vp_first, nblk, g);
+    const S2Block B = blk[b];
+    int t = (int)(g - vp_first[b]);
+    const int I = B.ch;
+    const int na = P.no[B.ia], nb = P.no[B.ib], ng = P.no[B.ig];
+    int ngs = t % ng, r = t / ng;
+    int nbs = r % nb; r /= nb;
+    int nas = r % na; int d = r / na;
+    if (B.ia == B.ib && nbs < nas + B.nJab) return;
+    int iid = P.orb_start[I] + d, iig = P.orb_start[B.ig] + ngs;
+    if (iig == iid && B.nJgd) return;
+    int iia = P.orb_start[B.ia] + nas, iib = P.orb_start[B.ib] + nbs;
+    double x3 = __dsqrt_rn(__ddiv_rn((double)(B.Jab + B.Jab + 1), (double)(1 + P.j2[I])));
+    double v = __dmul_rn(x3, vget(P, iia, iib, iid, iig, B.Jab));
+    if (iig == iid) v = __dmul_rn(v, kSqr2);
+    vp[B.vp_first + t] = v;
+}
+
+// K1: one thread per pole.  dir 0 = 2p1h (forward), 1 = 2h1p (backward);
+// source/BcDor-Self_energy_ext_Op_c.cpp:425-481 and :484-539.
+__global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_first, int nblk, long long g0,
+                        long long total, const ChanSig *cs, int dir, const double *vp, double *E, double *S2,
+                        double *M) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long g = g0 + idx;
+    int b = find_block(pole_first, nblk, g);
+    const S2Block B = blk[b];
+    int t = (int)(g - pole_first[b]);
+    const int I = B.ch, NS = P.nspb;
+    const ChanSig C = cs[I];
+    const int *nA = dir == 0 ? P.np : P.nh, *nGv = dir == 0 ? P.nh : P.np;
+    const int *sA = dir == 0 ? P.p_start : P.h_start, *sG = dir == 0 ? P.h_start : P.p_start;
+    const double *eA = dir == 0 ? P.ep : P.eh, *eG = dir == 0 ? P.eh : P.ep;
+    const double *fA = dir == 0 ? P.fqp : P.fqh, *fG = dir == 0 ? P.fqh : P.fqp;
+    const int nG = nGv[B.ig];
+    int na, nbf, ngf = t % nG, q = t / nG;
+    if (B.ia == B.ib) {
+        const int nAa = nA[B.ia];
+        na = 0;
+        while (na < nAa && q >= nAa - na - B.nJab) { q -= nAa - na - B.nJab; ++na; }
+        if (na >= nAa) return;  // index outside the block: leave the row untouched
+        nbf = na + B.nJab + q;
+    } else {
+        const int nB = nA[B.ib];
+        na = q / nB; nbf = q % nB;
+    }
+    const double *fa = fA + (size_t)(sA[B.ia] + na) * NS;
+    const double *fb = fA + (size_t)(sA[B.ib] + nbf) * NS;
+    const double *fg = fG + (size_t)(sG[B.ig] + ngf) * NS;
+    const double e = __dsub_rn(__dadd_rn(eA[sA[B.ia] + na], eA[sA[B.ib] + nbf]), eG[sG[B.ig] + ngf]);
+    const double xJab = (double)(1 - 2 * B.nJab);
+    double x4 = 1.0;
+    if (B.ia == B.ib && na == nbf) x4 = __ddiv_rn(x4, kSqr2);
+    const int noa = P.no[B.ia], nob = P.no[B.ib], nog = P.no[B.ig], D = C.D;
+    const int iid0 = P.orb_start[I], iig0 = P.orb_start[B.ig];
+    const double *V = vp + B.vp_first;
+    double s2 = 0.0;
+    const int N = dir == 0 ? C.nfw : C.nbk;
+    const long long k = g - (dir == 0 ? C.fw_off : C.bk_off);
+    double *Mout = M + (dir == 0 ? C.mfw_off : C.mbk_off) + k;
+    for (int nd = 0; nd < D; ++nd) {
+        double x1 = 0.0;
+        const int iid = iid0 + nd;
+        for (int nas = 0; nas < noa; ++nas) {
+            const int nst2 = (B.ia == B.ib) ? nas + B.nJab : 0;
+            for (int nbs = nst2; nbs < nob; ++nbs) {
+                double x2 = __dmul_rn(fa[nas], fb[nbs]);
+                if (B.ia == B.ib) {
+                    x2 = __dadd_rn(x2, __dmul_rn(__dmul_rn(xJab, fa[nbs]), fb[nas]));
+                    if (nas == nbs) x2 = __ddiv_rn(x2, kSqr2);
+                }
+                const double *Vr = V + (((size_t)nd * noa + nas) * nob + nbs) * nog;
+                for (int ngs = 0; ngs < nog; ++ngs) {
+                    if (iig0 + ngs == iid && B.nJgd) continue;
+                    x1 = __dadd_rn(x1, __dmul_rn(__dmul_rn(Vr[ngs], x2), fg[ngs]));
+                }
+            }
+        }
+        x1 = __dmul_rn(x1, x4);
+        Mout[(size_t)nd * N] = x1;
+        s2 = __dadd_rn(s2, __dmul_rn(x1, x1));
+    }
+    E[g] = e;
+    S2[g] = s2;
+}
+
+// Static self-energy: one CTA per (channel, nr >= nc) entry; thread c computes
+// the (iv, J2) partial x1*x7 in the reference's inner order, thread 0 adds the
+// partials in the reference's (iv, J2) order.
+__global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long long *out_off, double *out) {
+    __shared__ double part[2048];
+    __shared__ int ncomb;
+    const int e = blockIdx.x;
+    if (e >= nent) return;
+    const int I = entries[e].x, nr = entries[e].y, nc = entries[e].z;
+    const int D = P.no[I], NS = P.nspb;
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int iv = 0; iv < P.nsubsh; ++iv) c += (P.j2[I] + P.j2[iv] - abs(P.j2[I] - P.j2[iv])) / 2 + 1;
+        ncomb = c;
+    }
+    __syncthreads();
+    if (ncomb > 2048) return;
+    for (int c = threadIdx.x; c < ncomb; c += blockDim.x) {
+        int iv = 0, cc = c, nJ2 = 0;
+        for (; iv < P.nsubsh; ++iv) {
+            nJ2 = (P.j2[I] + P.j2[iv] - abs(P.j2[I] - P.j2[iv])) / 2 + 1;
+            if (cc < nJ2) break;
+            cc -= nJ2;
+        }
+        const int J2 = abs(P.j2[I] - P.j2[iv]) + 2 * cc;
+        const int nJ = ((P.j2[I] + P.j2[iv] + J2) / 2) % 2;
+        const double x1 = __ddiv_rn((double)(J2 + 1), (double)(P.j2[I] + 1));
+        double x7 = 0.0;
+        for (int nm = 0; nm < P.no[iv]; nm++) {
+            if (iv == I && nm == nr && nJ != 1) continue;
+            const double x2 = (iv == I && nm == nr) ? kSqr2 : 1.0;
+            const int ia = P.orb_start[I] + nr, im = P.orb_start[iv] + nm;
+            for (int nv = 0; nv < P.no[iv]; nv++) {
+                if (iv == I && nv == nc && nJ != 1) continue;
+                const double x3 = (iv == I && nv == nc) ? kSqr2 : 1.0;
+                const int ib = P.orb_start[I] + nc, iu = P.orb_start[iv] + nv;
+                double x6 = 0.0;
+                const double *q = P.fqh + (size_t)P.h_start[iv] * NS;
+                for (int kg = 0; kg < P.nh[iv]; ++kg) { x6 = __dadd_rn(x6, __dmul_rn(q[nv], q[nm])); q += NS; }
+                x7 = __dadd_rn(x7, __dmul_rn(__dmul_rn(__dmul_rn(x2, x3), x6), vget(P, ia, im, ib, iu, J2 / 2)));
+            }
+        }
+        part[c] = __dmul_rn(x1, x7);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double u = 0.0;
+        for (int c = 0; c < ncomb; ++c) u = __dadd_rn(u, part[c]);
+        double *U = out + out_off[I];
+        U[nr * D + nc] = u;
+        U[nc * D + nr] = u;
+    }
+}
+
+// Gather rows in a given order into separate SoA arrays (used after the sort).
+__global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
+                              const double *Ein, const double *Min, double *Eout, double *Mout) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const long long g = n0 + idx;
+    const int ch = seg_of[g];
+    const ChanSig C = cs[ch];
+    const long long off = dir == 0 ? C.fw_off : C.bk_off;
+    const long long moff = dir == 0 ? C.mfw_off : C.mbk_off;
+    const int N = dir == 0 ? C.nfw : C.nbk;
+    const long long k = g - off;
+    const long long src = perm[g];  // global source index (same segment)
+    Eout[g] = Ein[src];
+    for (int d = 0; d < C.D; ++d) Mout[moff + (long long)d * N + k] = Min[moff + (long long)d * N + (src - off)];
+}
+
+// AoS rows [E, S2, M_0..] of one channel, for host copies in the reference layout.
+__global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double *r = rows + (size_t)k * (2 + D);
+    r[0] = E[k]; r[1] = S2[k];
+    for (int d = 0; d < D; ++d) r[2 + d] = M[(size_t)d * N + k];
+}
+
+}  // namespace bd

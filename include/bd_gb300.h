@@ -1,0 +1,163 @@
+/*
+ * bd_gb300.h -- C ABI of the GB300 (sm_103a) implementation of BoccaDorata's
+ *               second-order self-energy -> Lanczos -> Dyson chain.
+ *
+ * All functions return BD_OK (0) or a negative status; none of them exits the
+ * process.  Buffers are caller-owned host memory; sizes are element counts.
+ * A context (bd_ctx) owns one CUDA device, one stream and the device-resident
+ * copies of the inputs.  Calls on one context are not thread-safe; use one
+ * context per host thread.
+ *
+ * Reference interfaces replaced (paths inside craolus/BoccaDorata-public):
+ *   bd_count_poles     Wide_self_energy_t::Count_2p1h_2h1p_poles
+ *                      source/BcDor-SlfEn_classes.hh:83, source/BcDor-Self_energy_ext_Op_c.cpp:35
+ *   bd_sigma2_build    Wide_self_energy_t::Build_Dynamic_SlfEn_2ndOrder
+ *                      source/BcDor-SlfEn_classes.hh:84, source/BcDor-Self_energy_ext_Op_c.cpp:323
+ *   bd_ehf             Wide_self_energy_t::Build_ExtendedHartreeFock -> SpProp_t::ExtendedHartreeFock_Pot
+ *                      source/BcDor-Self_energy_ext_Op_b.cpp:71, source/BcDor-Sp_Propagator_a.cpp:39
+ *   bd_lanczos_reduce  Wide_self_energy_t::Reduce_SelfEn_Lncz + Reduce_Mtx_Lncz
+ *                      source/BcDor-SlfEn_classes.hh:88, source/BcDor-Self_energy_ext_Op_e.cpp:55,
+ *                      source/BcDor-Run_vars.hh:193-195, source/BcDor-Lanczos.cpp:44
+ *   bd_dyson_solve     DysonMatrix (+ Calc_En, Seek_EFermi)
+ *   bd_dyson_rows      source/BcDor-Main.cpp:42, source/BcDor-DysonMatrix.cpp:123,542,619
+ *   bd_run_all         the per-channel loop of Run_itrs, source/BcDor-Main.cpp:241-391
+ */
+#ifndef BD_GB300_H
+#define BD_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BD_OK            0
+#define BD_ERR_ARG      -1   /* bad argument, size or index                      */
+#define BD_ERR_CUDA     -2   /* a CUDA runtime call failed (see bd_last_error)   */
+#define BD_ERR_CAPACITY -3   /* an output buffer is too small                    */
+#define BD_ERR_STATE    -4   /* call order: e.g. Dyson before any self-energy    */
+#define BD_ERR_NUMERIC  -5   /* eigensolver did not converge / non-finite input  */
+#define BD_ERR_TIMEOUT  -6   /* a bounded device wait gave up                    */
+
+/* run flags for bd_run_all */
+#define BD_RUN_LANCZOS   1   /* Lanczos-reduce Sigma(2) before Dyson (else full Dyson)  */
+#define BD_RUN_MIXED     2   /* FP32 Lanczos vectors / reorthogonalisation              */
+#define BD_RUN_PER_CHANNEL 4 /* launch channel by channel (the drop-in call pattern)   */
+
+typedef struct bd_ctx bd_ctx;
+
+/* Model space, ModSpace_t (source/BcDor-Sp_classes.hh:32-79).  Orbits are
+ * grouped by subshell in subshell order (MSp_n[ish] - Mor_n = first orbit). */
+typedef struct {
+    int nsubsh;            /* number of (l, j, parity, charge) subshells = channels */
+    int norb;              /* total number of orbits                                */
+    const int *l, *j2, *ip, *ch, *no;   /* per subshell: l, 2j, parity, charge, #orbits */
+    const int *orb_sh;     /* per orbit: subshell                                   */
+    const double *orb_xe;  /* per orbit: model-space xe column                      */
+} bd_modspace;
+
+/* Propagator, SpProp_t (source/BcDor-Sp_classes.hh:87-160): fragments listed
+ * subshell by subshell; amplitudes fragment-major with row stride nspb. */
+typedef struct {
+    int nspb;              /* N_SPB_MX = max orbits per subshell */
+    const int *np, *nh;    /* per subshell: quasiparticles, quasiholes */
+    const double *ep, *eh; /* energies */
+    const double *fqp, *fqh; /* amplitudes, rows of nspb */
+} bd_propagator;
+
+/* Interaction, VppInt_t after prepare_for_reading (source/BcDor-Int_classes.hh:20-85,
+ * source/BcDor-Vpp_potential.cpp:440-501): canonical keys (a<=b, c<=d, ab<=cd),
+ * key = (a*1024+b)*128+J, sorted by (charge, parity, J), iabJ, icdJ. */
+typedef struct {
+    int n_me;
+    const int *iabJ, *icdJ;
+    const double *V;
+} bd_interaction;
+
+/* Lanczos pivots as Make_LancPivots returns them (source/BcDor-Miscellanea.cpp:334-390):
+ * for subshell s, npvt[s] rows; iterations n_itr_fw/bk and D-vectors concatenated
+ * subshell by subshell. */
+typedef struct {
+    const int *npvt;
+    const int *n_itr_fw, *n_itr_bk;
+    const double *vec;
+} bd_pivots;
+
+int         bd_create(bd_ctx **ctx, int device);
+void        bd_destroy(bd_ctx *ctx);
+const char *bd_last_error(const bd_ctx *ctx);
+int         bd_version(void);
+
+/* Device-resident copies of the inputs (replaces the ModSpace_t / VppInt_t /
+ * SpProp_t objects the reference's calls read).  Must precede any other call. */
+int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp,
+                      const bd_propagator *prop);
+int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv);
+
+/* Pole counts of channel ish (all-poles branch, icut == 0). */
+int bd_count_poles(bd_ctx *ctx, int ish, int *n_fw, int *n_bk);
+
+/* Static self-energy of channel ish: D x D, row-major. */
+int bd_ehf(bd_ctx *ctx, int ish, double *sig_hf);
+
+/* Sigma(2) of channel ish, built on the device.  Rows of 2 + D doubles
+ * [E, sum_d M_d^2, M_0 .. M_{D-1}] in the reference's enumeration order are
+ * copied to sig_fw / sig_bk when those are non-NULL (capacities in rows).
+ * The device copy stays resident for bd_lanczos_reduce / bd_dyson_solve. */
+int bd_sigma2_build(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, int *n_fw,
+                    double *sig_bk, int cap_bk, int *n_bk);
+
+/* Lanczos reduction of the resident Sigma(2) of channel ish.
+ * pivots: n_pvt rows of D doubles, normalised in place (as the reference does);
+ * n_itr_fw / n_itr_bk: iterations per pivot, rescaled in place when they exceed
+ * the pole count (as the reference does).  Output rows have (n_pvt + 1) + D
+ * doubles [alpha, beta, g_0 .., m_0 .. m_{D-1}]; ipiv_* receive
+ * [n_used_pivots, 1, start_1, ...] and must hold n_pvt + 1 + D ints.
+ * flags: 0 = FP64, BD_RUN_MIXED = FP32 vectors. */
+int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_itr_fw, int *n_itr_bk,
+                      double *lz_fw, int cap_fw, int *L_fw, int *ipiv_fw,
+                      double *lz_bk, int cap_bk, int *L_bk, int *ipiv_bk, int flags);
+
+/* Dyson eigensolve of channel ish with the most recent resident self-energy
+ * (Lanczos-reduced if bd_lanczos_reduce was called after bd_sigma2_build).
+ * sig1b: one-body term (D x D); sig_hf: static self-energy (D x D, NULL = build
+ * it with bd_ehf); e_fermi: Fermi energy (NaN = Seek_EFermi on the input propagator).
+ * Solutions are rows of 2 + D doubles [W, Z, x_0 .. x_{D-1}], quasiparticles
+ * (W > E_F) and quasiholes each sorted by descending W, Z = sum x_d^2 as stored by
+ * SpProp_t::add_qp / add_qh.  koltun = {sum_qh x.S1b.x, sum_qh |x|^2 W, sum_qh |x|^2}
+ * times (2j+1), as Calc_En. */
+int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_hf, double e_fermi,
+                   double *sol_qp, int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh,
+                   double *koltun);
+
+/* DysonMatrix on a self-energy supplied by the caller (e.g. one loaded with
+ * Wide_self_energy_t::load_SelfEn_bin, the ExtSE path of source/BcDor-Main.cpp:350-356).
+ * Rows have nden + D doubles: nden = 2 for a plain Sigma(2) [E, *, M_0 ..], or
+ * n_pvt + 1 for Lanczos rows [alpha, beta, g_0 .., m_0 ..] with their i_piv array
+ * (ipiv_* = NULL marks plain rows).  Outputs as bd_dyson_solve. */
+int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_rows, const int *ipiv_fw,
+                  int n_bk, const double *bk_rows, const int *ipiv_bk, const double *sig1b, const double *sig_hf,
+                  double e_fermi, double *sol_qp, int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh,
+                  double *koltun);
+
+/* Copy of the Lanczos basis of the last reduction of channel ish (dir 0 forward,
+ * 1 backward) as L rows of N doubles; fp32 = 1 if it ran with BD_RUN_MIXED.  Used to
+ * check the basis' orthonormality. */
+int bd_lanczos_vectors(bd_ctx *ctx, int ish, int dir, int fp32, double *out, long long cap);
+
+/* Whole chain for every channel (flags BD_RUN_*), asynchronous on the context's
+ * stream; one-body term diag(orb_xe) (Trel=7 ExtU1=1).  bd_sync waits for it. */
+int bd_run_all(bd_ctx *ctx, int flags);
+int bd_sync(bd_ctx *ctx);
+
+/* Results of the last bd_run_all. */
+int bd_result_counts(bd_ctx *ctx, int ish, int *n_qp, int *n_qh);
+int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *sol_qh, int cap_qh,
+                    double *koltun);
+/* koltun[3 * nsubsh] for every channel with one copy. */
+int bd_result_koltun_all(bd_ctx *ctx, double *koltun);
+/* Device time of the phases of the last bd_run_all in ms: sigma2, sort, lanczos, dyson, total. */
+int bd_last_timings(bd_ctx *ctx, double *ms5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BD_GB300_H */
