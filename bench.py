@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Sigma(2) -> Lanczos -> Dyson chain.
+
+Default arm: ``python bench.py [--gpus N] [--steps K] [--warmup W]``
+  A step is the whole chain for every (l, j, parity, charge) channel of the N_max=10
+  workload (hw = 16 MeV, seed 2, 100 Lanczos iterations per pivot; 42 channels) in the
+  mixed-precision batched form (FP32 Lanczos vectors, FP64 elsewhere), with all inputs
+  resident in HBM.  ``value`` is channels solved per second over all ranks.  The same
+  run also times the plain FP64 forms, checks the mixed form against FP64, measures the
+  end-to-end rate through the C ABI with host buffers, and times the CPU oracle on a
+  bounded sample.  Multi-GPU (torchrun): every rank solves its own copy of the workload
+  (replicas; the channels share no data), rank 0 prints one JSON line.
+
+Reference arm: ``python bench.py --impl reference ...``
+  The reference's algorithm on the host cores: the C restatement in oracle/ (the
+  reference program itself is built only where its sources are mounted), channels
+  spread over all cores, single-pass Gram-Schmidt Lanczos and OpenBLAS dsyevd, as the
+  reference does.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "channels solved/s at N_max=10: mixed vs FP64 GPU at <=1 keV qp-energy error"
+WORKLOAD = "nmax10_lanczos100"
+CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2, 3, 5, 6
+# Per-launch DRAM traffic of the FP32 Lanczos kernel on this workload, from the ncu
+# capture summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum).
+LANCZOS_TRAFFIC_BYTES = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ------------------------------------------------------------------------------------------
+# shared helpers
+# ------------------------------------------------------------------------------------------
+def lanczos_sizes(ctx, prob):
+    """(N, L, n_pvt, D) of every Lanczos chain, with the sizing rules of Reduce_SelfEn_Lncz."""
+    out = []
+    for ish in range(prob.ms.nsubsh):
+        nfw, nbk = ctx.count_poles(ish)
+        D = int(prob.ms.no[ish])
+        for N, nit in ((nfw, prob.piv.n_fw[ish]), (nbk, prob.piv.n_bk[ish])):
+            tot = int(np.sum(nit[nit > 0]))
+            if N < 1 or tot < 1:
+                continue
+            if tot > N:
+                nit = np.array([int(N / tot * v + 1.0) for v in nit])
+            L = min(int(np.sum(nit[nit > 0])), N)
+            out.append((N, L, len(nit), D))
+    return out
+
+
+def lanczos_algorithmic_bytes(chains, w):
+    """Per-launch algorithmic HBM bytes of the Lanczos kernel: every step reads all
+    earlier vectors once for the dot products and once for the update (w*N*L^2 over a
+    chain), plus E, v and the g vectors (w*N*(4+n_pvt)*L) and the M, E streams
+    (8*N*(2+D)*L)."""
+    return float(sum(w * N * (L * L + (4 + npv) * L) + 8 * N * (2 + D) * L for N, L, npv, D in chains))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); mx = max(mx, float(r[2]))
+                for k, v in zip(names, r[5:9]):
+                    if v.strip() == "Active":
+                        reasons.add(k)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# CPU work (oracle) -- used for cpu_baseline and the reference arm only
+# ------------------------------------------------------------------------------------------
+_W = {}
+
+
+def _worker_init(workload):
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    synth = importlib.import_module("boccadorata-public_gb300.synth")
+    import oracle
+    prob = synth.make_workload(workload)
+    _W["prob"] = prob
+    _W["orc"] = oracle.Oracle().bind(prob)
+
+
+def _chain_channel(ish):
+    """The reference's three boundary calls for one channel; returns their wall time."""
+    orc, prob = _W["orc"], _W["prob"]
+    s1, sh = orc.sig1b(ish), orc.ehf(ish)
+    t0 = time.perf_counter()
+    fw, bk = orc.sigma2(ish)
+    pv = prob.piv
+    lz = orc.reduce_lanczos(ish, fw, bk, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish], 1)
+    orc.dyson(ish, s1, sh, lz["NDEN"], lz["lz_fw"], lz["lz_bk"], lz["n_piv_fw"], lz["ipiv_fw"], lz["n_piv_bk"],
+              lz["ipiv_bk"])
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(workload, sample):
+    env_before = os.environ.get("OPENBLAS_NUM_THREADS")
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    _worker_init(workload)
+    t = sum(_chain_channel(i) for i in sample)
+    if env_before is None:
+        os.environ.pop("OPENBLAS_NUM_THREADS", None)
+    return {"value": len(sample) / t, "unit": "channels/s", "cores": 1, "kind": "port",
+            "sample": f"channels {sample} of {workload} (D=1..6), Sigma(2) + single-pass Lanczos + dsyevd Dyson, "
+                      f"{t:.1f} s on 1 host core"}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    synth = importlib.import_module("boccadorata-public_gb300.synth")
+    nch = synth.make_modspace(synth.WORKLOADS[args.workload]["nmax"], 1.0).nsubsh
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    chans = list(range(nch))
+    # roughly most expensive first (low l within each charge) so the pool drains evenly
+    order = sorted(chans, key=lambda i: (i % (nch // 2), i))
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(args.workload,)) as pool:
+        pool.map(_chain_channel, [20] * cores)            # make sure every worker is initialised
+        times = []
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_chain_channel, order, chunksize=1)
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    value = nch / (ms / 1e3)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "channels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "channels": nch, "host_cores": cores},
+            "cpu_baseline": {"value": value, "unit": "channels/s", "cores": cores, "kind": "port",
+                             "sample": f"all {nch} channels of {args.workload} per step over {cores} processes; "
+                                       "oracle/ restatement of the reference chain (single-pass Lanczos, "
+                                       "OpenBLAS dsyevd), bit-identical to the reference on its fixtures"},
+            "e2e": {"value": value, "unit": "channels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def strong_errors(ref, got, zmin=1e-4):
+    """max |dW| (MeV) and max |dZ| over solutions with Z > zmin, nearest-energy match."""
+    dW = dZ = 0.0
+    for tag in ("qp", "qh"):
+        a, b = ref[tag], got[tag]
+        for r in a[a[:, 1] > zmin]:
+            k = np.argmin(np.abs(b[:, 0] - r[0]))
+            dW = max(dW, abs(b[k, 0] - r[0]))
+            win = 1e-5 * max(1.0, abs(r[0]))
+            dZ = max(dZ, abs(a[np.abs(a[:, 0] - r[0]) < win, 1].sum() - b[np.abs(b[:, 0] - r[0]) < win, 1].sum()))
+    return dW, dZ
+
+
+def pinned_problem(prob, torch):
+    """Copies of the problem's input arrays in page-locked host memory."""
+    import copy
+    q = copy.deepcopy(prob)
+
+    def pin(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.numpy()
+    q.vpp.iabJ, q.vpp.icdJ, q.vpp.V = pin(q.vpp.iabJ), pin(q.vpp.icdJ), pin(q.vpp.V)
+    q.prop.fqp, q.prop.fqh, q.prop.ep, q.prop.eh = pin(q.prop.fqp), pin(q.prop.fqh), pin(q.prop.ep), pin(q.prop.eh)
+    return q
+
+
+def gpu_arm(args):
+    rank, world, local = dist_env()
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    bd = importlib.import_module("boccadorata-public_gb300.bd")
+    synth = importlib.import_module("boccadorata-public_gb300.synth")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    prob = synth.make_workload(args.workload)
+    nch = prob.ms.nsubsh
+    ctx = bd.Context(local).upload(prob)
+
+    # ---- accuracy of the mixed form against FP64 (outside the timed region)
+    ctx.run_all(lanczos=True, mixed=False)
+    ref = [ctx.result(i) for i in range(nch)]
+    k64 = ctx.koltun_all()
+    ctx.run_all(lanczos=True, mixed=True)
+    got = [ctx.result(i) for i in range(nch)]
+    k32 = ctx.koltun_all()
+    dW = dZ = 0.0
+    for i in range(nch):
+        a, b = strong_errors(ref[i], got[i])
+        dW, dZ = max(dW, a), max(dZ, b)
+    e64 = float(((k64[:, 0] + k64[:, 1]) / 2).sum())
+    e32 = float(((k32[:, 0] + k32[:, 1]) / 2).sum())
+
+    def timed(flags_kw, steps, warmup):
+        for _ in range(warmup):
+            ctx.run_all(lanczos=True, **flags_kw)
+        barrier()
+        dev, lz = [], []
+        l0 = ctx.launch_count()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ctx.run_all(lanczos=True, **flags_kw)
+            dev.append(ctx.timings()["total"])
+            lz.append(ctx.lanczos_kernel_ms())
+        barrier()
+        wall = time.perf_counter() - t0
+        return statistics.mean(dev), wall / steps * 1e3, lz, ctx.launch_count() - l0
+
+    # ---- the headline: mixed-precision batched form
+    clocks = Clocks(local) if rank == 0 else None
+    dev_ms, wall_ms, lz_ms, launches = timed(dict(mixed=True), args.steps, args.warmup)
+    clk = clocks.stop() if clocks else None
+    step_s = max_over_ranks(dev_ms / 1e3)
+    value = world * nch / step_s
+
+    # ---- the plain FP64 forms
+    f64_ms, _, f64_lz, _ = timed(dict(mixed=False), max(2, min(args.steps, 3)), 1)
+    pc_ms, _, _, _ = timed(dict(mixed=False, per_channel=True), 1, 1)
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        pq = pinned_problem(prob, torch)
+        h2d = int(pq.vpp.iabJ.nbytes + pq.vpp.icdJ.nbytes + pq.vpp.V.nbytes + pq.prop.fqp.nbytes + pq.prop.fqh.nbytes
+                  + pq.prop.ep.nbytes + pq.prop.eh.nbytes + sum(np.asarray(v).nbytes for v in pq.piv.vec))
+        ctx2 = bd.Context(local)
+        times = []
+        d2h = 0
+        for step in range(1 + max(2, min(args.steps, 3))):
+            barrier()
+            t0 = time.perf_counter()
+            ctx2.upload(pq)
+            ctx2.run_all(lanczos=True, mixed=True)
+            res = [ctx2.result(i) for i in range(nch)]
+            barrier()
+            dt = time.perf_counter() - t0
+            d2h = int(sum(r["qp"].nbytes + r["qh"].nbytes + r["koltun"].nbytes for r in res))
+            if step > 0:
+                times.append(dt)
+        ctx2.close()
+        e2e_s = max_over_ranks(statistics.mean(times))
+        e2e = {"value": world * nch / e2e_s, "unit": "channels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": 1e3 * e2e_s}
+
+    if rank != 0:
+        ctx.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    chains = lanczos_sizes(ctx, prob)
+    alg = lanczos_algorithmic_bytes(chains, 4)
+    lz_mean = statistics.mean(lz_ms)
+    peak, src = measured_peaks()
+    achieved = alg / (lz_mean / 1e3) / 1e9
+    roof = {"kernel": "k_lanczos<float> (FP32 vectors, all 84 chains in one launch)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s",
+            "traffic": LANCZOS_TRAFFIC_BYTES, "algorithmic_bytes": alg, "kernel_ms": lz_mean}
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.workload, CPU_SAMPLE)
+    line = {
+        "metric": METRIC, "value": value, "unit": "channels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator in the reference's formats)",
+        "config": {"workload": args.workload, "nmax": 10, "hw": 16.0, "seed": 2, "lanczos_iterations_per_pivot": 100,
+                   "channels": nch, "form": "mixed precision (FP32 Lanczos vectors), all channels batched",
+                   "l2": "inputs larger than L2 (293 MB interaction, ~0.9 GB Lanczos basis); no flush",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "gpu_launches": launches,
+        "forms": {"mixed_batched_ms": dev_ms, "mixed_batched_wall_ms": wall_ms,
+                  "fp64_batched_ms": f64_ms, "fp64_batched_channels_per_s": nch / (f64_ms / 1e3),
+                  "fp64_per_channel_ms": pc_ms, "fp64_per_channel_channels_per_s": nch / (pc_ms / 1e3),
+                  "fp64_lanczos_kernel_ms": statistics.mean(f64_lz),
+                  "speedup_mixed_vs_fp64_per_channel": pc_ms / dev_ms, "speedup_mixed_vs_fp64_batched": f64_ms / dev_ms},
+        "accuracy": {"max_qp_energy_error_keV": dW * 1e3, "max_spectroscopic_factor_error": dZ,
+                     "koltun_energy_fp64": e64, "koltun_energy_mixed": e32,
+                     "koltun_rel_error": abs(e32 - e64) / abs(e64)},
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -86,6 +86,8 @@ def load_library(path: str = LIB_PATH):
     lib.bd_last_timings.argtypes = [vp, _dp]
     lib.bd_diag_two_pass.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+    lib.bd_lanczos_kernel_ms.argtypes = [vp]; lib.bd_lanczos_kernel_ms.restype = C.c_double
+    lib.bd_launch_count.argtypes = [vp]; lib.bd_launch_count.restype = C.c_longlong
     return lib
 
 
@@ -272,6 +274,12 @@ class Context:
 
     def two_pass_steps(self):
         return int(self.lib.bd_diag_two_pass(self.h))
+
+    def lanczos_kernel_ms(self):
+        return float(self.lib.bd_lanczos_kernel_ms(self.h))
+
+    def launch_count(self):
+        return int(self.lib.bd_launch_count(self.h))
 
     def koltun_all(self):
         k = np.zeros(3 * self.prob.ms.nsubsh)

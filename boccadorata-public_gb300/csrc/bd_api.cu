@@ -32,6 +32,7 @@ struct DevBuf {
 };
 
 enum ChanState { ST_NONE = 0, ST_SIGMA = 1, ST_LANCZOS = 2 };
+constexpr int kDysonKernels = 9;   // assemble, tridiag, qrows, bisect_prep, bisect, invit, cluster_orth, post, place
 
 struct ChainPlan {     // one Lanczos direction of one channel
     int N = 0, L = 0, n_used = 0, nden_out = 0, n_pvt = 0;
@@ -60,6 +61,10 @@ struct bd_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[6] = {};
+    cudaEvent_t ev_lz[2] = {};
+    bool lz_timed = false;
+    double lz_kernel_ms = 0.0;
+    long long launches = 0;   // kernels of this library launched since creation
     std::string err;
     bool uploaded = false, have_pivots = false;
     int lz_cluster = 8, dy_cluster = 8;
@@ -293,6 +298,7 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
                                                                         ctx->d_blk_vp_first + b0, nb, vp0, nvp,
                                                                         ctx->d_vp);
         CU(cudaGetLastError());
+        ctx->launches += 1;
     }
     const long long f0 = A.fw_off, nf = Z.fw_off + Z.nfw - f0;
     if (nf > 0) {
@@ -300,6 +306,7 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
                                                                      ctx->d_blk_fw_first + b0, nb, f0, nf, ctx->d_cs,
                                                                      0, ctx->d_vp, ctx->d_Efw, ctx->d_S2fw, ctx->d_Mfw);
         CU(cudaGetLastError());
+        ctx->launches += 1;
     }
     const long long k0 = A.bk_off, nk = Z.bk_off + Z.nbk - k0;
     if (nk > 0) {
@@ -307,6 +314,7 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
                                                                      ctx->d_blk_bk_first + b0, nb, k0, nk, ctx->d_cs,
                                                                      1, ctx->d_vp, ctx->d_Ebk, ctx->d_S2bk, ctx->d_Mbk);
         CU(cudaGetLastError());
+        ctx->launches += 1;
     }
     return BD_OK;
 }
@@ -323,6 +331,7 @@ int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
     if (e1 > e0) {
         k_ehf<<<e1 - e0, 128, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries + e0, e1 - e0, ctx->d_dd_off, ctx->d_sighf);
         CU(cudaGetLastError());
+        ctx->launches += 1;
     }
     return BD_OK;
 }
@@ -360,6 +369,7 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
             perm, n0, n, dir == 0 ? ctx->d_seg_fw : ctx->d_seg_bk, ctx->d_cs, dir, E, dir == 0 ? ctx->d_Mfw : ctx->d_Mbk,
             dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s, dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s);
         CU(cudaGetLastError());
+        ctx->launches += 1;
     }
     return BD_OK;
 }
@@ -406,7 +416,11 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     // chain descriptors live in a small device array (one slot per chain of the range)
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
     CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
+    CU(cudaEventRecord(ctx->ev_lz[0], ctx->st));
     CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, ctx->lz_cluster, ctx->eta, ctx->st));
+    CU(cudaEventRecord(ctx->ev_lz[1], ctx->st));
+    ctx->lz_timed = true;
+    ctx->launches += 1;
     return BD_OK;
 }
 
@@ -516,6 +530,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
                        cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(ctx->d_jobs + ch_lo, (int)jobs.size(), ctx->d_row_first + ch_lo, rows, nmax, Dmax,
                     ctx->dy_cluster, ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
+    ctx->launches += kDysonKernels;
     return BD_OK;
 }
 
@@ -589,6 +604,7 @@ int bd_create(bd_ctx **out, int device) {
         return BD_ERR_CUDA;
     }
     for (auto &e : ctx->ev) cudaEventCreate(&e);
+    for (auto &e : ctx->ev_lz) cudaEventCreate(&e);
     *out = ctx;
     return BD_OK;
 }
@@ -603,6 +619,7 @@ void bd_destroy(bd_ctx *ctx) {
     if (ctx->d_dyR) cudaFree(ctx->d_dyR);
     if (ctx->d_dywork) cudaFree(ctx->d_dywork);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -1020,6 +1037,7 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     CU(cudaMemcpyAsync(dwf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(cudaMemcpyAsync(drf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(dj, 1, drf, n, n, D, ctx->dy_cluster, dwork, dwf, ctx->st));
+    ctx->launches += kDysonKernels;
     int nq[2] = {0, 0};
     double kol[3];
     CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof nq, cudaMemcpyDeviceToHost, ctx->st));
@@ -1076,6 +1094,7 @@ int bd_run_all(bd_ctx *ctx, int flags) {
     const int ns = ctx->nsubsh;
     int rc;
     ctx->results_valid = false;
+    ctx->lz_timed = false;
     if ((rc = ensure_dyson(ctx, lanczos))) return rc;
     if (ctx->d_lzstat) CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
     CU(cudaEventRecord(ctx->ev[0], ctx->st));
@@ -1122,6 +1141,12 @@ int bd_sync(bd_ctx *ctx) {
         ctx->timings[4] = ms[0] + ms[1] + ms[2] + ms[3];
         ctx->lz_two_pass = 0;
         if (ctx->d_lzstat) CU(cudaMemcpy(&ctx->lz_two_pass, ctx->d_lzstat, sizeof(int), cudaMemcpyDeviceToHost));
+        ctx->lz_kernel_ms = 0.0;
+        if (ctx->lz_timed) {
+            float m = 0.f;
+            CU(cudaEventElapsedTime(&m, ctx->ev_lz[0], ctx->ev_lz[1]));
+            ctx->lz_kernel_ms = m;
+        }
         for (int I = 0; I < ctx->nsubsh; ++I)
             if (st[I]) {
                 ctx->results_valid = false;
@@ -1174,6 +1199,8 @@ int bd_last_timings(bd_ctx *ctx, double *ms5) {
 /* Not part of the public header: number of Lanczos steps that took a second
  * reorthogonalisation sweep in the last bd_run_all, and tuning knobs. */
 int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
+double bd_lanczos_kernel_ms(bd_ctx *ctx) { return ctx ? ctx->lz_kernel_ms : -1.0; }
+long long bd_launch_count(bd_ctx *ctx) { return ctx ? ctx->launches : -1; }
 int bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta) {
     if (!ctx) return BD_ERR_ARG;
     if (lz_cluster != 1 && lz_cluster != 2 && lz_cluster != 4 && lz_cluster != 8 && lz_cluster != 16)

@@ -20,10 +20,24 @@
 // and the iterated sweeps keep |V^T V - I| at 1e-15 and reproduce the un-reduced
 // Dyson solution.
 //
+// Exhausted subspace: when even the iterated sweeps leave nothing (the squared norm
+// falls below tau times its value before the first sweep, tau = 1e-48 in FP64 and
+// 1e-22 with FP32 vectors, or is exactly zero), the subspace the chain can reach is
+// spanned.  The reference then divides by beta ~ 0 and its rows become NaN.  Here the
+// chain continues with the unit vector of the first pole that no stored vector
+// touches (exact zeros: diag(E) and the projections never grow a vector's support),
+// an exact eigenvector of diag(E) orthogonal to the basis (alpha = E_k, beta = 0,
+// g = 0, m = M[k, :]); if every pole is touched, with a pseudo-random vector swept
+// orthogonal to the basis (beta = 0, alpha / g / m computed as usual).  Either way the
+// kept rows remain the exact projection: with full reorthogonalisation E v_t lies in
+// the span of v_0 .. v_{t+1}, so a vector orthogonal to the basis couples by E only
+// to the last vector of each earlier pivot chain, which is what g records.
+//
 // Work split: one thread-block cluster per chain; CTA r of the cluster owns the
 // pole rows [r*S, (r+1)*S) of every vector.  Partial sums are combined through
 // distributed shared memory; every CTA adds the peers' partials in rank order,
 // so all CTAs hold bit-identical totals and take identical branches.
+#include <climits>
 #include <cooperative_groups.h>
 #include "bd_common.cuh"
 #include "bd_kernels.h"
@@ -40,6 +54,13 @@ __device__ inline double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+// Deterministic pseudo-random restart value of pole i at Lanczos index j, in [0.5, 1.5).
+__host__ __device__ inline double restart_value(int i, int j) {
+    unsigned x = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return 0.5 + (double)(x & 0xffffffu) / 16777216.0;
 }
 
 constexpr int kLzThreads = 256;
@@ -72,10 +93,13 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
     double *B = A + rmax;
     double *c = B + kMaxScal;
     double *red = c + rmax;
+    unsigned char *touched = reinterpret_cast<unsigned char *>(red + kLzWarps * kMaxScal);
     __shared__ double tot[kMaxScal];
+    __shared__ int s_kmin;
 
     VT *V = reinterpret_cast<VT *>(C.V);
-    for (int i = tid; i < ns; i += kLzThreads) Es[i] = C.E[i0 + i];
+    for (int i = tid; i < ns; i += kLzThreads) { Es[i] = C.E[i0 + i]; touched[i] = 0; }
+    const double tau = (sizeof(VT) == 4) ? 1e-22 : 1e-48;
 
     int k = -1;           // current pivot chain
     int two_pass = 0;
@@ -95,7 +119,11 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
             const VT *vp = V + (size_t)(j - 1) * C.ld + i0;
             for (int i = tid; i < ns; i += kLzThreads) w[i] = (double)vp[i] * Es[i];
         }
+        bool injected = false;     // w replaced by a pseudo-random restart vector
+        bool done = false;         // step finished by an untouched-pole unit vector
+        for (int attempt = 0; attempt < 2 && !done; ++attempt) {
         int pass = 0;
+        double wn2_first = 0.0;
         for (;;) {
             __syncthreads();
             for (int i = tid; i < ns; i += kLzThreads) wc[i] = (CT)w[i];
@@ -129,6 +157,7 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
             }
             __syncthreads();
             const double wn2_before = c[j];
+            if (pass == 0) wn2_first = wn2_before;
             // (b3) w -= sum_t c_t v_t, then partial alpha / beta / m / g sums of the new w
             const int nq = k;  // earlier pivots
             const int nsc = 2 + D + nq;
@@ -172,16 +201,59 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
             if (j > 0 && pass < 3 && tot[1] < eta2 * wn2_before) { ++pass; ++two_pass; continue; }
             break;
         }
+        if (attempt > 0 || !(tot[1] <= tau * wn2_first || tot[1] == 0.0)) break;
+        // (c0) exhausted reachable subspace: an untouched pole's unit vector if one is left,
+        // else a pseudo-random vector swept orthogonal to the basis in the second attempt
+        int kl = INT_MAX;
+        for (int i = tid; i < ns; i += kLzThreads) if (!touched[i]) { kl = i0 + i; break; }
+        for (int o = 16; o > 0; o >>= 1) kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+        __shared__ int wmin[kLzWarps];
+        if (lane == 0) wmin[warp] = kl;
+        __syncthreads();
+        if (tid == 0) {
+            int m = INT_MAX;
+            for (int q = 0; q < kLzWarps; ++q) m = min(m, wmin[q]);
+            s_kmin = m;
+        }
+        cluster.sync();
+        int kmin = INT_MAX;
+        for (int r = 0; r < CL; ++r) kmin = min(kmin, *cluster.map_shared_rank(&s_kmin, r));
+        if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
+        if (kmin != INT_MAX) {
+            VT *vj = V + (size_t)j * C.ld + i0;
+            for (int i = tid; i < ns; i += kLzThreads) {
+                const bool hit = (i0 + i == kmin);
+                vj[i] = hit ? (VT)1 : (VT)0;
+                if (hit) touched[i] = 1;
+            }
+            if (rank == 0 && tid == 0) {
+                double *row = C.out + (size_t)j * NT;
+                for (int q = 0; q < NT; ++q) row[q] = 0.0;
+                row[0] = C.E[kmin];
+                for (int d = 0; d < D; ++d) row[C.nden_out + d] = C.M[(size_t)d * N + kmin];
+            }
+            done = true;
+        } else {
+            for (int i = tid; i < ns; i += kLzThreads) w[i] = restart_value(i0 + i, j);
+            injected = true;
+        }
+        cluster.sync();   // peers have read s_kmin before it can change again
+        }
+        if (done) continue;
         // (c) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216)
         const double xb2 = tot[1];
         const double xa = tot[0] / xb2;
         const double xb = sqrt(xb2);
         VT *vj = V + (size_t)j * C.ld + i0;
-        for (int i = tid; i < ns; i += kLzThreads) vj[i] = (VT)(w[i] / xb);
+        for (int i = tid; i < ns; i += kLzThreads) {
+            const VT v = (VT)(w[i] / xb);
+            vj[i] = v;
+            touched[i] |= (v != (VT)0);
+        }
         if (rank == 0 && tid == 0) {
             double *row = C.out + (size_t)j * NT;
             row[0] = xa;
-            row[1] = xb;
+            row[1] = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
             for (int q = 0; q < k; ++q) row[2 + q] = tot[2 + D + q] / xb;
             for (int d = 0; d < D; ++d) row[C.nden_out + d] = tot[2 + d] / xb;
             if (newv) row[1] = row[1 + k];
@@ -193,7 +265,7 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
 }
 
 size_t lanczos_smem_bytes(int S, int rmax) {
-    return sizeof(double) * ((size_t)3 * S + 2 * (size_t)rmax + kMaxScal + (size_t)kLzWarps * kMaxScal);
+    return sizeof(double) * ((size_t)3 * S + 2 * (size_t)rmax + kMaxScal + (size_t)kLzWarps * kMaxScal) + (size_t)S + 16;
 }
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,

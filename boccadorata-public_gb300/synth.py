@@ -252,6 +252,7 @@ def make_problem(nmax: int, hw: float, seed: int, n_itr: int = 100, sigma: float
 WORKLOADS = {
     "nmax4_full": dict(nmax=4, hw=20.0, seed=0, n_itr=0),
     "nmax6_lanczos50": dict(nmax=6, hw=20.0, seed=1, n_itr=50),
+    "nmax8_lanczos100": dict(nmax=8, hw=20.0, seed=1, n_itr=100),
     "nmax10_lanczos100": dict(nmax=10, hw=16.0, seed=2, n_itr=100),
     "nmax12_lanczos100": dict(nmax=12, hw=16.0, seed=3, n_itr=100),
 }

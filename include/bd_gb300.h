@@ -156,6 +156,14 @@ int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *so
 int bd_result_koltun_all(bd_ctx *ctx, double *koltun);
 /* Device time of the phases of the last bd_run_all in ms: sigma2, sort, lanczos, dyson, total. */
 int bd_last_timings(bd_ctx *ctx, double *ms5);
+/* Diagnostics: extra reorthogonalisation sweeps of the last bd_run_all; device time of
+ * its Lanczos kernel launch (ms, CUDA events on the context's stream) when the run was
+ * batched; kernels of this library launched on the context so far; tuning knobs
+ * (cluster sizes 1..16, DGKS threshold eta). */
+int       bd_diag_two_pass(bd_ctx *ctx);
+double    bd_lanczos_kernel_ms(bd_ctx *ctx);
+long long bd_launch_count(bd_ctx *ctx);
+int       bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta);
 
 #ifdef __cplusplus
 }

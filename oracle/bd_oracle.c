@@ -283,6 +283,14 @@ void bdo_sort_perm(int ntot, const double *key, int desc, int *perm) {
     free(rows);
 }
 
+/* Deterministic pseudo-random restart value of pole i at Lanczos index j, in [0.5, 1.5)
+ * (same function as the device's). */
+static double restart_value(int i, int j) {
+    unsigned x = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return 0.5 + (double)(x & 0xffffffu) / 16777216.0;
+}
+
 /* ---------------------------------------------------------------------------
  * Reduce_Mtx_Lncz (source/BcDor-Lanczos.cpp:44-286).  Min rows are
  * [E, *, M_0..M_{NB_in-1}] (NA_in leading doubles); Mout rows are
@@ -333,13 +341,49 @@ int bdo_reduce_mtx_lncz_passes(int NA_out, int NB_out, int NPLS_out, double *Mou
             const double *vi = vj - NPLS_in;
             for (int k = 0; k < NPLS_in; ++k) vj[k] = vi[k] * Min[(size_t)k * NT_in];
         }
+        double n0 = 0.0;
+        for (int k = 0; k < NPLS_in; ++k) n0 += vj[k] * vj[k];
         /* backward modified Gram-Schmidt, :160-173 (passes > 1 repeats it) */
         for (int pass = 0; pass < passes; ++pass)
         for (int i = j - 1; i >= 0; --i) {
             const double *vi = LV + (size_t)i * NPLS_in;
             double x1 = 0.0, x2 = 0.0;
             for (int k = 0; k < NPLS_in; ++k) { x1 += vi[k] * vj[k]; x2 += vi[k] * vi[k]; }
+            if (passes > 1 && x2 == 0.0) continue;   /* multi-sweep mode skips empty vectors */
             for (int k = 0; k < NPLS_in; ++k) vj[k] -= x1 * vi[k] / x2;
+        }
+        int injected = 0;
+        if (passes > 1) {
+            /* Exhausted reachable subspace (not part of the reference, whose rows become
+             * NaN here): continue with the unit vector of the first pole no stored vector
+             * touches (alpha = E_k, beta = 0, g = 0, m = M[k, :]), else with a
+             * pseudo-random vector swept orthogonal to the basis (beta = 0). */
+            double nn = 0.0;
+            for (int k = 0; k < NPLS_in; ++k) nn += vj[k] * vj[k];
+            if (nn <= 1e-48 * n0 || nn == 0.0) {
+                int kfree = -1;
+                for (int k = 0; k < NPLS_in && kfree < 0; ++k) {
+                    int used = 0;
+                    for (int i = 0; i < j && !used; ++i) used = (LV[(size_t)i * NPLS_in + k] != 0.0);
+                    if (!used) kfree = k;
+                }
+                if (kfree >= 0) {
+                    for (int k = 0; k < NPLS_in; ++k) vj[k] = (k == kfree) ? 1.0 : 0.0;
+                    re[0] = Min[(size_t)kfree * NT_in];
+                    for (int l = 0; l < NB_out; ++l) rm[l] = Min[(size_t)kfree * NT_in + NA_in + l];
+                    rm += NT_out; re += NT_out;
+                    continue;
+                }
+                for (int k = 0; k < NPLS_in; ++k) vj[k] = restart_value(k, j);
+                for (int pass = 0; pass < passes; ++pass)
+                    for (int i = j - 1; i >= 0; --i) {
+                        const double *vi = LV + (size_t)i * NPLS_in;
+                        double x1 = 0.0, x2 = 0.0;
+                        for (int k = 0; k < NPLS_in; ++k) { x1 += vi[k] * vj[k]; x2 += vi[k] * vi[k]; }
+                        if (x2 > 0.0) for (int k = 0; k < NPLS_in; ++k) vj[k] -= x1 * vi[k] / x2;
+                    }
+                injected = 1;
+            }
         }
         /* alpha, beta, coupling, :180-216 */
         double xa = 0.0, xb = 0.0;
@@ -362,6 +406,7 @@ int bdo_reduce_mtx_lncz_passes(int NA_out, int NB_out, int NPLS_out, double *Mou
             re[2 + i] = xg / xb;
         }
         for (int k = 0; k < NPLS_in; ++k) vj[k] /= xb;
+        if (injected) re[1] = 0.0;
         if (newv) re[1] = re[1 + n_pvt];
         if (n_pvt + 2 + NB_out > NT_out) { free(i_last); free(LV); return -200; }
         rm += NT_out; re += NT_out;

@@ -1,0 +1,81 @@
+"""All-channel launches, the mixed-precision form, and error reporting."""
+import numpy as np
+import pytest
+
+from helpers import strong_diffs
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batched_equals_per_channel_calls(bdmod, problems):
+    p = problems(4, 20.0, 0, 20)
+    a = bdmod.Context().upload(p)
+    a.run_all(lanczos=True)
+    b = bdmod.Context().upload(p)
+    b.run_all(lanczos=True, per_channel=True)
+    c = bdmod.Context().upload(p)
+    for ish in range(p.ms.nsubsh):
+        ra, rb = a.result(ish), b.result(ish)
+        for k in ("qp", "qh", "koltun"):
+            np.testing.assert_allclose(ra[k], rb[k], rtol=1e-12, atol=1e-12)
+        c.sigma2_build(ish, copy=False)
+        pv = p.piv
+        c.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish])
+        D = p.ms.no[ish]
+        rc = c.dyson_solve(ish, np.diag(p.ms.orb_xe[p.ms.orb_start[ish]:p.ms.orb_start[ish] + D]))
+        np.testing.assert_allclose(ra["koltun"], rc["koltun"], rtol=1e-12, atol=1e-12)
+        for tag in ("qp", "qh"):
+            e, z = strong_diffs(ra[tag], rc[tag])
+            assert e < 1e-12 and z < 1e-10
+    for x in (a, b, c):
+        x.close()
+
+
+def test_full_dyson_batched(bdmod, problems, golden):
+    g = golden("nmax4_full")
+    p = problems(4, 20.0, 0, 0)
+    ctx = bdmod.Context().upload(p)
+    ctx.run_all(lanczos=False)
+    k = ctx.koltun_all()
+    for ish in range(p.ms.nsubsh):
+        np.testing.assert_allclose(k[ish], g[f"c{ish}_koltun"], rtol=1e-7, atol=1e-9)
+    ctx.close()
+
+
+def test_mixed_precision_within_targets(bdmod, problems):
+    """FP32 Lanczos vectors: every strength-carrying quasiparticle energy within 1 keV
+    and every spectroscopic factor within 1e-5 of the FP64 path."""
+    p = problems(6, 20.0, 1, 50)
+    ctx = bdmod.Context().upload(p)
+    ctx.run_all(lanczos=True)
+    ref = [ctx.result(i) for i in range(p.ms.nsubsh)]
+    ctx.run_all(lanczos=True, mixed=True)
+    for ish in range(p.ms.nsubsh):
+        r = ctx.result(ish)
+        for tag in ("qp", "qh"):
+            e, z = strong_diffs(ref[ish][tag], r[tag], zmin=1e-4, etol=1e-5)
+            assert e * 300.0 < 1e-3 and z < 1e-5, (ish, tag, e, z)      # |W| < 300 MeV
+        np.testing.assert_allclose(r["koltun"], ref[ish]["koltun"], rtol=1e-6, atol=1e-8)
+    ctx.close()
+
+
+def test_errors_are_status_codes(bdmod, problems):
+    p = problems(4, 20.0, 0, 20)
+    ctx = bdmod.Context().upload(p)
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.count_poles(p.ms.nsubsh)
+    assert e.value.code == bdmod.BD_ERR_ARG
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.dyson_solve(0)                                   # no self-energy yet
+    assert e.value.code == bdmod.BD_ERR_STATE
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.result(0)                                        # no bd_run_all yet
+    assert e.value.code == bdmod.BD_ERR_STATE
+    fw = np.zeros((1, 2 + p.ms.no[0]))
+    import ctypes as C
+    n = C.c_int()
+    rc = ctx.lib.bd_sigma2_build(ctx.h, 0, fw.ctypes.data_as(C.POINTER(C.c_double)), 0, C.byref(n), None, 0, None)
+    assert rc == bdmod.BD_ERR_CAPACITY
+    ctx.run_all(lanczos=True)                                # the context stays usable
+    assert np.isfinite(ctx.koltun_all()).all()
+    ctx.close()
