@@ -385,7 +385,8 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             if (P.L <= 0) continue;
             LzChain z{};
             z.N = P.N; z.D = C.D; z.L = P.L; z.n_used = P.n_used; z.nden_out = P.nden_out;
-            z.ld = (P.N + 31) / 32 * 32;
+            z.ld = lz_ld(P.N);
+            z.S = ((P.N + ctx->lz_cluster - 1) / ctx->lz_cluster + 3) / 4 * 4;
             z.E = (dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s) + (dir == 0 ? C.fw_off : C.bk_off);
             z.M = (dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s) + (dir == 0 ? C.mfw_off : C.mbk_off);
             z.piv = ctx->d_lzpiv + ctx->lz_piv_off[dir][I];
@@ -395,7 +396,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             z.out = ctx->d_lzout + ctx->lz_out_off[dir][I];
             z.stat = ctx->d_lzstat;
             ch.push_back(z);
-            Smax = std::max(Smax, (P.N + ctx->lz_cluster - 1) / ctx->lz_cluster);
+            Smax = std::max(Smax, z.S);
             rmax = std::max(rmax, P.L + 1);
         }
     }
@@ -551,7 +552,7 @@ int alloc_lanczos(bd_ctx *ctx) {
             ChainPlan &P = ctx->chans[I].lz[dir];
             const int D = ctx->chans[I].D;
             ctx->lz_v_off[dir][I] = (long long)vbytes;
-            vbytes += sizeof(double) * (size_t)std::max(P.L, 0) * ((P.N + 31) / 32 * 32);
+            vbytes += sizeof(double) * (size_t)std::max(P.L, 0) * lz_ld(P.N);
             vbytes = (vbytes + 255) / 256 * 256;
             ctx->lz_out_off[dir][I] = out;
             out += (long long)std::max(P.L, 0) * (P.nden_out + D);
@@ -810,7 +811,7 @@ int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv) {
     int tot = 0;
     size_t vtot = 0;
     for (int s = 0; s < ctx->nsubsh; ++s) {
-        if (ctx->piv_npvt[s] < 0 || ctx->piv_npvt[s] + 1 + 2 + ctx->no[s] > 32)
+        if (ctx->piv_npvt[s] < 0 || ctx->piv_npvt[s] > 9)
             return fail(ctx, BD_ERR_ARG, "subshell %d: %d pivots", s, ctx->piv_npvt[s]);
         ctx->piv_first[s] = tot; tot += ctx->piv_npvt[s]; vtot += (size_t)ctx->piv_npvt[s] * ctx->no[s];
     }
@@ -894,7 +895,7 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
     Chan &C = ctx->chans[ish];
     if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no Sigma(2) built", ish);
     if (n_pvt < 0 || (n_pvt > 0 && (!pivots || !n_itr_fw || !n_itr_bk))) return fail(ctx, BD_ERR_ARG, "pivots");
-    if (n_pvt + 1 + 2 + C.D > 32) return fail(ctx, BD_ERR_ARG, "too many pivots (%d)", n_pvt);
+    if (n_pvt > 9) return fail(ctx, BD_ERR_ARG, "too many pivots (%d, at most 9)", n_pvt);
     // (re)plan this channel with the caller's pivots; same side effects as the reference:
     // started pivots normalised in place, iteration counts rescaled in place
     ChainPlan F, B;
@@ -1070,7 +1071,7 @@ int bd_lanczos_vectors(bd_ctx *ctx, int ish, int dir, int fp32, double *out, lon
     const ChainPlan &P = ctx->chans[ish].lz[dir];
     const long long need = (long long)P.L * P.N;
     if (!out || cap < need) return fail(ctx, BD_ERR_CAPACITY, "need %lld doubles", need);
-    const int ld = (P.N + 31) / 32 * 32;
+    const int ld = lz_ld(P.N);
     const char *base = ctx->d_lzV + ctx->lz_v_off[dir][ish];
     CU(cudaStreamSynchronize(ctx->st));
     if (fp32) {

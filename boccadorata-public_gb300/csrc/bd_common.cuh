@@ -46,12 +46,17 @@ struct ChanSig {
     long long mfw_off, mbk_off;  // offsets into the M arrays
 };
 
+// Leading dimension of a chain's vector store: room for any cluster size up to 16
+// with 4-aligned slices (CL * round4(ceil(N / CL)) <= N + 63).
+__host__ __device__ inline int lz_ld(int N) { return (N + 64 + 31) / 32 * 32; }
+
 // One Lanczos chain set (channel x direction), processed by one thread-block cluster.
 struct LzChain {
     int N, D, L;            // poles, orbitals, Lanczos vectors to compute
     int n_used;             // pivots actually iterated (n_itr > 0)
     int nden_out;           // leading doubles per output row (= n_pvt + 1)
-    int ld;                 // leading dimension of the vector store (>= N, multiple of 32)
+    int ld;                 // leading dimension of the vector store (>= CL * S, multiple of 32)
+    int S;                  // pole rows per CTA (multiple of 4)
     const double *E;        // [N]   sorted energies
     const double *M;        // [D][N] sorted couplings
     const double *piv;      // [n_used][D] normalised pivots in use order

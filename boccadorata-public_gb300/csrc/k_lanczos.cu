@@ -65,14 +65,34 @@ __host__ __device__ inline double restart_value(int i, int j) {
 
 constexpr int kLzThreads = 256;
 constexpr int kLzWarps = kLzThreads / 32;
-constexpr int kMaxScal = 32;   // 2 + D + n_used <= 32
+constexpr int kMaxScal = 32;   // 1 + D + n_used <= 17 (D <= 8, at most 8 earlier pivots)
 
-// Shared-memory layout (doubles): Es[S] | w[S] | wc[S] (compute-type copy) |
-// A[rmax] (dot partials) | B[kMaxScal] (scalar partials) | c[rmax] (totals) |
-// red[kLzWarps * kMaxScal] (block reduction scratch)
+// 16-byte vector of the storage type: 4 floats or 2 doubles
+template <typename VT> struct Vec16;
+template <> struct Vec16<float> { using T = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using T = double2; static constexpr int n = 2; };
+
 template <typename VT>
-__global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
+__device__ inline void load16(const VT *p, VT *out);
+template <> __device__ inline void load16<float>(const float *p, float *o) {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+template <> __device__ inline void load16<double>(const double *p, double *o) {
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    o[0] = v.x; o[1] = v.y;
+}
+
+// Slice of a CTA: S pole rows starting at rank*S, S a multiple of 4; rows past N are
+// zero in every vector (E, w, V), so the vector loads need no tail handling.
+//
+// Shared-memory layout (doubles): Es[S] | w[S] | wc[S] | A[rmax] (dot partials) |
+// c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | Bn[1] (norm partial) |
+// red[kLzWarps * kMaxScal] | touched[S] bytes
+template <typename VT>
+__global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
     using CT = typename LzTraits<VT>::CT;
+    constexpr int VW = Vec16<VT>::n;
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -80,9 +100,10 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
     if (cid >= nchains) return;  // whole clusters only: every CTA of a cluster has the same cid
     const LzChain C = chains[cid];
     const int N = C.N, D = C.D, L = C.L, NT = C.nden_out + C.D;
-    const int S = (N + CL - 1) / CL;
+    const int S = C.S;                       // multiple of 4
     const int i0 = rank * S;
     const int ns = max(0, min(N, i0 + S) - i0);
+    const int nv = S / VW;                   // 16-byte vectors per slice
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     extern __shared__ double sm[];
@@ -90,19 +111,32 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
     double *w = Es + S;
     CT *wc = reinterpret_cast<CT *>(w + S);
     double *A = w + 2 * S;
-    double *B = A + rmax;
-    double *c = B + kMaxScal;
-    double *red = c + rmax;
+    double *c = A + rmax;
+    double *Bs = c + rmax;
+    double *Bn = Bs + kMaxScal;
+    double *red = Bn + 1;
     unsigned char *touched = reinterpret_cast<unsigned char *>(red + kLzWarps * kMaxScal);
     __shared__ double tot[kMaxScal];
+    __shared__ double s_n2;
     __shared__ int s_kmin;
 
     VT *V = reinterpret_cast<VT *>(C.V);
-    for (int i = tid; i < ns; i += kLzThreads) { Es[i] = C.E[i0 + i]; touched[i] = 0; }
+    for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? C.E[i0 + i] : 0.0; touched[i] = 0; }
     const double tau = (sizeof(VT) == 4) ? 1e-22 : 1e-48;
 
+    // block-wide sum of one double per thread, result in every thread
+    auto block_sum = [&](double v) -> double {
+        v = warp_sum(v);
+        __syncthreads();
+        if (lane == 0) red[warp] = v;
+        __syncthreads();
+        double s = 0.0;
+        for (int q = 0; q < kLzWarps; ++q) s += red[q];
+        return s;
+    };
+
     int k = -1;           // current pivot chain
-    int two_pass = 0;
+    int extra = 0;        // sweeps beyond the first
     for (int j = 0; j < L; ++j) {
         const bool newv = (k + 1 < C.n_used) && (j == C.start[k + 1]);
         if (newv) ++k;
@@ -110,142 +144,190 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
         // (a) w = M.p  or  w = v_{j-1} * E   (source/BcDor-Lanczos.cpp:137-150)
         if (newv) {
             const double *p = C.piv + (size_t)k * D;
-            for (int i = tid; i < ns; i += kLzThreads) {
+            for (int i = tid; i < S; i += kLzThreads) {
                 double s = 0.0;
-                for (int d = 0; d < D; ++d) s = __dadd_rn(s, __dmul_rn(C.M[(size_t)d * N + i0 + i], p[d]));
+                if (i < ns)
+                    for (int d = 0; d < D; ++d) s = __dadd_rn(s, __dmul_rn(C.M[(size_t)d * N + i0 + i], p[d]));
                 w[i] = s;
             }
         } else {
             const VT *vp = V + (size_t)(j - 1) * C.ld + i0;
-            for (int i = tid; i < ns; i += kLzThreads) w[i] = (double)vp[i] * Es[i];
+            for (int i = tid; i < S; i += kLzThreads) w[i] = (double)vp[i] * Es[i];
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
         bool done = false;         // step finished by an untouched-pole unit vector
+        double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
-        int pass = 0;
-        double wn2_first = 0.0;
-        for (;;) {
-            __syncthreads();
-            for (int i = tid; i < ns; i += kLzThreads) wc[i] = (CT)w[i];
-            __syncthreads();
-            // (b1) partial dot products <v_t, w> over the own slice, one warp per t
-            for (int t = warp; t < j; t += kLzWarps) {
-                const VT *vt = V + (size_t)t * C.ld + i0;
-                CT acc = 0;
-                for (int i = lane; i < ns; i += 32) acc += (CT)vt[i] * wc[i];
-                double s = warp_sum((double)acc);
-                if (lane == 0) A[t] = s;
-            }
-            {   // partial |w|^2 before this sweep
-                double acc = 0.0;
-                for (int i = tid; i < ns; i += kLzThreads) acc += w[i] * w[i];
-                acc = warp_sum(acc);
-                if (lane == 0) red[warp] = acc;
+            int pass = 0;
+            double wn2_first = 0.0;
+            for (;;) {
                 __syncthreads();
+                for (int i = tid; i < S; i += kLzThreads) wc[i] = (CT)w[i];
+                __syncthreads();
+                // (b1) partial dot products <v_t, w> over the slice, one warp per t, 16-byte loads
+                for (int t = warp; t < j; t += kLzWarps) {
+                    const VT *vt = V + (size_t)t * C.ld + i0;
+                    CT acc = 0;
+                    for (int q = lane; q < nv; q += 32) {
+                        VT x[VW];
+                        load16<VT>(vt + q * VW, x);
+#pragma unroll
+                        for (int u = 0; u < VW; ++u) acc += x[u] * wc[q * VW + u];
+                    }
+                    const double s = warp_sum((double)acc);
+                    if (lane == 0) A[t] = s;
+                }
+                double nw = 0.0;
+                for (int i = tid; i < S; i += kLzThreads) nw += w[i] * w[i];
+                nw = block_sum(nw);
+                if (tid == 0) A[j] = nw;
+                cluster.sync();
+                // (b2) totals over the cluster, in rank order
+                for (int t = tid; t <= j; t += kLzThreads) {
+                    double s = 0.0;
+                    for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(A, r)[t];
+                    c[t] = s;
+                }
+                __syncthreads();
+                const double wn2_before = c[j];
+                if (pass == 0) wn2_first = wn2_before;
+                // (b3) w -= sum_t c_t v_t over 16-byte vectors, four rows in flight, and |w|^2
+                double pn = 0.0;
+                for (int q = tid; q < nv; q += kLzThreads) {
+                    CT acc[VW];
+#pragma unroll
+                    for (int u = 0; u < VW; ++u) acc[u] = 0;
+                    const VT *base = V + i0 + q * VW;
+                    int t = 0;
+                    for (; t + 3 < j; t += 4) {
+                        VT x0[VW], x1[VW], x2[VW], x3[VW];
+                        load16<VT>(base + (size_t)t * C.ld, x0);
+                        load16<VT>(base + (size_t)(t + 1) * C.ld, x1);
+                        load16<VT>(base + (size_t)(t + 2) * C.ld, x2);
+                        load16<VT>(base + (size_t)(t + 3) * C.ld, x3);
+                        const CT c0 = (CT)c[t], c1 = (CT)c[t + 1], c2 = (CT)c[t + 2], c3 = (CT)c[t + 3];
+#pragma unroll
+                        for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
+                    }
+                    for (; t < j; ++t) {
+                        VT x0[VW];
+                        load16<VT>(base + (size_t)t * C.ld, x0);
+                        const CT c0 = (CT)c[t];
+#pragma unroll
+                        for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
+                    }
+#pragma unroll
+                    for (int u = 0; u < VW; ++u) {
+                        const double wi = w[q * VW + u] - (double)acc[u];
+                        w[q * VW + u] = wi;
+                        pn += wi * wi;
+                    }
+                }
+                pn = block_sum(pn);
+                if (tid == 0) Bn[0] = pn;
+                cluster.sync();
                 if (tid == 0) {
                     double s = 0.0;
-                    for (int q = 0; q < kLzWarps; ++q) s += red[q];
-                    A[j] = s;
+                    for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(Bn, r)[0];
+                    s_n2 = s;
                 }
+                __syncthreads();
+                n2 = s_n2;
+                // another sweep while this one removed more than half of the squared norm
+                if (j > 0 && pass < 3 && n2 < eta2 * wn2_before) { ++pass; ++extra; continue; }
+                break;
+            }
+            if (attempt > 0 || !(n2 <= tau * wn2_first || n2 == 0.0)) break;
+            // (c0) exhausted reachable subspace: an untouched pole's unit vector if one is left,
+            // else a pseudo-random vector swept orthogonal to the basis in the second attempt
+            int kl = INT_MAX;
+            for (int i = tid; i < ns; i += kLzThreads) if (!touched[i]) { kl = i0 + i; break; }
+            for (int o = 16; o > 0; o >>= 1) kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+            __shared__ int wmin[kLzWarps];
+            if (lane == 0) wmin[warp] = kl;
+            __syncthreads();
+            if (tid == 0) {
+                int m = INT_MAX;
+                for (int q = 0; q < kLzWarps; ++q) m = min(m, wmin[q]);
+                s_kmin = m;
             }
             cluster.sync();
-            // (b2) totals over the cluster, in rank order
-            for (int t = tid; t <= j; t += kLzThreads) {
-                double s = 0.0;
-                for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(A, r)[t];
-                c[t] = s;
-            }
-            __syncthreads();
-            const double wn2_before = c[j];
-            if (pass == 0) wn2_first = wn2_before;
-            // (b3) w -= sum_t c_t v_t, then partial alpha / beta / m / g sums of the new w
-            const int nq = k;  // earlier pivots
-            const int nsc = 2 + D + nq;
-            double acc_s[kMaxScal];
-#pragma unroll
-            for (int q = 0; q < kMaxScal; ++q) acc_s[q] = 0.0;
-            for (int i = tid; i < ns; i += kLzThreads) {
-                CT a0 = 0, a1 = 0;
-                int t = 0;
-                for (; t + 1 < j; t += 2) {
-                    a0 += (CT)c[t] * (CT)V[(size_t)t * C.ld + i0 + i];
-                    a1 += (CT)c[t + 1] * (CT)V[(size_t)(t + 1) * C.ld + i0 + i];
+            int kmin = INT_MAX;
+            for (int r = 0; r < CL; ++r) kmin = min(kmin, *cluster.map_shared_rank(&s_kmin, r));
+            if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
+            if (kmin != INT_MAX) {
+                VT *vj = V + (size_t)j * C.ld + i0;
+                for (int i = tid; i < S; i += kLzThreads) {
+                    const bool hit = (i0 + i == kmin);
+                    vj[i] = hit ? (VT)1 : (VT)0;
+                    if (hit) touched[i] = 1;
                 }
-                if (t < j) a0 += (CT)c[t] * (CT)V[(size_t)t * C.ld + i0 + i];
-                const double wi = w[i] - ((double)a0 + (double)a1);
-                w[i] = wi;
-                const double e = Es[i];
-                acc_s[0] += e * wi * wi;
-                acc_s[1] += wi * wi;
-                for (int d = 0; d < D; ++d) acc_s[2 + d] += C.M[(size_t)d * N + i0 + i] * wi;
-                for (int q = 0; q < nq; ++q) acc_s[2 + D + q] += e * (double)V[(size_t)C.last[q] * C.ld + i0 + i] * wi;
+                if (rank == 0 && tid == 0) {
+                    double *row = C.out + (size_t)j * NT;
+                    for (int q = 0; q < NT; ++q) row[q] = 0.0;
+                    row[0] = C.E[kmin];
+                    for (int d = 0; d < D; ++d) row[C.nden_out + d] = C.M[(size_t)d * N + kmin];
+                }
+                done = true;
+            } else {
+                for (int i = tid; i < S; i += kLzThreads) w[i] = (i < ns) ? restart_value(i0 + i, j) : 0.0;
+                injected = true;
             }
-            for (int q = 0; q < nsc; ++q) {
-                double s = warp_sum(acc_s[q]);
-                if (lane == 0) red[warp * kMaxScal + q] = s;
-            }
-            __syncthreads();
-            if (tid < nsc) {
-                double s = 0.0;
-                for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal + tid];
-                B[tid] = s;
-            }
-            cluster.sync();
-            if (tid < nsc) {
-                double s = 0.0;
-                for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(B, r)[tid];
-                tot[tid] = s;
-            }
-            __syncthreads();
-            // another sweep while this one removed more than half of the squared norm
-            if (j > 0 && pass < 3 && tot[1] < eta2 * wn2_before) { ++pass; ++two_pass; continue; }
-            break;
-        }
-        if (attempt > 0 || !(tot[1] <= tau * wn2_first || tot[1] == 0.0)) break;
-        // (c0) exhausted reachable subspace: an untouched pole's unit vector if one is left,
-        // else a pseudo-random vector swept orthogonal to the basis in the second attempt
-        int kl = INT_MAX;
-        for (int i = tid; i < ns; i += kLzThreads) if (!touched[i]) { kl = i0 + i; break; }
-        for (int o = 16; o > 0; o >>= 1) kl = min(kl, __shfl_xor_sync(0xffffffffu, kl, o));
-        __shared__ int wmin[kLzWarps];
-        if (lane == 0) wmin[warp] = kl;
-        __syncthreads();
-        if (tid == 0) {
-            int m = INT_MAX;
-            for (int q = 0; q < kLzWarps; ++q) m = min(m, wmin[q]);
-            s_kmin = m;
-        }
-        cluster.sync();
-        int kmin = INT_MAX;
-        for (int r = 0; r < CL; ++r) kmin = min(kmin, *cluster.map_shared_rank(&s_kmin, r));
-        if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
-        if (kmin != INT_MAX) {
-            VT *vj = V + (size_t)j * C.ld + i0;
-            for (int i = tid; i < ns; i += kLzThreads) {
-                const bool hit = (i0 + i == kmin);
-                vj[i] = hit ? (VT)1 : (VT)0;
-                if (hit) touched[i] = 1;
-            }
-            if (rank == 0 && tid == 0) {
-                double *row = C.out + (size_t)j * NT;
-                for (int q = 0; q < NT; ++q) row[q] = 0.0;
-                row[0] = C.E[kmin];
-                for (int d = 0; d < D; ++d) row[C.nden_out + d] = C.M[(size_t)d * N + kmin];
-            }
-            done = true;
-        } else {
-            for (int i = tid; i < ns; i += kLzThreads) w[i] = restart_value(i0 + i, j);
-            injected = true;
-        }
-        cluster.sync();   // peers have read s_kmin before it can change again
+            cluster.sync();   // peers have read s_kmin before it can change again
         }
         if (done) continue;
-        // (c) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216)
-        const double xb2 = tot[1];
-        const double xa = tot[0] / xb2;
-        const double xb = sqrt(xb2);
+        // (c) alpha, m, g of the final w (FP64, once per step; source/BcDor-Lanczos.cpp:180-214)
+        const int nq = k;
+        const int nsc = 1 + D + nq;
+        {
+            double sa = 0.0, sm_[8], sg[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { sm_[q] = 0.0; sg[q] = 0.0; }
+            for (int i = tid; i < ns; i += kLzThreads) {
+                const double wi = w[i], e = Es[i];
+                sa += e * wi * wi;
+#pragma unroll
+                for (int d = 0; d < 8; ++d)
+                    if (d < D) sm_[d] += C.M[(size_t)d * N + i0 + i] * wi;
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q < nq) sg[q] += e * (double)V[(size_t)C.last[q] * C.ld + i0 + i] * wi;
+            }
+            sa = warp_sum(sa);
+            if (lane == 0) red[warp * kMaxScal] = sa;
+#pragma unroll
+            for (int d = 0; d < 8; ++d) {
+                if (d < D) {
+                    const double x = warp_sum(sm_[d]);
+                    if (lane == 0) red[warp * kMaxScal + 1 + d] = x;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                if (q < nq) {
+                    const double x = warp_sum(sg[q]);
+                    if (lane == 0) red[warp * kMaxScal + 1 + D + q] = x;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < nsc) {
+            double s = 0.0;
+            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal + tid];
+            Bs[tid] = s;
+        }
+        cluster.sync();
+        if (tid < nsc) {
+            double s = 0.0;
+            for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(Bs, r)[tid];
+            tot[tid] = s;
+        }
+        __syncthreads();
+        // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216)
+        const double xa = tot[0] / n2;
+        const double xb = sqrt(n2);
         VT *vj = V + (size_t)j * C.ld + i0;
-        for (int i = tid; i < ns; i += kLzThreads) {
+        for (int i = tid; i < S; i += kLzThreads) {
             const VT v = (VT)(w[i] / xb);
             vj[i] = v;
             touched[i] |= (v != (VT)0);
@@ -254,18 +336,19 @@ __global__ void __launch_bounds__(kLzThreads) k_lanczos(const LzChain *chains, i
             double *row = C.out + (size_t)j * NT;
             row[0] = xa;
             row[1] = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
-            for (int q = 0; q < k; ++q) row[2 + q] = tot[2 + D + q] / xb;
-            for (int d = 0; d < D; ++d) row[C.nden_out + d] = tot[2 + d] / xb;
+            for (int q = 0; q < k; ++q) row[2 + q] = tot[1 + D + q] / xb;
+            for (int d = 0; d < D; ++d) row[C.nden_out + d] = tot[1 + d] / xb;
             if (newv) row[1] = row[1 + k];
         }
         __syncthreads();
     }
-    if (rank == 0 && tid == 0) atomicAdd(&C.stat[0], two_pass);
+    if (rank == 0 && tid == 0) atomicAdd(&C.stat[0], extra);
     cluster.sync();  // no CTA leaves while peers may still read its shared memory
 }
 
 size_t lanczos_smem_bytes(int S, int rmax) {
-    return sizeof(double) * ((size_t)3 * S + 2 * (size_t)rmax + kMaxScal + (size_t)kLzWarps * kMaxScal) + (size_t)S + 16;
+    return sizeof(double) * ((size_t)3 * S + 2 * (size_t)rmax + kMaxScal + 1 + (size_t)kLzWarps * kMaxScal) +
+           (size_t)S + 16;
 }
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,

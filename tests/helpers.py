@@ -9,6 +9,8 @@ def strong_diffs(ref, got, zmin=1e-6, etol=1e-7):
     arbitrary, so strength is compared per degenerate group)."""
     ref = np.asarray(ref).reshape(-1, ref.shape[-1]) if len(ref) else np.zeros((0, 2))
     got = np.asarray(got).reshape(-1, got.shape[-1]) if len(got) else np.zeros((0, 2))
+    if not (np.isfinite(ref).all() and np.isfinite(got).all()):
+        return np.inf, np.inf
     wE = wZ = 0.0
     for r in ref[ref[:, 1] > zmin]:
         if not len(got):

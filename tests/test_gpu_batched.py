@@ -17,6 +17,7 @@ def test_batched_equals_per_channel_calls(bdmod, problems):
     for ish in range(p.ms.nsubsh):
         ra, rb = a.result(ish), b.result(ish)
         for k in ("qp", "qh", "koltun"):
+            assert np.isfinite(ra[k]).all() and np.isfinite(rb[k]).all(), (ish, k)
             np.testing.assert_allclose(ra[k], rb[k], rtol=1e-12, atol=1e-12)
         c.sigma2_build(ish, copy=False)
         pv = p.piv
@@ -37,6 +38,7 @@ def test_full_dyson_batched(bdmod, problems, golden):
     ctx = bdmod.Context().upload(p)
     ctx.run_all(lanczos=False)
     k = ctx.koltun_all()
+    assert np.isfinite(k).all()
     for ish in range(p.ms.nsubsh):
         np.testing.assert_allclose(k[ish], g[f"c{ish}_koltun"], rtol=1e-7, atol=1e-9)
     ctx.close()
@@ -52,6 +54,9 @@ def test_mixed_precision_within_targets(bdmod, problems):
     ctx.run_all(lanczos=True, mixed=True)
     for ish in range(p.ms.nsubsh):
         r = ctx.result(ish)
+        for k in ("qp", "qh", "koltun"):
+            assert np.isfinite(r[k]).all() and np.isfinite(ref[ish][k]).all(), (ish, k)
+        assert (r["qp"][:, 1] > 1e-4).sum() + (r["qh"][:, 1] > 1e-4).sum() > 0
         for tag in ("qp", "qh"):
             e, z = strong_diffs(ref[ish][tag], r[tag], zmin=1e-4, etol=1e-5)
             assert e * 300.0 < 1e-3 and z < 1e-5, (ish, tag, e, z)      # |W| < 300 MeV
