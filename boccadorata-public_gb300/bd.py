@@ -342,3 +342,27 @@ class WideSelfEnergy:
 def dyson_matrix(sfv: WideSelfEnergy, sig1b, sighf=None, efermi=float("nan")):
     """DysonMatrix: returns dict(qp=rows, qh=rows, koltun=[x1, x2, x3])."""
     return sfv.ctx.dyson_solve(sfv.I_SH, sig1b, sighf, efermi)
+
+
+def lanczos_chain_noalloc(d_E: int, d_M: int, N: int, D: int, pivots, n_itr, d_rows: int, cap_rows: int,
+                          mixed: bool = False, stream: int = 0):
+    """bd_lanczos_chain_noalloc: Lanczos rows of one pole set into caller-owned device
+    memory, with no device allocation by the library.  d_E [N], d_M [D][N] and
+    d_rows [cap_rows][n_pvt + 1 + D] are device addresses of float64 buffers on the
+    current device; pivots and n_itr are updated in place as bd_lanczos_reduce does.
+    Returns (L, ipiv, pivots, n_itr)."""
+    L_ = lib()
+    f = L_.bd_lanczos_chain_noalloc
+    vp = C.c_void_p
+    f.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, _dp, _ip, vp, C.c_int, _ip, _ip, C.c_int, vp, C.c_char_p,
+                  C.c_int]
+    piv = _d(np.array(pivots, np.float64).reshape(-1, D)).copy()
+    nit = _i(n_itr).copy()
+    ipiv = np.zeros(len(piv) + 1 + D, np.int32)
+    Lout = C.c_int()
+    err = C.create_string_buffer(512)
+    rc = f(d_E, d_M, N, D, len(piv), _pd(piv), _pi(nit), d_rows, cap_rows, C.byref(Lout), _pi(ipiv),
+           BD_RUN_MIXED if mixed else 0, stream, err, len(err))
+    if rc != BD_OK:
+        raise BDError(rc, err.value.decode(errors="replace"))
+    return Lout.value, ipiv, piv, nit

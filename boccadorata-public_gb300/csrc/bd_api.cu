@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1214,3 +1215,134 @@ int bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free Lanczos reduction of one pole set (bd_lanczos_chain_noalloc).
+//
+// Some host programs cannot let a library call cudaMalloc.  One case is an
+// application whose own pool allocator has already reserved nearly all of the
+// device's memory, so a second allocator would fail or fragment it.  Another is a
+// latency-bound caller that cannot accept the device-wide synchronisation that
+// cudaMalloc and cudaFree may imply.  Such callers pass their own device buffers
+// for the inputs and outputs.  The Lanczos vector store, the chain descriptor
+// and the counters then live in the file-scope array below.
+//
+// Every device on which this library's module is loaded holds the array
+// (BD_NOALLOC_SCRATCH_BYTES) until the process exits.  All calls share it and it
+// keeps the last call's contents.  Each call rewrites the descriptor, the
+// schedule and the counters (the counters start at zero), and the kernel writes
+// every vector before it reads it.  Calls that overlap on the GPU, from two
+// streams or two host threads, race on the array.
+
+static __device__ __align__(256) unsigned char g_lz_scratch[BD_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoallocDevices = 64;
+// scratch layout: [0, 256) descriptor | [256, 272) counters | [512, 1024) chain starts
+// and ends | [1024, 2048) pivots | [4096, end) Lanczos vectors
+constexpr size_t kNoallocCounters = 256, kNoallocInts = 512, kNoallocPiv = 1024, kNoallocStage = 2048;
+constexpr size_t kNoallocVectors = 4096;
+constexpr int kNoallocCluster = 8;                       // the context's default cluster size
+constexpr double kNoallocEta = 0.70710678118654752;      // and DGKS threshold
+static_assert(sizeof(LzChain) <= kNoallocCounters, "descriptor slot");
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_base[kNoallocDevices];
+
+int noalloc_fail(char *err, int err_len, int code, const char *fmt, ...) {
+    if (err && err_len > 0) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err, (size_t)err_len, fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+// Device address of the scratch array on the current device, looked up once per
+// device (the first call on a device does this set-up).
+int noalloc_scratch(char **base, char *err, int err_len) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return noalloc_fail(err, err_len, BD_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoallocDevices) return noalloc_fail(err, err_len, BD_ERR_ARG, "device %d", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_lz_scratch);
+        if (e != cudaSuccess || !p)
+            return noalloc_fail(err, err_len, BD_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+        g_noalloc_base[dev] = p;
+    }
+    *base = static_cast<char *>(g_noalloc_base[dev]);
+    return BD_OK;
+}
+
+}  // namespace
+
+extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, int N, int D, int n_pvt,
+                                        double *pivots, int *n_itr, double *d_rows, int cap_rows, int *L_out,
+                                        int *ipiv, int flags, void *stream, char *err, int err_len) {
+    if (err && err_len > 0) err[0] = 0;
+    if (N < 0) return noalloc_fail(err, err_len, BD_ERR_ARG, "N = %d", N);
+    if (D < 1 || D > 8) return noalloc_fail(err, err_len, BD_ERR_ARG, "D = %d (1..8 orbitals supported)", D);
+    if (n_pvt < 1 || n_pvt > 9 || !pivots || !n_itr)
+        return noalloc_fail(err, err_len, BD_ERR_ARG, "pivots: n_pvt = %d (1..9), pivots and n_itr required", n_pvt);
+    if ((flags & ~BD_RUN_MIXED) != 0) return noalloc_fail(err, err_len, BD_ERR_ARG, "flags 0x%x", flags);
+    ChainPlan P;
+    plan_chain(P, N, D, n_pvt, n_itr, pivots);
+    if (P.L > 0)
+        for (int p = 0; p < n_pvt; ++p) n_itr[p] = P.nitr[p];
+    if (L_out) *L_out = P.L;
+    if (ipiv) std::memcpy(ipiv, P.ipiv.data(), sizeof(int) * P.ipiv.size());
+    if (P.L == 0) return BD_OK;
+    if (!d_E || !d_M) return noalloc_fail(err, err_len, BD_ERR_ARG, "device pole arrays required");
+    if (!d_rows || cap_rows < P.L)
+        return noalloc_fail(err, err_len, BD_ERR_CAPACITY, "d_rows holds %d rows, %d needed", cap_rows, P.L);
+    const bool fp32 = (flags & BD_RUN_MIXED) != 0;
+    const int ld = lz_ld(N);
+    const size_t vbytes = (size_t)P.L * (size_t)ld * (fp32 ? sizeof(float) : sizeof(double));
+    if (vbytes > BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors)
+        return noalloc_fail(err, err_len, BD_ERR_CAPACITY,
+                            "%d Lanczos vectors of %d poles need %zu bytes of scratch; this entry point has %zu "
+                            "(use bd_lanczos_reduce for larger chains)",
+                            P.L, N, vbytes, (size_t)(BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors));
+    const int S = ((N + kNoallocCluster - 1) / kNoallocCluster + 3) / 4 * 4;
+    if (lanczos_smem_bytes(S, P.L + 1) > (size_t)227 * 1024)
+        return noalloc_fail(err, err_len, BD_ERR_CAPACITY, "%d poles per CTA exceed shared memory", S);
+    char *base = nullptr;
+    int rc = noalloc_scratch(&base, err, err_len);
+    if (rc) return rc;
+
+    // descriptor, zeroed counters, schedule and pivots, staged on the host and sent in one copy
+    unsigned char stage[kNoallocStage];
+    std::memset(stage, 0, sizeof(stage));
+    int *h_ints = reinterpret_cast<int *>(stage + kNoallocInts);
+    int ni = 0;
+    for (int v : P.start) h_ints[ni++] = v;
+    for (int v : P.last) h_ints[ni++] = v;
+    std::memcpy(stage + kNoallocPiv, P.piv.data(), sizeof(double) * P.piv.size());
+    LzChain z{};
+    z.N = N; z.D = D; z.L = P.L; z.n_used = P.n_used; z.nden_out = P.nden_out;
+    z.ld = ld; z.S = S;
+    z.E = d_E; z.M = d_M;
+    z.piv = reinterpret_cast<const double *>(base + kNoallocPiv);
+    z.start = reinterpret_cast<const int *>(base + kNoallocInts);
+    z.last = z.start + (P.n_used + 1);
+    z.V = base + kNoallocVectors;
+    z.out = d_rows;
+    z.stat = reinterpret_cast<int *>(base + kNoallocCounters);
+    std::memcpy(stage, &z, sizeof(z));
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t row_bytes = sizeof(double) * (size_t)P.L * (size_t)(P.nden_out + D);
+    cudaError_t e = cudaMemcpyAsync(base, stage, sizeof(stage), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_rows, 0, row_bytes, st);   // the reference clears the rows
+    if (e == cudaSuccess)
+        e = launch_lanczos(reinterpret_cast<const LzChain *>(base), 1, S, P.L + 1, fp32, kNoallocCluster, kNoallocEta,
+                           st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return noalloc_fail(err, err_len, BD_ERR_CUDA, "Lanczos launch: %s", cudaGetErrorString(e));
+    return BD_OK;
+}

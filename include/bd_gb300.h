@@ -165,6 +165,36 @@ double    bd_lanczos_kernel_ms(bd_ctx *ctx);
 long long bd_launch_count(bd_ctx *ctx);
 int       bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta);
 
+/* Allocation-free Lanczos reduction of one pole set.  This entry point has no
+ * counterpart in the reference.  It is for host programs that cannot let a
+ * library call cudaMalloc: one whose own pool allocator has already reserved the
+ * device's memory, or a latency-bound caller that cannot accept the device-wide
+ * synchronisation cudaMalloc and cudaFree may imply.  It needs no context.
+ *
+ * The caller passes device buffers: d_E [N] pole energies and d_M [D][N]
+ * couplings (column d of M at d_M + d * N), both in the order the chain should
+ * visit them (the reference sorts them first), and d_rows, which receives L rows
+ * of n_pvt + 1 + D doubles laid out as for bd_lanczos_reduce (cleared first).
+ * pivots, n_itr, L_out and ipiv are host memory with bd_lanczos_reduce's meaning
+ * and side effects.  flags: 0 = FP64, BD_RUN_MIXED = FP32 vectors.  stream is a
+ * cudaStream_t (NULL = the legacy default stream) of the current device; the call
+ * returns once the rows are written.  err (err_len bytes, may be NULL) receives a
+ * message for any non-zero status.
+ *
+ * Scratch: a file-scope device array of BD_NOALLOC_SCRATCH_BYTES, held on every
+ * device that loads the library until the process exits.  The Lanczos vectors
+ * must fit in it: L * ld * (8, or 4 with BD_RUN_MIXED) bytes, ld = N + 64 rounded
+ * up to a multiple of 32, at most BD_NOALLOC_SCRATCH_BYTES - 4096; larger chains
+ * are rejected with BD_ERR_CAPACITY.  D <= 8 and n_pvt <= 9.
+ * The first call on each device looks up the array's device address; make that
+ * first call before any stream capture on that device.  All calls share the
+ * array, so calls that overlap on the GPU (two streams, two host threads) race.
+ * The call itself allocates no device or pinned memory. */
+#define BD_NOALLOC_SCRATCH_BYTES (16u << 20)
+int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, int N, int D, int n_pvt,
+                             double *pivots, int *n_itr, double *d_rows, int cap_rows, int *L_out,
+                             int *ipiv, int flags, void *stream, char *err, int err_len);
+
 #ifdef __cplusplus
 }
 #endif
