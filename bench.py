@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64-per-channel"], default=None,
+                    help="run only this form's warm-up and timed steps (for ncu); prints its timings, not a bench line")
     return ap.parse_args()
 
 
@@ -271,6 +273,23 @@ def gpu_arm(args):
     prob = synth.make_workload(args.workload)
     nch = prob.ms.nsubsh
     ctx = bd.Context(local).upload(prob)
+
+    if args.profile:
+        kw = {"mixed": dict(mixed=True), "fp64": dict(mixed=False),
+              "fp64-per-channel": dict(mixed=False, per_channel=True)}[args.profile]
+        for _ in range(args.warmup):
+            ctx.run_all(lanczos=True, **kw)
+        ms = []
+        for _ in range(args.steps):
+            ctx.run_all(lanczos=True, **kw)
+            ms.append(ctx.timings())
+        if rank == 0:
+            print(json.dumps({"profile": args.profile, "workload": args.workload, "steps": args.steps,
+                              "timings_ms": ms, "lanczos_kernel_ms": ctx.lanczos_kernel_ms(),
+                              "extra_sweeps": ctx.two_pass_steps(),
+                              "lanczos_steps": sum(L for _, L, _, _ in lanczos_sizes(ctx, prob))}), flush=True)
+        ctx.close()
+        return 0
 
     # ---- accuracy of the mixed form against FP64 (outside the timed region)
     ctx.run_all(lanczos=True, mixed=False)

@@ -90,6 +90,7 @@ struct bd_ctx {
     double *d_vp = nullptr;
     double *d_Efw = nullptr, *d_S2fw = nullptr, *d_Mfw = nullptr, *d_Ebk = nullptr, *d_S2bk = nullptr, *d_Mbk = nullptr;
     double *d_Efw_s = nullptr, *d_Mfw_s = nullptr, *d_Ebk_s = nullptr, *d_Mbk_s = nullptr;  // sorted copies
+    float *d_Mfw_f = nullptr, *d_Mbk_f = nullptr;                                           // FP32 sorted M
     int *d_seg_fw = nullptr, *d_seg_bk = nullptr, *d_idx_fw = nullptr, *d_idx_bk = nullptr, *d_perm_fw = nullptr,
         *d_perm_bk = nullptr;
     double *d_keys_tmp = nullptr;
@@ -368,7 +369,8 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
         CU(e);
         k_permute_soa<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(
             perm, n0, n, dir == 0 ? ctx->d_seg_fw : ctx->d_seg_bk, ctx->d_cs, dir, E, dir == 0 ? ctx->d_Mfw : ctx->d_Mbk,
-            dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s, dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s);
+            dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s, dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s,
+            dir == 0 ? ctx->d_Mfw_f : ctx->d_Mbk_f);
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
@@ -390,6 +392,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             z.S = ((P.N + ctx->lz_cluster - 1) / ctx->lz_cluster + 3) / 4 * 4;
             z.E = (dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s) + (dir == 0 ? C.fw_off : C.bk_off);
             z.M = (dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s) + (dir == 0 ? C.mfw_off : C.mbk_off);
+            z.Mf = (dir == 0 ? ctx->d_Mfw_f : ctx->d_Mbk_f) + (dir == 0 ? C.mfw_off : C.mbk_off);
             z.piv = ctx->d_lzpiv + ctx->lz_piv_off[dir][I];
             z.start = ctx->d_lzint + ctx->lz_int_off[dir][I];
             z.last = z.start + (P.n_used + 1);
@@ -759,6 +762,8 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     if ((rc = dalloc(ctx, &ctx->d_Mfw_s, ctx->tot_mfw))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_Ebk_s, ctx->tot_bk))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_Mbk_s, ctx->tot_mbk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mfw_f, ctx->tot_mfw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_Mbk_f, ctx->tot_mbk))) return rc;
     {   // CUB scratch for the largest segmented sort
         size_t b1 = 0, b2 = 0;
         const int nmax = (int)std::max<long long>(1, std::max(ctx->tot_fw, ctx->tot_bk));
@@ -1303,11 +1308,14 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     const bool fp32 = (flags & BD_RUN_MIXED) != 0;
     const int ld = lz_ld(N);
     const size_t vbytes = (size_t)P.L * (size_t)ld * (fp32 ? sizeof(float) : sizeof(double));
-    if (vbytes > BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors)
+    // the FP32 form also keeps an FP32 copy of M behind the vectors
+    const size_t mf_off = kNoallocVectors + (vbytes + 255) / 256 * 256;
+    const size_t need = fp32 ? mf_off - kNoallocVectors + sizeof(float) * (size_t)D * (size_t)N : vbytes;
+    if (need > BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors)
         return noalloc_fail(err, err_len, BD_ERR_CAPACITY,
                             "%d Lanczos vectors of %d poles need %zu bytes of scratch; this entry point has %zu "
                             "(use bd_lanczos_reduce for larger chains)",
-                            P.L, N, vbytes, (size_t)(BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors));
+                            P.L, N, need, (size_t)(BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors));
     const int S = ((N + kNoallocCluster - 1) / kNoallocCluster + 3) / 4 * 4;
     if (lanczos_smem_bytes(S, P.L + 1) > (size_t)227 * 1024)
         return noalloc_fail(err, err_len, BD_ERR_CAPACITY, "%d poles per CTA exceed shared memory", S);
@@ -1327,6 +1335,7 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     z.N = N; z.D = D; z.L = P.L; z.n_used = P.n_used; z.nden_out = P.nden_out;
     z.ld = ld; z.S = S;
     z.E = d_E; z.M = d_M;
+    z.Mf = fp32 ? reinterpret_cast<const float *>(base + mf_off) : nullptr;
     z.piv = reinterpret_cast<const double *>(base + kNoallocPiv);
     z.start = reinterpret_cast<const int *>(base + kNoallocInts);
     z.last = z.start + (P.n_used + 1);
@@ -1339,6 +1348,8 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     const size_t row_bytes = sizeof(double) * (size_t)P.L * (size_t)(P.nden_out + D);
     cudaError_t e = cudaMemcpyAsync(base, stage, sizeof(stage), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_rows, 0, row_bytes, st);   // the reference clears the rows
+    if (e == cudaSuccess && fp32)
+        e = launch_to_float(d_M, reinterpret_cast<float *>(base + mf_off), (long long)D * N, st);
     if (e == cudaSuccess)
         e = launch_lanczos(reinterpret_cast<const LzChain *>(base), 1, S, P.L + 1, fp32, kNoallocCluster, kNoallocEta,
                            st);

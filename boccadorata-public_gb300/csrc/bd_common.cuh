@@ -59,6 +59,7 @@ struct LzChain {
     int S;                  // pole rows per CTA (multiple of 4)
     const double *E;        // [N]   sorted energies
     const double *M;        // [D][N] sorted couplings
+    const float *Mf;        // [D][N] FP32 copy of M (read by the FP32-vector form only)
     const double *piv;      // [n_used][D] normalised pivots in use order
     const int *start;       // [n_used + 1] first Lanczos index of each pivot chain
     const int *last;        // [n_used] last index of each chain (may exceed L-1)

@@ -13,12 +13,13 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
                         double *M);
 __global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long long *out_off, double *out);
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
-                              const double *Ein, const double *Min, double *Eout, double *Mout);
+                              const double *Ein, const double *Min, double *Eout, double *Mout, float *Mfout);
 __global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows);
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,
                            double eta, cudaStream_t st);
 size_t lanczos_smem_bytes(int S, int rmax);
+cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStream_t st);
 
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                          int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st);

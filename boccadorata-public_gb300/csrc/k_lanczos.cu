@@ -11,7 +11,11 @@
 // classical Gram-Schmidt projection (two streaming passes over the stored
 // vectors: dot products, then the update), repeated while a sweep removes more
 // than 1 - 1/sqrt(2) of the remaining norm (the Daniel-Gragg-Kaufman-Stewart
-// criterion), at most four sweeps.  On the degenerate unperturbed spectra the
+// criterion), at most four sweeps.  A continuing chain first projects out only
+// v_{j-1}, v_{j-2} and the last vector of each earlier chain, the only vectors on
+// which E v_{j-1} has more than rounding-size components; the full sweep that
+// follows then removes little, so one full sweep per step is the common case
+// instead of two.  On the degenerate unperturbed spectra the
 // chains break down every few steps and, with few distinct pole energies, the
 // reachable subspace (E is diagonal, so the support of M.p never grows) can be
 // spanned completely; a single sweep then leaves the new vectors far from
@@ -86,9 +90,15 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // Slice of a CTA: S pole rows starting at rank*S, S a multiple of 4; rows past N are
 // zero in every vector (E, w, V), so the vector loads need no tail handling.
 //
-// Shared-memory layout (doubles): Es[S] | w[S] | wc[S] | A[rmax] (dot partials) |
-// c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | Bn[1] (norm partial) |
-// red[kLzWarps * kMaxScal] | touched[S] bytes
+// Shared-memory layout: doubles A[rmax] (dot partials) | c[rmax] (totals) |
+// Bs[kMaxScal] (scalar partials) | Bn[2] (norm partial) | red[kLzWarps * kMaxScal],
+// then CT (the vectors' arithmetic type) Es[S] | w[S], then touched[S] bytes.
+//
+// Arithmetic: with FP64 vectors everything is FP64.  With FP32 vectors every
+// per-pole operation (products, the update, the per-thread partial sums of the dot
+// products, norms and scalars) is FP32, and only the sums across threads, warps and
+// CTAs are FP64: on this GPU FP64 issues at 1/64 of the FP32 rate, and a per-pole
+// FP64 operation would cost more than the whole FP32 sweep.
 template <typename VT>
 __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
     using CT = typename LzTraits<VT>::CT;
@@ -107,21 +117,24 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     extern __shared__ double sm[];
-    double *Es = sm;
-    double *w = Es + S;
-    CT *wc = reinterpret_cast<CT *>(w + S);
-    double *A = w + 2 * S;
+    double *A = sm;
     double *c = A + rmax;
     double *Bs = c + rmax;
     double *Bn = Bs + kMaxScal;
-    double *red = Bn + 1;
-    unsigned char *touched = reinterpret_cast<unsigned char *>(red + kLzWarps * kMaxScal);
+    double *red = Bn + 2;
+    CT *Es = reinterpret_cast<CT *>(red + kLzWarps * kMaxScal);   // 16-byte aligned: 2 rmax + 290 doubles before
+    CT *w = Es + S;
+    unsigned char *touched = reinterpret_cast<unsigned char *>(w + S);
     __shared__ double tot[kMaxScal];
     __shared__ double s_n2;
     __shared__ int s_kmin;
+    __shared__ int lt[16];       // vectors of a local pass
+    __shared__ int s_nl;
 
     VT *V = reinterpret_cast<VT *>(C.V);
-    for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? C.E[i0 + i] : 0.0; touched[i] = 0; }
+    const CT *Mc = reinterpret_cast<const CT *>(sizeof(CT) == 4 ? static_cast<const void *>(C.Mf)
+                                                                  : static_cast<const void *>(C.M));
+    for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? (CT)C.E[i0 + i] : (CT)0; touched[i] = 0; }
     const double tau = (sizeof(VT) == 4) ? 1e-22 : 1e-48;
 
     // block-wide sum of one double per thread, result in every thread
@@ -148,83 +161,96 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 double s = 0.0;
                 if (i < ns)
                     for (int d = 0; d < D; ++d) s = __dadd_rn(s, __dmul_rn(C.M[(size_t)d * N + i0 + i], p[d]));
-                w[i] = s;
+                w[i] = (CT)s;
             }
         } else {
             const VT *vp = V + (size_t)(j - 1) * C.ld + i0;
-            for (int i = tid; i < S; i += kLzThreads) w[i] = (double)vp[i] * Es[i];
+            for (int i = tid; i < S; i += kLzThreads) w[i] = (CT)vp[i] * Es[i];
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
         bool done = false;         // step finished by an untouched-pole unit vector
         double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
-            int pass = 0;
+            int pass = 0, nfull = 0;
             double wn2_first = 0.0;
+            // A continuing chain's w = E v_{j-1} has large components only on v_{j-1}, v_{j-2}
+            // and the last vector of every earlier chain (the fishbone couplings); everything
+            // else is rounding.  The first pass projects out just those few vectors, then
+            // full sweeps follow (at least one), each repeated under the DGKS criterion.
+            bool local = !newv && attempt == 0 && j > 0;
             for (;;) {
+                if (local && tid == 0) {
+                    int n = 0;
+                    lt[n++] = j - 1;
+                    if (j >= 2) lt[n++] = j - 2;
+                    for (int q = 0; q < k; ++q)
+                        if (C.last[q] < j - 2) lt[n++] = C.last[q];
+                    s_nl = n;
+                }
                 __syncthreads();
-                for (int i = tid; i < S; i += kLzThreads) wc[i] = (CT)w[i];
-                __syncthreads();
+                const int nl = local ? s_nl : j;          // vectors in this pass
+                auto tix = [&](int t) { return local ? lt[t] : t; };
                 // (b1) partial dot products <v_t, w> over the slice, one warp per t, 16-byte loads
-                for (int t = warp; t < j; t += kLzWarps) {
-                    const VT *vt = V + (size_t)t * C.ld + i0;
+                for (int t = warp; t < nl; t += kLzWarps) {
+                    const VT *vt = V + (size_t)tix(t) * C.ld + i0;
                     CT acc = 0;
                     for (int q = lane; q < nv; q += 32) {
                         VT x[VW];
                         load16<VT>(vt + q * VW, x);
 #pragma unroll
-                        for (int u = 0; u < VW; ++u) acc += x[u] * wc[q * VW + u];
+                        for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
                     }
                     const double s = warp_sum((double)acc);
                     if (lane == 0) A[t] = s;
                 }
-                double nw = 0.0;
-                for (int i = tid; i < S; i += kLzThreads) nw += w[i] * w[i];
-                nw = block_sum(nw);
-                if (tid == 0) A[j] = nw;
+                CT nwp = 0;
+                for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
+                const double nw = block_sum((double)nwp);
+                if (tid == 0) A[nl] = nw;
                 cluster.sync();
                 // (b2) totals over the cluster, in rank order
-                for (int t = tid; t <= j; t += kLzThreads) {
+                for (int t = tid; t <= nl; t += kLzThreads) {
                     double s = 0.0;
                     for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(A, r)[t];
                     c[t] = s;
                 }
                 __syncthreads();
-                const double wn2_before = c[j];
+                const double wn2_before = c[nl];
                 if (pass == 0) wn2_first = wn2_before;
                 // (b3) w -= sum_t c_t v_t over 16-byte vectors, four rows in flight, and |w|^2
-                double pn = 0.0;
+                CT pn = 0;
                 for (int q = tid; q < nv; q += kLzThreads) {
                     CT acc[VW];
 #pragma unroll
                     for (int u = 0; u < VW; ++u) acc[u] = 0;
                     const VT *base = V + i0 + q * VW;
                     int t = 0;
-                    for (; t + 3 < j; t += 4) {
+                    for (; t + 3 < nl; t += 4) {
                         VT x0[VW], x1[VW], x2[VW], x3[VW];
-                        load16<VT>(base + (size_t)t * C.ld, x0);
-                        load16<VT>(base + (size_t)(t + 1) * C.ld, x1);
-                        load16<VT>(base + (size_t)(t + 2) * C.ld, x2);
-                        load16<VT>(base + (size_t)(t + 3) * C.ld, x3);
+                        load16<VT>(base + (size_t)tix(t) * C.ld, x0);
+                        load16<VT>(base + (size_t)tix(t + 1) * C.ld, x1);
+                        load16<VT>(base + (size_t)tix(t + 2) * C.ld, x2);
+                        load16<VT>(base + (size_t)tix(t + 3) * C.ld, x3);
                         const CT c0 = (CT)c[t], c1 = (CT)c[t + 1], c2 = (CT)c[t + 2], c3 = (CT)c[t + 3];
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
                     }
-                    for (; t < j; ++t) {
+                    for (; t < nl; ++t) {
                         VT x0[VW];
-                        load16<VT>(base + (size_t)t * C.ld, x0);
+                        load16<VT>(base + (size_t)tix(t) * C.ld, x0);
                         const CT c0 = (CT)c[t];
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
                     }
 #pragma unroll
                     for (int u = 0; u < VW; ++u) {
-                        const double wi = w[q * VW + u] - (double)acc[u];
+                        const CT wi = w[q * VW + u] - acc[u];
                         w[q * VW + u] = wi;
                         pn += wi * wi;
                     }
                 }
-                pn = block_sum(pn);
-                if (tid == 0) Bn[0] = pn;
+                const double pns = block_sum((double)pn);
+                if (tid == 0) Bn[0] = pns;
                 cluster.sync();
                 if (tid == 0) {
                     double s = 0.0;
@@ -233,8 +259,10 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 }
                 __syncthreads();
                 n2 = s_n2;
-                // another sweep while this one removed more than half of the squared norm
-                if (j > 0 && pass < 3 && n2 < eta2 * wn2_before) { ++pass; ++extra; continue; }
+                if (local) { local = false; ++pass; continue; }
+                // another full sweep while this one removed more than half of the squared norm
+                if (nfull++ > 0) ++extra;
+                if (j > 0 && nfull < 4 && n2 < eta2 * wn2_before) { ++pass; continue; }
                 break;
             }
             if (attempt > 0 || !(n2 <= tau * wn2_first || n2 == 0.0)) break;
@@ -270,42 +298,42 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 }
                 done = true;
             } else {
-                for (int i = tid; i < S; i += kLzThreads) w[i] = (i < ns) ? restart_value(i0 + i, j) : 0.0;
+                for (int i = tid; i < S; i += kLzThreads) w[i] = (i < ns) ? (CT)restart_value(i0 + i, j) : (CT)0;
                 injected = true;
             }
             cluster.sync();   // peers have read s_kmin before it can change again
         }
         if (done) continue;
-        // (c) alpha, m, g of the final w (FP64, once per step; source/BcDor-Lanczos.cpp:180-214)
+        // (c) alpha, m, g of the final w (once per step; source/BcDor-Lanczos.cpp:180-214)
         const int nq = k;
         const int nsc = 1 + D + nq;
         {
-            double sa = 0.0, sm_[8], sg[8];
+            CT sa = 0, sm_[8], sg[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) { sm_[q] = 0.0; sg[q] = 0.0; }
+            for (int q = 0; q < 8; ++q) { sm_[q] = 0; sg[q] = 0; }
             for (int i = tid; i < ns; i += kLzThreads) {
-                const double wi = w[i], e = Es[i];
+                const CT wi = w[i], e = Es[i];
                 sa += e * wi * wi;
 #pragma unroll
                 for (int d = 0; d < 8; ++d)
-                    if (d < D) sm_[d] += C.M[(size_t)d * N + i0 + i] * wi;
+                    if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
-                    if (q < nq) sg[q] += e * (double)V[(size_t)C.last[q] * C.ld + i0 + i] * wi;
+                    if (q < nq) sg[q] += e * (CT)V[(size_t)C.last[q] * C.ld + i0 + i] * wi;
             }
-            sa = warp_sum(sa);
-            if (lane == 0) red[warp * kMaxScal] = sa;
+            const double sat = warp_sum((double)sa);
+            if (lane == 0) red[warp * kMaxScal] = sat;
 #pragma unroll
             for (int d = 0; d < 8; ++d) {
                 if (d < D) {
-                    const double x = warp_sum(sm_[d]);
+                    const double x = warp_sum((double)sm_[d]);
                     if (lane == 0) red[warp * kMaxScal + 1 + d] = x;
                 }
             }
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 if (q < nq) {
-                    const double x = warp_sum(sg[q]);
+                    const double x = warp_sum((double)sg[q]);
                     if (lane == 0) red[warp * kMaxScal + 1 + D + q] = x;
                 }
             }
@@ -327,10 +355,19 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         const double xa = tot[0] / n2;
         const double xb = sqrt(n2);
         VT *vj = V + (size_t)j * C.ld + i0;
-        for (int i = tid; i < S; i += kLzThreads) {
-            const VT v = (VT)(w[i] / xb);
-            vj[i] = v;
-            touched[i] |= (v != (VT)0);
+        if constexpr (sizeof(VT) == 4) {
+            const float inv = (float)(1.0 / xb);
+            for (int i = tid; i < S; i += kLzThreads) {
+                const VT v = w[i] * inv;
+                vj[i] = v;
+                touched[i] |= (v != (VT)0);
+            }
+        } else {
+            for (int i = tid; i < S; i += kLzThreads) {
+                const VT v = (VT)(w[i] / xb);
+                vj[i] = v;
+                touched[i] |= (v != (VT)0);
+            }
         }
         if (rank == 0 && tid == 0) {
             double *row = C.out + (size_t)j * NT;
@@ -347,7 +384,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 }
 
 size_t lanczos_smem_bytes(int S, int rmax) {
-    return sizeof(double) * ((size_t)3 * S + 2 * (size_t)rmax + kMaxScal + 1 + (size_t)kLzWarps * kMaxScal) +
+    // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
+    return sizeof(double) * ((size_t)2 * S + 2 * (size_t)rmax + kMaxScal + 2 + (size_t)kLzWarps * kMaxScal) +
            (size_t)S + 16;
 }
 
@@ -382,4 +420,17 @@ cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int 
     return cudaLaunchKernelEx(&cfg, k_lanczos<double>, d_chains, nchains, rmax, eta * eta);
 }
 
+}  // namespace bd
+
+namespace bd {
+__global__ void k_to_float(const double *in, float *out, long long n) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
+}
+
+cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
 }  // namespace bd

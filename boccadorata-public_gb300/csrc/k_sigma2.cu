@@ -169,9 +169,10 @@ __global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long lo
     }
 }
 
-// Gather rows in a given order into separate SoA arrays (used after the sort).
+// Gather rows in a given order into separate SoA arrays (used after the sort), plus an
+// FP32 copy of the couplings for the FP32-vector Lanczos form.
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
-                              const double *Ein, const double *Min, double *Eout, double *Mout) {
+                              const double *Ein, const double *Min, double *Eout, double *Mout, float *Mfout) {
     const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (idx >= n) return;
     const long long g = n0 + idx;
@@ -183,7 +184,11 @@ __global__ void k_permute_soa(const int *perm, long long n0, long long n, const 
     const long long k = g - off;
     const long long src = perm[g];  // global source index (same segment)
     Eout[g] = Ein[src];
-    for (int d = 0; d < C.D; ++d) Mout[moff + (long long)d * N + k] = Min[moff + (long long)d * N + (src - off)];
+    for (int d = 0; d < C.D; ++d) {
+        const double m = Min[moff + (long long)d * N + (src - off)];
+        Mout[moff + (long long)d * N + k] = m;
+        Mfout[moff + (long long)d * N + k] = (float)m;
+    }
 }
 
 // AoS rows [E, S2, M_0..] of one channel, for host copies in the reference layout.

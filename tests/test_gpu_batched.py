@@ -60,7 +60,11 @@ def test_mixed_precision_within_targets(bdmod, problems):
         for tag in ("qp", "qh"):
             e, z = strong_diffs(ref[ish][tag], r[tag], zmin=1e-4, etol=1e-5)
             assert e * 300.0 < 1e-3 and z < 1e-5, (ish, tag, e, z)      # |W| < 300 MeV
-        np.testing.assert_allclose(r["koltun"], ref[ish]["koltun"], rtol=1e-6, atol=1e-8)
+        # Koltun sums: the energy-weighted ones within 1 keV per unit of hole strength,
+        # the strength sum within the spectroscopic-factor target
+        x3 = abs(ref[ish]["koltun"][2]) + 1e-12
+        dk = np.abs(r["koltun"] - ref[ish]["koltun"])
+        assert dk[0] <= 1e-3 * x3 and dk[1] <= 1e-3 * x3 and dk[2] <= 1e-5 * x3, (ish, dk, x3)
     ctx.close()
 
 
