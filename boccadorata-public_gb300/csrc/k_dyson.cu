@@ -85,8 +85,25 @@ __device__ inline double block_sum(double v, double *scratch) {
     return s;
 }
 
-// Shared layout (doubles): v[nmax] | wfull[nmax] | wpart[RS] | part[4] | scratch[32]
-__global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int njobs, int nmax) {
+// Symmetric Householder reduction on the lower triangle.  Row i belongs to CTA
+// (i mod CL) of the cluster, so the shrinking triangle stays balanced; inside a
+// CTA the warps take its rows in turn.  One step k (trailing size m = n - k - 1):
+//   1. every CTA reads column k below the diagonal and forms the reflector v and
+//      tau itself (identical data and order, so identical results and branches);
+//   2. one pass over the own rows gives the symmetric product A v: each row's
+//      dot product (warp sum) and its transposed contributions A_ij v_i to p_j,
+//      gathered in per-warp shared partial vectors (shared atomics only when eight
+//      copies do not fit);
+//   3. the CTAs' partial vectors are summed through distributed shared memory in
+//      rank order; w = tau A v - (tau^2/2)(v^T A v) v;
+//   4. the own rows' lower parts get A -= v w^T + w v^T.
+// Two FP64 multiply-adds per stored element and step (against three with full
+// storage), two cluster barriers per step.  The reflector is kept in row k,
+// columns > k (unused by the lower triangle), for the back-transformation.
+//
+// Shared layout (doubles): v[nmax] | p[nmax] | pc[nmax] | pt[npriv][nmax] |
+// pr[nmax / CL + 1] | scratch[32]
+__global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int njobs, int nmax, int npriv) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
@@ -94,67 +111,104 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.n;
-    const int RS = (nmax + CL - 1) / CL;   // rows per CTA (upper bound for smem)
-    const int rs = (n + CL - 1) / CL;
-    const int r0 = rank * rs, r1 = min(n, r0 + rs);
     extern __shared__ double sm[];
     double *v = sm;
-    double *wfull = v + nmax;
-    double *wpart = wfull + nmax;
-    double *part = wpart + RS;
-    double *scratch = part + 4;
+    double *p = v + nmax;
+    double *pc = p + nmax;
+    double *pt = pc + nmax;
+    double *pr = pt + (size_t)npriv * nmax;
+    double *scratch = pr + (nmax / CL + 1);
     double *A = J.A;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kWarps = kTdThreads / 32;
+    const bool priv = (npriv >= kWarps);
+    double *ptw = pt + (size_t)(warp % npriv) * nmax;
     for (int k = 0; k + 2 < n; ++k) {
         const int b0 = k + 1, m = n - b0;
-        // reflector from column k (= row k by symmetry), computed identically by every CTA
+        // 1. reflector from column k (rows > k)
         double sig = 0.0;
-        for (int t = 1 + tid; t < m; t += kTdThreads) { double x = __ldcg(A + (size_t)k * n + b0 + t); sig += x * x; }
+        for (int t = 1 + tid; t < m; t += kTdThreads) { const double x = __ldcg(A + (size_t)(b0 + t) * n + k); sig += x * x; }
         sig = block_sum(sig, scratch);
-        const double alpha = __ldcg(A + (size_t)k * n + b0);
+        const double alpha = __ldcg(A + (size_t)b0 * n + k);
         double tau = 0.0, beta = alpha;
         if (sig != 0.0) {
             beta = -copysign(sqrt(alpha * alpha + sig), alpha);
             tau = (beta - alpha) / beta;
             const double scal = 1.0 / (alpha - beta);
-            for (int t = tid; t < m; t += kTdThreads) v[t] = (t == 0) ? 1.0 : __ldcg(A + (size_t)k * n + b0 + t) * scal;
+            for (int t = tid; t < m; t += kTdThreads) v[t] = (t == 0) ? 1.0 : __ldcg(A + (size_t)(b0 + t) * n + k) * scal;
         }
-        __syncthreads();
         if (rank == 0 && tid == 0) { J.e[k] = beta; J.tau[k] = tau; J.d[k] = __ldcg(A + (size_t)k * n + k); }
         if (sig != 0.0) {
-            // p_i = tau * sum_j A_ij v_j for own rows i >= b0; partial p.v
-            const int ra = max(r0, b0);
-            const int warp = tid >> 5, lane = tid & 31;
-            double pv = 0.0;
-            for (int i = ra + warp; i < r1; i += kTdThreads / 32) {
-                const double *Ai = A + (size_t)i * n + b0;
-                double s = 0.0;
-                for (int t = lane; t < m; t += 32) s += Ai[t] * v[t];
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                const double p = tau * s;
-                if (lane == 0) { wpart[i - r0] = p; pv += p * v[i - b0]; }
-            }
-            pv = block_sum(pv, scratch);
-            if (tid == 0) part[0] = pv;
-            cluster.sync();
-            double K = 0.0;
-            for (int q = 0; q < CL; ++q) K += cluster.map_shared_rank(part, q)[0];
-            // w_i = p_i - (tau/2) K v_i for own rows
-            for (int i = ra + tid; i < r1; i += kTdThreads) wpart[i - r0] -= 0.5 * tau * K * v[i - b0];
-            cluster.sync();
-            // all-gather w over the trailing index range
-            for (int t = tid; t < m; t += kTdThreads) {
-                const int i = b0 + t, owner = i / rs;
-                wfull[t] = cluster.map_shared_rank(wpart, owner)[i - owner * rs];
+            for (int t = tid; t < npriv * m; t += kTdThreads) pt[(size_t)(t / m) * nmax + t % m] = 0.0;
+            __syncthreads();
+            // 2. own rows i = first, first + CL, ...; row part and transposed part of A v
+            const int first = b0 + ((rank - b0 % CL) % CL + CL) % CL;
+            for (int i = first + warp * CL; i < n; i += CL * kWarps) {
+                const double *Ai = A + (size_t)i * n;
+                const double vi = v[i - b0];
+                double rs = 0.0;
+                int j = b0 + lane;
+                for (; j + 96 < i; j += 128) {
+                    const double a0 = __ldcg(Ai + j), a1 = __ldcg(Ai + j + 32), a2 = __ldcg(Ai + j + 64),
+                                 a3 = __ldcg(Ai + j + 96);
+                    const int t = j - b0;
+                    rs += a0 * v[t] + a1 * v[t + 32] + a2 * v[t + 64] + a3 * v[t + 96];
+                    if (priv) {
+                        ptw[t] += a0 * vi; ptw[t + 32] += a1 * vi; ptw[t + 64] += a2 * vi; ptw[t + 96] += a3 * vi;
+                    } else {
+                        atomicAdd(ptw + t, a0 * vi); atomicAdd(ptw + t + 32, a1 * vi);
+                        atomicAdd(ptw + t + 64, a2 * vi); atomicAdd(ptw + t + 96, a3 * vi);
+                    }
+                }
+                for (; j <= i; j += 32) {
+                    const double a = __ldcg(Ai + j);
+                    rs += a * v[j - b0];
+                    if (j < i) {
+                        if (priv) ptw[j - b0] += a * vi;
+                        else atomicAdd(ptw + (j - b0), a * vi);
+                    }
+                }
+                for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+                if (lane == 0) pr[(i - first) / CL] = rs;
             }
             __syncthreads();
-            // A_ij -= v_i w_j + w_i v_j on own rows
-            for (int i = ra; i < r1; ++i) {
-                const double vi = v[i - b0], wi = wfull[i - b0];
-                double *Ai = A + (size_t)i * n + b0;
-                for (int t = tid; t < m; t += kTdThreads) Ai[t] -= vi * wfull[t] + wi * v[t];
+            // this CTA's share of A v: transposed partials plus its own rows' sums
+            for (int t = tid; t < m; t += kTdThreads) {
+                double s = 0.0;
+                for (int q = 0; q < npriv; ++q) s += pt[(size_t)q * nmax + t];
+                const int i = b0 + t;
+                if (i >= first && (i - first) % CL == 0) s += pr[(i - first) / CL];
+                pc[t] = s;
             }
-            // keep the reflector in row k (columns > k) for the back-transformation
+            cluster.sync();
+            // 3. p = tau A v summed over the cluster in rank order; w = p - (tau/2)(p.v) v
+            double kv = 0.0;
+            for (int t = tid; t < m; t += kTdThreads) {
+                double s = 0.0;
+                for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(pc, r)[t];
+                s *= tau;
+                p[t] = s;
+                kv += s * v[t];
+            }
+            const double K = block_sum(kv, scratch);
+            for (int t = tid; t < m; t += kTdThreads) p[t] -= 0.5 * tau * K * v[t];
+            __syncthreads();
+            // 4. A_ij -= v_i w_j + w_i v_j on the own rows, j <= i
+            for (int i = first + warp * CL; i < n; i += CL * kWarps) {
+                double *Ai = A + (size_t)i * n;
+                const double vi = v[i - b0], wi = p[i - b0];
+                int j = b0 + lane;
+                for (; j + 96 <= i; j += 128) {
+                    const int t = j - b0;
+                    const double a0 = __ldcg(Ai + j), a1 = __ldcg(Ai + j + 32), a2 = __ldcg(Ai + j + 64),
+                                 a3 = __ldcg(Ai + j + 96);
+                    Ai[j] = a0 - (vi * p[t] + wi * v[t]);
+                    Ai[j + 32] = a1 - (vi * p[t + 32] + wi * v[t + 32]);
+                    Ai[j + 64] = a2 - (vi * p[t + 64] + wi * v[t + 64]);
+                    Ai[j + 96] = a3 - (vi * p[t + 96] + wi * v[t + 96]);
+                }
+                for (; j <= i; j += 32) Ai[j] = __ldcg(Ai + j) - (vi * p[j - b0] + wi * v[j - b0]);
+            }
             if (rank == 0)
                 for (int t = tid; t < m; t += kTdThreads) A[(size_t)k * n + b0 + t] = v[t];
         }
@@ -173,9 +227,17 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     cluster.sync();
 }
 
+// Per-warp partial vectors that fit next to the other arrays (8 = one per warp).
+int tridiag_npriv(int nmax, int cluster) {
+    const size_t fixed = (size_t)3 * nmax + (size_t)(nmax / cluster + 1) + 32;
+    const size_t cap = (size_t)200 * 1024 / sizeof(double);
+    int np = 8;
+    while (np > 1 && fixed + (size_t)np * nmax > cap) --np;
+    return np;
+}
+
 size_t tridiag_smem_bytes(int nmax, int cluster) {
-    const int RS = (nmax + cluster - 1) / cluster;
-    return sizeof(double) * ((size_t)2 * nmax + RS + 4 + 32);
+    return sizeof(double) * ((size_t)(3 + tridiag_npriv(nmax, cluster)) * nmax + (size_t)(nmax / cluster + 1) + 32);
 }
 
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
@@ -200,7 +262,7 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    e = cudaLaunchKernelEx(&cfg, k_tridiag, d_jobs, njobs, nmax);
+    e = cudaLaunchKernelEx(&cfg, k_tridiag, d_jobs, njobs, nmax, tridiag_npriv(nmax, cluster));
     if (e != cudaSuccess) return e;
     (void)Dmax;
     return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);

@@ -92,7 +92,8 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 //
 // Shared-memory layout: doubles A[rmax] (dot partials) | c[rmax] (totals) |
 // Bs[kMaxScal] (scalar partials) | Bn[2] (norm partial) | red[kLzWarps * kMaxScal],
-// then CT (the vectors' arithmetic type) Es[S] | w[S], then touched[S] bytes.
+// then CT (the vectors' arithmetic type) cf[rmax rounded up to 4] (totals in CT) |
+// Es[S] | w[S], then touched[S] bytes.
 //
 // Arithmetic: with FP64 vectors everything is FP64.  With FP32 vectors every
 // per-pole operation (products, the update, the per-thread partial sums of the dot
@@ -122,7 +123,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     double *Bs = c + rmax;
     double *Bn = Bs + kMaxScal;
     double *red = Bn + 2;
-    CT *Es = reinterpret_cast<CT *>(red + kLzWarps * kMaxScal);   // 16-byte aligned: 2 rmax + 290 doubles before
+    CT *cf = reinterpret_cast<CT *>(red + kLzWarps * kMaxScal);   // 16-byte aligned: 2 rmax + 290 doubles before
+    CT *Es = cf + (rmax + 3) / 4 * 4;
     CT *w = Es + S;
     unsigned char *touched = reinterpret_cast<unsigned char *>(w + S);
     __shared__ double tot[kMaxScal];
@@ -200,8 +202,10 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
                     }
-                    const double s = warp_sum((double)acc);
-                    if (lane == 0) A[t] = s;
+                    // lane partials combined in CT: FP32 shuffles for FP32 vectors
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    if (lane == 0) A[t] = (double)acc;
                 }
                 CT nwp = 0;
                 for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
@@ -213,6 +217,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     double s = 0.0;
                     for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(A, r)[t];
                     c[t] = s;
+                    cf[t] = (CT)s;
                 }
                 __syncthreads();
                 const double wn2_before = c[nl];
@@ -231,14 +236,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                         load16<VT>(base + (size_t)tix(t + 1) * C.ld, x1);
                         load16<VT>(base + (size_t)tix(t + 2) * C.ld, x2);
                         load16<VT>(base + (size_t)tix(t + 3) * C.ld, x3);
-                        const CT c0 = (CT)c[t], c1 = (CT)c[t + 1], c2 = (CT)c[t + 2], c3 = (CT)c[t + 3];
+                        const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
                     }
                     for (; t < nl; ++t) {
                         VT x0[VW];
                         load16<VT>(base + (size_t)tix(t) * C.ld, x0);
-                        const CT c0 = (CT)c[t];
+                        const CT c0 = cf[t];
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
                     }
@@ -385,7 +390,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
 size_t lanczos_smem_bytes(int S, int rmax) {
     // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
-    return sizeof(double) * ((size_t)2 * S + 2 * (size_t)rmax + kMaxScal + 2 + (size_t)kLzWarps * kMaxScal) +
+    return sizeof(double) * ((size_t)2 * S + 2 * (size_t)rmax + (size_t)(rmax + 3) / 4 * 4 + kMaxScal + 2 +
+                             (size_t)kLzWarps * kMaxScal) +
            (size_t)S + 16;
 }
 
