@@ -4,7 +4,9 @@
 // components x_k[0:D] of the corresponding eigenvector of A.
 //
 //   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows)
-//   k_bisect  W_k by bisection on Sturm counts, one thread per eigenvalue
+//   k_bisect  W_k by bisection on Sturm counts, one thread per eigenvalue: an FP32
+//             bracketing phase (FP64 issues at 1/64 of the FP32 rate), checked and
+//             finished in FP64 to max(1e-12 |W|, 1e-13 |T|)
 //   k_invit   y_k by inverse iteration on T - W_k I (tridiagonal LU with partial
 //             pivoting), one thread per eigenvalue, each from its own start vector
 //   k_cluster_orth  eigenvalues closer than 1e-6 |T| form a cluster (the Dyson
@@ -65,6 +67,20 @@ __global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int nj
     }
 }
 
+// 1/q by Newton-Raphson, r <- r + r (1 - q r), from the FP32 reciprocal: two steps
+// take the 24-bit seed past FP64 precision.  Outside the FP32 range, plain division.
+__device__ inline double rcp_nr(double q) {
+    const double aq = fabs(q);
+    if (aq > 1e-36 && aq < 1e36) {
+        double r = (double)__frcp_rn((float)q);
+        double t = fma(-q, r, 1.0);
+        r = fma(r, t, r);
+        t = fma(-q, r, 1.0);
+        return fma(r, t, r);
+    }
+    return 1.0 / q;
+}
+
 // number of eigenvalues of T strictly below x (negative pivots of the LDL^T of T - x I)
 __device__ inline int sturm_count(const double *d, const double *e2, int n, double x, double pivmin) {
     int c = 0;
@@ -72,25 +88,46 @@ __device__ inline int sturm_count(const double *d, const double *e2, int n, doub
     if (fabs(q) < pivmin) q = -pivmin;
     c += (q < 0.0);
     for (int i = 1; i < n; ++i) {
-        q = (d[i] - x) - e2[i - 1] / q;
+        q = fma(-e2[i - 1], rcp_nr(q), d[i] - x);
         if (fabs(q) < pivmin) q = -pivmin;
         c += (q < 0.0);
     }
     return c;
 }
 
+__device__ inline int sturm_count_f(const float *d, const float *e2, int n, float x, float pivmin) {
+    int c = 0;
+    float q = d[0] - x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    c += (q < 0.0f);
+    for (int i = 1; i < n; ++i) {
+        q = (d[i] - x) - e2[i - 1] / q;
+        if (fabsf(q) < pivmin) q = -pivmin;
+        c += (q < 0.0f);
+    }
+    return c;
+}
+
 // ------------------------------------------------------------------ K4c
 // One thread per eigenvalue index of every matrix; row_first maps a global index
-// to its matrix.  e2 (squared off-diagonals) is formed by the first thread of each
-// matrix into the tau array's slot, which k_qrows has consumed.
-__global__ void k_bisect_prep(const DyJob *jobs, int njobs) {
+// to its matrix.  e2 (squared off-diagonals) goes into the tau array's slot, which
+// k_qrows has consumed, and FP32 copies of d and e2 into the start of the job's
+// work area (free until k_invit).
+__global__ void k_bisect_prep(const DyJob *jobs, int njobs, double *work, const long long *work_first) {
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    for (int i = threadIdx.x; i < J.n; i += blockDim.x) J.tau[i] = (i + 1 < J.n) ? J.e[i] * J.e[i] : 0.0;
+    float *f = reinterpret_cast<float *>(work + work_first[jid]);
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) {
+        const double e2 = (i + 1 < J.n) ? J.e[i] * J.e[i] : 0.0;
+        J.tau[i] = e2;
+        f[i] = (float)J.d[i];
+        f[J.n + i] = (float)e2;
+    }
 }
 
-__global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total) {
+__global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total,
+                         const double *work, const long long *work_first) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total) return;
     int lo = 0, hi = njobs - 1;
@@ -107,11 +144,26 @@ __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_firs
     tnorm = fmax(fabs(glo), fabs(ghi));
     const double eps = 2.220446049250313e-16;
     const double pivmin = fmax(tnorm * 1e-300, 1e-290);
-    double a = glo - 2.0 * eps * tnorm - 1e-300, b = ghi + 2.0 * eps * tnorm + 1e-300;
-    // W_k is the unique x with count(x) <= k < count(x + 0)
+    const double g0 = glo - 2.0 * eps * tnorm - 1e-300, g1 = ghi + 2.0 * eps * tnorm + 1e-300;
+    // W_k is the unique x with count(x) <= k < count(x + 0).
+    // FP32 bracket to 1e-5 |T| on the rounded matrix (its eigenvalues move by ~1e-7 |T|)
+    const float *df = reinterpret_cast<const float *>(work + work_first[lo]), *e2f = df + n;
+    float e2max = 1.0f;
+    for (int i = 0; i + 1 < n; ++i) e2max = fmaxf(e2max, e2f[i]);
+    const float pivf = 1e-30f * e2max;
+    float af = (float)g0, bf = (float)g1;
+    for (int it = 0; it < 40 && (double)bf - (double)af > 1e-5 * tnorm; ++it) {
+        const float mid = 0.5f * (af + bf);
+        if (mid == af || mid == bf) break;
+        if (sturm_count_f(df, e2f, n, mid, pivf) > k) bf = mid; else af = mid;
+    }
+    // widen by 2e-5 |T|, check in FP64, else start over from the Gershgorin interval
+    const double margin = 2e-5 * tnorm;
+    double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
+    if (!(sturm_count(d, e2, n, a, pivmin) <= k && sturm_count(d, e2, n, b, pivmin) > k)) { a = g0; b = g1; }
     for (int it = 0; it < 200; ++it) {
         const double mid = 0.5 * (a + b);
-        if (b - a <= 2.0 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid == a || mid == b) break;
+        if (b - a <= fmax(1e-12 * fmax(fabs(a), fabs(b)), 1e-13 * tnorm) + pivmin || mid == a || mid == b) break;
         if (sturm_count(d, e2, n, mid, pivmin) > k) b = mid; else a = mid;
     }
     J.sol[(size_t)k * (2 + J.D)] = 0.5 * (a + b);   // eigenvalue parked in the W slot, ascending
@@ -308,11 +360,19 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.n, D = J.D, NS = 2 + D;
-    const double *st = J.R + (size_t)D * n;
+    double *st = J.R + (size_t)D * n;
     __shared__ int nbelow;
     if (threadIdx.x == 0) {
+        // independent bisections stop within their tolerance, so members of an exact
+        // degeneracy can come out in either order: restore the ascending order
         int c = 0;
-        for (int k = 0; k < n; ++k) c += !(st[(size_t)k * NS] > J.efermi);
+        double wmax = -INFINITY;
+        for (int k = 0; k < n; ++k) {
+            double w = st[(size_t)k * NS];
+            if (w < wmax) { w = wmax; st[(size_t)k * NS] = w; }
+            wmax = w;
+            c += !(w > J.efermi);
+        }
         nbelow = c;
     }
     __syncthreads();
@@ -346,9 +406,9 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
 cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                        double *work, const long long *d_work_first, cudaStream_t st) {
     k_qrows<<<njobs, kEigThreads, 0, st>>>(d_jobs, njobs);
-    k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs);
+    k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs, work, d_work_first);
     const unsigned nb = (unsigned)((total_rows + 127) / 128);
-    k_bisect<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_bisect<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
     k_invit<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
     k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_post<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
