@@ -195,13 +195,29 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 // (b1) partial dot products <v_t, w> over the slice, one warp per t, 16-byte loads
                 for (int t = warp; t < nl; t += kLzWarps) {
                     const VT *vt = V + (size_t)tix(t) * C.ld + i0;
-                    CT acc = 0;
-                    for (int q = lane; q < nv; q += 32) {
+                    CT acc = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+                    int q = lane;
+                    for (; q + 96 < nv; q += 128) {   // four 16-byte loads in flight per lane
+                        VT x0[VW], x1[VW], x2[VW], x3[VW];
+                        load16<VT>(vt + q * VW, x0);
+                        load16<VT>(vt + (q + 32) * VW, x1);
+                        load16<VT>(vt + (q + 64) * VW, x2);
+                        load16<VT>(vt + (q + 96) * VW, x3);
+#pragma unroll
+                        for (int u = 0; u < VW; ++u) {
+                            acc += x0[u] * w[q * VW + u];
+                            acc1 += x1[u] * w[(q + 32) * VW + u];
+                            acc2 += x2[u] * w[(q + 64) * VW + u];
+                            acc3 += x3[u] * w[(q + 96) * VW + u];
+                        }
+                    }
+                    for (; q < nv; q += 32) {
                         VT x[VW];
                         load16<VT>(vt + q * VW, x);
 #pragma unroll
                         for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
                     }
+                    acc += (acc1 + acc2) + acc3;
                     // lane partials combined in CT: FP32 shuffles for FP32 vectors
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -222,7 +238,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 __syncthreads();
                 const double wn2_before = c[nl];
                 if (pass == 0) wn2_first = wn2_before;
-                // (b3) w -= sum_t c_t v_t over 16-byte vectors, four rows in flight, and |w|^2
+                // (b3) w -= sum_t c_t v_t over 16-byte vectors, eight rows in flight, and |w|^2
                 CT pn = 0;
                 for (int q = tid; q < nv; q += kLzThreads) {
                     CT acc[VW];
@@ -230,6 +246,17 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     for (int u = 0; u < VW; ++u) acc[u] = 0;
                     const VT *base = V + i0 + q * VW;
                     int t = 0;
+                    for (; t + 7 < nl; t += 8) {      // eight rows in flight
+                        VT x[8][VW];
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) load16<VT>(base + (size_t)tix(t + r) * C.ld, x[r]);
+#pragma unroll
+                        for (int r = 0; r < 8; ++r) {
+                            const CT cr = cf[t + r];
+#pragma unroll
+                            for (int u = 0; u < VW; ++u) acc[u] += cr * x[r][u];
+                        }
+                    }
                     for (; t + 3 < nl; t += 4) {
                         VT x0[VW], x1[VW], x2[VW], x3[VW];
                         load16<VT>(base + (size_t)tix(t) * C.ld, x0);
