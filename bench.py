@@ -39,8 +39,9 @@ METRIC = "channels solved/s at N_max=10: mixed vs FP64 GPU at <=1 keV qp-energy 
 WORKLOAD = "nmax10_lanczos100"
 CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2, 3, 5, 6
 # Per-launch DRAM traffic of the FP32 Lanczos kernel on this workload, from the ncu
-# capture summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum).
-LANCZOS_TRAFFIC_BYTES = None
+# capture summarised in profiles/k_lanczos_float_nmax10_lanczos100_dram.md
+# (dram__bytes_read.sum 199 794 498 560 + dram__bytes_write.sum 606 455 040).
+LANCZOS_TRAFFIC_BYTES = 200_400_953_600
 
 
 def parse():
