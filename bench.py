@@ -62,6 +62,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def rank_reduce_max(x, dist, device):
+    """Maximum of a per-rank number over all ranks (the slowest rank's step time);
+    x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, channels, step_s):
+    """Channels per second of the whole job: every rank solves its own replica of the
+    workload (the channels share no data), timed by the slowest rank."""
+    return world * channels / step_s
+
+
 # ------------------------------------------------------------------------------------------
 # shared helpers
 # ------------------------------------------------------------------------------------------
@@ -265,11 +282,7 @@ def gpu_arm(args):
             dist.barrier()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rank_reduce_max(x, dist, f"cuda:{local}")
 
     prob = synth.make_workload(args.workload)
     nch = prob.ms.nsubsh
@@ -326,7 +339,7 @@ def gpu_arm(args):
     dev_ms, wall_ms, lz_ms, launches = timed(dict(mixed=True), args.steps, args.warmup)
     clk = clocks.stop() if clocks else None
     step_s = max_over_ranks(dev_ms / 1e3)
-    value = world * nch / step_s
+    value = whole_job_rate(world, nch, step_s)
 
     # ---- the plain FP64 forms
     f64_ms, _, f64_lz, _ = timed(dict(mixed=False), max(2, min(args.steps, 3)), 1)
@@ -354,7 +367,7 @@ def gpu_arm(args):
                 times.append(dt)
         ctx2.close()
         e2e_s = max_over_ranks(statistics.mean(times))
-        e2e = {"value": world * nch / e2e_s, "unit": "channels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        e2e = {"value": whole_job_rate(world, nch, e2e_s), "unit": "channels/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": 1e3 * e2e_s}
 
     if rank != 0:
