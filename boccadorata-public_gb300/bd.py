@@ -15,6 +15,8 @@ not been built, and every call goes through the device.
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
+import importlib
 import math
 import os
 
@@ -56,7 +58,7 @@ class BDError(RuntimeError):
 EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload_problem", "bd_upload_pivots",
             "bd_count_poles", "bd_ehf", "bd_sigma2_build", "bd_lanczos_reduce", "bd_dyson_solve", "bd_run_all",
             "bd_sync", "bd_result_counts", "bd_result_fetch", "bd_result_koltun_all", "bd_last_timings",
-            "bd_dyson_rows", "bd_lanczos_vectors"]
+            "bd_dyson_rows", "bd_lanczos_vectors", "bd_upload_propagator", "bd_dressed_propagator"]
 
 
 def load_library(path: str = LIB_PATH):
@@ -78,6 +80,9 @@ def load_library(path: str = LIB_PATH):
     lib.bd_dyson_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _ip, C.c_int, _dp, _ip, _dp, _dp, C.c_double,
                                   _dp, C.c_int, _ip, _dp, C.c_int, _ip, _dp]
     lib.bd_lanczos_vectors.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, C.c_longlong]
+    lib.bd_upload_propagator.argtypes = [vp, C.POINTER(_Propagator)]
+    lib.bd_dressed_propagator.argtypes = [vp, C.c_double, C.c_int, C.c_int, _ip, _ip, _dp, C.c_int, _dp, C.c_int,
+                                          _dp, _dp, _dp]
     lib.bd_run_all.argtypes = [vp, C.c_int]
     lib.bd_sync.argtypes = [vp]
     lib.bd_result_counts.argtypes = [vp, C.c_int, _ip, _ip]
@@ -165,6 +170,38 @@ class Context:
         if with_pivots and prob.piv is not None:
             self.upload_pivots(prob.piv)
         return self
+
+    def upload_propagator(self, prop):
+        """Replace the input propagator; model space, interaction and pivots stay."""
+        arrs = dict(np=_i(prop.np_), nh=_i(prop.nh), ep=_d(prop.ep if len(prop.ep) else np.zeros(1)),
+                    eh=_d(prop.eh if len(prop.eh) else np.zeros(1)),
+                    fqp=_d(prop.fqp.reshape(-1) if len(prop.ep) else np.zeros(prop.nspb)),
+                    fqh=_d(prop.fqh.reshape(-1) if len(prop.eh) else np.zeros(prop.nspb)))
+        p = _Propagator(prop.nspb, _pi(arrs["np"]), _pi(arrs["nh"]), _pd(arrs["ep"]), _pd(arrs["eh"]),
+                        _pd(arrs["fqp"]), _pd(arrs["fqh"]))
+        self._chk(self.lib.bd_upload_propagator(self.h, C.byref(p)))
+        self.prob = dataclasses.replace(self.prob, prop=prop)
+        return self
+
+    def dressed_propagator(self, z_cut: float, max_frag: int, keep_current: bool = False):
+        """The next iteration's (truncated) propagator from the last run_all; returns it and
+        the reference's quick_n_dirty_diff against the propagator the run used.  Unless
+        keep_current, it becomes the context's input propagator."""
+        ns, nspb = self.prob.ms.nsubsh, self.prob.prop.nspb
+        cnt = [self.result_counts(i) for i in range(ns)]
+        cap_p = max(1, sum(c[0] for c in cnt)); cap_h = max(1, sum(c[1] for c in cnt))
+        npo, nho = np.zeros(ns, np.int32), np.zeros(ns, np.int32)
+        ep, eh = np.zeros(cap_p), np.zeros(cap_h)
+        fqp, fqh = np.zeros(cap_p * nspb), np.zeros(cap_h * nspb)
+        diff = C.c_double()
+        self._chk(self.lib.bd_dressed_propagator(self.h, z_cut, max_frag, 1 if keep_current else 0, _pi(npo), _pi(nho),
+                                                 _pd(ep), cap_p, _pd(eh), cap_h, _pd(fqp), _pd(fqh), C.byref(diff)))
+        a, b = int(npo.sum()), int(nho.sum())
+        synth = importlib.import_module("boccadorata-public_gb300.synth")
+        prop = synth.propagator_from_arrays(nspb, npo, nho, ep[:a], eh[:b], fqp[:a * nspb], fqh[:b * nspb])
+        if not keep_current:
+            self.prob = dataclasses.replace(self.prob, prop=prop)
+        return prop, diff.value
 
     def upload_pivots(self, piv):
         npvt = _i([len(v) for v in piv.vec])
@@ -285,6 +322,11 @@ class Context:
         k = np.zeros(3 * self.prob.ms.nsubsh)
         self._chk(self.lib.bd_result_koltun_all(self.h, _pd(k)))
         return k.reshape(-1, 3)
+
+    def result_counts(self, ish):
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_result_counts(self.h, ish, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def result(self, ish):
         a, b = C.c_int(), C.c_int()

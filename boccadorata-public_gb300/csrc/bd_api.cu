@@ -81,8 +81,10 @@ struct bd_ctx {
     std::vector<S2Block> blocks;
     std::vector<long long> blk_fw_first, blk_bk_first, blk_vp_first;
     long long tot_fw = 0, tot_bk = 0, tot_mfw = 0, tot_mbk = 0, tot_vp = 0;
-    // device
-    std::vector<DevBuf> bufs;
+    // device: bufs follow the propagator, sbufs hold the model space and interaction
+    std::vector<DevBuf> bufs, sbufs;
+    std::vector<DevBuf> *cur = nullptr;   // where dalloc records (nullptr: bufs)
+    bool static_ok = false;
     DevProblem dp{};
     S2Block *d_blocks = nullptr;
     long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr, *d_blk_vp_first = nullptr;
@@ -155,7 +157,7 @@ int dalloc(bd_ctx *ctx, T **p, size_t count) {
     size_t bytes = sizeof(T) * (count > 0 ? count : 1);
     void *q = nullptr;
     CU(cudaMalloc(&q, bytes));
-    ctx->bufs.push_back({q, bytes});
+    (ctx->cur ? *ctx->cur : ctx->bufs).push_back({q, bytes});
     *p = reinterpret_cast<T *>(q);
     return BD_OK;
 }
@@ -173,6 +175,20 @@ void free_all(bd_ctx *ctx) {
     for (auto &b : ctx->bufs) cudaFree(b.p);
     ctx->bufs.clear();
 }
+
+void free_static(bd_ctx *ctx) {
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (auto &b : ctx->sbufs) cudaFree(b.p);
+    ctx->sbufs.clear();
+}
+
+// Allocations made while one of these is alive go to the given list.
+struct BufScope {
+    bd_ctx *c;
+    std::vector<DevBuf> *saved;
+    BufScope(bd_ctx *c_, std::vector<DevBuf> *to) : c(c_), saved(c_->cur) { c->cur = to; }
+    ~BufScope() { c->cur = saved; }
+};
 
 // Seek_EFermi on the input propagator (source/BcDor-DysonMatrix.cpp:619-635).
 double seek_efermi(const bd_ctx *c, int I) {
@@ -590,55 +606,32 @@ int alloc_lanczos(bd_ctx *ctx) {
     return BD_OK;
 }
 
-}  // namespace
-
-// ============================================================================ C ABI
-extern "C" {
-
-int bd_version(void) { return 1; }
-
-int bd_create(bd_ctx **out, int device) {
-    if (!out) return BD_ERR_ARG;
-    *out = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return BD_ERR_CUDA;
-    bd_ctx *ctx = new bd_ctx();
-    ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
-        delete ctx;
-        return BD_ERR_CUDA;
+// Chain schedules of every channel from the stored pivots (pole counts may have
+// changed with the propagator), then the Lanczos buffers.
+int plan_pivots(bd_ctx *ctx) {
+    size_t vo = 0;
+    for (int I = 0; I < ctx->nsubsh; ++I) {
+        const int D = ctx->no[I], npv = ctx->piv_npvt[I], p0 = ctx->piv_first[I];
+        Chan &C = ctx->chans[I];
+        std::vector<double> work(ctx->piv_vec.begin() + vo, ctx->piv_vec.begin() + vo + (size_t)npv * D);
+        std::vector<int> nf(ctx->piv_nfw.begin() + p0, ctx->piv_nfw.begin() + p0 + npv);
+        std::vector<int> nb(ctx->piv_nbk.begin() + p0, ctx->piv_nbk.begin() + p0 + npv);
+        plan_chain(C.lz[0], C.nfw, D, npv, nf.data(), work.data());
+        plan_chain(C.lz[1], C.nbk, D, npv, nb.data(), work.data());
+        vo += (size_t)npv * D;
     }
-    for (auto &e : ctx->ev) cudaEventCreate(&e);
-    for (auto &e : ctx->ev_lz) cudaEventCreate(&e);
-    *out = ctx;
+    int rc = alloc_lanczos(ctx);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(ctx->st));
+    ctx->have_pivots = true;
     return BD_OK;
 }
 
-void bd_destroy(bd_ctx *ctx) {
-    if (!ctx) return;
-    cudaSetDevice(ctx->device);
-    free_all(ctx);
-    if (ctx->d_dyA) cudaFree(ctx->d_dyA);
-    if (ctx->d_dyvec) cudaFree(ctx->d_dyvec);
-    if (ctx->d_dysol) cudaFree(ctx->d_dysol);
-    if (ctx->d_dyR) cudaFree(ctx->d_dyR);
-    if (ctx->d_dywork) cudaFree(ctx->d_dywork);
-    for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
-    for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
-    if (ctx->st) cudaStreamDestroy(ctx->st);
-    delete ctx;
-}
-
-const char *bd_last_error(const bd_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
-
-int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp, const bd_propagator *prop) {
-    if (!ctx || !ms || !vpp || !prop) return BD_ERR_ARG;
-    if (ms->nsubsh < 1 || ms->norb < 1 || prop->nspb < 1 || vpp->n_me < 0) return fail(ctx, BD_ERR_ARG, "empty problem");
-    CU(cudaSetDevice(ctx->device));
-    free_all(ctx);
-    ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false;
+// Model space and interaction: resident until the next bd_upload_problem (the
+// Wide_self_energy_t's MdSp and Vpp, which Run_itrs keeps across iterations).
+int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp) {
     const int ns = ms->nsubsh;
-    ctx->nsubsh = ns; ctx->norb = ms->norb; ctx->nspb = prop->nspb;
+    ctx->nsubsh = ns; ctx->norb = ms->norb;
     ctx->l.assign(ms->l, ms->l + ns); ctx->j2.assign(ms->j2, ms->j2 + ns); ctx->ip.assign(ms->ip, ms->ip + ns);
     ctx->ch.assign(ms->ch, ms->ch + ns); ctx->no.assign(ms->no, ms->no + ns);
     ctx->orb_sh.assign(ms->orb_sh, ms->orb_sh + ms->norb);
@@ -646,8 +639,8 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     ctx->jmax = 0;
     for (int s = 0; s < ns; ++s) {
         ctx->jmax = std::max(ctx->jmax, ctx->j2[s]);  // Calculate_Jch_bounds: Jmax = max 2j
-        if (ctx->no[s] < 1 || ctx->no[s] > prop->nspb || ctx->no[s] > 8)
-            return fail(ctx, BD_ERR_ARG, "subshell %d: %d orbits (1..min(nspb,8) supported)", s, ctx->no[s]);
+        if (ctx->no[s] < 1 || ctx->no[s] > 8)
+            return fail(ctx, BD_ERR_ARG, "subshell %d: %d orbits (1..8 supported)", s, ctx->no[s]);
         if (ctx->j2[s] < 1 || ctx->j2[s] % 2 != 1) return fail(ctx, BD_ERR_ARG, "subshell %d: 2j = %d", s, ctx->j2[s]);
     }
     if (ctx->jmax >= kJMult) return fail(ctx, BD_ERR_ARG, "2j too large");
@@ -659,16 +652,6 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
         for (int o = 0; o < ms->norb; ++o)
             if (ctx->orb_sh[o] < 0 || ctx->orb_sh[o] >= ns) return fail(ctx, BD_ERR_ARG, "orbit %d: bad subshell", o);
     }
-    ctx->np.assign(prop->np, prop->np + ns); ctx->nh.assign(prop->nh, prop->nh + ns);
-    ctx->p_start.assign(ns, 0); ctx->h_start.assign(ns, 0);
-    int nqp = 0, nqh = 0;
-    for (int s = 0; s < ns; ++s) {
-        if (ctx->np[s] < 0 || ctx->nh[s] < 0) return fail(ctx, BD_ERR_ARG, "negative fragment count");
-        ctx->p_start[s] = nqp; ctx->h_start[s] = nqh; nqp += ctx->np[s]; nqh += ctx->nh[s];
-    }
-    ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
-    std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
-    std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
     // segment table of the sorted interaction (prepare_for_reading, source/BcDor-Vpp_potential.cpp:478-496)
     std::vector<int> seg_str(kSegTable, -10), seg_end(kSegTable, -10);
     {
@@ -688,10 +671,10 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
         }
         if (prev >= 0) seg_end[prev] = vpp->n_me - 1;
     }
-    build_plan(ctx);
     int rc;
     DevProblem &P = ctx->dp;
-    P.nsubsh = ns; P.norb = ctx->norb; P.jmax = ctx->jmax; P.nspb = ctx->nspb; P.n_me = vpp->n_me;
+    BufScope scope(ctx, &ctx->sbufs);   // resident buffers
+    P.nsubsh = ns; P.norb = ctx->norb; P.jmax = ctx->jmax; P.n_me = vpp->n_me;
     int *t;
     double *td;
     if ((rc = dupload(ctx, &t, ctx->l))) return rc; P.l = t;
@@ -702,14 +685,6 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     if ((rc = dupload(ctx, &t, ctx->orb_start))) return rc; P.orb_start = t;
     if ((rc = dupload(ctx, &t, ctx->orb_sh))) return rc; P.orb_sh = t;
     if ((rc = dupload(ctx, &td, ctx->orb_xe))) return rc; P.orb_xe = td;
-    if ((rc = dupload(ctx, &t, ctx->np))) return rc; P.np = t;
-    if ((rc = dupload(ctx, &t, ctx->nh))) return rc; P.nh = t;
-    if ((rc = dupload(ctx, &t, ctx->p_start))) return rc; P.p_start = t;
-    if ((rc = dupload(ctx, &t, ctx->h_start))) return rc; P.h_start = t;
-    if ((rc = dupload(ctx, &td, ctx->ep))) return rc; P.ep = td;
-    if ((rc = dupload(ctx, &td, ctx->eh))) return rc; P.eh = td;
-    if ((rc = dupload(ctx, &td, fqp))) return rc; P.fqp = td;
-    if ((rc = dupload(ctx, &td, fqh))) return rc; P.fqh = td;
     {
         int *a, *b;
         double *v;
@@ -725,6 +700,42 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     }
     if ((rc = dupload(ctx, &t, seg_str))) return rc; P.seg_str = t;
     if ((rc = dupload(ctx, &t, seg_end))) return rc; P.seg_end = t;
+    return BD_OK;
+}
+
+// Propagator and everything that depends on it: fragments, the block plan, the
+// pole buffers and the chain schedules (Wide_self_energy_t::reset with a new gin,
+// source/BcDor-Main.cpp:225).
+int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
+    const int ns = ctx->nsubsh;
+    if (prop->nspb < 1) return fail(ctx, BD_ERR_ARG, "nspb = %d", prop->nspb);
+    for (int s = 0; s < ns; ++s)
+        if (ctx->no[s] > prop->nspb) return fail(ctx, BD_ERR_ARG, "subshell %d: %d orbits > nspb %d", s, ctx->no[s], prop->nspb);
+    ctx->nspb = prop->nspb;
+    ctx->np.assign(prop->np, prop->np + ns); ctx->nh.assign(prop->nh, prop->nh + ns);
+    ctx->p_start.assign(ns, 0); ctx->h_start.assign(ns, 0);
+    int nqp = 0, nqh = 0;
+    for (int s = 0; s < ns; ++s) {
+        if (ctx->np[s] < 0 || ctx->nh[s] < 0) return fail(ctx, BD_ERR_ARG, "negative fragment count");
+        ctx->p_start[s] = nqp; ctx->h_start[s] = nqh; nqp += ctx->np[s]; nqh += ctx->nh[s];
+    }
+    ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
+    std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
+    std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
+    build_plan(ctx);
+    int rc;
+    DevProblem &P = ctx->dp;
+    P.nspb = ctx->nspb;
+    int *t;
+    double *td;
+    if ((rc = dupload(ctx, &t, ctx->np))) return rc; P.np = t;
+    if ((rc = dupload(ctx, &t, ctx->nh))) return rc; P.nh = t;
+    if ((rc = dupload(ctx, &t, ctx->p_start))) return rc; P.p_start = t;
+    if ((rc = dupload(ctx, &t, ctx->h_start))) return rc; P.h_start = t;
+    if ((rc = dupload(ctx, &td, ctx->ep))) return rc; P.ep = td;
+    if ((rc = dupload(ctx, &td, ctx->eh))) return rc; P.eh = td;
+    if ((rc = dupload(ctx, &td, fqp))) return rc; P.fqp = td;
+    if ((rc = dupload(ctx, &td, fqh))) return rc; P.fqh = td;
     // plan arrays
     if ((rc = dupload(ctx, &ctx->d_blocks, ctx->blocks))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
@@ -805,8 +816,79 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     ctx->res_nq.assign(2 * ns, 0);
     CU(cudaStreamSynchronize(ctx->st));
     ctx->uploaded = true;
+    if (ctx->have_pivots) {
+        ctx->have_pivots = false;
+        if ((rc = plan_pivots(ctx))) return rc;
+    }
     return BD_OK;
 }
+
+}  // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+int bd_version(void) { return 1; }
+
+int bd_create(bd_ctx **out, int device) {
+    if (!out) return BD_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return BD_ERR_CUDA;
+    bd_ctx *ctx = new bd_ctx();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return BD_ERR_CUDA;
+    }
+    for (auto &e : ctx->ev) cudaEventCreate(&e);
+    for (auto &e : ctx->ev_lz) cudaEventCreate(&e);
+    *out = ctx;
+    return BD_OK;
+}
+
+void bd_destroy(bd_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    free_all(ctx);
+    free_static(ctx);
+    if (ctx->d_dyA) cudaFree(ctx->d_dyA);
+    if (ctx->d_dyvec) cudaFree(ctx->d_dyvec);
+    if (ctx->d_dysol) cudaFree(ctx->d_dysol);
+    if (ctx->d_dyR) cudaFree(ctx->d_dyR);
+    if (ctx->d_dywork) cudaFree(ctx->d_dywork);
+    for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+const char *bd_last_error(const bd_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+
+
+int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp, const bd_propagator *prop) {
+    if (!ctx || !ms || !vpp || !prop) return BD_ERR_ARG;
+    if (ms->nsubsh < 1 || ms->norb < 1 || prop->nspb < 1 || vpp->n_me < 0) return fail(ctx, BD_ERR_ARG, "empty problem");
+    CU(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    free_static(ctx);
+    ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false; ctx->static_ok = false;
+    int rc = upload_static(ctx, ms, vpp);
+    if (rc) return rc;
+    ctx->static_ok = true;
+    return upload_propagator(ctx, prop);
+}
+
+int bd_upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
+    if (!ctx || !prop) return BD_ERR_ARG;
+    if (!ctx->static_ok) return fail(ctx, BD_ERR_STATE, "no model space / interaction uploaded");
+    CU(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    ctx->uploaded = false; ctx->results_valid = false;
+    return upload_propagator(ctx, prop);
+}
+
 
 int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv) {
     if (!ctx || !piv) return BD_ERR_ARG;
@@ -825,20 +907,8 @@ int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv) {
     ctx->piv_nfw.assign(piv->n_itr_fw, piv->n_itr_fw + tot);
     ctx->piv_nbk.assign(piv->n_itr_bk, piv->n_itr_bk + tot);
     ctx->piv_vec.assign(piv->vec, piv->vec + vtot);
-    size_t vo = 0;
-    for (int I = 0; I < ctx->nsubsh; ++I) {
-        const int D = ctx->no[I], npv = ctx->piv_npvt[I], p0 = ctx->piv_first[I];
-        Chan &C = ctx->chans[I];
-        std::vector<double> work(ctx->piv_vec.begin() + vo, ctx->piv_vec.begin() + vo + (size_t)npv * D);
-        plan_chain(C.lz[0], C.nfw, D, npv, ctx->piv_nfw.data() + p0, work.data());
-        plan_chain(C.lz[1], C.nbk, D, npv, ctx->piv_nbk.data() + p0, work.data());
-        vo += (size_t)npv * D;
-    }
-    int rc = alloc_lanczos(ctx);
-    if (rc) return rc;
-    CU(cudaStreamSynchronize(ctx->st));
-    ctx->have_pivots = true;
-    return BD_OK;
+    ctx->have_pivots = false;
+    return plan_pivots(ctx);
 }
 
 int bd_count_poles(bd_ctx *ctx, int ish, int *n_fw, int *n_bk) {
@@ -1195,6 +1265,69 @@ int bd_result_koltun_all(bd_ctx *ctx, double *koltun) {
     CU(cudaSetDevice(ctx->device));
     CU(cudaMemcpy(koltun, ctx->d_dykol, sizeof(double) * 3 * ctx->nsubsh, cudaMemcpyDeviceToHost));
     return BD_OK;
+}
+
+int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_current, int *np_out, int *nh_out,
+                          double *ep_out, int cap_p, double *eh_out, int cap_h, double *fqp_out, double *fqh_out,
+                          double *diff) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
+    CU(cudaSetDevice(ctx->device));
+    const int ns = ctx->nsubsh, NSP = ctx->nspb;
+    std::vector<int> np(ns, 0), nh(ns, 0);
+    std::vector<double> ep, eh, fqp, fqh;
+    std::vector<double> rows;
+    for (int I = 0; I < ns; ++I) {
+        const int D = ctx->chans[I].D, NS = 2 + D;
+        const int nqp = ctx->res_nq[2 * I], nqh = ctx->res_nq[2 * I + 1];
+        rows.resize((size_t)(nqp + nqh) * NS);
+        if (nqp + nqh > 0)
+            CU(cudaMemcpy(rows.data(), ctx->d_dysol + ctx->dy_sol_off[I], sizeof(double) * rows.size(),
+                          cudaMemcpyDeviceToHost));
+        for (int side = 0; side < 2; ++side) {
+            const int n0 = side == 0 ? 0 : nqp, n = side == 0 ? nqp : nqh;
+            // candidates: Z >= z_cut; at most max_frag of them, largest Z first (earlier row on ties)
+            std::vector<int> keep;
+            for (int k = 0; k < n; ++k)
+                if (rows[(size_t)(n0 + k) * NS + 1] >= z_cut) keep.push_back(k);
+            if (max_frag > 0 && (int)keep.size() > max_frag) {
+                std::stable_sort(keep.begin(), keep.end(), [&](int a, int b) {
+                    return rows[(size_t)(n0 + a) * NS + 1] > rows[(size_t)(n0 + b) * NS + 1];
+                });
+                keep.resize(max_frag);
+                std::sort(keep.begin(), keep.end());   // back to descending W, as add_qp / add_qh store them
+            }
+            std::vector<double> &E = side == 0 ? ep : eh, &F = side == 0 ? fqp : fqh;
+            for (int k : keep) {
+                const double *r = rows.data() + (size_t)(n0 + k) * NS;
+                E.push_back(r[0]);
+                for (int q = 0; q < NSP; ++q) F.push_back(q < D ? r[2 + q] : 0.0);
+            }
+            (side == 0 ? np : nh)[I] = (int)keep.size();
+        }
+    }
+    // quick_n_dirty_diff between the propagator this iteration read and the new one
+    if (diff) {
+        double d = 0.0;
+        const size_t ip = std::max(ep.size(), ctx->ep.size()), ih = std::max(eh.size(), ctx->eh.size());
+        for (size_t i = 0; i < ip; ++i) d += std::fabs((i < ep.size() ? ep[i] : 0.0) - (i < ctx->ep.size() ? ctx->ep[i] : 0.0));
+        for (size_t i = 0; i < ih; ++i) d += std::fabs((i < eh.size() ? eh[i] : 0.0) - (i < ctx->eh.size() ? ctx->eh[i] : 0.0));
+        *diff = d;
+    }
+    if ((ep_out && cap_p < (int)ep.size()) || (eh_out && cap_h < (int)eh.size()))
+        return fail(ctx, BD_ERR_CAPACITY, "propagator buffers hold %d / %d fragments, %zu / %zu needed", cap_p, cap_h,
+                    ep.size(), eh.size());
+    if (np_out) std::memcpy(np_out, np.data(), sizeof(int) * ns);
+    if (nh_out) std::memcpy(nh_out, nh.data(), sizeof(int) * ns);
+    if (ep_out && !ep.empty()) std::memcpy(ep_out, ep.data(), sizeof(double) * ep.size());
+    if (eh_out && !eh.empty()) std::memcpy(eh_out, eh.data(), sizeof(double) * eh.size());
+    if (fqp_out && !fqp.empty()) std::memcpy(fqp_out, fqp.data(), sizeof(double) * fqp.size());
+    if (fqh_out && !fqh.empty()) std::memcpy(fqh_out, fqh.data(), sizeof(double) * fqh.size());
+    if (keep_current) return BD_OK;
+    bd_propagator P{NSP, np.data(), nh.data(), ep.data(), eh.data(), fqp.data(), fqh.data()};
+    free_all(ctx);
+    ctx->uploaded = false; ctx->results_valid = false;
+    return upload_propagator(ctx, &P);
 }
 
 int bd_last_timings(bd_ctx *ctx, double *ms5) {

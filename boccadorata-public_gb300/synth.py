@@ -175,6 +175,18 @@ def make_unperturbed_propagator(ms: ModelSpace) -> Propagator:
                       np.ones(len(ep)), np.ones(len(eh)), fqp, fqh)
 
 
+def propagator_from_arrays(nspb, np_, nh, ep, eh, fqp, fqh) -> Propagator:
+    """A Propagator from per-subshell fragment counts and flat arrays (fragments listed
+    subshell by subshell, amplitudes rows of nspb); Z = sum of squared amplitudes, as
+    SpProp_t::add_qp / add_qh store it."""
+    np_ = np.asarray(np_, np.int32); nh = np.asarray(nh, np.int32)
+    fqp = np.asarray(fqp, np.float64).reshape(-1, nspb); fqh = np.asarray(fqh, np.float64).reshape(-1, nspb)
+    p_start = np.concatenate([[0], np.cumsum(np_)[:-1]]).astype(np.int32)
+    h_start = np.concatenate([[0], np.cumsum(nh)[:-1]]).astype(np.int32)
+    return Propagator(int(nspb), np_, nh, p_start, h_start, np.asarray(ep, np.float64), np.asarray(eh, np.float64),
+                      (fqp ** 2).sum(1), (fqh ** 2).sum(1), fqp, fqh)
+
+
 def _triangle_ok(j2a: int, j2b: int, J: int) -> bool:
     return abs(j2a - j2b) <= 2 * J <= j2a + j2b
 

@@ -21,6 +21,12 @@
  *   bd_dyson_solve     DysonMatrix (+ Calc_En, Seek_EFermi)
  *   bd_dyson_rows      source/BcDor-Main.cpp:42, source/BcDor-DysonMatrix.cpp:123,542,619
  *   bd_run_all         the per-channel loop of Run_itrs, source/BcDor-Main.cpp:241-391
+ *   bd_upload_propagator  Wide_self_energy_t::reset with a new input propagator,
+ *                      source/BcDor-Main.cpp:225
+ *   bd_dressed_propagator  the next iteration's propagator: DysonMatrix -> SpProp_t::add_qp /
+ *                      add_qh (source/BcDor-DysonMatrix.cpp:487-488, source/BcDor-Sp_Propagator.cpp:683-809),
+ *                      g_ptr1 = g_ptr2 (source/BcDor-Main.cpp:438-441), SpProp_t::quick_n_dirty_diff
+ *                      (source/BcDor-Sp_Propagator.cpp:1189-1219)
  */
 #ifndef BD_GB300_H
 #define BD_GB300_H
@@ -154,6 +160,26 @@ int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *so
                     double *koltun);
 /* koltun[3 * nsubsh] for every channel with one copy. */
 int bd_result_koltun_all(bd_ctx *ctx, double *koltun);
+
+/* Replace the input propagator, keeping the model space and the interaction resident
+ * (a new iteration of Run_itrs).  Pole counts, the block plan and the Lanczos chain
+ * schedules (from the pivots already uploaded) follow the new propagator. */
+int bd_upload_propagator(bd_ctx *ctx, const bd_propagator *prop);
+
+/* The next iteration's propagator from the Dyson solutions of the last bd_run_all.
+ * The reference appends every solution (add_qp / add_qh), so the pole count of the
+ * next Sigma(2) grows with the cube of the fragment count; this build truncates:
+ * per subshell, the quasiparticles and the quasiholes with Z >= z_cut, at most
+ * max_frag of each (max_frag <= 0: no limit), the largest Z first, kept in the order
+ * add_qp / add_qh store them (descending W; amplitudes x_0..x_{D-1}, zero up to nspb).
+ * z_cut <= 0 and max_frag <= 0 reproduce the reference's update.
+ * Unless keep_current, the new propagator replaces the context's (bd_upload_propagator).
+ * np_out / nh_out [nsubsh], ep_out [cap_p], eh_out [cap_h], fqp_out [cap_p * nspb],
+ * fqh_out [cap_h * nspb] receive it when non-NULL; *diff receives quick_n_dirty_diff
+ * between the propagator the run used and the new one. */
+int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_current, int *np_out, int *nh_out,
+                          double *ep_out, int cap_p, double *eh_out, int cap_h, double *fqp_out, double *fqh_out,
+                          double *diff);
 /* Device time of the phases of the last bd_run_all in ms: sigma2, sort, lanczos, dyson, total. */
 int bd_last_timings(bd_ctx *ctx, double *ms5);
 /* Diagnostics: extra reorthogonalisation sweeps of the last bd_run_all; device time of

@@ -224,6 +224,52 @@ class Oracle:
 
 
 # ---------------------------------------------------------------------------------------------
+# the next iteration's propagator
+# ---------------------------------------------------------------------------------------------
+
+def dressed_propagator(ms, results, nspb, z_cut, max_frag):
+    """Propagator of the next iteration from every channel's Dyson solutions.
+
+    DysonMatrix hands its solutions, quasiparticles and quasiholes each sorted by
+    descending W, to SpProp_t::add_qp / add_qh (source/BcDor-DysonMatrix.cpp:481-488),
+    which append them subshell by subshell with amplitudes x_0..x_{D-1} padded with
+    zeros to N_SPB_MX and Z recomputed as sum x^2 (source/BcDor-Sp_Propagator.cpp:683-809);
+    Run_itrs then uses that propagator as the next input (source/BcDor-Main.cpp:438-441).
+    The truncation is this build's (the reference keeps everything): per subshell and
+    side, the solutions with Z >= z_cut, at most max_frag of them (max_frag <= 0: all)
+    with the largest Z, earlier rows first on ties, kept in their stored order.
+    results[ish] = dict(qp=rows, qh=rows), rows [W, Z, x...] as DysonMatrix returns them."""
+    out = {"np": [], "nh": [], "ep": [], "eh": [], "fqp": [], "fqh": []}
+    for ish in range(ms.nsubsh):
+        D = int(ms.no[ish])
+        for side, (kn, ke, kf) in (("qp", ("np", "ep", "fqp")), ("qh", ("nh", "eh", "fqh"))):
+            rows = np.asarray(results[ish][side]).reshape(-1, 2 + D)
+            z = (rows[:, 2:2 + D] ** 2).sum(1)
+            keep = [k for k in range(len(rows)) if z[k] >= z_cut]
+            if max_frag > 0 and len(keep) > max_frag:
+                keep = sorted(sorted(keep, key=lambda k: -z[k])[:max_frag])
+            for k in keep:
+                out[ke].append(rows[k, 0])
+                amp = np.zeros(nspb); amp[:D] = rows[k, 2:2 + D]
+                out[kf].append(amp)
+            out[kn].append(len(keep))
+    return out
+
+
+def quick_n_dirty_diff(ep_a, eh_a, ep_b, eh_b):
+    """SpProp_t::quick_n_dirty_diff (source/BcDor-Sp_Propagator.cpp:1189-1219): sum of
+    |E_a - E_b| over the flat quasiparticle and quasihole lists, the shorter padded
+    with zeros."""
+    d = 0.0
+    for a, b in ((np.asarray(ep_a), np.asarray(ep_b)), (np.asarray(eh_a), np.asarray(eh_b))):
+        n = max(len(a), len(b))
+        aa = np.zeros(n); aa[:len(a)] = a
+        bb = np.zeros(n); bb[:len(b)] = b
+        d += float(np.abs(aa - bb).sum())
+    return d
+
+
+# ---------------------------------------------------------------------------------------------
 # reference dumps
 # ---------------------------------------------------------------------------------------------
 

@@ -1,0 +1,115 @@
+"""Iterations with a dressed propagator on the device: the next propagator from the
+device's Dyson solutions, the second iteration against the reference program, and
+the mixed form against FP64 over several iterations."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from helpers import strong_diffs
+
+pytestmark = pytest.mark.gpu
+
+
+def _fixture(synth, golden, problems, name):
+    g = golden(name)
+    nmax, hw, seed, nit = (int(g["meta"][0]), float(g["meta"][1]), int(g["meta"][2]), int(g["meta"][3]))
+    p1 = problems(nmax, hw, seed, nit)
+    prop2 = synth.propagator_from_arrays(p1.prop.nspb, g["p_np"], g["p_nh"], g["p_ep"], g["p_eh"], g["p_fqp"],
+                                         g["p_fqh"])
+    return g, p1, prop2, nit
+
+
+def test_next_propagator_from_device_solutions(synth, golden, problems, oracle_mod, bdmod):
+    g, p1, prop2, _ = _fixture(synth, golden, problems, "nmax2_full_iter2")
+    ctx = bdmod.Context().upload(p1)
+    ctx.run_all(lanczos=False)
+    z_cut, max_frag = float(g["trunc"][0]), int(g["trunc"][1])
+    prop, diff = ctx.dressed_propagator(z_cut, max_frag, keep_current=True)
+    assert np.array_equal(prop.np_, prop2.np_) and np.array_equal(prop.nh, prop2.nh)
+    np.testing.assert_allclose(prop.ep, prop2.ep, rtol=1e-10)
+    np.testing.assert_allclose(prop.eh, prop2.eh, rtol=1e-10)
+    np.testing.assert_allclose(prop.zp, prop2.zp, atol=1e-9)
+    np.testing.assert_allclose(prop.zh, prop2.zh, atol=1e-9)
+    # the same rule applied by the oracle to the device's own solutions
+    res = [ctx.result(i) for i in range(p1.ms.nsubsh)]
+    dp = oracle_mod.dressed_propagator(p1.ms, res, p1.prop.nspb, z_cut, max_frag)
+    assert np.array_equal(prop.ep, np.asarray(dp["ep"])) and np.array_equal(prop.eh, np.asarray(dp["eh"]))
+    assert np.array_equal(prop.fqp, np.asarray(dp["fqp"]).reshape(prop.fqp.shape))
+    assert diff == pytest.approx(oracle_mod.quick_n_dirty_diff(p1.prop.ep, p1.prop.eh, prop.ep, prop.eh), rel=1e-12)
+    ctx.close()
+
+
+def test_second_iteration_full_dyson_matches_reference(synth, golden, problems, bdmod):
+    g, p1, prop2, _ = _fixture(synth, golden, problems, "nmax2_full_iter2")
+    ctx = bdmod.Context().upload(p1).upload_propagator(prop2)
+    ctx.run_all(lanczos=False)
+    for ish in range(p1.ms.nsubsh):
+        nfw, nbk = ctx.count_poles(ish)
+        assert (nfw, nbk) == (int(g[f"c{ish}_sig_fw_sum"][0]), int(g[f"c{ish}_sig_bk_sum"][0]))
+        r = ctx.result(ish)
+        for tag in ("qp", "qh"):
+            assert np.isfinite(r[tag]).all()
+            assert len(r[tag]) == int(g[f"c{ish}_{tag}_n"][0]), (ish, tag)
+            e, z = strong_diffs(g[f"c{ish}_{tag}_strong"], r[tag])
+            assert e < 1e-8 and z < 1e-8, (ish, tag, e, z)
+        np.testing.assert_allclose(r["koltun"], g[f"c{ish}_koltun"], rtol=1e-7, atol=1e-9)
+    ctx.close()
+
+
+def test_second_iteration_sigma2_bit_exact(synth, golden, problems, bdmod):
+    g, p1, prop2, _ = _fixture(synth, golden, problems, "nmax4_lanczos20_iter2")
+    ctx = bdmod.Context().upload(p1).upload_propagator(prop2)
+    for ish in range(p1.ms.nsubsh):
+        fw, bk = ctx.sigma2_build(ish)
+        for tag, a in (("sig_fw", fw), ("sig_bk", bk)):
+            got = np.array([len(a), a.sum(), (a * a).sum(), np.abs(a).max() if len(a) else 0.0])
+            assert np.array_equal(got, g[f"c{ish}_{tag}_sum"]), (ish, tag)
+        assert np.array_equal(ctx.ehf(ish), g[f"c{ish}_sig_hf"]), ish
+    ctx.close()
+
+
+def test_second_iteration_lanczos_dyson(synth, golden, problems, oracle_mod, bdmod):
+    """Lanczos-reduced: device rows equal the reference's until its first breakdown; the
+    solutions equal the oracle's iterated-sweep chain (the reference's single sweep is
+    rounding-dependent after a breakdown)."""
+    g, p1, prop2, _ = _fixture(synth, golden, problems, "nmax4_lanczos20_iter2")
+    p2 = dataclasses.replace(p1, prop=prop2)
+    ctx = bdmod.Context().upload(p1).upload_propagator(prop2)
+    ctx.run_all(lanczos=True)
+    orc = oracle_mod.Oracle().bind(p2)
+    for ish in range(p1.ms.nsubsh):
+        r = ctx.result(ish)
+        o2 = orc.run_channel(ish, True, passes=2)
+        for tag in ("qp", "qh"):
+            assert np.isfinite(r[tag]).all()
+            e, z = strong_diffs(o2[tag], r[tag])
+            assert e < 1e-9 and z < 1e-8, (ish, tag, e, z)
+        np.testing.assert_allclose(r["koltun"], o2["koltun"], rtol=1e-9, atol=1e-9)
+    ctx.close()
+
+
+def test_iterations_mixed_within_targets(problems, bdmod):
+    """Three iterations (N_max=4, 20 Lanczos iterations per pivot, Z >= 1e-3, at most 4
+    fragments per side): the mixed form stays within 1 keV / 1e-5 of FP64."""
+    p = problems(4, 20.0, 0, 20)
+    runs = {}
+    for mixed in (False, True):
+        ctx = bdmod.Context().upload(p)
+        diffs = []
+        for it in range(3):
+            ctx.run_all(lanczos=True, mixed=mixed)
+            if it < 2:
+                _, d = ctx.dressed_propagator(1e-3, 4)
+                diffs.append(d)
+        runs[mixed] = ([ctx.result(i) for i in range(p.ms.nsubsh)], diffs, ctx.prob.prop)
+        ctx.close()
+    ref, d64, prop64 = runs[False]
+    got, d32, prop32 = runs[True]
+    assert np.array_equal(prop64.np_, prop32.np_) and np.array_equal(prop64.nh, prop32.nh)
+    assert all(np.isfinite(d) for d in d64 + d32)
+    for ish in range(p.ms.nsubsh):
+        for tag in ("qp", "qh"):
+            assert np.isfinite(got[ish][tag]).all()
+            e, z = strong_diffs(ref[ish][tag], got[ish][tag], zmin=1e-4, etol=1e-5)
+            assert e * 300.0 < 1e-3 and z < 1e-5, (ish, tag, e, z)
