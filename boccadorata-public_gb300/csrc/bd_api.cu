@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <mutex>
@@ -69,6 +70,7 @@ struct bd_ctx {
     std::string err;
     bool uploaded = false, have_pivots = false;
     int lz_cluster = 8, dy_cluster = 8;
+    int lz_slices = 0;   // Lanczos slices: 0 by size, 1 shared memory, 2 global memory
     double eta = 0.70710678118654752;
     // host copies of the inputs
     int nsubsh = 0, norb = 0, jmax = 0, nspb = 0;
@@ -113,7 +115,8 @@ struct bd_ctx {
     int *d_lzstat = nullptr;
     size_t lzV_bytes = 0;
     long long lzout_total = 0;
-    std::vector<long long> lz_int_off[2], lz_piv_off[2];
+    std::vector<long long> lz_int_off[2], lz_piv_off[2], lz_slice_off[2];
+    char *d_lzslice = nullptr;
     LzChain *d_chains = nullptr;
     int lz_two_pass = 0;
     // Dyson
@@ -415,6 +418,11 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             z.V = ctx->d_lzV + ctx->lz_v_off[dir][I];
             z.out = ctx->d_lzout + ctx->lz_out_off[dir][I];
             z.stat = ctx->d_lzstat;
+            z.slice = ctx->d_lzslice + ctx->lz_slice_off[dir][I];
+            z.slice_stride = ((long long)z.S * 17 + 255) / 256 * 256;
+            if (reinterpret_cast<uintptr_t>(z.slice) % 256 != 0 ||
+                z.slice_stride * ctx->lz_cluster > lz_slice_bytes(P.N))
+                return fail(ctx, BD_ERR_STATE, "channel %d: Lanczos slice scratch misplaced", I);
             ch.push_back(z);
             Smax = std::max(Smax, z.S);
             rmax = std::max(rmax, P.L + 1);
@@ -438,7 +446,11 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
     CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
     CU(cudaEventRecord(ctx->ev_lz[0], ctx->st));
-    CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, ctx->lz_cluster, ctx->eta, ctx->st));
+    // chains whose slices do not fit next to the scalars keep them in global memory
+    const bool gslices = ctx->lz_slices == 2 || (ctx->lz_slices == 0 && lanczos_smem_bytes(Smax, rmax) > kLanczosSmemSliceCap);
+    if (!gslices && lanczos_smem_bytes(Smax, rmax) > (size_t)227 * 1024)
+        return fail(ctx, BD_ERR_CAPACITY, "Lanczos slices of %d poles do not fit in shared memory", Smax);
+    CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, ctx->lz_cluster, ctx->eta, gslices, ctx->st));
     CU(cudaEventRecord(ctx->ev_lz[1], ctx->st));
     ctx->lz_timed = true;
     ctx->launches += 1;
@@ -564,7 +576,9 @@ int alloc_lanczos(bd_ctx *ctx) {
         ctx->lz_out_off[dir].assign(ctx->nsubsh, 0);
         ctx->lz_int_off[dir].assign(ctx->nsubsh, 0);
         ctx->lz_piv_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_slice_off[dir].assign(ctx->nsubsh, 0);
     }
+    long long slices = 0;
     std::vector<int> hints;
     std::vector<double> hpiv;
     for (int I = 0; I < ctx->nsubsh; ++I)
@@ -576,6 +590,8 @@ int alloc_lanczos(bd_ctx *ctx) {
             vbytes = (vbytes + 255) / 256 * 256;
             ctx->lz_out_off[dir][I] = out;
             out += (long long)std::max(P.L, 0) * (P.nden_out + D);
+            ctx->lz_slice_off[dir][I] = slices;
+            if (P.L > 0) slices += lz_slice_bytes(P.N);
             ctx->lz_int_off[dir][I] = ints;
             // start[n_used+1] | last[n_used+1] | ipiv[nden_out + D]
             std::vector<int> st = P.start, la = P.last;
@@ -603,6 +619,7 @@ int alloc_lanczos(bd_ctx *ctx) {
     if ((rc = dalloc(ctx, &ctx->d_lzstat, 4))) return rc;
     CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
     if ((rc = dalloc(ctx, &ctx->d_chains, (size_t)2 * ctx->nsubsh))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_lzslice, (size_t)slices))) return rc;
     return BD_OK;
 }
 
@@ -1341,6 +1358,13 @@ int bd_last_timings(bd_ctx *ctx, double *ms5) {
 int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
 double bd_lanczos_kernel_ms(bd_ctx *ctx) { return ctx ? ctx->lz_kernel_ms : -1.0; }
 long long bd_launch_count(bd_ctx *ctx) { return ctx ? ctx->launches : -1; }
+int bd_set_lanczos_slices(bd_ctx *ctx, int mode) {
+    if (!ctx) return BD_ERR_ARG;
+    if (mode < 0 || mode > 2) return fail(ctx, BD_ERR_ARG, "slice mode %d", mode);
+    ctx->lz_slices = mode;
+    return BD_OK;
+}
+
 int bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta) {
     if (!ctx) return BD_ERR_ARG;
     if (lz_cluster != 1 && lz_cluster != 2 && lz_cluster != 4 && lz_cluster != 8 && lz_cluster != 16)
@@ -1485,7 +1509,7 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
         e = launch_to_float(d_M, reinterpret_cast<float *>(base + mf_off), (long long)D * N, st);
     if (e == cudaSuccess)
         e = launch_lanczos(reinterpret_cast<const LzChain *>(base), 1, S, P.L + 1, fp32, kNoallocCluster, kNoallocEta,
-                           st);
+                           false, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return noalloc_fail(err, err_len, BD_ERR_CUDA, "Lanczos launch: %s", cudaGetErrorString(e));
     return BD_OK;

@@ -66,7 +66,16 @@ struct LzChain {
     void *V;                // [L][ld] Lanczos vectors (double or float)
     double *out;            // [L][nden_out + D] rows
     int *stat;              // [2]: number of two-pass steps, error flag
+    char *slice;            // per-CTA E / w / touched slices in global memory (large chains), CTA r at
+    long long slice_stride; //   slice + r * slice_stride; unused when the slices live in shared memory
 };
+
+// Global scratch of one chain's slices: enough for any cluster size up to 16 with FP64
+// slices (17 bytes per pole, each CTA's share rounded up to 256 bytes); a multiple of
+// 256 bytes, so consecutive chains' slices stay aligned.
+__host__ __device__ inline long long lz_slice_bytes(long long N) {
+    return (17 * N + 16 * (17 * 4 + 256) + 255) / 256 * 256;
+}
 
 // One Dyson eigenproblem.
 struct DyJob {

@@ -17,8 +17,9 @@ __global__ void k_permute_soa(const int *perm, long long n0, long long n, const 
 __global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows);
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,
-                           double eta, cudaStream_t st);
-size_t lanczos_smem_bytes(int S, int rmax);
+                           double eta, bool global_slices, cudaStream_t st);
+size_t lanczos_smem_bytes(int S, int rmax, bool global_slices = false);
+constexpr size_t kLanczosSmemSliceCap = 100 * 1024;   // above this the slices go to global memory
 cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStream_t st);
 
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,

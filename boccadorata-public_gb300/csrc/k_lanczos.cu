@@ -100,7 +100,7 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // products, norms and scalars) is FP32, and only the sums across threads, warps and
 // CTAs are FP64: on this GPU FP64 issues at 1/64 of the FP32 rate, and a per-pole
 // FP64 operation would cost more than the whole FP32 sweep.
-template <typename VT>
+template <typename VT, bool kGlobalSlices>
 __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
     using CT = typename LzTraits<VT>::CT;
     constexpr int VW = Vec16<VT>::n;
@@ -124,9 +124,17 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     double *Bn = Bs + kMaxScal;
     double *red = Bn + 2;
     CT *cf = reinterpret_cast<CT *>(red + kLzWarps * kMaxScal);   // 16-byte aligned: 2 rmax + 290 doubles before
-    CT *Es = cf + (rmax + 3) / 4 * 4;
-    CT *w = Es + S;
-    unsigned char *touched = reinterpret_cast<unsigned char *>(w + S);
+    CT *Es, *w;
+    unsigned char *touched;
+    if constexpr (kGlobalSlices) {   // chains too long for shared memory: this CTA's slices in global scratch
+        Es = reinterpret_cast<CT *>(C.slice + (size_t)rank * C.slice_stride);
+        w = Es + S;
+        touched = reinterpret_cast<unsigned char *>(w + S);
+    } else {
+        Es = cf + (rmax + 3) / 4 * 4;
+        w = Es + S;
+        touched = reinterpret_cast<unsigned char *>(w + S);
+    }
     __shared__ double tot[kMaxScal];
     __shared__ double s_n2;
     __shared__ int s_kmin;
@@ -415,17 +423,28 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     cluster.sync();  // no CTA leaves while peers may still read its shared memory
 }
 
-size_t lanczos_smem_bytes(int S, int rmax) {
+size_t lanczos_smem_bytes(int S, int rmax, bool global_slices) {
     // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
-    return sizeof(double) * ((size_t)2 * S + 2 * (size_t)rmax + (size_t)(rmax + 3) / 4 * 4 + kMaxScal + 2 +
-                             (size_t)kLzWarps * kMaxScal) +
-           (size_t)S + 16;
+    const size_t fixed = sizeof(double) * (2 * (size_t)rmax + (size_t)(rmax + 3) / 4 * 4 + kMaxScal + 2 +
+                                           (size_t)kLzWarps * kMaxScal) + 16;
+    return global_slices ? fixed : fixed + sizeof(double) * 2 * (size_t)S + (size_t)S;
+}
+
+template <typename VT, bool G>
+static cudaError_t launch_lz(const cudaLaunchConfig_t &cfg, int cluster, const LzChain *d_chains, int nchains, int rmax,
+                             double eta2) {
+    cudaError_t e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cfg.dynamicSmemBytes);
+    if (e == cudaSuccess && cluster > 8)
+        e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&cfg, k_lanczos<VT, G>, d_chains, nchains, rmax, eta2);
 }
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,
-                           double eta, cudaStream_t st) {
+                           double eta, bool global_slices, cudaStream_t st) {
     if (nchains <= 0) return cudaSuccess;
-    size_t smem = lanczos_smem_bytes(S_max, rmax);
+    const size_t smem = lanczos_smem_bytes(S_max, rmax, global_slices);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nchains * cluster, 1, 1);
     cfg.blockDim = dim3(kLzThreads, 1, 1);
@@ -438,19 +457,12 @@ cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e;
-    if (fp32) {
-        e = cudaFuncSetAttribute(k_lanczos<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess && cluster > 8)
-            e = cudaFuncSetAttribute(k_lanczos<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return e;
-        return cudaLaunchKernelEx(&cfg, k_lanczos<float>, d_chains, nchains, rmax, eta * eta);
-    }
-    e = cudaFuncSetAttribute(k_lanczos<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess && cluster > 8)
-        e = cudaFuncSetAttribute(k_lanczos<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_lanczos<double>, d_chains, nchains, rmax, eta * eta);
+    const double eta2 = eta * eta;
+    if (fp32)
+        return global_slices ? launch_lz<float, true>(cfg, cluster, d_chains, nchains, rmax, eta2)
+                             : launch_lz<float, false>(cfg, cluster, d_chains, nchains, rmax, eta2);
+    return global_slices ? launch_lz<double, true>(cfg, cluster, d_chains, nchains, rmax, eta2)
+                         : launch_lz<double, false>(cfg, cluster, d_chains, nchains, rmax, eta2);
 }
 
 }  // namespace bd

@@ -190,6 +190,10 @@ int       bd_diag_two_pass(bd_ctx *ctx);
 double    bd_lanczos_kernel_ms(bd_ctx *ctx);
 long long bd_launch_count(bd_ctx *ctx);
 int       bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta);
+/* Where the Lanczos kernel keeps each CTA's slice of the pole energies and of the
+ * working vector: 0 = shared memory unless it would exceed 100 KB (default),
+ * 1 = shared memory, 2 = global memory (for chains of any length). */
+int       bd_set_lanczos_slices(bd_ctx *ctx, int mode);
 
 /* Allocation-free Lanczos reduction of one pole set.  This entry point has no
  * counterpart in the reference.  It is for host programs that cannot let a
