@@ -10,12 +10,14 @@
 //   * all channels at once (bd_run_all), one launch per phase over every channel.
 #include <cub/cub.cuh>
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -87,6 +89,10 @@ struct bd_ctx {
     std::vector<DevBuf> bufs, sbufs;
     std::vector<DevBuf> *cur = nullptr;   // where dalloc records (nullptr: bufs)
     bool static_ok = false;
+    // freed buffers kept for reuse by size: a repeated upload of a problem of the same
+    // shape allocates nothing (cudaMalloc / cudaFree synchronise the device)
+    std::multimap<size_t, void *> pool;
+    size_t pool_bytes = 0;
     DevProblem dp{};
     S2Block *d_blocks = nullptr;
     long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr, *d_blk_vp_first = nullptr;
@@ -154,15 +160,41 @@ int fail(bd_ctx *c, int code, const char *fmt, ...) {
                                            cudaGetErrorString(e_), __FILE__, __LINE__);            \
     } while (0)
 
+constexpr size_t kPoolCap = (size_t)16 << 30;   // idle bytes the pool may hold
+
+void drain_pool(bd_ctx *ctx) {
+    for (auto &e : ctx->pool) cudaFree(e.second);
+    ctx->pool.clear();
+    ctx->pool_bytes = 0;
+}
+
+// Device bytes from the pool (same size) or from cudaMalloc, recorded in the current list.
+int dmalloc(bd_ctx *ctx, void **q, size_t bytes) {
+    *q = nullptr;
+    auto it = ctx->pool.find(bytes);
+    if (it != ctx->pool.end()) {
+        *q = it->second;
+        ctx->pool.erase(it);
+        ctx->pool_bytes -= bytes;
+    } else {
+        cudaError_t e = cudaMalloc(q, bytes);
+        if (e == cudaErrorMemoryAllocation && !ctx->pool.empty()) {
+            cudaGetLastError();
+            drain_pool(ctx);
+            e = cudaMalloc(q, bytes);
+        }
+        if (e != cudaSuccess) return fail(ctx, BD_ERR_CUDA, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    (ctx->cur ? *ctx->cur : ctx->bufs).push_back({*q, bytes});
+    return BD_OK;
+}
+
 template <typename T>
 int dalloc(bd_ctx *ctx, T **p, size_t count) {
-    *p = nullptr;
-    size_t bytes = sizeof(T) * (count > 0 ? count : 1);
     void *q = nullptr;
-    CU(cudaMalloc(&q, bytes));
-    (ctx->cur ? *ctx->cur : ctx->bufs).push_back({q, bytes});
+    const int rc = dmalloc(ctx, &q, sizeof(T) * (count > 0 ? count : 1));
     *p = reinterpret_cast<T *>(q);
-    return BD_OK;
+    return rc;
 }
 
 template <typename T>
@@ -173,17 +205,22 @@ int dupload(bd_ctx *ctx, T **p, const std::vector<T> &h) {
     return BD_OK;
 }
 
-void free_all(bd_ctx *ctx) {
+// Buffers of a list go back to the pool (beyond kPoolCap idle bytes: to the driver).
+void release(bd_ctx *ctx, std::vector<DevBuf> &list) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (auto &b : ctx->bufs) cudaFree(b.p);
-    ctx->bufs.clear();
+    for (auto &b : list) {
+        if (ctx->pool_bytes + b.bytes <= kPoolCap) {
+            ctx->pool.emplace(b.bytes, b.p);
+            ctx->pool_bytes += b.bytes;
+        } else {
+            cudaFree(b.p);
+        }
+    }
+    list.clear();
 }
 
-void free_static(bd_ctx *ctx) {
-    if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (auto &b : ctx->sbufs) cudaFree(b.p);
-    ctx->sbufs.clear();
-}
+void free_all(bd_ctx *ctx) { release(ctx, ctx->bufs); }
+void free_static(bd_ctx *ctx) { release(ctx, ctx->sbufs); }
 
 // Allocations made while one of these is alive go to the given list.
 struct BufScope {
@@ -227,6 +264,9 @@ void build_plan(bd_ctx *c) {
             for (int ia = 0; ia < ns; ++ia)
                 for (int ib = ia; ib < ns; ++ib) {
                     if (tri_fail(c->j2[ia], c->j2[ib], 2 * Jab)) continue;
+                    // blocks without poles add nothing to either list: skip them (and the
+                    // whole ig loop when (ia, ib) can carry neither 2p1h nor 2h1p poles)
+                    if (!(c->np[ia] > 0 && c->np[ib] > 0) && !(c->nh[ia] > 0 && c->nh[ib] > 0)) continue;
                     const int nJab = std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2;
                     for (int ig : gl) {
                         if (c->ch[ia] + c->ch[ib] - c->ch[ig] != c->ch[I]) continue;
@@ -241,6 +281,7 @@ void build_plan(bd_ctx *c) {
                         na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; s = na * nb * ng;
                         if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
                         B.nbk = s;
+                        if (B.nfw <= 0 && B.nbk <= 0) continue;
                         B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
                         B.vp_first = vp;
                         B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
@@ -396,8 +437,15 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
     return BD_OK;
 }
 
+// Cluster size of a launch: the tuned size when many channels share the GPU; a
+// channel launched alone (the per-channel call pattern) spreads each chain and each
+// Dyson matrix over 16 CTAs, since its few clusters would otherwise leave most SMs idle.
+int lz_cluster_for(const bd_ctx *ctx, int nch) { return nch == 1 ? std::max(ctx->lz_cluster, 16) : ctx->lz_cluster; }
+int dy_cluster_for(const bd_ctx *ctx, int nch) { return nch == 1 ? std::max(ctx->dy_cluster, 16) : ctx->dy_cluster; }
+
 // Lanczos chains of channels [ch_lo, ch_hi), both directions.
 int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
+    const int CL = lz_cluster_for(ctx, ch_hi - ch_lo);
     std::vector<LzChain> ch;
     int Smax = 1, rmax = 1;
     for (int I = ch_lo; I < ch_hi; ++I) {
@@ -408,7 +456,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             LzChain z{};
             z.N = P.N; z.D = C.D; z.L = P.L; z.n_used = P.n_used; z.nden_out = P.nden_out;
             z.ld = lz_ld(P.N);
-            z.S = ((P.N + ctx->lz_cluster - 1) / ctx->lz_cluster + 3) / 4 * 4;
+            z.S = ((P.N + CL - 1) / CL + 3) / 4 * 4;
             z.E = (dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s) + (dir == 0 ? C.fw_off : C.bk_off);
             z.M = (dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s) + (dir == 0 ? C.mfw_off : C.mbk_off);
             z.Mf = (dir == 0 ? ctx->d_Mfw_f : ctx->d_Mbk_f) + (dir == 0 ? C.mfw_off : C.mbk_off);
@@ -421,7 +469,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             z.slice = ctx->d_lzslice + ctx->lz_slice_off[dir][I];
             z.slice_stride = ((long long)z.S * 17 + 255) / 256 * 256;
             if (reinterpret_cast<uintptr_t>(z.slice) % 256 != 0 ||
-                z.slice_stride * ctx->lz_cluster > lz_slice_bytes(P.N))
+                z.slice_stride * CL > lz_slice_bytes(P.N))
                 return fail(ctx, BD_ERR_STATE, "channel %d: Lanczos slice scratch misplaced", I);
             ch.push_back(z);
             Smax = std::max(Smax, z.S);
@@ -450,7 +498,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     const bool gslices = ctx->lz_slices == 2 || (ctx->lz_slices == 0 && lanczos_smem_bytes(Smax, rmax) > kLanczosSmemSliceCap);
     if (!gslices && lanczos_smem_bytes(Smax, rmax) > (size_t)227 * 1024)
         return fail(ctx, BD_ERR_CAPACITY, "Lanczos slices of %d poles do not fit in shared memory", Smax);
-    CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, ctx->lz_cluster, ctx->eta, gslices, ctx->st));
+    CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, CL, ctx->eta, gslices, ctx->st));
     CU(cudaEventRecord(ctx->ev_lz[1], ctx->st));
     ctx->lz_timed = true;
     ctx->launches += 1;
@@ -471,7 +519,7 @@ int ensure_dyson(bd_ctx *ctx, bool lanczos) {
     for (int I = 0; I < ns; ++I) {
         const size_t n = (size_t)dyson_order(ctx, I, lanczos), D = ctx->chans[I].D;
         ctx->dy_A_off[I] = (long long)a; a += n * n;
-        ctx->dy_vec_off[I] = (long long)v; v += 3 * n;
+        ctx->dy_vec_off[I] = (long long)v; v += 4 * n;   // d, e, tau, block bounds (2n ints)
         ctx->dy_sol_off[I] = (long long)s; s += n * (2 + D);
         ctx->dy_R_off[I] = (long long)r; r += D * n + n * (2 + D);
         ctx->dy_work_off[I] = (long long)w; w += 5 * n * n;
@@ -543,6 +591,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
         J.efermi = C.efermi;
         J.A = ctx->d_dyA + ctx->dy_A_off[I];
         J.d = ctx->d_dyvec + ctx->dy_vec_off[I]; J.e = J.d + J.n; J.tau = J.e + J.n;
+        J.blk = reinterpret_cast<int *>(J.tau + J.n);
         J.R = ctx->d_dyR + ctx->dy_R_off[I];
         J.sol = ctx->d_dysol + ctx->dy_sol_off[I];
         J.nq = ctx->d_dynq + 2 * I;
@@ -562,7 +611,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
     CU(cudaMemcpyAsync(ctx->d_work_first + ch_lo, ctx->dy_work_off.data() + ch_lo, sizeof(long long) * jobs.size(),
                        cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(ctx->d_jobs + ch_lo, (int)jobs.size(), ctx->d_row_first + ch_lo, rows, nmax, Dmax,
-                    ctx->dy_cluster, ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
+                    dy_cluster_for(ctx, ch_hi - ch_lo), ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
     ctx->launches += kDysonKernels;
     return BD_OK;
 }
@@ -606,8 +655,8 @@ int alloc_lanczos(bd_ctx *ctx) {
         }
     if (vbytes) {
         void *p = nullptr;
-        CU(cudaMalloc(&p, vbytes));
-        ctx->bufs.push_back({p, vbytes});
+        int rc0 = dmalloc(ctx, &p, vbytes);
+        if (rc0) return rc0;
         ctx->d_lzV = reinterpret_cast<char *>(p);
     }
     ctx->lzV_bytes = vbytes;
@@ -669,25 +718,6 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         for (int o = 0; o < ms->norb; ++o)
             if (ctx->orb_sh[o] < 0 || ctx->orb_sh[o] >= ns) return fail(ctx, BD_ERR_ARG, "orbit %d: bad subshell", o);
     }
-    // segment table of the sorted interaction (prepare_for_reading, source/BcDor-Vpp_potential.cpp:478-496)
-    std::vector<int> seg_str(kSegTable, -10), seg_end(kSegTable, -10);
-    {
-        int prev = -1;
-        for (int i = 0; i < vpp->n_me; ++i) {
-            const int k = vpp->iabJ[i], J = k % kJMult, ab = k / kJMult, a = ab / kABMult, b = ab % kABMult;
-            if (a < 0 || b < 0 || a >= ms->norb || b >= ms->norb) return fail(ctx, BD_ERR_ARG, "element %d: orbit out of range", i);
-            const int cs = ctx->ch[ctx->orb_sh[a]] + ctx->ch[ctx->orb_sh[b]];
-            const int ps = (ctx->ip[ctx->orb_sh[a]] + ctx->ip[ctx->orb_sh[b]]) % 2;
-            const int key = ind_chipJ(cs, ps, J);
-            if (key < 0 || key >= kSegTable) return fail(ctx, BD_ERR_ARG, "element %d: bad channel key", i);
-            if (key != prev) {
-                if (prev >= 0) seg_end[prev] = i - 1;
-                if (seg_str[key] >= 0) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
-                seg_str[key] = i; prev = key;
-            }
-        }
-        if (prev >= 0) seg_end[prev] = vpp->n_me - 1;
-    }
     int rc;
     DevProblem &P = ctx->dp;
     BufScope scope(ctx, &ctx->sbufs);   // resident buffers
@@ -715,8 +745,31 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         }
         P.iabJ = a; P.icdJ = b; P.V = v;
     }
-    if ((rc = dupload(ctx, &t, seg_str))) return rc; P.seg_str = t;
-    if ((rc = dupload(ctx, &t, seg_end))) return rc; P.seg_end = t;
+    // segment table of the sorted interaction, on the device (k_segments)
+    {
+        const std::vector<int> init(kSegTable, -10), zero(kSegTable + 2, 0);
+        int *cnt, *sstr, *send;
+        if ((rc = dupload(ctx, &sstr, init))) return rc; P.seg_str = sstr;
+        if ((rc = dupload(ctx, &send, init))) return rc; P.seg_end = send;
+        if ((rc = dupload(ctx, &cnt, zero))) return rc;
+        int *bad = cnt + kSegTable;
+        const int big[2] = {INT_MAX, 0};
+        CU(cudaMemcpyAsync(bad, big, sizeof(big), cudaMemcpyHostToDevice, ctx->st));
+        if (vpp->n_me > 0) {
+            k_segments<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
+                P.iabJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad);
+            CU(cudaGetLastError());
+            ctx->launches += 1;
+        }
+        std::vector<int> h(kSegTable + 2);
+        CU(cudaMemcpyAsync(h.data(), cnt, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
+        CU(cudaStreamSynchronize(ctx->st));
+        if (h[kSegTable] != INT_MAX)
+            return fail(ctx, BD_ERR_ARG, "element %d: %s", h[kSegTable],
+                        h[kSegTable + 1] == 1 ? "orbit out of range" : "bad channel key");
+        for (int k = 0; k < kSegTable; ++k)
+            if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
+    }
     return BD_OK;
 }
 
@@ -869,6 +922,7 @@ void bd_destroy(bd_ctx *ctx) {
     cudaSetDevice(ctx->device);
     free_all(ctx);
     free_static(ctx);
+    drain_pool(ctx);
     if (ctx->d_dyA) cudaFree(ctx->d_dyA);
     if (ctx->d_dyvec) cudaFree(ctx->d_dyvec);
     if (ctx->d_dysol) cudaFree(ctx->d_dysol);
@@ -1102,7 +1156,7 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     CU(cudaMallocAsync(&dipf, sizeof(int) * nip, ctx->st));
     CU(cudaMallocAsync(&dipb, sizeof(int) * nip, ctx->st));
     CU(cudaMallocAsync(&dA, sizeof(double) * (size_t)n * n, ctx->st));
-    CU(cudaMallocAsync(&dv, sizeof(double) * 3 * (size_t)n, ctx->st));
+    CU(cudaMallocAsync(&dv, sizeof(double) * 4 * (size_t)n, ctx->st));
     CU(cudaMallocAsync(&dR, sizeof(double) * ((size_t)D * n + (size_t)n * (2 + D)), ctx->st));
     CU(cudaMallocAsync(&dsol, sizeof(double) * (size_t)n * (2 + D), ctx->st));
     CU(cudaMallocAsync(&dwork, sizeof(double) * 5 * (size_t)n * n, ctx->st));
@@ -1124,13 +1178,14 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     J.sighf = ctx->d_sighf + ctx->chan_dd_off[ish];
     J.sig1b = ctx->d_sig1b + ctx->chan_dd_off[ish];
     J.efermi = std::isnan(e_fermi) ? C.efermi : e_fermi;
-    J.A = dA; J.d = dv; J.e = dv + n; J.tau = dv + 2 * n; J.R = dR; J.sol = dsol;
+    J.A = dA; J.d = dv; J.e = dv + n; J.tau = dv + 2 * n; J.blk = reinterpret_cast<int *>(dv + 3 * n);
+    J.R = dR; J.sol = dsol;
     J.nq = ctx->d_dynq + 2 * ish; J.koltun = ctx->d_dykol + 3 * ish; J.stat = ctx->d_dystat + ish;
     long long zero[2] = {0, 0};
     CU(cudaMemcpyAsync(dj, &J, sizeof(DyJob), cudaMemcpyHostToDevice, ctx->st));
     CU(cudaMemcpyAsync(dwf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(cudaMemcpyAsync(drf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
-    CU(launch_dyson(dj, 1, drf, n, n, D, ctx->dy_cluster, dwork, dwf, ctx->st));
+    CU(launch_dyson(dj, 1, drf, n, n, D, dy_cluster_for(ctx, 1), dwork, dwf, ctx->st));
     ctx->launches += kDysonKernels;
     int nq[2] = {0, 0};
     double kol[3];
@@ -1405,8 +1460,8 @@ constexpr int kNoallocDevices = 64;
 // and ends | [1024, 2048) pivots | [4096, end) Lanczos vectors
 constexpr size_t kNoallocCounters = 256, kNoallocInts = 512, kNoallocPiv = 1024, kNoallocStage = 2048;
 constexpr size_t kNoallocVectors = 4096;
-constexpr int kNoallocCluster = 8;                       // the context's default cluster size
-constexpr double kNoallocEta = 0.70710678118654752;      // and DGKS threshold
+constexpr int kNoallocCluster = 16;                      // as for a channel launched alone
+constexpr double kNoallocEta = 0.70710678118654752;      // the context's DGKS threshold
 static_assert(sizeof(LzChain) <= kNoallocCounters, "descriptor slot");
 
 std::mutex g_noalloc_mu;

@@ -93,6 +93,7 @@ struct DyJob {
     double efermi;
     double *A;               // [n][n] scratch (row-major)
     double *d, *e, *tau;     // [n] tridiagonal diagonal, off-diagonal, reflector scalars
+    int *blk;                // [2n] first and last position of each position's tridiagonal block
     double *R;               // [D][n] first D rows of Q, then n staged rows of 2 + D
     double *sol;             // [n][2 + D] output rows (qp first, then qh)
     int *nq;                 // [2] n_qp, n_qh

@@ -4,17 +4,20 @@
 // components x_k[0:D] of the corresponding eigenvector of A.
 //
 //   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows)
-//   k_bisect  W_k by bisection on Sturm counts, one thread per eigenvalue: an FP32
-//             bracketing phase (FP64 issues at 1/64 of the FP32 rate), checked and
-//             finished in FP64 to max(1e-12 |W|, 1e-13 |T|)
-//   k_invit   y_k by inverse iteration on T - W_k I (tridiagonal LU with partial
-//             pivoting), one thread per eigenvalue, each from its own start vector
-//   k_cluster_orth  eigenvalues closer than 1e-6 |T| form a cluster (the Dyson
-//             spectra hold exactly degenerate groups of tens to hundreds of
-//             zero-strength solutions); its vectors are orthonormalised together
-//   k_post    x_k[0:D] = R y_k, Z_k = sum_d x_k[d]^2, quasiparticle / quasihole split
-//             by E_F with both lists by descending W, Koltun partial sums (Calc_En,
-//             source/BcDor-DysonMatrix.cpp:542-594)
+//   k_bisect_prep  splits T into unreduced blocks at negligible off-diagonals
+//   k_bisect  W_k by bisection on Sturm counts over its block, one thread per
+//             eigenvalue: an FP32 bracketing phase (FP64 issues at 1/64 of the FP32
+//             rate), checked and finished in FP64 to max(1e-12 |W|, 1e-13 |T_b|)
+//   k_invit   y_k by inverse iteration on T_b - W_k I (tridiagonal LU with partial
+//             pivoting) over its block, one thread per eigenvalue, each from its own
+//             start vector
+//   k_cluster_orth  eigenvalues of one block closer than 1e-6 |T_b| form a cluster;
+//             its vectors are orthonormalised together (the exactly degenerate
+//             groups of tens to hundreds of zero-strength solutions in the Dyson
+//             spectra fall into different blocks and need nothing)
+//   k_post    x_k[0:D] = R y_k, Z_k = sum_d x_k[d]^2
+//   k_place   quasiparticle / quasihole split by E_F with both lists by descending W,
+//             Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
 #include "bd_common.cuh"
 #include "bd_kernels.h"
 
@@ -109,74 +112,117 @@ __device__ inline int sturm_count_f(const float *d, const float *e2, int n, floa
 }
 
 // ------------------------------------------------------------------ K4c
-// One thread per eigenvalue index of every matrix; row_first maps a global index
-// to its matrix.  e2 (squared off-diagonals) goes into the tau array's slot, which
-// k_qrows has consumed, and FP32 copies of d and e2 into the start of the job's
-// work area (free until k_invit).
+// Split T where an off-diagonal is negligible, |e_i| <= eps (|d_i| + |d_{i+1}|) (the
+// relative split test of the QR / bisection codes; the perturbation is below the
+// rounding of T).  The Dyson matrices' tridiagonal forms fall apart into many blocks:
+// the exactly degenerate poles of the HO spectrum give identical eigenvalues in
+// different blocks, whose eigenvectors then have disjoint supports and need no
+// orthogonalisation.  Every later kernel works on the block of its own position:
+// positions are block-major, eigenvalues ascending within a block.
+//
+// One CTA per matrix: e2 (squared off-diagonals, zero at splits) into the tau slot,
+// which k_qrows has consumed; FP32 copies of d and e2 at the start of the job's work
+// area (free until k_invit); the block bounds of every position into J.blk.
+constexpr double kEps = 2.220446049250313e-16;
+
 __global__ void k_bisect_prep(const DyJob *jobs, int njobs, double *work, const long long *work_first) {
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
+    const int n = J.n;
     float *f = reinterpret_cast<float *>(work + work_first[jid]);
-    for (int i = threadIdx.x; i < J.n; i += blockDim.x) {
-        const double e2 = (i + 1 < J.n) ? J.e[i] * J.e[i] : 0.0;
-        J.tau[i] = e2;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double e = (i + 1 < n) ? J.e[i] : 0.0;
+        if (i + 1 < n && fabs(e) <= kEps * (fabs(J.d[i]) + fabs(J.d[i + 1]))) e = 0.0;
+        if (i + 1 < n) J.e[i] = e;
+        J.tau[i] = e * e;
         f[i] = (float)J.d[i];
-        f[J.n + i] = (float)e2;
+        f[n + i] = (float)(e * e);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int *bs = J.blk, *be = J.blk + n;
+        int b0 = 0;
+        for (int i = 0; i < n; ++i) {
+            if (i + 1 == n || J.e[i] == 0.0) {
+                for (int k = b0; k <= i; ++k) { bs[k] = b0; be[k] = i; }
+                b0 = i + 1;
+            }
+        }
     }
 }
 
+// matrix and position of a global eigenvalue index
+__device__ inline int job_of(const long long *row_first, int njobs, long long g) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    return lo;
+}
+
+// Gershgorin interval and norm of the block [b0, b1]
+__device__ inline void block_bounds(const double *d, const double *e, int b0, int b1, double *glo, double *ghi,
+                                    double *tnorm) {
+    double lo = d[b0], hi = d[b0];
+    for (int i = b0; i <= b1; ++i) {
+        const double r = (i > b0 ? fabs(e[i - 1]) : 0.0) + (i < b1 ? fabs(e[i]) : 0.0);
+        lo = fmin(lo, d[i] - r); hi = fmax(hi, d[i] + r);
+    }
+    *glo = lo; *ghi = hi; *tnorm = fmax(fabs(lo), fabs(hi));
+}
+
+// One thread per position: the eigenvalue of its block with the position's local index.
 __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total,
                          const double *work, const long long *work_first) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total) return;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
-    const int k = (int)(g - row_first[lo]), n = J.n;
-    const double *d = J.d, *e = J.e, *e2 = J.tau;
-    // Gershgorin interval
-    double glo = d[0] - fabs(e[0]), ghi = d[0] + fabs(e[0]), tnorm = 0.0;
-    for (int i = 0; i < n; ++i) {
-        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-        glo = fmin(glo, d[i] - r); ghi = fmax(ghi, d[i] + r);
+    const int t = (int)(g - row_first[lo]), n = J.n;
+    const int b0 = J.blk[t], b1 = J.blk[n + t], m = b1 - b0 + 1, k = t - b0;
+    const double *d = J.d + b0, *e2 = J.tau + b0;
+    double glo, ghi, tnorm;
+    block_bounds(J.d, J.e, b0, b1, &glo, &ghi, &tnorm);
+    double W;
+    if (m == 1) {
+        W = d[0];
+    } else {
+        const double pivmin = fmax(tnorm * 1e-300, 1e-290);
+        const double g0 = glo - 2.0 * kEps * tnorm - 1e-300, g1 = ghi + 2.0 * kEps * tnorm + 1e-300;
+        // W_k is the unique x with count(x) <= k < count(x + 0).
+        // FP32 bracket to 1e-5 |T| on the rounded block (its eigenvalues move by ~1e-7 |T|)
+        const float *df = reinterpret_cast<const float *>(work + work_first[lo]) + b0;
+        const float *e2f = reinterpret_cast<const float *>(work + work_first[lo]) + n + b0;
+        float e2max = 1.0f;
+        for (int i = 0; i + 1 < m; ++i) e2max = fmaxf(e2max, e2f[i]);
+        const float pivf = 1e-30f * e2max;
+        float af = (float)g0, bf = (float)g1;
+        for (int it = 0; it < 40 && (double)bf - (double)af > 1e-5 * tnorm; ++it) {
+            const float mid = 0.5f * (af + bf);
+            if (mid == af || mid == bf) break;
+            if (sturm_count_f(df, e2f, m, mid, pivf) > k) bf = mid; else af = mid;
+        }
+        // widen by 2e-5 |T|, check in FP64, else start over from the Gershgorin interval
+        const double margin = 2e-5 * tnorm;
+        double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
+        if (!(sturm_count(d, e2, m, a, pivmin) <= k && sturm_count(d, e2, m, b, pivmin) > k)) { a = g0; b = g1; }
+        for (int it = 0; it < 200; ++it) {
+            const double mid = 0.5 * (a + b);
+            if (b - a <= fmax(1e-12 * fmax(fabs(a), fabs(b)), 1e-13 * tnorm) + pivmin || mid == a || mid == b) break;
+            if (sturm_count(d, e2, m, mid, pivmin) > k) b = mid; else a = mid;
+        }
+        W = 0.5 * (a + b);
     }
-    tnorm = fmax(fabs(glo), fabs(ghi));
-    const double eps = 2.220446049250313e-16;
-    const double pivmin = fmax(tnorm * 1e-300, 1e-290);
-    const double g0 = glo - 2.0 * eps * tnorm - 1e-300, g1 = ghi + 2.0 * eps * tnorm + 1e-300;
-    // W_k is the unique x with count(x) <= k < count(x + 0).
-    // FP32 bracket to 1e-5 |T| on the rounded matrix (its eigenvalues move by ~1e-7 |T|)
-    const float *df = reinterpret_cast<const float *>(work + work_first[lo]), *e2f = df + n;
-    float e2max = 1.0f;
-    for (int i = 0; i + 1 < n; ++i) e2max = fmaxf(e2max, e2f[i]);
-    const float pivf = 1e-30f * e2max;
-    float af = (float)g0, bf = (float)g1;
-    for (int it = 0; it < 40 && (double)bf - (double)af > 1e-5 * tnorm; ++it) {
-        const float mid = 0.5f * (af + bf);
-        if (mid == af || mid == bf) break;
-        if (sturm_count_f(df, e2f, n, mid, pivf) > k) bf = mid; else af = mid;
-    }
-    // widen by 2e-5 |T|, check in FP64, else start over from the Gershgorin interval
-    const double margin = 2e-5 * tnorm;
-    double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
-    if (!(sturm_count(d, e2, n, a, pivmin) <= k && sturm_count(d, e2, n, b, pivmin) > k)) { a = g0; b = g1; }
-    for (int it = 0; it < 200; ++it) {
-        const double mid = 0.5 * (a + b);
-        if (b - a <= fmax(1e-12 * fmax(fabs(a), fabs(b)), 1e-13 * tnorm) + pivmin || mid == a || mid == b) break;
-        if (sturm_count(d, e2, n, mid, pivmin) > k) b = mid; else a = mid;
-    }
-    J.sol[(size_t)k * (2 + J.D)] = 0.5 * (a + b);   // eigenvalue parked in the W slot, ascending
+    J.sol[(size_t)t * (2 + J.D)] = W;   // eigenvalue parked in the W slot of its position
 }
 
 // ------------------------------------------------------------------ K4d
-// Inverse iteration, one thread per eigenvalue.  Eigenvalues closer than
-// ortol = 1e-6 |T| to their predecessor belong to the same cluster; inside a
-// cluster the shifts are kept at least pertol apart (the shift rule of LAPACK's
-// dstein) and every member starts from its own pseudo-random vector, so the
-// members span the cluster's invariant subspace; k_cluster_orth then makes them
-// orthonormal.  Y (the n x n region of A, column k at stride n) receives y_k; the
-// LU factors live in the job's work buffer, columns at stride n.
+// Inverse iteration, one thread per position, on its block only.  Eigenvalues of
+// the block closer than ortol = 1e-6 |T_b| to their predecessor belong to the same
+// cluster; inside a cluster the shifts are kept at least pertol apart (the shift
+// rule of LAPACK's dstein) and every member starts from its own pseudo-random vector,
+// so the members span the cluster's invariant subspace; k_cluster_orth then makes
+// them orthonormal.  Y (the n x n region of A, column t at stride n) receives y_t on
+// the block's rows; the LU factors live in the job's work buffer, columns at stride n.
 __device__ inline unsigned hash32(unsigned x) {
     x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
     return x;
@@ -184,14 +230,14 @@ __device__ inline unsigned hash32(unsigned x) {
 
 struct EigTol { double onenrm, ortol, pertol; };
 
-__device__ inline EigTol eig_tol(const double *d, const double *e, int n) {
+__device__ inline EigTol eig_tol(const double *d, const double *e, int b0, int b1) {
     double onenrm = 0.0;
-    for (int i = 0; i < n; ++i)
-        onenrm = fmax(onenrm, fabs(d[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0));
+    for (int i = b0; i <= b1; ++i)
+        onenrm = fmax(onenrm, fabs(d[i]) + (i > b0 ? fabs(e[i - 1]) : 0.0) + (i < b1 ? fabs(e[i]) : 0.0));
     EigTol t;
     t.onenrm = onenrm;
     t.ortol = 1e-6 * onenrm;
-    t.pertol = 10.0 * 2.220446049250313e-16 * fmax(onenrm, 1e-300);
+    t.pertol = 10.0 * kEps * fmax(onenrm, 1e-300);
     return t;
 }
 
@@ -199,30 +245,31 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
                         const long long *work_first) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total) return;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
     const int k = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D;
+    const int b0 = J.blk[k], b1 = J.blk[n + k];
     const double *d = J.d, *e = J.e;
-    const EigTol tl = eig_tol(d, e, n);
+    double *Y = J.A;
+    if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
+    const EigTol tl = eig_tol(d, e, b0, b1);
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
-    // shift: walk to the start of the cluster, then apply the separation rule forward
+    // shift: walk to the start of the cluster inside the block, then apply the separation rule forward
     int k0 = k;
-    while (k0 > 0 && W(k0) - W(k0 - 1) <= tl.ortol) --k0;
+    while (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) --k0;
     double x = W(k0);
     for (int q = k0 + 1; q <= k; ++q) x = fmax(W(q), x + tl.pertol);
-    double *Y = J.A;
     double *wk = work + work_first[lo];   // 5 arrays of n*n: super, super-super, diagonal, multipliers, interchanges
     double *U1 = wk, *U2 = wk + (size_t)n * n, *DD = wk + 2 * (size_t)n * n, *LL = wk + 3 * (size_t)n * n,
            *PV = wk + 4 * (size_t)n * n;
-    // LU with partial pivoting of T - x I; rows i and i+1 may swap (PV = 1)
-    for (int i = 0; i < n; ++i) {
+    // LU with partial pivoting of T_b - x I; rows i and i+1 may swap (PV = 1)
+    for (int i = b0; i <= b1; ++i) {
         DD[(size_t)i * n + k] = d[i] - x;
-        U1[(size_t)i * n + k] = (i + 1 < n) ? e[i] : 0.0;
-        LL[(size_t)i * n + k] = (i + 1 < n) ? e[i] : 0.0;
+        U1[(size_t)i * n + k] = (i < b1) ? e[i] : 0.0;
+        LL[(size_t)i * n + k] = (i < b1) ? e[i] : 0.0;
         U2[(size_t)i * n + k] = 0.0;
     }
-    for (int i = 0; i + 1 < n; ++i) {
+    for (int i = b0; i < b1; ++i) {
         const double di = DD[(size_t)i * n + k], li = LL[(size_t)i * n + k];
         if (fabs(di) >= fabs(li)) {
             PV[(size_t)i * n + k] = 0.0;
@@ -234,32 +281,32 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
             const double f = di / li;
             DD[(size_t)i * n + k] = li;
             LL[(size_t)i * n + k] = f;
-            const double t = U1[(size_t)i * n + k];
+            const double tt = U1[(size_t)i * n + k];
             U1[(size_t)i * n + k] = DD[(size_t)(i + 1) * n + k];
-            DD[(size_t)(i + 1) * n + k] = t - f * DD[(size_t)(i + 1) * n + k];
-            if (i + 2 < n) {
+            DD[(size_t)(i + 1) * n + k] = tt - f * DD[(size_t)(i + 1) * n + k];
+            if (i + 1 < b1) {
                 U2[(size_t)i * n + k] = U1[(size_t)(i + 1) * n + k];
                 U1[(size_t)(i + 1) * n + k] = -f * U1[(size_t)(i + 1) * n + k];
             }
         }
     }
-    for (int i = 0; i < n; ++i)
+    for (int i = b0; i <= b1; ++i)
         if (fabs(DD[(size_t)i * n + k]) < tl.pertol) DD[(size_t)i * n + k] = (DD[(size_t)i * n + k] < 0 ? -tl.pertol : tl.pertol);
-    for (int i = 0; i < n; ++i)
+    for (int i = b0; i <= b1; ++i)
         Y[(size_t)i * n + k] = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
     for (int it = 0; it < 3; ++it) {
-        for (int i = 0; i + 1 < n; ++i) {   // L^-1 with the interchanges
+        for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges
             double bi = Y[(size_t)i * n + k], bi1 = Y[(size_t)(i + 1) * n + k];
             const double f = LL[(size_t)i * n + k];
             if (PV[(size_t)i * n + k] == 0.0) bi1 -= f * bi;
-            else { const double t = bi; bi = bi1; bi1 = t - f * bi1; }
+            else { const double tt = bi; bi = bi1; bi1 = tt - f * bi1; }
             Y[(size_t)i * n + k] = bi; Y[(size_t)(i + 1) * n + k] = bi1;
         }
         double y1 = 0.0, y2 = 0.0, nrm = 0.0;
-        for (int i = n - 1; i >= 0; --i) {   // U y = b, two superdiagonals
+        for (int i = b1; i >= b0; --i) {   // U y = b, two superdiagonals
             double v = Y[(size_t)i * n + k];
-            if (i + 1 < n) v -= U1[(size_t)i * n + k] * y1;
-            if (i + 2 < n) v -= U2[(size_t)i * n + k] * y2;
+            if (i + 1 <= b1) v -= U1[(size_t)i * n + k] * y1;
+            if (i + 2 <= b1) v -= U2[(size_t)i * n + k] * y2;
             v /= DD[(size_t)i * n + k];
             Y[(size_t)i * n + k] = v;
             y2 = y1; y1 = v;
@@ -267,47 +314,50 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
         }
         const double sc = (nrm > 0.0) ? 1.0 / nrm : 1.0;
         double s2 = 0.0;
-        for (int i = 0; i < n; ++i) { const double v = Y[(size_t)i * n + k] * sc; Y[(size_t)i * n + k] = v; s2 += v * v; }
+        for (int i = b0; i <= b1; ++i) { const double v = Y[(size_t)i * n + k] * sc; Y[(size_t)i * n + k] = v; s2 += v * v; }
         const double inv = (s2 > 0.0) ? 1.0 / sqrt(s2) : 0.0;
-        for (int i = 0; i < n; ++i) Y[(size_t)i * n + k] *= inv;
+        for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] *= inv;
     }
 }
 
-// One CTA per eigenvalue index; the CTA of a cluster's first member (cluster of
-// two or more) orthonormalises the members with two classical Gram-Schmidt sweeps.
+// One CTA per position; the CTA of a cluster's first member (cluster of two or more,
+// inside one block) orthonormalises the members with two classical Gram-Schmidt
+// sweeps over the block's rows.
 __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs, int njobs, const long long *row_first,
                                                                long long total) {
     const long long g = blockIdx.x;
     if (g >= total) return;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
     const int k0 = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31,
               warp = tid >> 5;
+    const int b0 = J.blk[k0], b1 = J.blk[n + k0];
+    if (b0 == b1) return;
     __shared__ EigTol tl;
     __shared__ double cbuf[1024];
     __shared__ double red[kEigThreads / 32];
-    if (tid == 0) tl = eig_tol(J.d, J.e, n);
+    if (tid == 0) tl = eig_tol(J.d, J.e, b0, b1);
     __syncthreads();
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
-    if (k0 > 0 && W(k0) - W(k0 - 1) <= tl.ortol) return;
+    if (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) return;
     int k1 = k0 + 1;
-    while (k1 < n && W(k1) - W(k1 - 1) <= tl.ortol) ++k1;
+    while (k1 <= b1 && W(k1) - W(k1 - 1) <= tl.ortol) ++k1;
     if (k1 - k0 < 2) return;
-    double *Y = J.A;
+    double *Y = J.A;   // y_p is column p: element (i, p) at i * n + p
     for (int q = k0; q < k1; ++q) {
         for (int sweep = 0; sweep < 2; ++sweep) {
-            // c_p = <y_p, y_q> for the earlier members, blocks of 1024
+            // c_p = <y_p, y_q> for the earlier members, blocks of 1024: a warp per member
             for (int p0 = k0; p0 < q; p0 += 1024) {
                 const int p1 = min(q, p0 + 1024);
                 for (int p = p0 + warp; p < p1; p += kEigThreads / 32) {
                     double s = 0.0;
-                    for (int i = lane; i < n; i += 32) s += Y[(size_t)i * n + p] * Y[(size_t)i * n + q];
+                    for (int i = b0 + lane; i <= b1; i += 32) s += Y[(size_t)i * n + p] * Y[(size_t)i * n + q];
                     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
                     if (lane == 0) cbuf[p - p0] = s;
                 }
                 __syncthreads();
-                for (int i = tid; i < n; i += kEigThreads) {
+                // y_q -= sum_p c_p y_p: a thread per row, running along the row's members
+                for (int i = b0 + tid; i <= b1; i += kEigThreads) {
                     double acc = 0.0;
                     for (int p = p0; p < p1; ++p) acc += cbuf[p - p0] * Y[(size_t)i * n + p];
                     Y[(size_t)i * n + q] -= acc;
@@ -316,14 +366,14 @@ __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs,
             }
         }
         double s = 0.0;
-        for (int i = tid; i < n; i += kEigThreads) s += Y[(size_t)i * n + q] * Y[(size_t)i * n + q];
+        for (int i = b0 + tid; i <= b1; i += kEigThreads) s += Y[(size_t)i * n + q] * Y[(size_t)i * n + q];
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) red[warp] = s;
         __syncthreads();
         double tot = 0.0;
         for (int w = 0; w < kEigThreads / 32; ++w) tot += red[w];
         const double inv = (tot > 0.0) ? 1.0 / sqrt(tot) : 0.0;
-        for (int i = tid; i < n; i += kEigThreads) Y[(size_t)i * n + q] *= inv;
+        for (int i = b0 + tid; i <= b1; i += kEigThreads) Y[(size_t)i * n + q] *= inv;
         __syncthreads();
     }
 }
@@ -332,19 +382,19 @@ __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs,
 __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first, long long total) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total) return;
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
     const int k = (int)(g - row_first[lo]), n = J.n, D = J.D, NS = 2 + D;
+    const int b0 = J.blk[k], b1 = J.blk[n + k];
     double x[8];
 #pragma unroll
     for (int dd = 0; dd < 8; ++dd) x[dd] = 0.0;
-    for (int i = 0; i < n; ++i) {
+    for (int i = b0; i <= b1; ++i) {
         const double y = J.A[(size_t)i * n + k];
 #pragma unroll
         for (int dd = 0; dd < 8; ++dd) if (dd < D) x[dd] += J.R[(size_t)dd * n + i] * y;
     }
-    // rows [W, Z, x] staged behind R in ascending W; k_place orders them
+    // rows [W, Z, x] staged behind R, by position; k_place orders them
     double z = 0.0;
     for (int dd = 0; dd < D; ++dd) z += x[dd] * x[dd];
     double *st = J.R + (size_t)D * n + (size_t)k * NS;
@@ -354,31 +404,30 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
 }
 
 // Places the staged rows: quasiparticles (W > E_F) then quasiholes, each by
-// descending W, and forms the Koltun partial sums.  One CTA per matrix.
+// descending W (ties by position), and forms the Koltun partial sums.  One CTA per
+// matrix; the staged rows are block-major, so each finds its rank among all of them.
 __global__ void k_place(const DyJob *jobs, int njobs) {
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.n, D = J.D, NS = 2 + D;
-    double *st = J.R + (size_t)D * n;
+    const double *st = J.R + (size_t)D * n;
     __shared__ int nbelow;
-    if (threadIdx.x == 0) {
-        // independent bisections stop within their tolerance, so members of an exact
-        // degeneracy can come out in either order: restore the ascending order
-        int c = 0;
-        double wmax = -INFINITY;
-        for (int k = 0; k < n; ++k) {
-            double w = st[(size_t)k * NS];
-            if (w < wmax) { w = wmax; st[(size_t)k * NS] = w; }
-            wmax = w;
-            c += !(w > J.efermi);
-        }
-        nbelow = c;
-    }
+    if (threadIdx.x == 0) nbelow = 0;
+    __syncthreads();
+    int c = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) c += !(st[(size_t)k * NS] > J.efermi);
+    atomicAdd(&nbelow, c);
     __syncthreads();
     const int nqh = nbelow, nqp = n - nbelow;
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const int row = (k >= nqh) ? (n - 1 - k) : (nqp + (nqh - 1 - k));
+        const double w = st[(size_t)k * NS];
+        int r = 0;   // ascending rank
+        for (int q = 0; q < n; ++q) {
+            const double wq = st[(size_t)q * NS];
+            r += (wq < w) || (wq == w && q < k);
+        }
+        const int row = (r >= nqh) ? (n - 1 - r) : (nqp + (nqh - 1 - r));
         for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
     }
     __syncthreads();
@@ -390,7 +439,7 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
             double x1 = 0.0, x2 = 0.0;
             for (int r = 0; r < D; ++r) {
                 x1 += x[r] * x[r];
-                for (int c = 0; c < D; ++c) x2 += J.sig1b[r * D + c] * x[r] * x[c];
+                for (int cc = 0; cc < D; ++cc) x2 += J.sig1b[r * D + cc] * x[r] * x[cc];
             }
             if (x1 > 0.01) { a1 += x2; b1 += x1 * p1[0]; c1 += x1; }
             else if (x1 > 1.e-5) { a2 += x2; b2 += x1 * p1[0]; c2 += x1; }

@@ -169,6 +169,36 @@ __global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long lo
     }
 }
 
+// Segment table of the sorted interaction (prepare_for_reading,
+// source/BcDor-Vpp_potential.cpp:478-496): element i opens the segment of its
+// (charge sum, parity, J) key when the previous element's key differs and closes it
+// when the next one's differs.  A key opened twice means the list is not sorted by
+// key; an element with an orbit out of range or a key off the table is reported by
+// the smallest such index (bad[0]) and its reason (bad[1]: 1 orbit, 2 key).
+__device__ inline int interaction_key(int k, int norb, const int *orb_sh, const int *ch, const int *ip, int *why) {
+    const int J = k % kJMult, ab = k / kJMult, a = ab / kABMult, b = ab % kABMult;
+    if (k < 0 || a < 0 || b < 0 || a >= norb || b >= norb) { *why = 1; return -1; }
+    const int key = ind_chipJ(ch[orb_sh[a]] + ch[orb_sh[b]], (ip[orb_sh[a]] + ip[orb_sh[b]]) % 2, J);
+    if (key < 0 || key >= kSegTable) { *why = 2; return -1; }
+    return key;
+}
+
+__global__ void k_segments(const int *iabJ, int n, int norb, const int *orb_sh, const int *ch, const int *ip,
+                           int *seg_str, int *seg_end, int *seg_cnt, int *bad) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int why = 0, w2 = 0;
+    const int key = interaction_key(iabJ[i], norb, orb_sh, ch, ip, &why);
+    if (key < 0) {
+        if (atomicMin(&bad[0], i) > i) atomicExch(&bad[1], why);
+        return;
+    }
+    const int prev = i > 0 ? interaction_key(iabJ[i - 1], norb, orb_sh, ch, ip, &w2) : -1;
+    const int next = i + 1 < n ? interaction_key(iabJ[i + 1], norb, orb_sh, ch, ip, &w2) : -1;
+    if (key != prev) { seg_str[key] = i; atomicAdd(&seg_cnt[key], 1); }
+    if (key != next) seg_end[key] = i;
+}
+
 // Gather rows in a given order into separate SoA arrays (used after the sort), plus an
 // FP32 copy of the couplings for the FP32-vector Lanczos form.
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,

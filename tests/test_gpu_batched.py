@@ -18,16 +18,23 @@ def test_batched_equals_per_channel_calls(bdmod, problems):
         ra, rb = a.result(ish), b.result(ish)
         for k in ("qp", "qh", "koltun"):
             assert np.isfinite(ra[k]).all() and np.isfinite(rb[k]).all(), (ish, k)
-            np.testing.assert_allclose(ra[k], rb[k], rtol=1e-12, atol=1e-12)
+        # a channel launched alone runs on 16-CTA clusters, batched ones on 8: the sums
+        # differ in order, so members of exact degeneracies may rotate; compare what is
+        # basis-independent
+        for tag in ("qp", "qh"):
+            assert len(ra[tag]) == len(rb[tag])
+            e, z = strong_diffs(ra[tag], rb[tag])
+            assert e < 1e-10 and z < 1e-10, (ish, tag, e, z)
+        np.testing.assert_allclose(ra["koltun"], rb["koltun"], rtol=1e-10, atol=1e-12)
         c.sigma2_build(ish, copy=False)
         pv = p.piv
         c.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish])
         D = p.ms.no[ish]
         rc = c.dyson_solve(ish, np.diag(p.ms.orb_xe[p.ms.orb_start[ish]:p.ms.orb_start[ish] + D]))
-        np.testing.assert_allclose(ra["koltun"], rc["koltun"], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(ra["koltun"], rc["koltun"], rtol=1e-10, atol=1e-12)
         for tag in ("qp", "qh"):
             e, z = strong_diffs(ra[tag], rc[tag])
-            assert e < 1e-12 and z < 1e-10
+            assert e < 1e-10 and z < 1e-10
     for x in (a, b, c):
         x.close()
 
@@ -86,5 +93,27 @@ def test_errors_are_status_codes(bdmod, problems):
     rc = ctx.lib.bd_sigma2_build(ctx.h, 0, fw.ctypes.data_as(C.POINTER(C.c_double)), 0, C.byref(n), None, 0, None)
     assert rc == bdmod.BD_ERR_CAPACITY
     ctx.run_all(lanczos=True)                                # the context stays usable
+    assert np.isfinite(ctx.koltun_all()).all()
+    ctx.close()
+
+
+def test_bad_interaction_lists_are_refused(bdmod, problems):
+    """The device scan of the interaction list rejects an orbit out of range and a list
+    that is not grouped by (charge, parity, J); the context stays usable."""
+    import dataclasses
+    p = problems(2, 20.0, 0, 0)
+    v = p.vpp
+    bad_orbit = v.iabJ.copy()
+    bad_orbit[5] = ((p.ms.norb + 3) * 1024 + 0) * 128 + 1
+    order = np.arange(v.n)
+    order[[0, v.n - 1]] = order[[v.n - 1, 0]]                  # first and last element swapped
+    ctx = bdmod.Context()
+    for vv, msg in ((dataclasses.replace(v, iabJ=bad_orbit), "orbit out of range"),
+                    (dataclasses.replace(v, iabJ=v.iabJ[order], icdJ=v.icdJ[order], V=v.V[order]), "not sorted")):
+        with pytest.raises(bdmod.BDError) as e:
+            ctx.upload(dataclasses.replace(p, vpp=vv))
+        assert e.value.code == bdmod.BD_ERR_ARG and msg in str(e.value)
+    ctx.upload(p)
+    ctx.run_all(lanczos=False)
     assert np.isfinite(ctx.koltun_all()).all()
     ctx.close()
