@@ -121,8 +121,10 @@ struct bd_ctx {
     int *d_lzstat = nullptr;
     size_t lzV_bytes = 0;
     long long lzout_total = 0;
-    std::vector<long long> lz_int_off[2], lz_piv_off[2], lz_slice_off[2];
+    std::vector<long long> lz_int_off[2], lz_piv_off[2], lz_slice_off[2], lz_grp_off[2], lz_slot_off[2];
     char *d_lzslice = nullptr;
+    char *d_lzgrp = nullptr;     // per chain: energy groups (2N doubles, then N + 1 ints)
+    int *d_lzslot = nullptr;     // per chain: vector slot of every row
     LzChain *d_chains = nullptr;
     int lz_two_pass = 0;
     // Dyson
@@ -466,6 +468,12 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
             z.V = ctx->d_lzV + ctx->lz_v_off[dir][I];
             z.out = ctx->d_lzout + ctx->lz_out_off[dir][I];
             z.stat = ctx->d_lzstat;
+            {
+                char *g = ctx->d_lzgrp + ctx->lz_grp_off[dir][I];
+                z.gE = reinterpret_cast<const double *>(g);
+                z.gInfo = reinterpret_cast<const int *>(g + (size_t)16 * P.N);
+                z.rowslot = ctx->d_lzslot + ctx->lz_slot_off[dir][I];
+            }
             z.slice = ctx->d_lzslice + ctx->lz_slice_off[dir][I];
             z.slice_stride = ((long long)z.S * 17 + 255) / 256 * 256;
             if (reinterpret_cast<uintptr_t>(z.slice) % 256 != 0 ||
@@ -493,6 +501,8 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     // chain descriptors live in a small device array (one slot per chain of the range)
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
     CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
+    CU(launch_lz_groups(d_ch, (int)ch.size(), ctx->st));   // energy groups for the deflated tails
+    ctx->launches += 1;
     CU(cudaEventRecord(ctx->ev_lz[0], ctx->st));
     // chains whose slices do not fit next to the scalars keep them in global memory
     const bool gslices = ctx->lz_slices == 2 || (ctx->lz_slices == 0 && lanczos_smem_bytes(Smax, rmax) > kLanczosSmemSliceCap);
@@ -585,6 +595,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
             J.E_bk = ctx->d_Ebk + C.bk_off; J.M_bk = ctx->d_Mbk + C.mbk_off;
         }
         J.n = C.D + J.nfw + J.nbk;
+        J.nc = J.n;   // k_dyson_deflate sets the order after deflation
         if (J.n != dyson_order(ctx, I, lanczos)) return fail(ctx, BD_ERR_STATE, "Dyson layout mismatch");
         J.sighf = ctx->d_sighf + ctx->chan_dd_off[I];
         J.sig1b = ctx->d_sig1b + ctx->chan_dd_off[I];
@@ -626,8 +637,10 @@ int alloc_lanczos(bd_ctx *ctx) {
         ctx->lz_int_off[dir].assign(ctx->nsubsh, 0);
         ctx->lz_piv_off[dir].assign(ctx->nsubsh, 0);
         ctx->lz_slice_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_grp_off[dir].assign(ctx->nsubsh, 0);
+        ctx->lz_slot_off[dir].assign(ctx->nsubsh, 0);
     }
-    long long slices = 0;
+    long long slices = 0, groups = 0, slots = 0;
     std::vector<int> hints;
     std::vector<double> hpiv;
     for (int I = 0; I < ctx->nsubsh; ++I)
@@ -641,6 +654,10 @@ int alloc_lanczos(bd_ctx *ctx) {
             out += (long long)std::max(P.L, 0) * (P.nden_out + D);
             ctx->lz_slice_off[dir][I] = slices;
             if (P.L > 0) slices += lz_slice_bytes(P.N);
+            ctx->lz_grp_off[dir][I] = groups;
+            if (P.L > 0) groups += ((long long)16 * P.N + 4 * ((long long)P.N + 1) + 255) / 256 * 256;
+            ctx->lz_slot_off[dir][I] = slots;
+            slots += std::max(P.L, 0);
             ctx->lz_int_off[dir][I] = ints;
             // start[n_used+1] | last[n_used+1] | ipiv[nden_out + D]
             std::vector<int> st = P.start, la = P.last;
@@ -669,6 +686,8 @@ int alloc_lanczos(bd_ctx *ctx) {
     CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
     if ((rc = dalloc(ctx, &ctx->d_chains, (size_t)2 * ctx->nsubsh))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_lzslice, (size_t)slices))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_lzgrp, (size_t)groups))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_lzslot, (size_t)slots))) return rc;
     return BD_OK;
 }
 
@@ -1171,7 +1190,7 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     if (sig_hf) CU(cudaMemcpyAsync(ctx->d_sighf + ctx->chan_dd_off[ish], sig_hf, sizeof(double) * D * D, cudaMemcpyHostToDevice, ctx->st));
     else if ((rc = launch_ehf(ctx, ish, ish + 1))) return rc;
     DyJob J{};
-    J.ch = ish; J.D = D; J.j2 = C.j2; J.n = n; J.nfw = n_fw; J.nbk = n_bk; J.nden = nden;
+    J.ch = ish; J.D = D; J.j2 = C.j2; J.n = n; J.nc = n; J.nfw = n_fw; J.nbk = n_bk; J.nden = nden;
     J.lanczos_fw = (ipiv_fw != nullptr) && n_fw > 0 && ipiv_fw[0] > 0;
     J.lanczos_bk = (ipiv_bk != nullptr) && n_bk > 0 && ipiv_bk[0] > 0;
     J.fw_rows = dfw; J.bk_rows = dbk; J.ipiv_fw = dipf; J.ipiv_bk = dipb;
@@ -1222,14 +1241,20 @@ int bd_lanczos_vectors(bd_ctx *ctx, int ish, int dir, int fp32, double *out, lon
     const int ld = lz_ld(P.N);
     const char *base = ctx->d_lzV + ctx->lz_v_off[dir][ish];
     CU(cudaStreamSynchronize(ctx->st));
+    // rows of a deflated tail have no stored vector: zero rows
+    std::vector<int> slot(std::max(P.L, 0));
+    if (P.L > 0)
+        CU(cudaMemcpy(slot.data(), ctx->d_lzslot + ctx->lz_slot_off[dir][ish], sizeof(int) * P.L, cudaMemcpyDeviceToHost));
     if (fp32) {
         std::vector<float> tmp((size_t)P.L * ld);
         CU(cudaMemcpy(tmp.data(), base, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost));
-        for (int j = 0; j < P.L; ++j) for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = tmp[(size_t)j * ld + i];
+        for (int j = 0; j < P.L; ++j)
+            for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = slot[j] < 0 ? 0.0 : tmp[(size_t)slot[j] * ld + i];
     } else {
         std::vector<double> tmp((size_t)P.L * ld);
         CU(cudaMemcpy(tmp.data(), base, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost));
-        for (int j = 0; j < P.L; ++j) for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = tmp[(size_t)j * ld + i];
+        for (int j = 0; j < P.L; ++j)
+            for (int i = 0; i < P.N; ++i) out[(size_t)j * P.N + i] = slot[j] < 0 ? 0.0 : tmp[(size_t)slot[j] * ld + i];
     }
     return BD_OK;
 }
@@ -1520,9 +1545,12 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     const bool fp32 = (flags & BD_RUN_MIXED) != 0;
     const int ld = lz_ld(N);
     const size_t vbytes = (size_t)P.L * (size_t)ld * (fp32 ? sizeof(float) : sizeof(double));
-    // the FP32 form also keeps an FP32 copy of M behind the vectors
+    // behind the vectors: an FP32 copy of M (FP32 form), the energy groups of the
+    // deflated tails (16 N + 4 (N + 1) bytes) and the row slots (4 L bytes)
     const size_t mf_off = kNoallocVectors + (vbytes + 255) / 256 * 256;
-    const size_t need = fp32 ? mf_off - kNoallocVectors + sizeof(float) * (size_t)D * (size_t)N : vbytes;
+    const size_t grp_off = mf_off + (fp32 ? (sizeof(float) * (size_t)D * (size_t)N + 255) / 256 * 256 : 0);
+    const size_t slot_off = grp_off + ((size_t)16 * N + 4 * ((size_t)N + 1) + 255) / 256 * 256;
+    const size_t need = slot_off + sizeof(int) * (size_t)P.L - kNoallocVectors;
     if (need > BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors)
         return noalloc_fail(err, err_len, BD_ERR_CAPACITY,
                             "%d Lanczos vectors of %d poles need %zu bytes of scratch; this entry point has %zu "
@@ -1548,6 +1576,9 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     z.ld = ld; z.S = S;
     z.E = d_E; z.M = d_M;
     z.Mf = fp32 ? reinterpret_cast<const float *>(base + mf_off) : nullptr;
+    z.gE = reinterpret_cast<const double *>(base + grp_off);
+    z.gInfo = reinterpret_cast<const int *>(base + grp_off + (size_t)16 * N);
+    z.rowslot = reinterpret_cast<int *>(base + slot_off);
     z.piv = reinterpret_cast<const double *>(base + kNoallocPiv);
     z.start = reinterpret_cast<const int *>(base + kNoallocInts);
     z.last = z.start + (P.n_used + 1);
@@ -1562,6 +1593,7 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     if (e == cudaSuccess) e = cudaMemsetAsync(d_rows, 0, row_bytes, st);   // the reference clears the rows
     if (e == cudaSuccess && fp32)
         e = launch_to_float(d_M, reinterpret_cast<float *>(base + mf_off), (long long)D * N, st);
+    if (e == cudaSuccess) e = launch_lz_groups(reinterpret_cast<const LzChain *>(base), 1, st);
     if (e == cudaSuccess)
         e = launch_lanczos(reinterpret_cast<const LzChain *>(base), 1, S, P.L + 1, fp32, kNoallocCluster, kNoallocEta,
                            false, st);

@@ -68,6 +68,12 @@ struct LzChain {
     int *stat;              // [2]: number of two-pass steps, error flag
     char *slice;            // per-CTA E / w / touched slices in global memory (large chains), CTA r at
     long long slice_stride; //   slice + r * slice_stride; unused when the slices live in shared memory
+    // Energy groups of the sorted poles (runs of equal E), from k_lz_groups: gE[q], and
+    // gInfo[0] = number of groups, gInfo[1 + q] = m_q - rank(M_q), the dimension of the
+    // group's eigenvectors of E that no coupling reaches.  nullptr: no deflation.
+    const double *gE;
+    const int *gInfo;
+    int *rowslot;           // [L] vector slot of every row, -1 for a deflated row (written at the end)
 };
 
 // Global scratch of one chain's slices: enough for any cluster size up to 16 with FP64
@@ -80,6 +86,7 @@ __host__ __device__ inline long long lz_slice_bytes(long long N) {
 // One Dyson eigenproblem.
 struct DyJob {
     int ch, D, n, j2;
+    int nc;                  // order of the matrix after deflation (set by k_dyson_deflate)
     int nfw, nbk;            // pole-block sizes in the matrix
     int nden;                // leading doubles of the self-energy rows
     int lanczos_fw, lanczos_bk;  // whether the fw / bk parts are Lanczos rows

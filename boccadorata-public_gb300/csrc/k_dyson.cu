@@ -18,29 +18,131 @@ namespace cg = cooperative_groups;
 namespace bd {
 
 // ---------------------------------------------------------------- K3 assembly
-// One thread per matrix row.  Row order: D one-body rows, nfw forward poles,
-// nbk backward poles.
-__global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *row_first, long long total_rows) {
+// Row order of the full matrix: D one-body rows, nfw forward poles, nbk backward poles.
+//
+// Deflation: a pole row whose every off-diagonal entry is exactly zero (no coupling to
+// the orbitals, no beta to its neighbours, no fishbone entry) is an eigenvector of
+// the Dyson matrix by itself: eigenvalue its diagonal, no strength.  The deflated
+// tails of exhausted Lanczos chains are such rows, often most of a chain.  They are
+// taken out before the eigensolve; the matrix keeps the other rows in their order.
+
+// value of the coupling of pole i of part (0 fw, 1 bk) to orbital d
+__device__ inline double dy_mcoup(const DyJob &J, int part, int i, int d) {
+    const int NT = J.nden + J.D;
+    if (part == 0) return J.fw_rows ? J.fw_rows[(size_t)i * NT + J.nden + d] : J.M_fw[(size_t)d * J.nfw + i];
+    return J.bk_rows ? J.bk_rows[(size_t)i * NT + J.nden + d] : J.M_bk[(size_t)d * J.nbk + i];
+}
+
+__device__ inline double dy_diag(const DyJob &J, int part, int i) {
+    const int NT = J.nden + J.D;
+    const double *rows = part == 0 ? J.fw_rows : J.bk_rows;
+    return rows ? rows[(size_t)i * NT] : (part == 0 ? J.E_fw[i] : J.E_bk[i]);
+}
+
+// whether full-matrix row r has an off-diagonal entry
+__device__ inline bool dy_coupled(const DyJob &J, int r) {
+    const int D = J.D;
+    if (r < D) return true;
+    const int part = (r < D + J.nfw) ? 0 : 1;
+    const int i = r - (part == 0 ? D : D + J.nfw);
+    const int np = part == 0 ? J.nfw : J.nbk;
+    for (int d = 0; d < D; ++d) if (dy_mcoup(J, part, i, d) != 0.0) return true;
+    const bool lz = part == 0 ? J.lanczos_fw : J.lanczos_bk;
+    if (!lz) return false;
+    const int NT = J.nden + D;
+    const double *rows = part == 0 ? J.fw_rows : J.bk_rows;
+    const int *ipiv = part == 0 ? J.ipiv_fw : J.ipiv_bk;
+    if (i >= 1 && rows[(size_t)i * NT + 1] != 0.0) return true;
+    if (i + 1 < np && rows[(size_t)(i + 1) * NT + 1] != 0.0) return true;
+    for (int nc = 1; nc < ipiv[0]; ++nc) {
+        const int s = ipiv[nc + 1];
+        if (s < 1 || s >= np) continue;
+        if (i == s - 1)
+            for (int nr = s; nr < np; ++nr) if (rows[(size_t)nr * NT + 1 + nc] != 0.0) return true;
+        if (i >= s && rows[(size_t)i * NT + 1 + nc] != 0.0) return true;
+    }
+    return false;
+}
+
+// One CTA per matrix: the compact index of every kept row (work area, ints; -1 for a
+// deflated row), the compact order into the job, and the deflated rows' solutions
+// [W, 0, 0 ..] staged behind R after the nc rows the eigensolver will stage.
+constexpr int kDfThreads = 256;
+
+__global__ void __launch_bounds__(kDfThreads) k_dyson_deflate(DyJob *jobs, int njobs, double *work,
+                                                              const long long *work_first) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.n, D = J.D, NS = 2 + D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int *map = reinterpret_cast<int *>(work + work_first[jid]);
+    __shared__ int wsum[kDfThreads / 32][2];
+    __shared__ int s_keep, s_defl;
+    if (tid == 0) { s_keep = 0; s_defl = 0; }
+    __syncthreads();
+    double *st = J.R + (size_t)D * n;
+    int nkept_total = 0;
+    // first pass: count kept rows (the deflated rows' staged positions start after them)
+    for (int b = 0; b < n; b += kDfThreads) {
+        const int r = b + tid;
+        const int keep = (r < n) && dy_coupled(J, r);
+        if (r < n) map[r] = keep;
+        int x = __syncthreads_count(keep);
+        nkept_total += x;
+    }
+    // second pass: ranks among kept / deflated rows, in row order
+    for (int b = 0; b < n; b += kDfThreads) {
+        const int r = b + tid;
+        const int keep = (r < n) ? map[r] : 0, defl = (r < n) ? !keep : 0;
+        int xk = keep, xd = defl;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int yk = __shfl_up_sync(0xffffffffu, xk, o), yd = __shfl_up_sync(0xffffffffu, xd, o);
+            if (lane >= o) { xk += yk; xd += yd; }
+        }
+        if (lane == 31) { wsum[warp][0] = xk; wsum[warp][1] = xd; }
+        __syncthreads();
+        int ok = s_keep, od = s_defl;
+        for (int q = 0; q < warp; ++q) { ok += wsum[q][0]; od += wsum[q][1]; }
+        if (r < n) {
+            if (keep) {
+                map[r] = ok + xk - 1;
+            } else {
+                map[r] = -1;
+                const int part = (r < D + J.nfw) ? 0 : 1;
+                const int i = r - (part == 0 ? D : D + J.nfw);
+                double *row = st + (size_t)(nkept_total + od + xd - 1) * NS;
+                row[0] = dy_diag(J, part, i);
+                for (int q = 1; q < NS; ++q) row[q] = 0.0;
+            }
+        }
+        __syncthreads();
+        if (tid == kDfThreads - 1) { s_keep = ok + xk; s_defl = od + xd; }
+        __syncthreads();
+    }
+    if (tid == 0) jobs[jid].nc = nkept_total;
+}
+
+// One thread per full-matrix row; kept rows are written at their compact index, in a
+// matrix of order nc (deflated columns hold zeros in every kept row).
+__global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *row_first, long long total_rows,
+                                 const double *work, const long long *work_first) {
     long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total_rows) return;
     int lo = 0, hi = njobs - 1;
     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (row_first[mid] <= g) lo = mid; else hi = mid - 1; }
     const DyJob J = jobs[lo];
     const int r = (int)(g - row_first[lo]);
-    const int n = J.n, D = J.D, nfw = J.nfw, nbk = J.nbk;
-    double *Ar = J.A + (size_t)r * n;
-    for (int c = 0; c < n; ++c) Ar[c] = 0.0;
-    // couplings of pole i of part (0 fw, 1 bk) to orbital d: from self-energy rows
-    // [E/alpha, *, .., M_0 ..] when given, else from the structure-of-arrays Sigma(2)
-    const int NT = J.nden + D;
-    auto mcoup = [&](int part, int i, int d) -> double {
-        if (part == 0) return J.fw_rows ? J.fw_rows[(size_t)i * NT + J.nden + d] : J.M_fw[(size_t)d * nfw + i];
-        return J.bk_rows ? J.bk_rows[(size_t)i * NT + J.nden + d] : J.M_bk[(size_t)d * nbk + i];
-    };
+    const int *map = reinterpret_cast<const int *>(work + work_first[lo]);
+    const int cr = map[r];
+    if (cr < 0) return;
+    const int nc = J.nc, D = J.D, nfw = J.nfw, nbk = J.nbk;
+    double *Ar = J.A + (size_t)cr * nc;
+    for (int c = 0; c < nc; ++c) Ar[c] = 0.0;
+    auto put = [&](int c, double v) { const int cc = map[c]; if (cc >= 0) Ar[cc] = v; };
     if (r < D) {
         for (int c = 0; c < D; ++c) Ar[c] = J.sig1b[r * D + c] + J.sighf[r * D + c];
-        for (int i = 0; i < nfw; ++i) Ar[D + i] = mcoup(0, i, r);
-        for (int i = 0; i < nbk; ++i) Ar[D + nfw + i] = mcoup(1, i, r);
+        for (int i = 0; i < nfw; ++i) put(D + i, dy_mcoup(J, 0, i, r));
+        for (int i = 0; i < nbk; ++i) put(D + nfw + i, dy_mcoup(J, 1, i, r));
         return;
     }
     const int part = (r < D + nfw) ? 0 : 1;
@@ -48,26 +150,23 @@ __global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *
     const int np = part == 0 ? nfw : nbk;
     const int i = r - off;
     const bool lz = part == 0 ? J.lanczos_fw : J.lanczos_bk;
-    const double *rowsp = part == 0 ? J.fw_rows : J.bk_rows;
-    for (int d = 0; d < D; ++d) Ar[d] = mcoup(part, i, d);
-    if (!lz) {
-        Ar[r] = rowsp ? rowsp[(size_t)i * NT] : (part == 0 ? J.E_fw[i] : J.E_bk[i]);
-        return;
-    }
-    const double *rows = rowsp;
+    for (int d = 0; d < D; ++d) Ar[d] = dy_mcoup(J, part, i, d);
+    Ar[cr] = dy_diag(J, part, i);
+    if (!lz) return;
+    const int NT = J.nden + D;
+    const double *rows = part == 0 ? J.fw_rows : J.bk_rows;
     const int *ipiv = part == 0 ? J.ipiv_fw : J.ipiv_bk;
     const int nbr = ipiv[0];  // branches (pivots used)
-    Ar[r] = rows[(size_t)i * NT + 0];
-    if (i >= 1) Ar[r - 1] = rows[(size_t)i * NT + 1];
-    if (i + 1 < np) Ar[r + 1] = rows[(size_t)(i + 1) * NT + 1];
+    if (i >= 1) put(r - 1, rows[(size_t)i * NT + 1]);
+    if (i + 1 < np) put(r + 1, rows[(size_t)(i + 1) * NT + 1]);
     // fishbone (:303-333): branch nc (1 .. nbr-1) starts at s = ipiv[nc+1];
     // row s-1 couples to every later row nr >= s with row_nr[1 + nc]
-    for (int nc = 1; nc < nbr; ++nc) {
-        const int s = ipiv[nc + 1];
+    for (int nc2 = 1; nc2 < nbr; ++nc2) {
+        const int s = ipiv[nc2 + 1];
         if (s < 1 || s >= np) continue;
         if (i == s - 1)
-            for (int nr = s; nr < np; ++nr) Ar[off + nr] = rows[(size_t)nr * NT + 1 + nc];
-        if (i >= s) Ar[off + s - 1] = rows[(size_t)i * NT + 1 + nc];
+            for (int nr = s; nr < np; ++nr) put(off + nr, rows[(size_t)nr * NT + 1 + nc2]);
+        if (i >= s) put(off + s - 1, rows[(size_t)i * NT + 1 + nc2]);
     }
 }
 
@@ -110,7 +209,7 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     const int jid = blockIdx.x / CL;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    const int n = J.n;
+    const int n = J.nc;   // order after deflation
     extern __shared__ double sm[];
     double *v = sm;
     double *p = v + nmax;
@@ -243,7 +342,9 @@ size_t tridiag_smem_bytes(int nmax, int cluster) {
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                          int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
-    k_dyson_assemble<<<(unsigned)((total_rows + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_dyson_deflate<<<njobs, kDfThreads, 0, st>>>(const_cast<DyJob *>(d_jobs), njobs, work, d_work_first);
+    k_dyson_assemble<<<(unsigned)((total_rows + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
+                                                                       d_work_first);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     size_t smem = tridiag_smem_bytes(nmax, cluster);

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int nj
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    const int n = J.n, D = J.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = J.nc, D = J.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;   // order after deflation
     __shared__ double red[kEigThreads / 32][8];
     __shared__ double sums[8];
     double *R = J.R;
@@ -129,7 +129,7 @@ __global__ void k_bisect_prep(const DyJob *jobs, int njobs, double *work, const 
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    const int n = J.n;
+    const int n = J.nc;
     float *f = reinterpret_cast<float *>(work + work_first[jid]);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double e = (i + 1 < n) ? J.e[i] : 0.0;
@@ -177,7 +177,8 @@ __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_firs
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
-    const int t = (int)(g - row_first[lo]), n = J.n;
+    const int t = (int)(g - row_first[lo]), n = J.nc;
+    if (t >= n) return;   // deflated rows need no eigenvalue
     const int b0 = J.blk[t], b1 = J.blk[n + t], m = b1 - b0 + 1, k = t - b0;
     const double *d = J.d + b0, *e2 = J.tau + b0;
     double glo, ghi, tnorm;
@@ -247,7 +248,8 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
-    const int k = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D;
+    const int k = (int)(g - row_first[lo]), n = J.nc, NS = 2 + J.D;
+    if (k >= n) return;
     const int b0 = J.blk[k], b1 = J.blk[n + k];
     const double *d = J.d, *e = J.e;
     double *Y = J.A;
@@ -329,8 +331,9 @@ __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs,
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
-    const int k0 = (int)(g - row_first[lo]), n = J.n, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31,
+    const int k0 = (int)(g - row_first[lo]), n = J.nc, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31,
               warp = tid >> 5;
+    if (k0 >= n) return;
     const int b0 = J.blk[k0], b1 = J.blk[n + k0];
     if (b0 == b1) return;
     __shared__ EigTol tl;
@@ -384,7 +387,8 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
-    const int k = (int)(g - row_first[lo]), n = J.n, D = J.D, NS = 2 + D;
+    const int k = (int)(g - row_first[lo]), n = J.nc, D = J.D, NS = 2 + D;
+    if (k >= n) return;
     const int b0 = J.blk[k], b1 = J.blk[n + k];
     double x[8];
 #pragma unroll
@@ -397,7 +401,7 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
     // rows [W, Z, x] staged behind R, by position; k_place orders them
     double z = 0.0;
     for (int dd = 0; dd < D; ++dd) z += x[dd] * x[dd];
-    double *st = J.R + (size_t)D * n + (size_t)k * NS;
+    double *st = J.R + (size_t)D * J.n + (size_t)k * NS;   // staging behind R sized for the full order
     st[0] = J.sol[(size_t)k * NS];
     st[1] = z;
     for (int dd = 0; dd < D; ++dd) st[2 + dd] = x[dd];

@@ -123,7 +123,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     double *Bs = c + rmax;
     double *Bn = Bs + kMaxScal;
     double *red = Bn + 2;
-    CT *cf = reinterpret_cast<CT *>(red + kLzWarps * kMaxScal);   // 16-byte aligned: 2 rmax + 290 doubles before
+    int *rowslot = reinterpret_cast<int *>(red + kLzWarps * kMaxScal);   // vector slot of every row, -1: deflated
+    CT *cf = reinterpret_cast<CT *>(rowslot + (rmax + 3) / 4 * 4);     // 16-byte aligned
     CT *Es, *w;
     unsigned char *touched;
     if constexpr (kGlobalSlices) {   // chains too long for shared memory: this CTA's slices in global scratch
@@ -140,12 +141,39 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int s_kmin;
     __shared__ int lt[16];       // vectors of a local pass
     __shared__ int s_nl;
+    __shared__ int lslot[8];     // slots of the earlier chains' last vectors (-1: deflated)
 
     VT *V = reinterpret_cast<VT *>(C.V);
     const CT *Mc = reinterpret_cast<const CT *>(sizeof(CT) == 4 ? static_cast<const void *>(C.Mf)
                                                                   : static_cast<const void *>(C.M));
     for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? (CT)C.E[i0 + i] : (CT)0; touched[i] = 0; }
     const double tau = (sizeof(VT) == 4) ? 1e-22 : 1e-48;
+    // Exhausted Krylov space: the squared residual after the sweeps at rounding level
+    // relative to its value before them.  The chain's remaining rows then continue with
+    // eigenvectors of E that no coupling reaches (energy groups from k_lz_groups): each
+    // such row is (E_q, 0, ..., 0), needs no vector, and deflates out of the Dyson matrix.
+    const double thr_exh = (sizeof(VT) == 4) ? 1e-9 : 1e-20;
+    const int Qg = C.gE ? C.gInfo[0] : 0;
+    int gq = 0, gused = 0;       // group cursor (identical in every CTA)
+    int nvec = 0;                // vectors stored so far
+    bool tail = false;           // rest of the current pivot chain deflated
+    bool contaminated = false;   // a restart vector was stored: no deflation from here on
+    int ndefl = 0;
+    auto next_slot = [&]() -> bool {   // advance to a group with an unused direction
+        while (gq < Qg && gused >= C.gInfo[1 + gq]) { ++gq; gused = 0; }
+        return gq < Qg;
+    };
+    auto deflated_row = [&](int jr) {  // consume a direction and write its row
+        double a = (gq < Qg) ? C.gE[gq] : C.gE[Qg - 1];
+        if (gq < Qg) ++gused;
+        if (rank == 0 && tid == 0) {
+            double *row = C.out + (size_t)jr * NT;
+            for (int q = 0; q < NT; ++q) row[q] = 0.0;
+            row[0] = a;
+        }
+        if (tid == 0) rowslot[jr] = -1;
+        ++ndefl;
+    };
 
     // block-wide sum of one double per thread, result in every thread
     auto block_sum = [&](double v) -> double {
@@ -162,8 +190,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     int extra = 0;        // sweeps beyond the first
     for (int j = 0; j < L; ++j) {
         const bool newv = (k + 1 < C.n_used) && (j == C.start[k + 1]);
-        if (newv) ++k;
+        if (newv) { ++k; tail = false; }
         __syncthreads();
+        if (tail) {
+            next_slot();
+            deflated_row(j);
+            continue;
+        }
         // (a) w = M.p  or  w = v_{j-1} * E   (source/BcDor-Lanczos.cpp:137-150)
         if (newv) {
             const double *p = C.piv + (size_t)k * D;
@@ -174,7 +207,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 w[i] = (CT)s;
             }
         } else {
-            const VT *vp = V + (size_t)(j - 1) * C.ld + i0;
+            const VT *vp = V + (size_t)rowslot[j - 1] * C.ld + i0;
             for (int i = tid; i < S; i += kLzThreads) w[i] = (CT)vp[i] * Es[i];
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
@@ -189,16 +222,16 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             // full sweeps follow (at least one), each repeated under the DGKS criterion.
             bool local = !newv && attempt == 0 && j > 0;
             for (;;) {
-                if (local && tid == 0) {
+                if (local && tid == 0) {   // slots of v_{j-1}, v_{j-2} and the earlier chains' last vectors
                     int n = 0;
-                    lt[n++] = j - 1;
-                    if (j >= 2) lt[n++] = j - 2;
+                    lt[n++] = rowslot[j - 1];
+                    if (j >= 2 && rowslot[j - 2] >= 0) lt[n++] = rowslot[j - 2];
                     for (int q = 0; q < k; ++q)
-                        if (C.last[q] < j - 2) lt[n++] = C.last[q];
+                        if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) lt[n++] = rowslot[C.last[q]];
                     s_nl = n;
                 }
                 __syncthreads();
-                const int nl = local ? s_nl : j;          // vectors in this pass
+                const int nl = local ? s_nl : nvec;       // stored vectors in this pass
                 auto tix = [&](int t) { return local ? lt[t] : t; };
                 // (b1) partial dot products <v_t, w> over the slice, one warp per t, 16-byte loads
                 for (int t = warp; t < nl; t += kLzWarps) {
@@ -302,10 +335,17 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (local) { local = false; ++pass; continue; }
                 // another full sweep while this one removed more than half of the squared norm
                 if (nfull++ > 0) ++extra;
-                if (j > 0 && nfull < 4 && n2 < eta2 * wn2_before) { ++pass; continue; }
+                if (nvec > 0 && nfull < 4 && n2 < eta2 * wn2_before) { ++pass; continue; }
+                break;
+            }
+            if (attempt == 0 && !contaminated && (n2 <= thr_exh * wn2_first || n2 == 0.0) && next_slot()) {
+                deflated_row(j);   // this chain's Krylov space is exhausted
+                tail = true;
+                done = true;
                 break;
             }
             if (attempt > 0 || !(n2 <= tau * wn2_first || n2 == 0.0)) break;
+            contaminated = true;
             // (c0) exhausted reachable subspace: an untouched pole's unit vector if one is left,
             // else a pseudo-random vector swept orthogonal to the basis in the second attempt
             int kl = INT_MAX;
@@ -324,7 +364,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             for (int r = 0; r < CL; ++r) kmin = min(kmin, *cluster.map_shared_rank(&s_kmin, r));
             if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
             if (kmin != INT_MAX) {
-                VT *vj = V + (size_t)j * C.ld + i0;
+                VT *vj = V + (size_t)nvec * C.ld + i0;
                 for (int i = tid; i < S; i += kLzThreads) {
                     const bool hit = (i0 + i == kmin);
                     vj[i] = hit ? (VT)1 : (VT)0;
@@ -336,6 +376,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     row[0] = C.E[kmin];
                     for (int d = 0; d < D; ++d) row[C.nden_out + d] = C.M[(size_t)d * N + kmin];
                 }
+                if (tid == 0) rowslot[j] = nvec;
+                ++nvec;
                 done = true;
             } else {
                 for (int i = tid; i < S; i += kLzThreads) w[i] = (i < ns) ? (CT)restart_value(i0 + i, j) : (CT)0;
@@ -347,6 +389,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         // (c) alpha, m, g of the final w (once per step; source/BcDor-Lanczos.cpp:180-214)
         const int nq = k;
         const int nsc = 1 + D + nq;
+        if (tid < nq) lslot[tid] = rowslot[C.last[tid]];
+        __syncthreads();
         {
             CT sa = 0, sm_[8], sg[8];
 #pragma unroll
@@ -359,7 +403,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
-                    if (q < nq) sg[q] += e * (CT)V[(size_t)C.last[q] * C.ld + i0 + i] * wi;
+                    if (q < nq && lslot[q] >= 0) sg[q] += e * (CT)V[(size_t)lslot[q] * C.ld + i0 + i] * wi;
             }
             const double sat = warp_sum((double)sa);
             if (lane == 0) red[warp * kMaxScal] = sat;
@@ -394,7 +438,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216)
         const double xa = tot[0] / n2;
         const double xb = sqrt(n2);
-        VT *vj = V + (size_t)j * C.ld + i0;
+        VT *vj = V + (size_t)nvec * C.ld + i0;
         if constexpr (sizeof(VT) == 4) {
             const float inv = (float)(1.0 / xb);
             for (int i = tid; i < S; i += kLzThreads) {
@@ -417,16 +461,22 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             for (int d = 0; d < D; ++d) row[C.nden_out + d] = tot[1 + d] / xb;
             if (newv) row[1] = row[1 + k];
         }
+        if (tid == 0) rowslot[j] = nvec;
+        ++nvec;
         __syncthreads();
     }
-    if (rank == 0 && tid == 0) atomicAdd(&C.stat[0], extra);
+    if (rank == 0 && tid == 0) { atomicAdd(&C.stat[0], extra); atomicAdd(&C.stat[2], ndefl); }
+    __syncthreads();
+    if (rank == 0 && C.rowslot)
+        for (int q = tid; q < L; q += kLzThreads) C.rowslot[q] = rowslot[q];
     cluster.sync();  // no CTA leaves while peers may still read its shared memory
 }
 
 size_t lanczos_smem_bytes(int S, int rmax, bool global_slices) {
     // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
     const size_t fixed = sizeof(double) * (2 * (size_t)rmax + (size_t)(rmax + 3) / 4 * 4 + kMaxScal + 2 +
-                                           (size_t)kLzWarps * kMaxScal) + 16;
+                                           (size_t)kLzWarps * kMaxScal) +
+                         sizeof(int) * (size_t)(rmax + 3) / 4 * 4 + 16;
     return global_slices ? fixed : fixed + sizeof(double) * 2 * (size_t)S + (size_t)S;
 }
 
@@ -476,6 +526,103 @@ __global__ void k_to_float(const double *in, float *out, long long n) {
 cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+}  // namespace bd
+
+namespace bd {
+// Energy groups of one chain's sorted poles (a CTA per chain): runs of bit-equal E,
+// and for each the dimension of its eigenvectors of E orthogonal to every coupling,
+// m_q - rank(M_q), M_q the group's rows of M.  The rank comes from the Gram matrix
+// M_q^T M_q by pivoted elimination, pivots above 1e-12 of the largest diagonal.
+constexpr int kGrpThreads = 256;
+
+__global__ void __launch_bounds__(kGrpThreads) k_lz_groups(const LzChain *chains, int nchains) {
+    const int cid = blockIdx.x;
+    if (cid >= nchains) return;
+    const LzChain C = chains[cid];
+    if (!C.gE) return;
+    double *gE = const_cast<double *>(C.gE);
+    int *gInfo = const_cast<int *>(C.gInfo);
+    const int N = C.N, D = C.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ int wsum[kGrpThreads / 32];
+    __shared__ int s_base;
+    // group starts by a chunked block scan of the "new energy" flags; gInfo[1 + q] holds
+    // the start of group q until the counts replace it
+    if (tid == 0) s_base = 0;
+    __syncthreads();
+    for (int b = 0; b < N; b += kGrpThreads) {
+        const int i = b + tid;
+        const int f = (i < N) && (i == 0 || C.E[i] != C.E[i - 1]);
+        int x = f;
+        for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        int off = s_base;
+        for (int q = 0; q < warp; ++q) off += wsum[q];
+        if (f) { gInfo[1 + off + x - 1] = i; gE[off + x - 1] = C.E[i]; }
+        __syncthreads();
+        if (tid == kGrpThreads - 1) s_base = off + x;
+        __syncthreads();
+    }
+    const int Q = s_base;
+    // availability per group, a warp per group
+    for (int q = warp; q < Q; q += kGrpThreads / 32) {
+        const int g0 = gInfo[1 + q];
+        const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
+        double G[8][8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) G[a][b] = 0.0;
+        for (int i = g0 + lane; i < g1; i += 32) {
+            double m[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) m[a] = (a < D) ? C.M[(size_t)a * N + i] : 0.0;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b <= a; ++b) G[a][b] += m[a] * m[b];
+        }
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b <= a; ++b)
+                for (int o = 16; o > 0; o >>= 1) G[a][b] += __shfl_xor_sync(0xffffffffu, G[a][b], o);
+        __syncwarp();
+        if (lane == 0) {
+            for (int a = 0; a < 8; ++a) for (int b = a + 1; b < 8; ++b) G[a][b] = G[b][a];
+            double gmax = 0.0;
+            for (int a = 0; a < D; ++a) gmax = fmax(gmax, G[a][a]);
+            int rank = 0;
+            bool used[8] = {false, false, false, false, false, false, false, false};
+            for (int st = 0; st < D && gmax > 0.0; ++st) {
+                int pv = -1;
+                double best = 1e-12 * gmax;
+                for (int a = 0; a < D; ++a) if (!used[a] && G[a][a] > best) { best = G[a][a]; pv = a; }
+                if (pv < 0) break;
+                used[pv] = true;
+                ++rank;
+                const double inv = 1.0 / G[pv][pv];
+                for (int a = 0; a < D; ++a) {
+                    if (used[a]) continue;
+                    const double f = G[a][pv] * inv;
+                    for (int b = 0; b < D; ++b) if (!used[b]) G[a][b] -= f * G[pv][b];
+                }
+            }
+            const int m = g1 - g0;
+            // starts are still needed by the next warps' groups: write the count aside first
+            gE[N + q] = (double)max(0, m - rank);
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < Q; q += kGrpThreads) gInfo[1 + q] = (int)gE[N + q];
+    if (tid == 0) gInfo[0] = Q;
+}
+
+cudaError_t launch_lz_groups(const LzChain *d_chains, int nchains, cudaStream_t st) {
+    if (nchains <= 0) return cudaSuccess;
+    k_lz_groups<<<nchains, kGrpThreads, 0, st>>>(d_chains, nchains);
     return cudaGetLastError();
 }
 }  // namespace bd

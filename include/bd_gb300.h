@@ -213,10 +213,12 @@ int       bd_set_lanczos_slices(bd_ctx *ctx, int mode);
  *
  * Scratch: a file-scope device array of BD_NOALLOC_SCRATCH_BYTES, held on every
  * device that loads the library until the process exits.  The Lanczos vectors
- * must fit in it: L * ld * 8 bytes, ld = N + 64 rounded up to a multiple of 32, at
- * most BD_NOALLOC_SCRATCH_BYTES - 4096; with BD_RUN_MIXED, L * ld * 4 bytes (rounded
- * up to 256) plus an FP32 copy of M (D * N * 4 bytes).  Larger chains are rejected
- * with BD_ERR_CAPACITY.  D <= 8 and n_pvt <= 9.
+ * must fit in it with their companions: L * ld * 8 bytes (L * ld * 4 with
+ * BD_RUN_MIXED, plus an FP32 copy of M, D * N * 4 bytes), ld = N + 64 rounded up to a
+ * multiple of 32, plus 20 N + 4 L bytes for the energy groups and row slots of the
+ * deflated tails, each part rounded up to 256 bytes, at most
+ * BD_NOALLOC_SCRATCH_BYTES - 4096 in all.  Larger chains are rejected with
+ * BD_ERR_CAPACITY.  D <= 8 and n_pvt <= 9.
  * The first call on each device looks up the array's device address; make that
  * first call before any stream capture on that device.  All calls share the
  * array, so calls that overlap on the GPU (two streams, two host threads) race.

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from helpers import first_breakdown
+from helpers import first_breakdown, strong_diffs
 
 pytestmark = pytest.mark.gpu
 
@@ -65,7 +65,11 @@ def test_basis_orthonormal_and_deterministic(bdmod, problems, mixed, tol):
         nfw, nbk = ctx.count_poles(ish)
         for d, N, tag in ((0, nfw, "lz_fw"), (1, nbk, "lz_bk")):
             V = ctx.lanczos_vectors(ish, d, len(lz1[tag]), N, fp32=mixed)
-            assert np.abs(V @ V.T - np.eye(len(V))).max() < tol, (ish, d)
+            stored = np.abs(V).max(1) > 0          # deflated rows keep no vector
+            Vs = V[stored]
+            assert np.abs(Vs @ Vs.T - np.eye(len(Vs))).max() < tol, (ish, d)
+            rows = lz1[tag]
+            assert np.all(rows[~stored, 1:] == 0.0), (ish, d)
         lz2 = ctx.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish], mixed=mixed)
         assert np.array_equal(lz1["lz_fw"], lz2["lz_fw"]) and np.array_equal(lz1["lz_bk"], lz2["lz_bk"])
     ctx.close()
@@ -95,7 +99,41 @@ def test_rows_are_an_exact_projection(bdmod, problems):
                 if 1 <= s < L:
                     for nr in range(s, L):
                         K[s - 1, nr] = K[nr, s - 1] = rows[nr, 1 + nc]
-            assert np.abs(T - K).max() < 1e-10 * np.abs(E).max(), (ish, d)
+            stored = np.abs(V).max(1) > 0
+            Ts, Ks = T[np.ix_(stored, stored)], K[np.ix_(stored, stored)]
+            assert np.abs(Ts - Ks).max() < 1e-10 * np.abs(E).max(), (ish, d)
+            # a deflated row: no coupling to any row, a pole energy on the diagonal
+            defl = ~stored
+            assert np.all(K[defl][:, ~defl] == 0.0) and np.all(K[~defl][:, defl] == 0.0)
+            assert np.all(np.isin(np.diag(K)[defl], E)), (ish, d)
+    ctx.close()
+
+
+def test_exhausted_chains_deflate(bdmod, problems, oracle):
+    """The unperturbed spectra have few distinct pole energies, so every pivot's Krylov
+    space is exhausted within a few steps.  The rest of each chain continues with
+    eigenvectors of E that no coupling reaches (deflated rows, no stored vector), and
+    the solution equals the oracle's sweep-continued chain on every strength-carrying
+    solution."""
+    p = problems(6, 20.0, 1, 50)
+    orc = oracle(6, 20.0, 1, 50)
+    ctx = bdmod.Context().upload(p)
+    ndefl = 0
+    for ish in (0, 12):
+        ctx.sigma2_build(ish, copy=False)
+        pv = p.piv
+        lz = ctx.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish])
+        nfw, nbk = ctx.count_poles(ish)
+        V = ctx.lanczos_vectors(ish, 0, len(lz["lz_fw"]), nfw)
+        ndefl += int((np.abs(V).max(1) == 0).sum())
+        D = p.ms.no[ish]
+        r = ctx.dyson_solve(ish, np.diag(p.ms.orb_xe[p.ms.orb_start[ish]:p.ms.orb_start[ish] + D]))
+        o2 = orc.run_channel(ish, True, passes=2)
+        for tag in ("qp", "qh"):
+            e, z = strong_diffs(o2[tag], r[tag])
+            assert e < 1e-9 and z < 1e-8, (ish, tag, e, z)
+        np.testing.assert_allclose(r["koltun"], o2["koltun"], rtol=1e-9, atol=1e-9)
+    assert ndefl > 0
     ctx.close()
 
 
