@@ -40,8 +40,8 @@ WORKLOAD = "nmax10_lanczos100"
 CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2, 3, 5, 6
 # Per-launch DRAM traffic of the FP32 Lanczos kernel on this workload, from the ncu
 # capture summarised in profiles/k_lanczos_float_nmax10_lanczos100_dram.md
-# (dram__bytes_read.sum 199 794 498 560 + dram__bytes_write.sum 606 455 040).
-LANCZOS_TRAFFIC_BYTES = 200_400_953_600
+# (dram__bytes_read.sum 23 065 856 + dram__bytes_write.sum 7 211 008).
+LANCZOS_TRAFFIC_BYTES = 30_276_864
 
 
 def parse():
@@ -82,29 +82,35 @@ def whole_job_rate(world, channels, step_s):
 # ------------------------------------------------------------------------------------------
 # shared helpers
 # ------------------------------------------------------------------------------------------
-def lanczos_sizes(ctx, prob):
-    """(N, L, n_pvt, D) of every Lanczos chain, with the sizing rules of Reduce_SelfEn_Lncz."""
+def lanczos_sizes(ctx, prob, with_index=False):
+    """(N, L, n_pvt, D) of every Lanczos chain, with the sizing rules of Reduce_SelfEn_Lncz
+    (with_index: also (ish, dir) of each)."""
     out = []
     for ish in range(prob.ms.nsubsh):
         nfw, nbk = ctx.count_poles(ish)
         D = int(prob.ms.no[ish])
-        for N, nit in ((nfw, prob.piv.n_fw[ish]), (nbk, prob.piv.n_bk[ish])):
+        for d, (N, nit) in enumerate(((nfw, prob.piv.n_fw[ish]), (nbk, prob.piv.n_bk[ish]))):
             tot = int(np.sum(nit[nit > 0]))
             if N < 1 or tot < 1:
                 continue
             if tot > N:
                 nit = np.array([int(N / tot * v + 1.0) for v in nit])
             L = min(int(np.sum(nit[nit > 0])), N)
-            out.append((N, L, len(nit), D))
+            out.append(((N, L, len(nit), D), (ish, d)) if with_index else (N, L, len(nit), D))
     return out
 
 
-def lanczos_algorithmic_bytes(chains, w):
-    """Per-launch algorithmic HBM bytes of the Lanczos kernel: every step reads all
-    earlier vectors once for the dot products and once for the update (w*N*L^2 over a
-    chain), plus E, v and the g vectors (w*N*(4+n_pvt)*L) and the M, E streams
-    (8*N*(2+D)*L)."""
-    return float(sum(w * N * (L * L + (4 + npv) * L) + 8 * N * (2 + D) * L for N, L, npv, D in chains))
+def lanczos_algorithmic_bytes(chains, w, stored=None):
+    """Per-launch algorithmic HBM bytes of the Lanczos kernel.  A built step reads all
+    earlier built vectors once for the dot products and once for the update (w*N*R^2
+    over a chain of R built vectors), plus E, v and the g vectors (w*N*(4+n_pvt)*R) and
+    the M, E streams (8*N*(2+D)*R); deflated rows of an exhausted Krylov space read
+    nothing.  stored: R per chain (default: every row built, R = L)."""
+    tot = 0.0
+    for q, (N, L, npv, D) in enumerate(chains):
+        R = L if stored is None else stored[q]
+        tot += w * N * (R * R + (4 + npv) * R) + 8 * N * (2 + D) * R
+    return float(tot)
 
 
 def measured_peaks():
@@ -301,7 +307,8 @@ def gpu_arm(args):
             print(json.dumps({"profile": args.profile, "workload": args.workload, "steps": args.steps,
                               "timings_ms": ms, "lanczos_kernel_ms": ctx.lanczos_kernel_ms(),
                               "extra_sweeps": ctx.two_pass_steps(),
-                              "lanczos_steps": sum(L for _, L, _, _ in lanczos_sizes(ctx, prob))}), flush=True)
+                              "lanczos_steps": sum(L for _, L, _, _ in lanczos_sizes(ctx, prob)),
+                              "lanczos_vectors_built": int(ctx.lanczos_stored().sum())}), flush=True)
         ctx.close()
         return 0
 
@@ -376,15 +383,20 @@ def gpu_arm(args):
             dist.destroy_process_group()
         return 0
 
-    chains = lanczos_sizes(ctx, prob)
-    alg = lanczos_algorithmic_bytes(chains, 4)
+    ctx.run_all(lanczos=True, mixed=True)           # the timed form's chains, for their built vectors
+    st = ctx.lanczos_stored()
+    chi = lanczos_sizes(ctx, prob, with_index=True)
+    chains = [c for c, _ in chi]
+    stored = [int(st[i, d]) for _, (i, d) in chi]
+    alg = lanczos_algorithmic_bytes(chains, 4, stored)
     lz_mean = statistics.mean(lz_ms)
     peak, src = measured_peaks()
     achieved = alg / (lz_mean / 1e3) / 1e9
     roof = {"kernel": "k_lanczos<float> (FP32 vectors, all 84 chains in one launch)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s",
-            "traffic": LANCZOS_TRAFFIC_BYTES, "algorithmic_bytes": alg, "kernel_ms": lz_mean}
+            "traffic": LANCZOS_TRAFFIC_BYTES, "algorithmic_bytes": alg, "kernel_ms": lz_mean,
+            "lanczos_rows": int(sum(c[1] for c in chains)), "lanczos_vectors_built": int(sum(stored))}
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args.workload, CPU_SAMPLE)

@@ -92,6 +92,7 @@ def load_library(path: str = LIB_PATH):
     lib.bd_diag_two_pass.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
     lib.bd_set_lanczos_slices.argtypes = [vp, C.c_int]
+    lib.bd_lanczos_stored.argtypes = [vp, _ip]
     lib.bd_lanczos_kernel_ms.argtypes = [vp]; lib.bd_lanczos_kernel_ms.restype = C.c_double
     lib.bd_launch_count.argtypes = [vp]; lib.bd_launch_count.restype = C.c_longlong
     return lib
@@ -214,6 +215,12 @@ class Context:
 
     def set_tuning(self, lz_cluster=8, dy_cluster=8, eta=0.70710678118654752):
         self._chk(self.lib.bd_set_tuning(self.h, lz_cluster, dy_cluster, eta))
+
+    def lanczos_stored(self):
+        """(nsubsh, 2) vectors built per chain in the last reduction (fw, bk)."""
+        out = np.zeros(2 * self.prob.ms.nsubsh, np.int32)
+        self._chk(self.lib.bd_lanczos_stored(self.h, _pi(out)))
+        return out.reshape(-1, 2)
 
     def set_lanczos_slices(self, mode: int):
         """0: by size (default), 1: shared memory, 2: global memory."""

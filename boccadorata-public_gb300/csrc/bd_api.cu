@@ -1438,6 +1438,24 @@ int bd_last_timings(bd_ctx *ctx, double *ms5) {
 int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
 double bd_lanczos_kernel_ms(bd_ctx *ctx) { return ctx ? ctx->lz_kernel_ms : -1.0; }
 long long bd_launch_count(bd_ctx *ctx) { return ctx ? ctx->launches : -1; }
+int bd_lanczos_stored(bd_ctx *ctx, int *stored) {
+    if (!ctx || !stored) return BD_ERR_ARG;
+    if (!ctx->have_pivots || !ctx->d_lzslot) return fail(ctx, BD_ERR_STATE, "no Lanczos reduction yet");
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->st));
+    for (int I = 0; I < ctx->nsubsh; ++I)
+        for (int dir = 0; dir < 2; ++dir) {
+            const int L = std::max(ctx->chans[I].lz[dir].L, 0);
+            std::vector<int> slot(L);
+            if (L) CU(cudaMemcpy(slot.data(), ctx->d_lzslot + ctx->lz_slot_off[dir][I], sizeof(int) * L,
+                                 cudaMemcpyDeviceToHost));
+            int c = 0;
+            for (int v : slot) c += (v >= 0);
+            stored[2 * I + dir] = c;
+        }
+    return BD_OK;
+}
+
 int bd_set_lanczos_slices(bd_ctx *ctx, int mode) {
     if (!ctx) return BD_ERR_ARG;
     if (mode < 0 || mode > 2) return fail(ctx, BD_ERR_ARG, "slice mode %d", mode);

@@ -190,6 +190,9 @@ int       bd_diag_two_pass(bd_ctx *ctx);
 double    bd_lanczos_kernel_ms(bd_ctx *ctx);
 long long bd_launch_count(bd_ctx *ctx);
 int       bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta);
+/* stored[2 * ish + dir]: Lanczos vectors the last reduction of each chain actually
+ * built (the other rows are the deflated tail of an exhausted Krylov space). */
+int       bd_lanczos_stored(bd_ctx *ctx, int *stored);
 /* Where the Lanczos kernel keeps each CTA's slice of the pole energies and of the
  * working vector: 0 = shared memory unless it would exceed 100 KB (default),
  * 1 = shared memory, 2 = global memory (for chains of any length). */
