@@ -252,7 +252,16 @@ void build_plan(bd_ctx *c) {
     c->blk_fw_first.clear(); c->blk_bk_first.clear(); c->blk_vp_first.clear();
     long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
     const int ns = c->nsubsh;
-    // triangle-valid (ia, ib) per Jab, and valid ig per (I, Jab)
+    // (ia <= ib) pairs satisfying the Jab triangle, in the reference's (ia, ib) order, kept
+    // only when they can carry 2p1h (particles in both) or 2h1p (holes in both) poles
+    std::vector<std::vector<int>> pairs(c->jmax + 1);
+    for (int Jab = 0; Jab <= c->jmax; ++Jab)
+        for (int ia = 0; ia < ns; ++ia)
+            for (int ib = ia; ib < ns; ++ib) {
+                if (tri_fail(c->j2[ia], c->j2[ib], 2 * Jab)) continue;
+                if (!(c->np[ia] > 0 && c->np[ib] > 0) && !(c->nh[ia] > 0 && c->nh[ib] > 0)) continue;
+                pairs[Jab].push_back(ia * ns + ib);
+            }
     for (int I = 0; I < ns; ++I) {
         Chan &C = c->chans[I];
         C.D = c->no[I]; C.j2 = c->j2[I]; C.ch = c->ch[I];
@@ -260,40 +269,46 @@ void build_plan(bd_ctx *c) {
         C.blk_first = (int)c->blocks.size(); C.vp_first = vp;
         int nfw = 0, nbk = 0;
         for (int Jab = 0; Jab <= c->jmax; ++Jab) {
-            std::vector<int> gl;
-            for (int ig = 0; ig < ns; ++ig) if (!tri_fail(c->j2[ig], c->j2[I], 2 * Jab)) gl.push_back(ig);
+            // triangle-valid ig for (I, Jab): all of them, those with holes (2p1h needs a
+            // hole in g) and those with particles (2h1p needs a particle in g)
+            std::vector<int> gl, gh, gp;
+            for (int ig = 0; ig < ns; ++ig) {
+                if (tri_fail(c->j2[ig], c->j2[I], 2 * Jab)) continue;
+                gl.push_back(ig);
+                if (c->nh[ig] > 0) gh.push_back(ig);
+                if (c->np[ig] > 0) gp.push_back(ig);
+            }
             if (gl.empty()) continue;
-            for (int ia = 0; ia < ns; ++ia)
-                for (int ib = ia; ib < ns; ++ib) {
-                    if (tri_fail(c->j2[ia], c->j2[ib], 2 * Jab)) continue;
-                    // blocks without poles add nothing to either list: skip them (and the
-                    // whole ig loop when (ia, ib) can carry neither 2p1h nor 2h1p poles)
-                    if (!(c->np[ia] > 0 && c->np[ib] > 0) && !(c->nh[ia] > 0 && c->nh[ib] > 0)) continue;
-                    const int nJab = std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2;
-                    for (int ig : gl) {
-                        if (c->ch[ia] + c->ch[ib] - c->ch[ig] != c->ch[I]) continue;
-                        if ((c->ip[ia] + c->ip[ib] + c->ip[ig] + c->ip[I]) % 2 != 0) continue;
-                        S2Block B{};
-                        B.ch = I; B.Jab = Jab; B.ia = ia; B.ib = ib; B.ig = ig;
-                        B.nJab = nJab;
-                        B.nJgd = std::abs((c->j2[ig] + c->j2[I]) / 2 - Jab + 1) % 2;
-                        int na = c->np[ia], nb = c->np[ib], ng = c->nh[ig], s = na * nb * ng;
-                        if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
-                        B.nfw = s;
-                        na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; s = na * nb * ng;
-                        if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
-                        B.nbk = s;
-                        if (B.nfw <= 0 && B.nbk <= 0) continue;
-                        B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
-                        B.vp_first = vp;
-                        B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
-                        c->blk_fw_first.push_back(fw + nfw);
-                        c->blk_bk_first.push_back(bk + nbk);
-                        c->blk_vp_first.push_back(vp);
-                        nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
-                        c->blocks.push_back(B);
-                    }
+            for (int ab : pairs[Jab]) {
+                const int ia = ab / ns, ib = ab % ns;
+                const bool pfw = c->np[ia] > 0 && c->np[ib] > 0, pbk = c->nh[ia] > 0 && c->nh[ib] > 0;
+                const std::vector<int> &cand = (pfw && pbk) ? gl : (pfw ? gh : gp);
+                const int nJab = std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2;
+                for (int ig : cand) {
+                    if (c->ch[ia] + c->ch[ib] - c->ch[ig] != c->ch[I]) continue;
+                    if ((c->ip[ia] + c->ip[ib] + c->ip[ig] + c->ip[I]) % 2 != 0) continue;
+                    S2Block B{};
+                    B.ch = I; B.Jab = Jab; B.ia = ia; B.ib = ib; B.ig = ig;
+                    B.nJab = nJab;
+                    B.nJgd = std::abs((c->j2[ig] + c->j2[I]) / 2 - Jab + 1) % 2;
+                    int na = c->np[ia], nb = c->np[ib], ng = c->nh[ig], s = na * nb * ng;
+                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
+                    B.nfw = s;
+                    na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; s = na * nb * ng;
+                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
+                    B.nbk = s;
+                    // blocks without poles add nothing to either list
+                    if (B.nfw <= 0 && B.nbk <= 0) continue;
+                    B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
+                    B.vp_first = vp;
+                    B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
+                    c->blk_fw_first.push_back(fw + nfw);
+                    c->blk_bk_first.push_back(bk + nbk);
+                    c->blk_vp_first.push_back(vp);
+                    nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
+                    c->blocks.push_back(B);
                 }
+            }
         }
         C.nfw = nfw; C.nbk = nbk;
         C.nblk = (int)c->blocks.size() - C.blk_first;

@@ -70,16 +70,14 @@ __global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int nj
     }
 }
 
-// 1/q by Newton-Raphson, r <- r + r (1 - q r), from the FP32 reciprocal: two steps
-// take the 24-bit seed past FP64 precision.  Outside the FP32 range, plain division.
+// 1/q by one Newton-Raphson step, r <- r + r (1 - q r), from the FP32 reciprocal: the
+// 24-bit seed becomes ~48 bits, a relative error of ~4e-15 in each pivot, far inside
+// the bisection's 1e-12 stopping width.  Outside the FP32 range, plain division.
 __device__ inline double rcp_nr(double q) {
     const double aq = fabs(q);
     if (aq > 1e-36 && aq < 1e36) {
-        double r = (double)__frcp_rn((float)q);
-        double t = fma(-q, r, 1.0);
-        r = fma(r, t, r);
-        t = fma(-q, r, 1.0);
-        return fma(r, t, r);
+        const double r = (double)__frcp_rn((float)q);
+        return fma(r, fma(-q, r, 1.0), r);
     }
     return 1.0 / q;
 }
@@ -190,20 +188,20 @@ __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_firs
         const double pivmin = fmax(tnorm * 1e-300, 1e-290);
         const double g0 = glo - 2.0 * kEps * tnorm - 1e-300, g1 = ghi + 2.0 * kEps * tnorm + 1e-300;
         // W_k is the unique x with count(x) <= k < count(x + 0).
-        // FP32 bracket to 1e-5 |T| on the rounded block (its eigenvalues move by ~1e-7 |T|)
+        // FP32 bracket to 2e-6 |T| on the rounded block (its eigenvalues move by ~1e-7 |T|)
         const float *df = reinterpret_cast<const float *>(work + work_first[lo]) + b0;
         const float *e2f = reinterpret_cast<const float *>(work + work_first[lo]) + n + b0;
         float e2max = 1.0f;
         for (int i = 0; i + 1 < m; ++i) e2max = fmaxf(e2max, e2f[i]);
         const float pivf = 1e-30f * e2max;
         float af = (float)g0, bf = (float)g1;
-        for (int it = 0; it < 40 && (double)bf - (double)af > 1e-5 * tnorm; ++it) {
+        for (int it = 0; it < 40 && (double)bf - (double)af > 2e-6 * tnorm; ++it) {
             const float mid = 0.5f * (af + bf);
             if (mid == af || mid == bf) break;
             if (sturm_count_f(df, e2f, m, mid, pivf) > k) bf = mid; else af = mid;
         }
-        // widen by 2e-5 |T|, check in FP64, else start over from the Gershgorin interval
-        const double margin = 2e-5 * tnorm;
+        // widen by 4e-6 |T|, check in FP64, else start over from the Gershgorin interval
+        const double margin = 4e-6 * tnorm;
         double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
         if (!(sturm_count(d, e2, m, a, pivmin) <= k && sturm_count(d, e2, m, b, pivmin) > k)) { a = g0; b = g1; }
         for (int it = 0; it < 200; ++it) {
@@ -424,15 +422,51 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
     atomicAdd(&nbelow, c);
     __syncthreads();
     const int nqh = nbelow, nqp = n - nbelow;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double w = st[(size_t)k * NS];
-        int r = 0;   // ascending rank
-        for (int q = 0; q < n; ++q) {
-            const double wq = st[(size_t)q * NS];
-            r += (wq < w) || (wq == w && q < k);
+    // ascending rank of every staged row (ties by position): rows in tiles of eight per
+    // thread, compared against the energies staged in shared memory 2048 at a time.
+    // The energies are compared as order-preserving 64-bit integer keys (negative
+    // values bit-inverted, others with the sign bit set): FP64 compares would issue on
+    // the FP64 pipe, 1/64 of the integer rate here.
+    constexpr int kChunk = 2048, kPer = 8;
+    __shared__ unsigned long long wbuf[kChunk];
+    auto key = [](double x) -> unsigned long long {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+        return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+    };
+    const int tile = kPer * blockDim.x;
+    for (int k0 = 0; k0 < n; k0 += tile) {
+        int r[kPer];
+        unsigned long long w[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int k = k0 + threadIdx.x + u * blockDim.x;
+            r[u] = 0;
+            w[u] = key((k < n) ? st[(size_t)k * NS] : 0.0);
         }
-        const int row = (r >= nqh) ? (n - 1 - r) : (nqp + (nqh - 1 - r));
-        for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
+        for (int q0 = 0; q0 < n; q0 += kChunk) {
+            const int qn = min(kChunk, n - q0);
+            __syncthreads();
+            for (int q = threadIdx.x; q < qn; q += blockDim.x) wbuf[q] = key(st[(size_t)(q0 + q) * NS]);
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) {
+                const int k = k0 + threadIdx.x + u * blockDim.x;
+                if (k >= n) continue;
+                int c2 = 0;
+                for (int q = 0; q < qn; ++q) {
+                    const unsigned long long wq = wbuf[q];
+                    c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
+                }
+                r[u] += c2;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int k = k0 + threadIdx.x + u * blockDim.x;
+            if (k >= n) continue;
+            const int row = (r[u] >= nqh) ? (n - 1 - r[u]) : (nqp + (nqh - 1 - r[u]));
+            for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -461,8 +495,11 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
     k_qrows<<<njobs, kEigThreads, 0, st>>>(d_jobs, njobs);
     k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs, work, d_work_first);
     const unsigned nb = (unsigned)((total_rows + 127) / 128);
-    k_bisect<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
-    k_invit<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
+    // a warp per CTA: a matrix's few hundred eigenvalues spread over as many SMs
+    k_bisect<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
+                                                                d_work_first);
+    k_invit<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
+                                                               d_work_first);
     k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_post<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_place<<<njobs, 256, 0, st>>>(d_jobs, njobs);

@@ -100,9 +100,14 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
                     x2 = __dadd_rn(x2, __dmul_rn(__dmul_rn(xJab, fa[nbs]), fb[nas]));
                     if (nas == nbs) x2 = __ddiv_rn(x2, kSqr2);
                 }
+                // Terms with a zero amplitude factor add an exact zero to x1, which starts
+                // at +0 and so is never -0: skipping them changes no bit of the sum (with the
+                // one-hot amplitudes of an unperturbed propagator, all but one term go).
+                if (x2 == 0.0) continue;
                 const double *Vr = V + (((size_t)nd * noa + nas) * nob + nbs) * nog;
                 for (int ngs = 0; ngs < nog; ++ngs) {
                     if (iig0 + ngs == iid && B.nJgd) continue;
+                    if (fg[ngs] == 0.0) continue;
                     x1 = __dadd_rn(x1, __dmul_rn(__dmul_rn(Vr[ngs], x2), fg[ngs]));
                 }
             }
