@@ -366,7 +366,7 @@ def gpu_arm(args):
             t0 = time.perf_counter()
             ctx2.upload(pq)
             ctx2.run_all(lanczos=True, mixed=True)
-            res = [ctx2.result(i) for i in range(nch)]
+            res = ctx2.results_all()
             barrier()
             dt = time.perf_counter() - t0
             d2h = int(sum(r["qp"].nbytes + r["qh"].nbytes + r["koltun"].nbytes for r in res))

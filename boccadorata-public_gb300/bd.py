@@ -58,7 +58,8 @@ class BDError(RuntimeError):
 EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload_problem", "bd_upload_pivots",
             "bd_count_poles", "bd_ehf", "bd_sigma2_build", "bd_lanczos_reduce", "bd_dyson_solve", "bd_run_all",
             "bd_sync", "bd_result_counts", "bd_result_fetch", "bd_result_koltun_all", "bd_last_timings",
-            "bd_dyson_rows", "bd_lanczos_vectors", "bd_upload_propagator", "bd_dressed_propagator"]
+            "bd_dyson_rows", "bd_lanczos_vectors", "bd_upload_propagator", "bd_dressed_propagator",
+            "bd_result_fetch_all"]
 
 
 def load_library(path: str = LIB_PATH):
@@ -88,6 +89,7 @@ def load_library(path: str = LIB_PATH):
     lib.bd_result_counts.argtypes = [vp, C.c_int, _ip, _ip]
     lib.bd_result_fetch.argtypes = [vp, C.c_int, _dp, C.c_int, _dp, C.c_int, _dp]
     lib.bd_result_koltun_all.argtypes = [vp, _dp]
+    lib.bd_result_fetch_all.argtypes = [vp, _dp, C.c_longlong, _ip, _dp]
     lib.bd_last_timings.argtypes = [vp, _dp]
     lib.bd_diag_two_pass.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
@@ -334,6 +336,20 @@ class Context:
         k = np.zeros(3 * self.prob.ms.nsubsh)
         self._chk(self.lib.bd_result_koltun_all(self.h, _pd(k)))
         return k.reshape(-1, 3)
+
+    def results_all(self):
+        """Every channel's result (as result()) from one device copy."""
+        ms = self.prob.ms
+        n = [sum(self.result_counts(i)) for i in range(ms.nsubsh)]
+        tot = sum(n[i] * (2 + int(ms.no[i])) for i in range(ms.nsubsh))
+        sol = np.zeros(max(tot, 1)); cnt = np.zeros(2 * ms.nsubsh, np.int32); kol = np.zeros(3 * ms.nsubsh)
+        self._chk(self.lib.bd_result_fetch_all(self.h, _pd(sol), len(sol), _pi(cnt), _pd(kol)))
+        out, o = [], 0
+        for i in range(ms.nsubsh):
+            NS = 2 + int(ms.no[i]); a, b = int(cnt[2 * i]), int(cnt[2 * i + 1])
+            rows = sol[o:o + (a + b) * NS].reshape(-1, NS); o += (a + b) * NS
+            out.append(dict(qp=rows[:a], qh=rows[a:a + b], koltun=kol[3 * i:3 * i + 3]))
+        return out
 
     def result_counts(self, ish):
         a, b = C.c_int(), C.c_int()

@@ -1371,6 +1371,21 @@ int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *so
     return BD_OK;
 }
 
+int bd_result_fetch_all(bd_ctx *ctx, double *sol, long long cap, int *counts, double *koltun) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
+    CU(cudaSetDevice(ctx->device));
+    long long need = 0;
+    for (int I = 0; I < ctx->nsubsh; ++I)
+        need += (long long)(ctx->res_nq[2 * I] + ctx->res_nq[2 * I + 1]) * (2 + ctx->chans[I].D);
+    if (sol && cap < need) return fail(ctx, BD_ERR_CAPACITY, "sol holds %lld doubles, %lld needed", cap, need);
+    // the channels' rows are contiguous on the device (every Dyson solution is kept)
+    if (sol && need) CU(cudaMemcpy(sol, ctx->d_dysol, sizeof(double) * need, cudaMemcpyDeviceToHost));
+    if (counts) std::memcpy(counts, ctx->res_nq.data(), sizeof(int) * 2 * ctx->nsubsh);
+    if (koltun) CU(cudaMemcpy(koltun, ctx->d_dykol, sizeof(double) * 3 * ctx->nsubsh, cudaMemcpyDeviceToHost));
+    return BD_OK;
+}
+
 int bd_result_koltun_all(bd_ctx *ctx, double *koltun) {
     if (!ctx || !koltun) return BD_ERR_ARG;
     if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");

@@ -469,24 +469,43 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
         }
     }
     __syncthreads();
+    // Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594): each thread
+    // takes quasiholes ne = tid, tid + blockDim, ... into its own three buckets by |x|^2
+    // (> 0.01, > 1e-5, the rest); the partials meet in a fixed order, so the sums are
+    // deterministic (the reference adds the rows one by one, ne from nqh - 1 down)
+    double acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = 0.0;
+    for (int ne = threadIdx.x; ne < nqh; ne += blockDim.x) {
+        const double *p1 = J.sol + (size_t)(nqp + ne) * NS, *x = p1 + 2;
+        double x1 = 0.0, x2 = 0.0;
+        for (int r = 0; r < D; ++r) {
+            x1 += x[r] * x[r];
+            for (int cc = 0; cc < D; ++cc) x2 += J.sig1b[r * D + cc] * x[r] * x[cc];
+        }
+        const int b = (x1 > 0.01) ? 0 : (x1 > 1.e-5) ? 1 : 2;
+        acc[b] += x2; acc[3 + b] += x1 * p1[0]; acc[6 + b] += x1;
+    }
+    __shared__ double kred[9][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        double v = acc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) kred[q][warp] = v;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
         J.nq[0] = nqp; J.nq[1] = nqh;
-        double a1 = 0, a2 = 0, a3 = 0, b1 = 0, b2 = 0, b3 = 0, c1 = 0, c2 = 0, c3 = 0;
-        for (int ne = nqh - 1; ne >= 0; --ne) {
-            const double *p1 = J.sol + (size_t)(nqp + ne) * NS, *x = p1 + 2;
-            double x1 = 0.0, x2 = 0.0;
-            for (int r = 0; r < D; ++r) {
-                x1 += x[r] * x[r];
-                for (int cc = 0; cc < D; ++cc) x2 += J.sig1b[r * D + cc] * x[r] * x[cc];
-            }
-            if (x1 > 0.01) { a1 += x2; b1 += x1 * p1[0]; c1 += x1; }
-            else if (x1 > 1.e-5) { a2 += x2; b2 += x1 * p1[0]; c2 += x1; }
-            else { a3 += x2; b3 += x1 * p1[0]; c3 += x1; }
+        double t[9];
+        for (int q = 0; q < 9; ++q) {
+            t[q] = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t[q] += kred[q][w];
         }
         const double xj = (double)J.j2 + 1.0;
-        J.koltun[0] = (a1 + a2 + a3) * xj;
-        J.koltun[1] = (b1 + b2 + b3) * xj;
-        J.koltun[2] = (c1 + c2 + c3) * xj;
+        J.koltun[0] = (t[0] + t[1] + t[2]) * xj;
+        J.koltun[1] = (t[3] + t[4] + t[5]) * xj;
+        J.koltun[2] = (t[6] + t[7] + t[8]) * xj;
     }
 }
 

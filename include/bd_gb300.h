@@ -160,6 +160,11 @@ int bd_result_fetch(bd_ctx *ctx, int ish, double *sol_qp, int cap_qp, double *so
                     double *koltun);
 /* koltun[3 * nsubsh] for every channel with one copy. */
 int bd_result_koltun_all(bd_ctx *ctx, double *koltun);
+/* Every channel's solutions with one copy: sol receives, channel after channel, the
+ * rows bd_result_fetch gives (n_qp quasiparticles, then n_qh quasiholes, 2 + D doubles
+ * each); counts[2 * ish] = n_qp, counts[2 * ish + 1] = n_qh; koltun[3 * nsubsh].  cap is
+ * the number of doubles sol holds (any pointer may be NULL). */
+int bd_result_fetch_all(bd_ctx *ctx, double *sol, long long cap, int *counts, double *koltun);
 
 /* Replace the input propagator, keeping the model space and the interaction resident
  * (a new iteration of Run_itrs).  Pole counts, the block plan and the Lanczos chain

@@ -117,3 +117,15 @@ def test_bad_interaction_lists_are_refused(bdmod, problems):
     ctx.run_all(lanczos=False)
     assert np.isfinite(ctx.koltun_all()).all()
     ctx.close()
+
+
+def test_results_all_in_one_copy(bdmod, problems):
+    p = problems(4, 20.0, 0, 20)
+    ctx = bdmod.Context().upload(p)
+    ctx.run_all(lanczos=True)
+    allr = ctx.results_all()
+    for ish in range(p.ms.nsubsh):
+        r = ctx.result(ish)
+        for k in ("qp", "qh", "koltun"):
+            assert np.array_equal(allr[ish][k], r[k]), (ish, k)
+    ctx.close()
