@@ -6,8 +6,9 @@
 //   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows)
 //   k_bisect_prep  splits T into unreduced blocks at negligible off-diagonals
 //   k_bisect  W_k by bisection on Sturm counts over its block, one thread per
-//             eigenvalue: an FP32 bracketing phase (FP64 issues at 1/64 of the FP32
-//             rate), checked and finished in FP64 to max(1e-12 |W|, 1e-13 |T_b|)
+//             eigenvalue (eig_sturm.cuh): an FP32 bracket, checked and finished in
+//             double-float arithmetic (FP64 issues at 1/64 of the FP32 rate) to
+//             max(1e-12 |W|, 1e-13 |T_b|)
 //   k_invit   y_k by inverse iteration on T_b - W_k I (tridiagonal LU with partial
 //             pivoting) over its block, one thread per eigenvalue, each from its own
 //             start vector
@@ -20,6 +21,7 @@
 //             Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
 #include "bd_common.cuh"
 #include "bd_kernels.h"
+#include "eig_sturm.cuh"
 
 namespace bd {
 
@@ -70,83 +72,90 @@ __global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int nj
     }
 }
 
-// 1/q by one Newton-Raphson step, r <- r + r (1 - q r), from the FP32 reciprocal: the
-// 24-bit seed becomes ~48 bits, a relative error of ~4e-15 in each pivot, far inside
-// the bisection's 1e-12 stopping width.  Outside the FP32 range, plain division.
-__device__ inline double rcp_nr(double q) {
-    const double aq = fabs(q);
-    if (aq > 1e-36 && aq < 1e36) {
-        const double r = (double)__frcp_rn((float)q);
-        return fma(r, fma(-q, r, 1.0), r);
-    }
-    return 1.0 / q;
-}
-
-// number of eigenvalues of T strictly below x (negative pivots of the LDL^T of T - x I)
-__device__ inline int sturm_count(const double *d, const double *e2, int n, double x, double pivmin) {
-    int c = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    c += (q < 0.0);
-    for (int i = 1; i < n; ++i) {
-        q = fma(-e2[i - 1], rcp_nr(q), d[i] - x);
-        if (fabs(q) < pivmin) q = -pivmin;
-        c += (q < 0.0);
-    }
-    return c;
-}
-
-__device__ inline int sturm_count_f(const float *d, const float *e2, int n, float x, float pivmin) {
-    int c = 0;
-    float q = d[0] - x;
-    if (fabsf(q) < pivmin) q = -pivmin;
-    c += (q < 0.0f);
-    for (int i = 1; i < n; ++i) {
-        q = (d[i] - x) - e2[i - 1] / q;
-        if (fabsf(q) < pivmin) q = -pivmin;
-        c += (q < 0.0f);
-    }
-    return c;
-}
-
 // ------------------------------------------------------------------ K4c
-// Split T where an off-diagonal is negligible, |e_i| <= eps (|d_i| + |d_{i+1}|) (the
-// relative split test of the QR / bisection codes; the perturbation is below the
-// rounding of T).  The Dyson matrices' tridiagonal forms fall apart into many blocks:
-// the exactly degenerate poles of the HO spectrum give identical eigenvalues in
-// different blocks, whose eigenvectors then have disjoint supports and need no
-// orthogonalisation.  Every later kernel works on the block of its own position:
-// positions are block-major, eigenvalues ascending within a block.
+// Split T where an off-diagonal is negligible (sturm::negligible, the relative split
+// test of the QR / bisection codes; the perturbation is below the rounding of T).
+// The Dyson matrices' tridiagonal forms fall apart into many blocks: the exactly
+// degenerate poles of the HO spectrum give identical eigenvalues in different blocks,
+// whose eigenvectors then have disjoint supports and need no orthogonalisation.
+// Every later kernel works on the block of its own position: positions are
+// block-major, eigenvalues ascending within a block.
 //
-// One CTA per matrix: e2 (squared off-diagonals, zero at splits) into the tau slot,
-// which k_qrows has consumed; FP32 copies of d and e2 at the start of the job's work
-// area (free until k_invit); the block bounds of every position into J.blk.
-constexpr double kEps = 2.220446049250313e-16;
+// One CTA per matrix.  Outputs:
+//   J.e        split off-diagonals (zero between blocks)
+//   J.blk      first and last position of each position's block
+//   J.tau      the block's 1-norm, max_i |d_i| + |e_{i-1}| + |e_i| (rounded up), at
+//              every position (k_qrows has consumed the reflector scalars)
+//   work       FP32 tables at the start of the job's work area (free until k_invit),
+//              n = J.nc entries each: d 2^-s as hi / lo pair, e_i^2 2^-2s as hi / lo
+//              pair (zero at a block's last row), and at each block's first position
+//              its scaled Gershgorin bounds and the exponent s (2^-s |T_b| in [1/2, 1))
+//   scratch    split flags and row sums behind them
+struct BisectTables {
+    float *dh, *dl, *eh, *el, *glo, *ghi, *rn;
+    int *sx, *flag;
+};
+
+__device__ inline BisectTables bisect_tables(double *work, int n) {
+    float *f = reinterpret_cast<float *>(work);
+    BisectTables t;
+    t.dh = f; t.dl = f + n; t.eh = f + 2 * n; t.el = f + 3 * n; t.glo = f + 4 * n; t.ghi = f + 5 * n;
+    t.sx = reinterpret_cast<int *>(f + 6 * n);
+    t.flag = reinterpret_cast<int *>(f + 7 * n);
+    t.rn = f + 8 * n;
+    return t;
+}
 
 __global__ void k_bisect_prep(const DyJob *jobs, int njobs, double *work, const long long *work_first) {
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.nc;
-    float *f = reinterpret_cast<float *>(work + work_first[jid]);
+    const BisectTables T = bisect_tables(work + work_first[jid], n);
+    int *bs = J.blk, *be = J.blk + n;
+    // 1. split flags, row Gershgorin intervals and row sums (each thread repeats the
+    //    split test of its left neighbour: identical inputs, identical answer)
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double e = (i + 1 < n) ? J.e[i] : 0.0;
-        if (i + 1 < n && fabs(e) <= kEps * (fabs(J.d[i]) + fabs(J.d[i + 1]))) e = 0.0;
-        if (i + 1 < n) J.e[i] = e;
-        J.tau[i] = e * e;
-        f[i] = (float)J.d[i];
-        f[n + i] = (float)(e * e);
+        const double di = J.d[i];
+        double er = 0.0, el = 0.0;
+        if (i + 1 < n) { er = J.e[i]; if (sturm::negligible(er, di, J.d[i + 1])) er = 0.0; }
+        if (i > 0) { el = J.e[i - 1]; if (sturm::negligible(el, J.d[i - 1], di)) el = 0.0; }
+        T.flag[i] = (i + 1 == n || er == 0.0);
+        float lo, hi, r;
+        sturm::gershgorin_row(di, fabs(el), fabs(er), lo, hi, r);
+        T.glo[i] = lo; T.ghi[i] = hi; T.rn[i] = r;
     }
     __syncthreads();
+    // 2. block bounds: one integer pass
     if (threadIdx.x == 0) {
-        int *bs = J.blk, *be = J.blk + n;
         int b0 = 0;
-        for (int i = 0; i < n; ++i) {
-            if (i + 1 == n || J.e[i] == 0.0) {
+        for (int i = 0; i < n; ++i)
+            if (T.flag[i]) {
                 for (int k = b0; k <= i; ++k) { bs[k] = b0; be[k] = i; }
                 b0 = i + 1;
             }
-        }
+    }
+    __syncthreads();
+    // 3. each block's first position reduces its block and picks the scale
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (bs[i] != i) continue;
+        const int b1 = be[i];
+        float lo = T.glo[i], hi = T.ghi[i], r = T.rn[i];
+        for (int q = i + 1; q <= b1; ++q) { lo = fminf(lo, T.glo[q]); hi = fmaxf(hi, T.ghi[q]); r = fmaxf(r, T.rn[q]); }
+        const int s = sturm::scale_exponent(fmaxf(fabsf(lo), fabsf(hi)));
+        const float sc = sturm::pow2f(-s);
+        T.glo[i] = lo * sc; T.ghi[i] = hi * sc; T.rn[i] = r; T.sx[i] = s;
+    }
+    __syncthreads();
+    // 4. scaled FP32 pairs; split off-diagonals back into J.e; block norms into J.tau
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int b0 = bs[i], b1 = be[i];
+        const double sc = sturm::pow2(-T.sx[b0]);
+        sturm::split(J.d[i] * sc, T.dh[i], T.dl[i]);
+        double e = (i + 1 < n) ? J.e[i] : 0.0;
+        if (i + 1 < n && i == b1) { e = 0.0; J.e[i] = 0.0; }
+        sturm::split(e * e * sc * sc, T.eh[i], T.el[i]);
+        J.tau[i] = (double)T.rn[b0];
     }
 }
 
@@ -157,20 +166,10 @@ __device__ inline int job_of(const long long *row_first, int njobs, long long g)
     return lo;
 }
 
-// Gershgorin interval and norm of the block [b0, b1]
-__device__ inline void block_bounds(const double *d, const double *e, int b0, int b1, double *glo, double *ghi,
-                                    double *tnorm) {
-    double lo = d[b0], hi = d[b0];
-    for (int i = b0; i <= b1; ++i) {
-        const double r = (i > b0 ? fabs(e[i - 1]) : 0.0) + (i < b1 ? fabs(e[i]) : 0.0);
-        lo = fmin(lo, d[i] - r); hi = fmax(hi, d[i] + r);
-    }
-    *glo = lo; *ghi = hi; *tnorm = fmax(fabs(lo), fabs(hi));
-}
-
-// One thread per position: the eigenvalue of its block with the position's local index.
+// One thread per position: the eigenvalue of its block with the position's local
+// index, by sturm::bisect (FP32 bracket, double-float finish; no FP64 in the counts).
 __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total,
-                         const double *work, const long long *work_first) {
+                         double *work, const long long *work_first) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
@@ -178,38 +177,12 @@ __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_firs
     const int t = (int)(g - row_first[lo]), n = J.nc;
     if (t >= n) return;   // deflated rows need no eigenvalue
     const int b0 = J.blk[t], b1 = J.blk[n + t], m = b1 - b0 + 1, k = t - b0;
-    const double *d = J.d + b0, *e2 = J.tau + b0;
-    double glo, ghi, tnorm;
-    block_bounds(J.d, J.e, b0, b1, &glo, &ghi, &tnorm);
     double W;
     if (m == 1) {
-        W = d[0];
+        W = J.d[t];
     } else {
-        const double pivmin = fmax(tnorm * 1e-300, 1e-290);
-        const double g0 = glo - 2.0 * kEps * tnorm - 1e-300, g1 = ghi + 2.0 * kEps * tnorm + 1e-300;
-        // W_k is the unique x with count(x) <= k < count(x + 0).
-        // FP32 bracket to 2e-6 |T| on the rounded block (its eigenvalues move by ~1e-7 |T|)
-        const float *df = reinterpret_cast<const float *>(work + work_first[lo]) + b0;
-        const float *e2f = reinterpret_cast<const float *>(work + work_first[lo]) + n + b0;
-        float e2max = 1.0f;
-        for (int i = 0; i + 1 < m; ++i) e2max = fmaxf(e2max, e2f[i]);
-        const float pivf = 1e-30f * e2max;
-        float af = (float)g0, bf = (float)g1;
-        for (int it = 0; it < 40 && (double)bf - (double)af > 2e-6 * tnorm; ++it) {
-            const float mid = 0.5f * (af + bf);
-            if (mid == af || mid == bf) break;
-            if (sturm_count_f(df, e2f, m, mid, pivf) > k) bf = mid; else af = mid;
-        }
-        // widen by 4e-6 |T|, check in FP64, else start over from the Gershgorin interval
-        const double margin = 4e-6 * tnorm;
-        double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
-        if (!(sturm_count(d, e2, m, a, pivmin) <= k && sturm_count(d, e2, m, b, pivmin) > k)) { a = g0; b = g1; }
-        for (int it = 0; it < 200; ++it) {
-            const double mid = 0.5 * (a + b);
-            if (b - a <= fmax(1e-12 * fmax(fabs(a), fabs(b)), 1e-13 * tnorm) + pivmin || mid == a || mid == b) break;
-            if (sturm_count(d, e2, m, mid, pivmin) > k) b = mid; else a = mid;
-        }
-        W = 0.5 * (a + b);
+        const BisectTables T = bisect_tables(work + work_first[lo], n);
+        W = sturm::bisect(T.dh + b0, T.dl + b0, T.eh + b0, T.el + b0, m, k, T.glo[b0], T.ghi[b0], T.sx[b0], nullptr);
     }
     J.sol[(size_t)t * (2 + J.D)] = W;   // eigenvalue parked in the W slot of its position
 }
@@ -227,12 +200,11 @@ __device__ inline unsigned hash32(unsigned x) {
     return x;
 }
 
+constexpr double kEps = 2.220446049250313e-16;
+
 struct EigTol { double onenrm, ortol, pertol; };
 
-__device__ inline EigTol eig_tol(const double *d, const double *e, int b0, int b1) {
-    double onenrm = 0.0;
-    for (int i = b0; i <= b1; ++i)
-        onenrm = fmax(onenrm, fabs(d[i]) + (i > b0 ? fabs(e[i - 1]) : 0.0) + (i < b1 ? fabs(e[i]) : 0.0));
+__device__ inline EigTol eig_tol(double onenrm) {
     EigTol t;
     t.onenrm = onenrm;
     t.ortol = 1e-6 * onenrm;
@@ -252,7 +224,7 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
     const double *d = J.d, *e = J.e;
     double *Y = J.A;
     if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
-    const EigTol tl = eig_tol(d, e, b0, b1);
+    const EigTol tl = eig_tol(J.tau[k]);
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
     // shift: walk to the start of the cluster inside the block, then apply the separation rule forward
     int k0 = k;
@@ -337,7 +309,7 @@ __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs,
     __shared__ EigTol tl;
     __shared__ double cbuf[1024];
     __shared__ double red[kEigThreads / 32];
-    if (tid == 0) tl = eig_tol(J.d, J.e, b0, b1);
+    if (tid == 0) tl = eig_tol(J.tau[k0]);
     __syncthreads();
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
     if (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) return;
