@@ -146,4 +146,8 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
     return 0.0;
 }
 
+// Largest Dyson order (after deflation) reduced in one CTA's shared memory; larger
+// matrices go to the cluster kernel.
+constexpr int kTsMax = 160;
+
 }  // namespace bd

@@ -5,10 +5,13 @@
 // (:542-594).  The reference calls LAPACK dsyevd for all eigenvectors but only
 // uses the first D components of each (:448-470).  Here:
 //   K3 k_dyson_assemble   fills the dense matrix row by row (:269-390),
-//   K4a k_tridiag         Householder reduction A = Q T Q^T, one thread-block
-//                         cluster per matrix (rows split across the CTAs),
+//   K4a k_tridiag_small   Householder reduction A = Q T Q^T of a matrix of order
+//                         <= 160 in one CTA's shared memory, with the first D rows of Q,
+//       k_tridiag         the same for larger orders, one thread-block cluster per
+//                         matrix (rows split across the CTAs, Q's rows by k_qrows),
 //   K4b..K5 (k_eig.cu)    eigenvalues and the first D eigenvector components of T,
 //                         back-transformed, split by E_F, Koltun sums.
+#include <algorithm>
 #include <cooperative_groups.h>
 #include "bd_common.cuh"
 #include "bd_kernels.h"
@@ -210,6 +213,7 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.nc;   // order after deflation
+    if (n <= kTsMax) return;   // k_tridiag_small's (the whole cluster leaves together)
     extern __shared__ double sm[];
     double *v = sm;
     double *p = v + nmax;
@@ -326,6 +330,150 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     cluster.sync();
 }
 
+// ---------------------------------------------------------------- K4a' small matrices
+// Matrices of order nc <= kTsMax (after deflation nearly all: the N_max = 10 channels
+// reduce to 11..94) are reduced by one CTA with the lower triangle resident in shared
+// memory, and the first D rows of Q = H_0 ... H_{n-3} (what k_qrows forms for the
+// cluster path) are updated in the same pass.  The SM's FP64 rate (two FMAs a cycle)
+// is the bound, so the symmetric product and the rank-2 update each take one FMA per
+// stored element with every lane busy:
+//   - p = A v: thread i walks row i of the lower triangle and then column i below the
+//     diagonal, which is row i of the upper triangle: p_i = sum_q A(max(i,q), min(i,q)) v_q,
+//     split in two halves of q over two threads, no atomics and no shuffles;
+//   - A -= v w^T + w v^T on the lower triangle: a warp takes rows i and m-1-i together,
+//     m+1 elements, so the triangle's rows balance;
+//   - sums (column norm, R v, p.v) are single-warp reductions.
+// Step k (trailing order m = n-k-1) has six barriers.
+constexpr int kTsThreads = 256;
+
+__device__ inline double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.nc, D = J.D;
+    if (n > kTsMax) return;   // the cluster kernel's
+    const int ld = n | 1;     // odd stride: column reads hit distinct bank pairs
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    extern __shared__ double sm[];
+    double *A = sm;                          // [n][ld], lower triangle
+    double *v = A + (size_t)n * ld;          // [n]
+    double *ph = v + n;                      // [2][n] halves of A v
+    double *w = ph + 2 * n;                  // [n]
+    double *R = w + n;                       // [D][n]
+    double *scb = R + (size_t)D * n;         // [2][4] tau, scal, K, flag by step parity | s_d[8] | rx[8]
+    for (int q = tid; q < n * n; q += kTsThreads) {
+        const int i = q / n, j = q - i * n;
+        if (j <= i) A[(size_t)i * ld + j] = __ldcg(J.A + q);
+    }
+    for (int q = tid; q < D * n; q += kTsThreads) R[q] = ((q % n) == (q / n)) ? 1.0 : 0.0;
+    __syncthreads();
+    for (int k = 0; k + 2 < n; ++k) {
+        const int b0 = k + 1, m = n - b0;
+        const double *col = A + k;           // A(b0 + t, k) = col[(b0 + t) * ld]
+        // the step's scalars alternate between two slots: a warp that skips a step
+        // (H_k = I) may write step k+1's while another still reads step k's
+        double *sc = scb + 4 * (k & 1), *sd = scb + 8, *rx = scb + 16;
+        // 1. warp 0: sigma = |x_{1:}|^2 and the reflector; warps 1..D: rx_d = R_d[b0+1:] . x[1:]
+        if (warp == 0) {
+            double s2 = 0.0;
+            for (int t = 1 + lane; t < m; t += 32) { const double x = col[(size_t)(b0 + t) * ld]; s2 += x * x; }
+            s2 = warp_sum(s2);
+            if (lane == 0) {
+                const double alpha = col[(size_t)b0 * ld];
+                double tau = 0.0, beta = alpha, scal = 0.0;
+                if (s2 != 0.0) {
+                    beta = -copysign(sqrt(alpha * alpha + s2), alpha);
+                    tau = (beta - alpha) / beta;
+                    scal = 1.0 / (alpha - beta);
+                }
+                sc[0] = tau; sc[1] = scal; sc[3] = (s2 != 0.0) ? 1.0 : 0.0;
+                J.d[k] = A[(size_t)k * ld + k]; J.e[k] = beta; J.tau[k] = tau;
+            }
+        } else {
+            for (int d = warp - 1; d < D; d += kTsThreads / 32 - 1) {
+                double s = 0.0;
+                for (int t = 1 + lane; t < m; t += 32) s += R[(size_t)d * n + b0 + t] * col[(size_t)(b0 + t) * ld];
+                s = warp_sum(s);
+                if (lane == 0) rx[d] = s;
+            }
+        }
+        __syncthreads();
+        if (sc[3] == 0.0) continue;          // column already reduced: H_k = I
+        const double tau = sc[0], scal = sc[1];
+        // 2. v, and s_d = R_d[b0:] . v
+        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? 1.0 : col[(size_t)(b0 + t) * ld] * scal;
+        if (tid < D) sd[tid] = R[(size_t)tid * n + b0] + scal * rx[tid];
+        __syncthreads();
+        // 3. halves of A v (trailing block, local indices), and R <- R H_k
+        for (int u = tid; u < 2 * m; u += kTsThreads) {
+            const int i = u >> 1, h = u & 1;
+            const int q0 = h ? (m >> 1) : 0, q1 = h ? m : (m >> 1);
+            const double *Ai = A + (size_t)(b0 + i) * ld + b0;
+            double acc = 0.0;
+            for (int q = q0; q < q1; ++q) {
+                const double a = (q <= i) ? Ai[q] : A[(size_t)(b0 + q) * ld + b0 + i];
+                acc += a * v[q];
+            }
+            ph[h * n + i] = acc;
+        }
+        for (int u = tid; u < D * m; u += kTsThreads) {
+            const int d = u / m, t = u - d * m;
+            R[(size_t)d * n + b0 + t] -= tau * sd[d] * v[t];
+        }
+        __syncthreads();
+        // 4. p = tau A v; K = (tau / 2) p . v
+        if (warp == 0) {
+            double s = 0.0;
+            for (int t = lane; t < m; t += 32) {
+                const double pt = tau * (ph[t] + ph[n + t]);
+                w[t] = pt;
+                s += pt * v[t];
+            }
+            s = warp_sum(s);
+            if (lane == 0) sc[2] = 0.5 * tau * s;
+        }
+        __syncthreads();
+        // 5. w = p - K v
+        {
+            const double K = sc[2];
+            for (int t = tid; t < m; t += kTsThreads) w[t] -= K * v[t];
+        }
+        __syncthreads();
+        // 6. A -= v w^T + w v^T on the trailing lower triangle, rows i and m-1-i per warp
+        for (int i1 = warp; i1 < (m + 1) / 2; i1 += kTsThreads / 32) {
+            const int i2 = m - 1 - i1;
+            const int len = (i1 == i2) ? (i1 + 1) : (m + 1);
+            for (int u = lane; u < len; u += 32) {
+                const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
+                double *a = A + (size_t)(b0 + r) * ld + b0 + c;
+                *a -= v[r] * w[c] + w[r] * v[c];
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (n >= 2) {
+            J.d[n - 2] = A[(size_t)(n - 2) * ld + (n - 2)];
+            J.e[n - 2] = A[(size_t)(n - 1) * ld + (n - 2)];
+            J.tau[n - 2] = 0.0;
+        }
+        J.d[n - 1] = A[(size_t)(n - 1) * ld + (n - 1)];
+        J.e[n - 1] = 0.0;
+        J.tau[n - 1] = 0.0;
+    }
+    for (int q = tid; q < D * n; q += kTsThreads) J.R[q] = R[q];
+}
+
+size_t tridiag_small_smem_bytes(int nmax, int Dmax) {
+    const size_t n = (size_t)std::min(nmax, kTsMax);
+    return sizeof(double) * (n * (n | 1) + 4 * n + (size_t)Dmax * n + 32);
+}
+
 // Per-warp partial vectors that fit next to the other arrays (8 = one per warp).
 int tridiag_npriv(int nmax, int cluster) {
     const size_t fixed = (size_t)3 * nmax + (size_t)(nmax / cluster + 1) + 32;
@@ -347,6 +495,13 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
                                                                        d_work_first);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    const size_t ssmem = tridiag_small_smem_bytes(nmax, Dmax);
+    e = cudaFuncSetAttribute(k_tridiag_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem);
+    if (e != cudaSuccess) return e;
+    k_tridiag_small<<<njobs, kTsThreads, ssmem, st>>>(d_jobs, njobs);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (nmax <= kTsMax) return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);
     size_t smem = tridiag_smem_bytes(nmax, cluster);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(njobs * cluster, 1, 1);
@@ -365,7 +520,6 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernelEx(&cfg, k_tridiag, d_jobs, njobs, nmax, tridiag_npriv(nmax, cluster));
     if (e != cudaSuccess) return e;
-    (void)Dmax;
     return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);
 }
 

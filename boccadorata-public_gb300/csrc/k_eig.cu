@@ -3,7 +3,8 @@
 // (source/BcDor-DysonMatrix.cpp:442-488): every eigenvalue W_k and the first D
 // components x_k[0:D] of the corresponding eigenvector of A.
 //
-//   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows)
+//   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows;
+//             matrices of order <= kTsMax get R from k_tridiag_small)
 //   k_bisect_prep  splits T into unreduced blocks at negligible off-diagonals
 //   k_bisect  W_k by bisection on Sturm counts over its block, one thread per
 //             eigenvalue (eig_sturm.cuh): an FP32 bracket, checked and finished in
@@ -33,6 +34,7 @@ __global__ void __launch_bounds__(kEigThreads) k_qrows(const DyJob *jobs, int nj
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.nc, D = J.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;   // order after deflation
+    if (n <= kTsMax) return;   // k_tridiag_small formed R
     __shared__ double red[kEigThreads / 32][8];
     __shared__ double sums[8];
     double *R = J.R;
