@@ -408,7 +408,7 @@ int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
         if (I == ch_hi - 1) e1 = acc;
     }
     if (e1 > e0) {
-        k_ehf<<<e1 - e0, 128, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries + e0, e1 - e0, ctx->d_dd_off, ctx->d_sighf);
+        k_ehf<<<e1 - e0, 256, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries + e0, e1 - e0, ctx->d_dd_off, ctx->d_sighf);
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
@@ -781,7 +781,7 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
     }
     // segment table of the sorted interaction, on the device (k_segments)
     {
-        const std::vector<int> init(kSegTable, -10), zero(kSegTable + 2, 0);
+        const std::vector<int> init(kSegTable, -10), zero(kSegTable + 3, 0);
         int *cnt, *sstr, *send;
         if ((rc = dupload(ctx, &sstr, init))) return rc; P.seg_str = sstr;
         if ((rc = dupload(ctx, &send, init))) return rc; P.seg_end = send;
@@ -789,13 +789,21 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         int *bad = cnt + kSegTable;
         const int big[2] = {INT_MAX, 0};
         CU(cudaMemcpyAsync(bad, big, sizeof(big), cudaMemcpyHostToDevice, ctx->st));
+        // row table: norb^2 (2jmax + 1) pairs of ints, skipped beyond 256 MiB
+        int2 *rows = nullptr;
+        const int nJ = ctx->jmax + 1;
+        const size_t nrow = (size_t)ms->norb * ms->norb * nJ;
+        if (vpp->n_me > 0 && nrow * sizeof(int2) <= ((size_t)256 << 20)) {
+            if ((rc = dalloc(ctx, &rows, nrow))) return rc;
+            CU(cudaMemsetAsync(rows, 0xff, sizeof(int2) * nrow, ctx->st));
+        }
         if (vpp->n_me > 0) {
             k_segments<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
-                P.iabJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad);
+                P.iabJ, P.icdJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad, rows, nJ);
             CU(cudaGetLastError());
             ctx->launches += 1;
         }
-        std::vector<int> h(kSegTable + 2);
+        std::vector<int> h(kSegTable + 3);
         CU(cudaMemcpyAsync(h.data(), cnt, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
         CU(cudaStreamSynchronize(ctx->st));
         if (h[kSegTable] != INT_MAX)
@@ -803,6 +811,8 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
                         h[kSegTable + 1] == 1 ? "orbit out of range" : "bad channel key");
         for (int k = 0; k < kSegTable; ++k)
             if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
+        P.rows = (rows && h[kSegTable + 2] == 0) ? rows : nullptr;
+        P.nJ = nJ;
     }
     return BD_OK;
 }

@@ -22,6 +22,11 @@ struct DevProblem {
     const int *iabJ, *icdJ;
     const double *V;
     const int *seg_str, *seg_end;
+    // Row table of the sorted interaction: first and last element of the run with
+    // pair index iabJ = ind_i1i2J(a, b, J), at (a * norb + b) * nJ + J; set only when
+    // the list is strictly sorted by (iabJ, icdJ) inside every segment (else null).
+    const int2 *rows;
+    int nJ;
 };
 
 // One (Jab, ia, ib, ig) block of the Sigma(2) build of one channel.  Its poles
@@ -131,6 +136,23 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
     int key = ind_chipJ(ch, ip, J);
     int lo = P.seg_str[key], hi = P.seg_end[key];
     if (lo < 0 || hi < 0) return 0.0;
+    if (P.rows) {
+        // On a list sorted by (iabJ, icdJ) inside the segment the reference's search
+        // below finds the one element with both indices, or nothing; so does a search
+        // of icdJ inside iab's run, when the run lies in this segment.
+        if (J >= P.nJ) return 0.0;
+        const int a = iab / (kJMult * kABMult), b = (iab / kJMult) % kABMult;
+        const int2 rw = P.rows[((size_t)a * P.norb + b) * P.nJ + J];
+        if (rw.x < lo || rw.y > hi) return 0.0;
+        int f = rw.x, l = rw.y;
+        while (f <= l) {
+            const int mid = (f + l) >> 1;
+            const int cm = P.icdJ[mid];
+            if (cm == icd) return __dmul_rn(P.V[mid], xph);
+            if (cm < icd) f = mid + 1; else l = mid - 1;
+        }
+        return 0.0;
+    }
     for (int it = 0; it < 100; ++it) {   // the reference's bounded search
         int mid = (hi + lo) / 2;
         int am = P.iabJ[mid];

@@ -12,6 +12,9 @@
 
 namespace bd {
 
+// x == +0 or -0, by the bits (no FP64 instruction)
+__device__ inline bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
 __device__ inline int find_block(const long long *first, int nblk, long long g) {
     int lo = 0, hi = nblk - 1;
     while (lo < hi) {  // largest b with first[b] <= g
@@ -89,6 +92,55 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
     const int N = dir == 0 ? C.nfw : C.nbk;
     const long long k = g - (dir == 0 ? C.fw_off : C.bk_off);
     double *Mout = M + (dir == 0 ? C.mfw_off : C.mbk_off) + k;
+    // The amplitude products x2(alpha, beta) do not depend on the orbital d: form the
+    // non-zero ones once, in the reference's (alpha, beta) order, and reuse them for
+    // every d.  A product with an exactly zero factor is an exact zero (skipped by the
+    // reference's test below), so integer tests on the factors' bits spare its FP64
+    // operations.  Each kept term is computed by the same operations as before.
+    constexpr int kMaxTerms = 48;
+    double x2v[kMaxTerms];
+    int ab[kMaxTerms];
+    int nterm = 0;
+    bool listed = true;
+    for (int nas = 0; nas < noa && listed; ++nas) {
+        const int nst2 = (B.ia == B.ib) ? nas + B.nJab : 0;
+        for (int nbs = nst2; nbs < nob; ++nbs) {
+            const bool z1 = is_zero(fa[nas]) || is_zero(fb[nbs]);
+            const bool z2 = (B.ia != B.ib) || is_zero(fa[nbs]) || is_zero(fb[nas]);
+            if (z1 && z2) continue;
+            double x2 = __dmul_rn(fa[nas], fb[nbs]);
+            if (B.ia == B.ib) {
+                x2 = __dadd_rn(x2, __dmul_rn(__dmul_rn(xJab, fa[nbs]), fb[nas]));
+                if (nas == nbs) x2 = __ddiv_rn(x2, kSqr2);
+            }
+            if (x2 == 0.0) continue;
+            if (nterm == kMaxTerms) { listed = false; break; }
+            x2v[nterm] = x2;
+            ab[nterm] = nas * nob + nbs;
+            ++nterm;
+        }
+    }
+    if (listed) {
+        for (int nd = 0; nd < D; ++nd) {
+            double x1 = 0.0;
+            const int iid = iid0 + nd;
+            for (int q = 0; q < nterm; ++q) {
+                const double x2 = x2v[q];
+                const double *Vr = V + ((size_t)nd * noa * nob + ab[q]) * nog;
+                for (int ngs = 0; ngs < nog; ++ngs) {
+                    if (iig0 + ngs == iid && B.nJgd) continue;
+                    if (is_zero(fg[ngs])) continue;
+                    x1 = __dadd_rn(x1, __dmul_rn(__dmul_rn(Vr[ngs], x2), fg[ngs]));
+                }
+            }
+            x1 = __dmul_rn(x1, x4);
+            Mout[(size_t)nd * N] = x1;
+            s2 = __dadd_rn(s2, __dmul_rn(x1, x1));
+        }
+        E[g] = e;
+        S2[g] = s2;
+        return;
+    }
     for (int nd = 0; nd < D; ++nd) {
         double x1 = 0.0;
         const int iid = iid0 + nd;
@@ -107,7 +159,7 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
                 const double *Vr = V + (((size_t)nd * noa + nas) * nob + nbs) * nog;
                 for (int ngs = 0; ngs < nog; ++ngs) {
                     if (iig0 + ngs == iid && B.nJgd) continue;
-                    if (fg[ngs] == 0.0) continue;
+                    if (is_zero(fg[ngs])) continue;
                     x1 = __dadd_rn(x1, __dmul_rn(__dmul_rn(Vr[ngs], x2), fg[ngs]));
                 }
             }
@@ -120,51 +172,79 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
     S2[g] = s2;
 }
 
-// Static self-energy: one CTA per (channel, nr >= nc) entry; thread c computes
-// the (iv, J2) partial x1*x7 in the reference's inner order, thread 0 adds the
-// partials in the reference's (iv, J2) order.
-__global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long long *out_off, double *out) {
-    __shared__ double part[2048];
+// Static self-energy: one CTA per (channel, nr >= nc) entry.
+//   U = sum_c x1(c) x7(c),   x7(c) = sum_{nm, nv} (x2 x3) x6(nm, nv) V(...)
+// over the (iv, J2) combinations c.  The terms are independent of one another, so the
+// CTA's threads form them in parallel (their interaction lookups overlap); then one
+// thread per c adds its terms in the reference's (nm, nv) order and thread 0 adds the
+// c partials in the reference's (iv, J2) order: every sum keeps the reference's
+// sequence of roundings.  Terms go through shared memory in windows of whole c.
+constexpr int kEhfThreads = 256, kEhfComb = 2048, kEhfTerms = 1536;
+
+__device__ inline bool ehf_skip(int iv, int I, int nm, int nv, int nr, int nc, int nJ) {
+    return iv == I && nJ != 1 && (nm == nr || nv == nc);
+}
+
+__global__ void __launch_bounds__(kEhfThreads) k_ehf(DevProblem P, const int3 *entries, int nent,
+                                                     const long long *out_off, double *out) {
+    __shared__ double term[kEhfTerms];
+    __shared__ double part[kEhfComb];
+    __shared__ int cmb[kEhfComb];        // iv | J2 << 16
+    __shared__ int toff[kEhfComb + 1];   // first term of each c
     __shared__ int ncomb;
     const int e = blockIdx.x;
     if (e >= nent) return;
     const int I = entries[e].x, nr = entries[e].y, nc = entries[e].z;
-    const int D = P.no[I], NS = P.nspb;
+    const int D = P.no[I], NS = P.nspb, j2I = P.j2[I];
     if (threadIdx.x == 0) {
-        int c = 0;
-        for (int iv = 0; iv < P.nsubsh; ++iv) c += (P.j2[I] + P.j2[iv] - abs(P.j2[I] - P.j2[iv])) / 2 + 1;
+        int c = 0, acc = 0;
+        for (int iv = 0; iv < P.nsubsh; ++iv) {
+            const int nJ2 = (j2I + P.j2[iv] - abs(j2I - P.j2[iv])) / 2 + 1;
+            for (int cc = 0; cc < nJ2; ++cc, ++c) {
+                if (c < kEhfComb) { cmb[c] = iv | ((abs(j2I - P.j2[iv]) + 2 * cc) << 16); toff[c] = acc; }
+                acc += P.no[iv] * P.no[iv];
+            }
+        }
+        if (c <= kEhfComb) toff[c] = acc;
         ncomb = c;
     }
     __syncthreads();
-    if (ncomb > 2048) return;
-    for (int c = threadIdx.x; c < ncomb; c += blockDim.x) {
-        int iv = 0, cc = c, nJ2 = 0;
-        for (; iv < P.nsubsh; ++iv) {
-            nJ2 = (P.j2[I] + P.j2[iv] - abs(P.j2[I] - P.j2[iv])) / 2 + 1;
-            if (cc < nJ2) break;
-            cc -= nJ2;
-        }
-        const int J2 = abs(P.j2[I] - P.j2[iv]) + 2 * cc;
-        const int nJ = ((P.j2[I] + P.j2[iv] + J2) / 2) % 2;
-        const double x1 = __ddiv_rn((double)(J2 + 1), (double)(P.j2[I] + 1));
-        double x7 = 0.0;
-        for (int nm = 0; nm < P.no[iv]; nm++) {
-            if (iv == I && nm == nr && nJ != 1) continue;
+    if (ncomb > kEhfComb) return;
+    for (int c0 = 0; c0 < ncomb;) {
+        int c1 = c0 + 1;
+        while (c1 < ncomb && toff[c1 + 1] - toff[c0] <= kEhfTerms) ++c1;
+        const int u0 = toff[c0], nu = toff[c1] - u0;
+        for (int u = threadIdx.x; u < nu; u += kEhfThreads) {
+            int lo = c0, hi = c1 - 1;   // c of term u0 + u
+            while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (toff[mid] <= u0 + u) lo = mid; else hi = mid - 1; }
+            const int iv = cmb[lo] & 0xffff, J2 = cmb[lo] >> 16, no = P.no[iv];
+            const int r = u0 + u - toff[lo], nm = r / no, nv = r - nm * no;
+            const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
+            if (ehf_skip(iv, I, nm, nv, nr, nc, nJ)) continue;
             const double x2 = (iv == I && nm == nr) ? kSqr2 : 1.0;
+            const double x3 = (iv == I && nv == nc) ? kSqr2 : 1.0;
             const int ia = P.orb_start[I] + nr, im = P.orb_start[iv] + nm;
-            for (int nv = 0; nv < P.no[iv]; nv++) {
-                if (iv == I && nv == nc && nJ != 1) continue;
-                const double x3 = (iv == I && nv == nc) ? kSqr2 : 1.0;
-                const int ib = P.orb_start[I] + nc, iu = P.orb_start[iv] + nv;
-                double x6 = 0.0;
-                const double *q = P.fqh + (size_t)P.h_start[iv] * NS;
-                for (int kg = 0; kg < P.nh[iv]; ++kg) { x6 = __dadd_rn(x6, __dmul_rn(q[nv], q[nm])); q += NS; }
-                x7 = __dadd_rn(x7, __dmul_rn(__dmul_rn(__dmul_rn(x2, x3), x6), vget(P, ia, im, ib, iu, J2 / 2)));
-            }
+            const int ib = P.orb_start[I] + nc, iu = P.orb_start[iv] + nv;
+            double x6 = 0.0;
+            const double *q = P.fqh + (size_t)P.h_start[iv] * NS;
+            for (int kg = 0; kg < P.nh[iv]; ++kg) { x6 = __dadd_rn(x6, __dmul_rn(q[nv], q[nm])); q += NS; }
+            term[u] = __dmul_rn(__dmul_rn(__dmul_rn(x2, x3), x6), vget(P, ia, im, ib, iu, J2 / 2));
         }
-        part[c] = __dmul_rn(x1, x7);
+        __syncthreads();
+        for (int c = c0 + threadIdx.x; c < c1; c += kEhfThreads) {
+            const int iv = cmb[c] & 0xffff, J2 = cmb[c] >> 16, no = P.no[iv];
+            const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
+            const double x1 = __ddiv_rn((double)(J2 + 1), (double)(j2I + 1));
+            double x7 = 0.0;
+            const double *t = term + (toff[c] - u0);
+            for (int nm = 0; nm < no; ++nm)
+                for (int nv = 0; nv < no; ++nv)
+                    if (!ehf_skip(iv, I, nm, nv, nr, nc, nJ)) x7 = __dadd_rn(x7, t[nm * no + nv]);
+            part[c] = __dmul_rn(x1, x7);
+        }
+        __syncthreads();
+        c0 = c1;
     }
-    __syncthreads();
     if (threadIdx.x == 0) {
         double u = 0.0;
         for (int c = 0; c < ncomb; ++c) u = __dadd_rn(u, part[c]);
@@ -188,12 +268,18 @@ __device__ inline int interaction_key(int k, int norb, const int *orb_sh, const 
     return key;
 }
 
-__global__ void k_segments(const int *iabJ, int n, int norb, const int *orb_sh, const int *ch, const int *ip,
-                           int *seg_str, int *seg_end, int *seg_cnt, int *bad) {
+//
+// The same pass fills the row table (DevProblem::rows) when rows is non-null: each run
+// of equal iabJ records its first and last element.  bad[2] is set when the table
+// cannot stand in for the reference's search: a pair out of order or repeated inside
+// a segment, a run that appears twice, or a J beyond the table.
+__global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, const int *orb_sh, const int *ch,
+                           const int *ip, int *seg_str, int *seg_end, int *seg_cnt, int *bad, int2 *rows, int nJ) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int why = 0, w2 = 0;
-    const int key = interaction_key(iabJ[i], norb, orb_sh, ch, ip, &why);
+    const int iab = iabJ[i];
+    const int key = interaction_key(iab, norb, orb_sh, ch, ip, &why);
     if (key < 0) {
         if (atomicMin(&bad[0], i) > i) atomicExch(&bad[1], why);
         return;
@@ -202,6 +288,17 @@ __global__ void k_segments(const int *iabJ, int n, int norb, const int *orb_sh, 
     const int next = i + 1 < n ? interaction_key(iabJ[i + 1], norb, orb_sh, ch, ip, &w2) : -1;
     if (key != prev) { seg_str[key] = i; atomicAdd(&seg_cnt[key], 1); }
     if (key != next) seg_end[key] = i;
+    if (!rows) return;
+    if (key == prev) {
+        const int pa = iabJ[i - 1], pc = icdJ[i - 1], c = icdJ[i];
+        if (!(pa < iab || (pa == iab && pc < c))) bad[2] = 1;
+    }
+    const int J = iab % kJMult, a = iab / (kJMult * kABMult), b = (iab / kJMult) % kABMult;
+    if (J >= nJ) { bad[2] = 1; return; }
+    int2 *rw = rows + ((size_t)a * norb + b) * nJ + J;
+    if (i == 0 || iabJ[i - 1] != iab)
+        if (atomicCAS(&rw->x, -1, i) != -1) bad[2] = 1;
+    if (i + 1 == n || iabJ[i + 1] != iab) rw->y = i;
 }
 
 // Gather rows in a given order into separate SoA arrays (used after the sort), plus an
