@@ -83,7 +83,7 @@ struct bd_ctx {
     // plan
     std::vector<Chan> chans;
     std::vector<S2Block> blocks;
-    std::vector<long long> blk_fw_first, blk_bk_first, blk_vp_first;
+    std::vector<long long> blk_fw_first, blk_bk_first;
     long long tot_fw = 0, tot_bk = 0, tot_mfw = 0, tot_mbk = 0, tot_vp = 0;
     // device: bufs follow the propagator, sbufs hold the model space and interaction
     std::vector<DevBuf> bufs, sbufs;
@@ -95,7 +95,7 @@ struct bd_ctx {
     size_t pool_bytes = 0;
     DevProblem dp{};
     S2Block *d_blocks = nullptr;
-    long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr, *d_blk_vp_first = nullptr;
+    long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr;
     ChanSig *d_cs = nullptr;
     double *d_vp = nullptr;
     double *d_Efw = nullptr, *d_S2fw = nullptr, *d_Mfw = nullptr, *d_Ebk = nullptr, *d_S2bk = nullptr, *d_Mbk = nullptr;
@@ -249,7 +249,7 @@ double seek_efermi(const bd_ctx *c, int I) {
 void build_plan(bd_ctx *c) {
     c->chans.assign(c->nsubsh, Chan());
     c->blocks.clear();
-    c->blk_fw_first.clear(); c->blk_bk_first.clear(); c->blk_vp_first.clear();
+    c->blk_fw_first.clear(); c->blk_bk_first.clear();
     long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
     const int ns = c->nsubsh;
     // (ia <= ib) pairs satisfying the Jab triangle, in the reference's (ia, ib) order, kept
@@ -304,7 +304,6 @@ void build_plan(bd_ctx *c) {
                     B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
                     c->blk_fw_first.push_back(fw + nfw);
                     c->blk_bk_first.push_back(bk + nbk);
-                    c->blk_vp_first.push_back(vp);
                     nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
                     c->blocks.push_back(B);
                 }
@@ -373,9 +372,7 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
     if (nb <= 0) return BD_OK;
     const long long vp0 = A.vp_first, nvp = Z.vp_first + Z.nvp - vp0;
     if (nvp > 0) {
-        k_vgather<<<(unsigned)((nvp + 255) / 256), 256, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
-                                                                        ctx->d_blk_vp_first + b0, nb, vp0, nvp,
-                                                                        ctx->d_vp);
+        k_vgather<<<(unsigned)((nb + 7) / 8), 256, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0, nb, ctx->d_vp);
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
@@ -854,7 +851,6 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &ctx->d_blocks, ctx->blocks))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
-    if ((rc = dupload(ctx, &ctx->d_blk_vp_first, ctx->blk_vp_first))) return rc;
     std::vector<ChanSig> cs(ns);
     std::vector<int> seg_fw(ctx->tot_fw), seg_bk(ctx->tot_bk), segoff_fw(ns + 1), segoff_bk(ns + 1);
     std::vector<int> idx_fw(ctx->tot_fw), idx_bk(ctx->tot_bk);

@@ -6,8 +6,7 @@
 
 namespace bd {
 
-__global__ void k_vgather(DevProblem P, const S2Block *blk, const long long *vp_first, int nblk,
-                          long long g0, long long total, double *vp);
+__global__ void k_vgather(DevProblem P, const S2Block *blk, int nblk, double *vp);
 __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_first, int nblk, long long g0,
                         long long total, const ChanSig *cs, int dir, const double *vp, double *E, double *S2,
                         double *M);

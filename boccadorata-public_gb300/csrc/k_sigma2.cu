@@ -25,28 +25,28 @@ __device__ inline int find_block(const long long *first, int nblk, long long g) 
 }
 
 // K0: V'[d][alpha][beta][gamma] = sqrt((2Jab+1)/(2j_I+1)) * V^Jab_{ab,dg} (* sqrt2 if g == d),
-// source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One thread per coefficient.
-__global__ void k_vgather(DevProblem P, const S2Block *blk, const long long *vp_first, int nblk,
-                          long long g0, long long total, double *vp) {
-    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (idx >= total) return;
-    const long long g = g0 + idx;
-    int b = find_block(vp_first, nblk, g);
-    const S2Block B = blk[b];
-    int t = (int)(g - vp_first[b]);
+// source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One warp per (Jab, ia, ib, ig) block,
+// lanes over its coefficients: the block's descriptor and prefactor are read and
+// formed once, and the lanes' lookups of one (a, b) row share its first levels.
+__global__ void k_vgather(DevProblem P, const S2Block *blk, int nblk, double *vp) {
+    const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= nblk) return;
+    const S2Block B = blk[w];
     const int I = B.ch;
     const int na = P.no[B.ia], nb = P.no[B.ib], ng = P.no[B.ig];
-    int ngs = t % ng, r = t / ng;
-    int nbs = r % nb; r /= nb;
-    int nas = r % na; int d = r / na;
-    if (B.ia == B.ib && nbs < nas + B.nJab) return;
-    int iid = P.orb_start[I] + d, iig = P.orb_start[B.ig] + ngs;
-    if (iig == iid && B.nJgd) return;
-    int iia = P.orb_start[B.ia] + nas, iib = P.orb_start[B.ib] + nbs;
-    double x3 = __dsqrt_rn(__ddiv_rn((double)(B.Jab + B.Jab + 1), (double)(1 + P.j2[I])));
-    double v = __dmul_rn(x3, vget(P, iia, iib, iid, iig, B.Jab));
-    if (iig == iid) v = __dmul_rn(v, kSqr2);
-    vp[B.vp_first + t] = v;
+    const double x3 = __dsqrt_rn(__ddiv_rn((double)(B.Jab + B.Jab + 1), (double)(1 + P.j2[I])));
+    for (int t = lane; t < B.nvp; t += 32) {
+        int ngs = t % ng, r = t / ng;
+        int nbs = r % nb; r /= nb;
+        int nas = r % na; int d = r / na;
+        if (B.ia == B.ib && nbs < nas + B.nJab) continue;
+        int iid = P.orb_start[I] + d, iig = P.orb_start[B.ig] + ngs;
+        if (iig == iid && B.nJgd) continue;
+        int iia = P.orb_start[B.ia] + nas, iib = P.orb_start[B.ib] + nbs;
+        double v = __dmul_rn(x3, vget(P, iia, iib, iid, iig, B.Jab));
+        if (iig == iid) v = __dmul_rn(v, kSqr2);
+        vp[B.vp_first + t] = v;
+    }
 }
 
 // K1: one thread per pole.  dir 0 = 2p1h (forward), 1 = 2h1p (backward);
