@@ -302,6 +302,7 @@ void build_plan(bd_ctx *c) {
                     B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
                     B.vp_first = vp;
                     B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
+                    B.x3 = std::sqrt((double)(Jab + Jab + 1) / (double)(1 + c->j2[I]));
                     c->blk_fw_first.push_back(fw + nfw);
                     c->blk_bk_first.push_back(bk + nbk);
                     nfw += B.nfw; nbk += B.nbk; vp += B.nvp;

@@ -41,6 +41,7 @@ struct S2Block {
     int bk_first, nbk;
     long long vp_first;  // offset into the V' scratch
     int nvp;             // D * no[ia] * no[ib] * no[ig]
+    double x3;           // sqrt((2Jab+1)/(2j_I+1)), correctly rounded (formed on the host)
 };
 
 // Per-channel layout of the structure-of-arrays Sigma(2) on the device:

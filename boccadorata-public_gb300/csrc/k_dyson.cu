@@ -42,7 +42,9 @@ __device__ inline double dy_diag(const DyJob &J, int part, int i) {
     return rows ? rows[(size_t)i * NT] : (part == 0 ? J.E_fw[i] : J.E_bk[i]);
 }
 
-// whether full-matrix row r has an off-diagonal entry
+// whether full-matrix row r has an off-diagonal entry, apart from the fishbone
+// entries of a branch's start row s-1 to the later rows (k_dyson_deflate marks
+// those from the later rows' side)
 __device__ inline bool dy_coupled(const DyJob &J, int r) {
     const int D = J.D;
     if (r < D) return true;
@@ -60,11 +62,27 @@ __device__ inline bool dy_coupled(const DyJob &J, int r) {
     for (int nc = 1; nc < ipiv[0]; ++nc) {
         const int s = ipiv[nc + 1];
         if (s < 1 || s >= np) continue;
-        if (i == s - 1)
-            for (int nr = s; nr < np; ++nr) if (rows[(size_t)nr * NT + 1 + nc] != 0.0) return true;
         if (i >= s && rows[(size_t)i * NT + 1 + nc] != 0.0) return true;
     }
     return false;
+}
+
+// Row r >= s of a branch starting at s with a fishbone entry: row s-1 is coupled.
+__device__ inline void dy_mark_branch_starts(const DyJob &J, int r, int *flag) {
+    const int D = J.D;
+    if (r < D) return;
+    const int part = (r < D + J.nfw) ? 0 : 1;
+    const int off = part == 0 ? D : D + J.nfw;
+    const int i = r - off, np = part == 0 ? J.nfw : J.nbk;
+    if (!(part == 0 ? J.lanczos_fw : J.lanczos_bk)) return;
+    const int NT = J.nden + D;
+    const double *rows = part == 0 ? J.fw_rows : J.bk_rows;
+    const int *ipiv = part == 0 ? J.ipiv_fw : J.ipiv_bk;
+    for (int nc = 1; nc < ipiv[0]; ++nc) {
+        const int s = ipiv[nc + 1];
+        if (s < 1 || s >= np) continue;
+        if (i >= s && rows[(size_t)i * NT + 1 + nc] != 0.0) flag[off + s - 1] = 1;
+    }
 }
 
 // One CTA per matrix: the compact index of every kept row (work area, ints; -1 for a
@@ -85,11 +103,15 @@ __global__ void __launch_bounds__(kDfThreads) k_dyson_deflate(DyJob *jobs, int n
     __syncthreads();
     double *st = J.R + (size_t)D * n;
     int nkept_total = 0;
-    // first pass: count kept rows (the deflated rows' staged positions start after them)
+    // first pass: keep flags (a branch's start row from its later rows' side), then
+    // the count of kept rows (the deflated rows' staged positions start after them)
+    for (int r = tid; r < n; r += kDfThreads) map[r] = dy_coupled(J, r);
+    __syncthreads();
+    for (int r = tid; r < n; r += kDfThreads) dy_mark_branch_starts(J, r, map);
+    __syncthreads();
     for (int b = 0; b < n; b += kDfThreads) {
         const int r = b + tid;
-        const int keep = (r < n) && dy_coupled(J, r);
-        if (r < n) map[r] = keep;
+        const int keep = (r < n) ? map[r] : 0;
         int x = __syncthreads_count(keep);
         nkept_total += x;
     }
@@ -126,7 +148,11 @@ __global__ void __launch_bounds__(kDfThreads) k_dyson_deflate(DyJob *jobs, int n
 }
 
 // One thread per full-matrix row; kept rows are written at their compact index, in a
-// matrix of order nc (deflated columns hold zeros in every kept row).
+// matrix of order nc (deflated columns hold zeros in every kept row).  Only the lower
+// triangle (columns up to the row's own) is written: the reductions read nothing else,
+// and every entry right of the diagonal (a model-space row's pole couplings, the beta
+// to the next row, a branch start's fishbone entries) is also left of it in its
+// partner row.
 __global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *row_first, long long total_rows,
                                  const double *work, const long long *work_first) {
     long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -140,12 +166,10 @@ __global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *
     if (cr < 0) return;
     const int nc = J.nc, D = J.D, nfw = J.nfw, nbk = J.nbk;
     double *Ar = J.A + (size_t)cr * nc;
-    for (int c = 0; c < nc; ++c) Ar[c] = 0.0;
-    auto put = [&](int c, double v) { const int cc = map[c]; if (cc >= 0) Ar[cc] = v; };
-    if (r < D) {
-        for (int c = 0; c < D; ++c) Ar[c] = J.sig1b[r * D + c] + J.sighf[r * D + c];
-        for (int i = 0; i < nfw; ++i) put(D + i, dy_mcoup(J, 0, i, r));
-        for (int i = 0; i < nbk; ++i) put(D + nfw + i, dy_mcoup(J, 1, i, r));
+    for (int c = 0; c <= cr; ++c) Ar[c] = 0.0;
+    auto put = [&](int c, double v) { const int cc = map[c]; if (cc >= 0 && cc <= cr) Ar[cc] = v; };
+    if (r < D) {   // the model-space rows are never deflated and come first: cr == r
+        for (int c = 0; c <= r; ++c) Ar[c] = J.sig1b[r * D + c] + J.sighf[r * D + c];
         return;
     }
     const int part = (r < D + nfw) ? 0 : 1;
@@ -161,14 +185,11 @@ __global__ void k_dyson_assemble(const DyJob *jobs, int njobs, const long long *
     const int *ipiv = part == 0 ? J.ipiv_fw : J.ipiv_bk;
     const int nbr = ipiv[0];  // branches (pivots used)
     if (i >= 1) put(r - 1, rows[(size_t)i * NT + 1]);
-    if (i + 1 < np) put(r + 1, rows[(size_t)(i + 1) * NT + 1]);
     // fishbone (:303-333): branch nc (1 .. nbr-1) starts at s = ipiv[nc+1];
-    // row s-1 couples to every later row nr >= s with row_nr[1 + nc]
+    // row s-1 couples to every later row nr >= s with row_nr[1 + nc] (held by row nr)
     for (int nc2 = 1; nc2 < nbr; ++nc2) {
         const int s = ipiv[nc2 + 1];
         if (s < 1 || s >= np) continue;
-        if (i == s - 1)
-            for (int nr = s; nr < np; ++nr) put(off + nr, rows[(size_t)nr * NT + 1 + nc2]);
         if (i >= s) put(off + s - 1, rows[(size_t)i * NT + 1 + nc2]);
     }
 }

@@ -214,6 +214,18 @@ __device__ inline EigTol eig_tol(double onenrm) {
     return t;
 }
 
+// 1/q to ~2^-48 relative: the FP32 reciprocal refined by one Newton step,
+// r <- r + r (1 - q r) (the error squares); plain division outside the FP32 range.
+// An FP64 division is a dependent chain of about ten FP64 instructions.
+__device__ inline double rcp_newton(double q) {
+    const double aq = fabs(q);
+    if (aq > 1e-36 && aq < 1e36) {
+        const double r = (double)__frcp_rn((float)q);
+        return fma(r, fma(-q, r, 1.0), r);
+    }
+    return 1.0 / q;
+}
+
 __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first, long long total, double *work,
                         const long long *work_first) {
     const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -247,12 +259,12 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
         const double di = DD[(size_t)i * n + k], li = LL[(size_t)i * n + k];
         if (fabs(di) >= fabs(li)) {
             PV[(size_t)i * n + k] = 0.0;
-            const double f = (di != 0.0) ? li / di : 0.0;
+            const double f = (di != 0.0) ? li * rcp_newton(di) : 0.0;
             LL[(size_t)i * n + k] = f;
             DD[(size_t)(i + 1) * n + k] -= f * U1[(size_t)i * n + k];
         } else {
             PV[(size_t)i * n + k] = 1.0;
-            const double f = di / li;
+            const double f = di * rcp_newton(li);
             DD[(size_t)i * n + k] = li;
             LL[(size_t)i * n + k] = f;
             const double tt = U1[(size_t)i * n + k];
@@ -264,8 +276,12 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
             }
         }
     }
-    for (int i = b0; i <= b1; ++i)
-        if (fabs(DD[(size_t)i * n + k]) < tl.pertol) DD[(size_t)i * n + k] = (DD[(size_t)i * n + k] < 0 ? -tl.pertol : tl.pertol);
+    // pivots no smaller than pertol, kept as reciprocals for the solves
+    for (int i = b0; i <= b1; ++i) {
+        double p = DD[(size_t)i * n + k];
+        if (fabs(p) < tl.pertol) p = (p < 0 ? -tl.pertol : tl.pertol);
+        DD[(size_t)i * n + k] = rcp_newton(p);
+    }
     for (int i = b0; i <= b1; ++i)
         Y[(size_t)i * n + k] = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
     for (int it = 0; it < 3; ++it) {
@@ -281,12 +297,12 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
             double v = Y[(size_t)i * n + k];
             if (i + 1 <= b1) v -= U1[(size_t)i * n + k] * y1;
             if (i + 2 <= b1) v -= U2[(size_t)i * n + k] * y2;
-            v /= DD[(size_t)i * n + k];
+            v *= DD[(size_t)i * n + k];
             Y[(size_t)i * n + k] = v;
             y2 = y1; y1 = v;
             nrm = fmax(nrm, fabs(v));
         }
-        const double sc = (nrm > 0.0) ? 1.0 / nrm : 1.0;
+        const double sc = (nrm > 0.0) ? rcp_newton(nrm) : 1.0;
         double s2 = 0.0;
         for (int i = b0; i <= b1; ++i) { const double v = Y[(size_t)i * n + k] * sc; Y[(size_t)i * n + k] = v; s2 += v * v; }
         const double inv = (s2 > 0.0) ? 1.0 / sqrt(s2) : 0.0;

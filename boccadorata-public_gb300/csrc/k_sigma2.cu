@@ -26,15 +26,17 @@ __device__ inline int find_block(const long long *first, int nblk, long long g) 
 
 // K0: V'[d][alpha][beta][gamma] = sqrt((2Jab+1)/(2j_I+1)) * V^Jab_{ab,dg} (* sqrt2 if g == d),
 // source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One warp per (Jab, ia, ib, ig) block,
-// lanes over its coefficients: the block's descriptor and prefactor are read and
-// formed once, and the lanes' lookups of one (a, b) row share its first levels.
+// lanes over its coefficients: the block's descriptor is read once, and the lanes'
+// lookups of one (a, b) row share its first levels.  The prefactor comes with the
+// block: FP64 division and square root take tens of FP64 instructions, each a full
+// warp slot on a pipe that issues at 1/64 of the FP32 rate.
 __global__ void k_vgather(DevProblem P, const S2Block *blk, int nblk, double *vp) {
     const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (w >= nblk) return;
     const S2Block B = blk[w];
     const int I = B.ch;
     const int na = P.no[B.ia], nb = P.no[B.ib], ng = P.no[B.ig];
-    const double x3 = __dsqrt_rn(__ddiv_rn((double)(B.Jab + B.Jab + 1), (double)(1 + P.j2[I])));
+    const double x3 = B.x3;   // IEEE division and square root: the same bits on the host as here
     for (int t = lane; t < B.nvp; t += 32) {
         int ngs = t % ng, r = t / ng;
         int nbs = r % nb; r /= nb;
