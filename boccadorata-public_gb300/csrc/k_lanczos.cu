@@ -54,7 +54,8 @@ template <typename VT> struct LzTraits;
 template <> struct LzTraits<double> { using CT = double; };
 template <> struct LzTraits<float> { using CT = float; };
 
-__device__ inline double warp_sum(double v) {
+template <typename T>
+__device__ inline T warp_sum_ct(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -90,8 +91,8 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // Slice of a CTA: S pole rows starting at rank*S, S a multiple of 4; rows past N are
 // zero in every vector (E, w, V), so the vector loads need no tail handling.
 //
-// Shared-memory layout: doubles A[rmax] (dot partials) | c[rmax] (totals) |
-// Bs[kMaxScal] (scalar partials) | Bn[2] (norm partial) | red[kLzWarps * kMaxScal],
+// Shared-memory layout: doubles A[2][rmax] (dot partials of alternate passes) |
+// c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | red[kLzWarps * kMaxScal],
 // then CT (the vectors' arithmetic type) cf[rmax rounded up to 4] (totals in CT) |
 // Es[S] | w[S], then touched[S] bytes.
 //
@@ -118,11 +119,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     extern __shared__ double sm[];
-    double *A = sm;
-    double *c = A + rmax;
-    double *Bs = c + rmax;
-    double *Bn = Bs + kMaxScal;
-    double *red = Bn + 2;
+    const int rmax2 = (rmax + 1) & ~1;   // even: keeps the arrays behind 16-byte aligned
+    double *A = sm;                      // [2][rmax2] dot partials, alternating by pass
+    double *c = A + 2 * rmax2;
+    double *Bs = c + rmax2;
+    double *red = Bs + kMaxScal;
     int *rowslot = reinterpret_cast<int *>(red + kLzWarps * kMaxScal);   // vector slot of every row, -1: deflated
     CT *cf = reinterpret_cast<CT *>(rowslot + (rmax + 3) / 4 * 4);     // 16-byte aligned
     CT *Es, *w;
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         touched = reinterpret_cast<unsigned char *>(w + S);
     }
     __shared__ double tot[kMaxScal];
-    __shared__ double s_n2;
+    __shared__ double s_xb, s_ixb;
     __shared__ int s_kmin;
     __shared__ int lt[16];       // vectors of a local pass
     __shared__ int s_nl;
@@ -175,15 +176,170 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         ++ndefl;
     };
 
-    // block-wide sum of one double per thread, result in every thread
-    auto block_sum = [&](double v) -> double {
-        v = warp_sum(v);
-        __syncthreads();
-        if (lane == 0) red[warp] = v;
-        __syncthreads();
+    // Sum over the cluster of one value per CTA held at buf[t], in rank order (the
+    // loads first, then the adds: one DSMEM round trip instead of CL).
+    auto cluster_sum = [&](const double *buf, int t) -> double {
+        double x[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) x[r] = (r < CL) ? cluster.map_shared_rank(const_cast<double *>(buf), r)[t] : 0.0;
         double s = 0.0;
-        for (int q = 0; q < kLzWarps; ++q) s += red[q];
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+            if (r < CL) s += x[r];
         return s;
+    };
+
+    // (b1) dots pass: <v_t, w> for the pass's vectors t < nl and |w|^2, summed over
+    // the cluster into c[0..nl] (c[nl] = |w|^2) and cf[0..nl).  The per-CTA partials
+    // alternate between two buffers: a peer may still gather the previous pass's
+    // while this CTA writes the next (no cluster barrier between a local update and
+    // the full sweep's dot products).
+    int dpar = 0;
+    auto dots_pass = [&](bool loc, int nl) {
+        double *Ap = A + (size_t)dpar * rmax2;
+        dpar ^= 1;
+        for (int t = warp; t < nl; t += kLzWarps) {
+            const VT *vt = V + (size_t)(loc ? lt[t] : t) * C.ld + i0;
+            CT acc = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+            int q = lane;
+            for (; q + 96 < nv; q += 128) {   // four 16-byte loads in flight per lane
+                VT x0[VW], x1[VW], x2[VW], x3[VW];
+                load16<VT>(vt + q * VW, x0);
+                load16<VT>(vt + (q + 32) * VW, x1);
+                load16<VT>(vt + (q + 64) * VW, x2);
+                load16<VT>(vt + (q + 96) * VW, x3);
+#pragma unroll
+                for (int u = 0; u < VW; ++u) {
+                    acc += x0[u] * w[q * VW + u];
+                    acc1 += x1[u] * w[(q + 32) * VW + u];
+                    acc2 += x2[u] * w[(q + 64) * VW + u];
+                    acc3 += x3[u] * w[(q + 96) * VW + u];
+                }
+            }
+            for (; q < nv; q += 32) {
+                VT x[VW];
+                load16<VT>(vt + q * VW, x);
+#pragma unroll
+                for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
+            }
+            acc += (acc1 + acc2) + acc3;
+            acc = warp_sum_ct(acc);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
+            if (lane == 0) Ap[t] = (double)acc;
+        }
+        CT nwp = 0;
+        for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
+        nwp = warp_sum_ct(nwp);
+        if (lane == 0) red[warp * kMaxScal] = (double)nwp;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0.0;
+            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal];
+            Ap[nl] = s;
+        }
+        cluster.sync();
+        for (int t = tid; t <= nl; t += kLzThreads) {   // (b2) totals over the cluster
+            const double s = cluster_sum(Ap, t);
+            c[t] = s;
+            cf[t] = (CT)s;
+        }
+        __syncthreads();
+    };
+
+    // (b3) w -= sum_t cf_t v_t over the pass's vectors: 16-byte vectors, eight rows in
+    // flight.  Each thread updates the 16-byte groups q = tid, tid + kLzThreads, ...
+    auto update_pass = [&](bool loc, int nl) {
+        for (int q = tid; q < nv; q += kLzThreads) {
+            CT acc[VW];
+#pragma unroll
+            for (int u = 0; u < VW; ++u) acc[u] = 0;
+            const VT *base = V + i0 + q * VW;
+            int t = 0;
+            for (; t + 7 < nl; t += 8) {
+                VT x[8][VW];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) load16<VT>(base + (size_t)(loc ? lt[t + r] : t + r) * C.ld, x[r]);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const CT cr = cf[t + r];
+#pragma unroll
+                    for (int u = 0; u < VW; ++u) acc[u] += cr * x[r][u];
+                }
+            }
+            for (; t + 3 < nl; t += 4) {
+                VT x0[VW], x1[VW], x2[VW], x3[VW];
+                load16<VT>(base + (size_t)(loc ? lt[t] : t) * C.ld, x0);
+                load16<VT>(base + (size_t)(loc ? lt[t + 1] : t + 1) * C.ld, x1);
+                load16<VT>(base + (size_t)(loc ? lt[t + 2] : t + 2) * C.ld, x2);
+                load16<VT>(base + (size_t)(loc ? lt[t + 3] : t + 3) * C.ld, x3);
+                const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
+#pragma unroll
+                for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
+            }
+            for (; t < nl; ++t) {
+                VT x0[VW];
+                load16<VT>(base + (size_t)(loc ? lt[t] : t) * C.ld, x0);
+                const CT c0 = cf[t];
+#pragma unroll
+                for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
+            }
+#pragma unroll
+            for (int u = 0; u < VW; ++u) w[q * VW + u] -= acc[u];
+        }
+    };
+
+    // After a full sweep's update: |w|^2 and the scalars of step (c) of the updated w
+    // (source/BcDor-Lanczos.cpp:180-214), alpha = <w|E|w>, m_d = <M_d|w> and, for each
+    // earlier pivot q, g_q = <v_last(q)|E|w>, summed over the cluster into tot[0] =
+    // |w|^2, tot[1] = alpha, tot[2 + d] = m_d, tot[2 + D + q] = g_q.  Each thread reads
+    // back only the groups it updated, so no barrier separates this from the update.
+    // When another sweep follows, these sums are simply recomputed.
+    auto scalar_pass = [&](int nq) {
+        CT pn = 0, sa = 0, sm_[8], sg[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { sm_[q] = 0; sg[q] = 0; }
+        for (int q = tid; q < nv; q += kLzThreads) {
+#pragma unroll
+            for (int u = 0; u < VW; ++u) {
+                const int i = q * VW + u;
+                const CT wi = w[i];
+                pn += wi * wi;
+                if (i < ns) {
+                    const CT e = Es[i];
+                    sa += e * wi * wi;
+#pragma unroll
+                    for (int d = 0; d < 8; ++d)
+                        if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
+#pragma unroll
+                    for (int g = 0; g < 8; ++g)
+                        if (g < nq && lslot[g] >= 0) sg[g] += e * (CT)V[(size_t)lslot[g] * C.ld + i0 + i] * wi;
+                }
+            }
+        }
+        pn = warp_sum_ct(pn);
+        sa = warp_sum_ct(sa);
+        if (lane == 0) { red[warp * kMaxScal] = (double)pn; red[warp * kMaxScal + 1] = (double)sa; }
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+            if (d < D) {
+                const CT x = warp_sum_ct(sm_[d]);
+                if (lane == 0) red[warp * kMaxScal + 2 + d] = (double)x;
+            }
+#pragma unroll
+        for (int g = 0; g < 8; ++g)
+            if (g < nq) {
+                const CT x = warp_sum_ct(sg[g]);
+                if (lane == 0) red[warp * kMaxScal + 2 + D + g] = (double)x;
+            }
+        __syncthreads();
+        const int nsc = 2 + D + nq;
+        if (tid < nsc) {
+            double s = 0.0;
+            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal + tid];
+            Bs[tid] = s;
+        }
+        cluster.sync();
+        if (tid < nsc) tot[tid] = cluster_sum(Bs, tid);
+        __syncthreads();
     };
 
     int k = -1;           // current pivot chain
@@ -197,6 +353,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             deflated_row(j);
             continue;
         }
+        const int nq = k;   // earlier pivot chains
+        if (tid < nq) lslot[tid] = rowslot[C.last[tid]];
         // (a) w = M.p  or  w = v_{j-1} * E   (source/BcDor-Lanczos.cpp:137-150)
         if (newv) {
             const double *p = C.piv + (size_t)k * D;
@@ -214,128 +372,44 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         bool done = false;         // step finished by an untouched-pole unit vector
         double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
-            int pass = 0, nfull = 0;
-            double wn2_first = 0.0;
+            int nfull = 0;
             // A continuing chain's w = E v_{j-1} has large components only on v_{j-1}, v_{j-2}
             // and the last vector of every earlier chain (the fishbone couplings); everything
             // else is rounding.  The first pass projects out just those few vectors, then
             // full sweeps follow (at least one), each repeated under the DGKS criterion.
             bool local = !newv && attempt == 0 && j > 0;
+            if (local && tid == 0) {   // slots of v_{j-1}, v_{j-2} and the earlier chains' last vectors
+                int n = 0;
+                lt[n++] = rowslot[j - 1];
+                if (j >= 2 && rowslot[j - 2] >= 0) lt[n++] = rowslot[j - 2];
+                for (int q = 0; q < k; ++q)
+                    if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) lt[n++] = rowslot[C.last[q]];
+                s_nl = n;
+            }
+            __syncthreads();
+            int nl = local ? s_nl : nvec;
+            dots_pass(local, nl);
+            const double wn2_first = c[nl];
+            double wn2_before = wn2_first;
             for (;;) {
-                if (local && tid == 0) {   // slots of v_{j-1}, v_{j-2} and the earlier chains' last vectors
-                    int n = 0;
-                    lt[n++] = rowslot[j - 1];
-                    if (j >= 2 && rowslot[j - 2] >= 0) lt[n++] = rowslot[j - 2];
-                    for (int q = 0; q < k; ++q)
-                        if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) lt[n++] = rowslot[C.last[q]];
-                    s_nl = n;
+                update_pass(local, nl);
+                if (local) {   // the full sweep's dot products follow the local update directly
+                    local = false;
+                    nl = nvec;
+                    __syncthreads();
+                    dots_pass(false, nl);
+                    wn2_before = c[nl];
+                    continue;
                 }
-                __syncthreads();
-                const int nl = local ? s_nl : nvec;       // stored vectors in this pass
-                auto tix = [&](int t) { return local ? lt[t] : t; };
-                // (b1) partial dot products <v_t, w> over the slice, one warp per t, 16-byte loads
-                for (int t = warp; t < nl; t += kLzWarps) {
-                    const VT *vt = V + (size_t)tix(t) * C.ld + i0;
-                    CT acc = 0, acc1 = 0, acc2 = 0, acc3 = 0;
-                    int q = lane;
-                    for (; q + 96 < nv; q += 128) {   // four 16-byte loads in flight per lane
-                        VT x0[VW], x1[VW], x2[VW], x3[VW];
-                        load16<VT>(vt + q * VW, x0);
-                        load16<VT>(vt + (q + 32) * VW, x1);
-                        load16<VT>(vt + (q + 64) * VW, x2);
-                        load16<VT>(vt + (q + 96) * VW, x3);
-#pragma unroll
-                        for (int u = 0; u < VW; ++u) {
-                            acc += x0[u] * w[q * VW + u];
-                            acc1 += x1[u] * w[(q + 32) * VW + u];
-                            acc2 += x2[u] * w[(q + 64) * VW + u];
-                            acc3 += x3[u] * w[(q + 96) * VW + u];
-                        }
-                    }
-                    for (; q < nv; q += 32) {
-                        VT x[VW];
-                        load16<VT>(vt + q * VW, x);
-#pragma unroll
-                        for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
-                    }
-                    acc += (acc1 + acc2) + acc3;
-                    // lane partials combined in CT: FP32 shuffles for FP32 vectors
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                    if (lane == 0) A[t] = (double)acc;
-                }
-                CT nwp = 0;
-                for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
-                const double nw = block_sum((double)nwp);
-                if (tid == 0) A[nl] = nw;
-                cluster.sync();
-                // (b2) totals over the cluster, in rank order
-                for (int t = tid; t <= nl; t += kLzThreads) {
-                    double s = 0.0;
-                    for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(A, r)[t];
-                    c[t] = s;
-                    cf[t] = (CT)s;
-                }
-                __syncthreads();
-                const double wn2_before = c[nl];
-                if (pass == 0) wn2_first = wn2_before;
-                // (b3) w -= sum_t c_t v_t over 16-byte vectors, eight rows in flight, and |w|^2
-                CT pn = 0;
-                for (int q = tid; q < nv; q += kLzThreads) {
-                    CT acc[VW];
-#pragma unroll
-                    for (int u = 0; u < VW; ++u) acc[u] = 0;
-                    const VT *base = V + i0 + q * VW;
-                    int t = 0;
-                    for (; t + 7 < nl; t += 8) {      // eight rows in flight
-                        VT x[8][VW];
-#pragma unroll
-                        for (int r = 0; r < 8; ++r) load16<VT>(base + (size_t)tix(t + r) * C.ld, x[r]);
-#pragma unroll
-                        for (int r = 0; r < 8; ++r) {
-                            const CT cr = cf[t + r];
-#pragma unroll
-                            for (int u = 0; u < VW; ++u) acc[u] += cr * x[r][u];
-                        }
-                    }
-                    for (; t + 3 < nl; t += 4) {
-                        VT x0[VW], x1[VW], x2[VW], x3[VW];
-                        load16<VT>(base + (size_t)tix(t) * C.ld, x0);
-                        load16<VT>(base + (size_t)tix(t + 1) * C.ld, x1);
-                        load16<VT>(base + (size_t)tix(t + 2) * C.ld, x2);
-                        load16<VT>(base + (size_t)tix(t + 3) * C.ld, x3);
-                        const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
-#pragma unroll
-                        for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
-                    }
-                    for (; t < nl; ++t) {
-                        VT x0[VW];
-                        load16<VT>(base + (size_t)tix(t) * C.ld, x0);
-                        const CT c0 = cf[t];
-#pragma unroll
-                        for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
-                    }
-#pragma unroll
-                    for (int u = 0; u < VW; ++u) {
-                        const CT wi = w[q * VW + u] - acc[u];
-                        w[q * VW + u] = wi;
-                        pn += wi * wi;
-                    }
-                }
-                const double pns = block_sum((double)pn);
-                if (tid == 0) Bn[0] = pns;
-                cluster.sync();
-                if (tid == 0) {
-                    double s = 0.0;
-                    for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(Bn, r)[0];
-                    s_n2 = s;
-                }
-                __syncthreads();
-                n2 = s_n2;
-                if (local) { local = false; ++pass; continue; }
+                scalar_pass(nq);
+                n2 = tot[0];
                 // another full sweep while this one removed more than half of the squared norm
                 if (nfull++ > 0) ++extra;
-                if (nvec > 0 && nfull < 4 && n2 < eta2 * wn2_before) { ++pass; continue; }
+                if (nvec > 0 && nfull < 4 && n2 < eta2 * wn2_before) {
+                    dots_pass(false, nl);
+                    wn2_before = c[nl];
+                    continue;
+                }
                 break;
             }
             if (attempt == 0 && !contaminated && (n2 <= thr_exh * wn2_first || n2 == 0.0) && next_slot()) {
@@ -386,80 +460,34 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             cluster.sync();   // peers have read s_kmin before it can change again
         }
         if (done) continue;
-        // (c) alpha, m, g of the final w (once per step; source/BcDor-Lanczos.cpp:180-214)
-        const int nq = k;
-        const int nsc = 1 + D + nq;
-        if (tid < nq) lslot[tid] = rowslot[C.last[tid]];
-        __syncthreads();
-        {
-            CT sa = 0, sm_[8], sg[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) { sm_[q] = 0; sg[q] = 0; }
-            for (int i = tid; i < ns; i += kLzThreads) {
-                const CT wi = w[i], e = Es[i];
-                sa += e * wi * wi;
-#pragma unroll
-                for (int d = 0; d < 8; ++d)
-                    if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < nq && lslot[q] >= 0) sg[q] += e * (CT)V[(size_t)lslot[q] * C.ld + i0 + i] * wi;
-            }
-            const double sat = warp_sum((double)sa);
-            if (lane == 0) red[warp * kMaxScal] = sat;
-#pragma unroll
-            for (int d = 0; d < 8; ++d) {
-                if (d < D) {
-                    const double x = warp_sum((double)sm_[d]);
-                    if (lane == 0) red[warp * kMaxScal + 1 + d] = x;
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                if (q < nq) {
-                    const double x = warp_sum((double)sg[q]);
-                    if (lane == 0) red[warp * kMaxScal + 1 + D + q] = x;
-                }
-            }
+        // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216);
+        // the scalars are formed once (FP64 division and square root are long FP64 chains)
+        if (tid == 0) {
+            const double xb = sqrt(n2);
+            s_xb = xb;
+            s_ixb = 1.0 / xb;
         }
         __syncthreads();
-        if (tid < nsc) {
-            double s = 0.0;
-            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal + tid];
-            Bs[tid] = s;
-        }
-        cluster.sync();
-        if (tid < nsc) {
-            double s = 0.0;
-            for (int r = 0; r < CL; ++r) s += cluster.map_shared_rank(Bs, r)[tid];
-            tot[tid] = s;
-        }
-        __syncthreads();
-        // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216)
-        const double xa = tot[0] / n2;
-        const double xb = sqrt(n2);
+        const double xb = s_xb, ixb = s_ixb;
         VT *vj = V + (size_t)nvec * C.ld + i0;
-        if constexpr (sizeof(VT) == 4) {
-            const float inv = (float)(1.0 / xb);
+        {
+            const CT inv = (CT)ixb;
             for (int i = tid; i < S; i += kLzThreads) {
-                const VT v = w[i] * inv;
-                vj[i] = v;
-                touched[i] |= (v != (VT)0);
-            }
-        } else {
-            for (int i = tid; i < S; i += kLzThreads) {
-                const VT v = (VT)(w[i] / xb);
+                const VT v = (VT)(w[i] * inv);
                 vj[i] = v;
                 touched[i] |= (v != (VT)0);
             }
         }
-        if (rank == 0 && tid == 0) {
+        if (rank == 0 && tid < NT) {   // one output element per thread
             double *row = C.out + (size_t)j * NT;
-            row[0] = xa;
-            row[1] = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
-            for (int q = 0; q < k; ++q) row[2 + q] = tot[1 + D + q] / xb;
-            for (int d = 0; d < D; ++d) row[C.nden_out + d] = tot[1 + d] / xb;
-            if (newv) row[1] = row[1 + k];
+            double x = 0.0;
+            if (tid == 0) x = tot[1] / n2;
+            else if (tid == 1) x = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
+            else if (tid < 2 + k) x = tot[2 + D + (tid - 2)] * ixb;
+            else if (tid >= C.nden_out && tid < C.nden_out + D) x = tot[2 + (tid - C.nden_out)] * ixb;
+            if (newv && tid == 1) x = (k >= 1) ? tot[2 + D + (k - 1)] * ixb : x;
+            if (tid < 2 + k || tid >= C.nden_out) row[tid] = x;
+            else if (tid < C.nden_out) row[tid] = 0.0;
         }
         if (tid == 0) rowslot[j] = nvec;
         ++nvec;
@@ -474,7 +502,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
 size_t lanczos_smem_bytes(int S, int rmax, bool global_slices) {
     // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
-    const size_t fixed = sizeof(double) * (2 * (size_t)rmax + (size_t)(rmax + 3) / 4 * 4 + kMaxScal + 2 +
+    const size_t rmax2 = ((size_t)rmax + 1) & ~(size_t)1;
+    const size_t fixed = sizeof(double) * (3 * rmax2 + (size_t)(rmax + 3) / 4 * 4 + kMaxScal +
                                            (size_t)kLzWarps * kMaxScal) +
                          sizeof(int) * (size_t)(rmax + 3) / 4 * 4 + 16;
     return global_slices ? fixed : fixed + sizeof(double) * 2 * (size_t)S + (size_t)S;
