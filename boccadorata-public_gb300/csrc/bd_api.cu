@@ -503,14 +503,9 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     std::sort(ch.begin(), ch.end(), [](const LzChain &a, const LzChain &b) {
         return (double)a.N * a.L * a.L > (double)b.N * b.L * b.L;
     });
-    // zero the output rows (the reference clears them, source/BcDor-Lanczos.cpp:88)
-    for (int I = ch_lo; I < ch_hi; ++I)
-        for (int dir = 0; dir < 2; ++dir) {
-            const ChainPlan &P = ctx->chans[I].lz[dir];
-            if (P.L > 0)
-                CU(cudaMemsetAsync(ctx->d_lzout + ctx->lz_out_off[dir][I], 0,
-                                   sizeof(double) * (size_t)P.L * (P.nden_out + ctx->chans[I].D), ctx->st));
-        }
+    // The reference clears the output rows first (source/BcDor-Lanczos.cpp:88); the
+    // kernel writes every element of every row itself (zeros where the reference's
+    // stay), so no clearing pass is needed.
     // chain descriptors live in a small device array (one slot per chain of the range)
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
     CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));

@@ -566,6 +566,95 @@ namespace bd {
 // M_q^T M_q by pivoted elimination, pivots above 1e-12 of the largest diagonal.
 constexpr int kGrpThreads = 256;
 
+// Directions of energy group q (poles [g0, g1) of equal E) that no coupling reaches:
+// m - rank(M_q), M_q the D x m couplings, the rank from the Gram matrix G = M_q M_q^T
+// by pivoted elimination (pivots above 1e-12 of the largest diagonal entry).  A warp
+// per group; the D(D+1)/2 entries of G are summed over the lanes.  A one-pole group
+// has rank 1 exactly when a coupling is non-zero (the elimination's second pivot is
+// rounding); it needs no Gram matrix.  The count is written to gE[N + q] (the starts
+// in gInfo are still read by other warps).
+template <int D>
+__device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gInfo, int warp, int lane) {
+    constexpr int P = D * (D + 1) / 2;
+    const int N = C.N;
+    for (int q = warp; q < Q; q += kGrpThreads / 32) {
+        const int g0 = gInfo[1 + q];
+        const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
+        const int m = g1 - g0;
+        if (m == 1) {
+            if (lane == 0) {
+                bool any = false;
+#pragma unroll
+                for (int a = 0; a < D; ++a) any |= (C.M[(size_t)a * N + g0] != 0.0);
+                gE[N + q] = any ? 0.0 : 1.0;
+            }
+            continue;
+        }
+        double G[P];
+#pragma unroll
+        for (int u = 0; u < P; ++u) G[u] = 0.0;
+        for (int i = g0 + lane; i < g1; i += 32) {
+            double mv[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) mv[a] = C.M[(size_t)a * N + i];
+            int u = 0;
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b = 0; b <= a; ++b) G[u++] += mv[a] * mv[b];
+        }
+#pragma unroll
+        for (int u = 0; u < P; ++u)
+            for (int o = 16; o > 0; o >>= 1) G[u] += __shfl_xor_sync(0xffffffffu, G[u], o);
+        if (lane == 0) {
+            double H[D][D];
+            {
+                int u = 0;
+#pragma unroll
+                for (int a = 0; a < D; ++a)
+#pragma unroll
+                    for (int b = 0; b <= a; ++b) { H[a][b] = G[u]; H[b][a] = G[u]; ++u; }
+            }
+            double gmax = 0.0;
+#pragma unroll
+            for (int a = 0; a < D; ++a) gmax = fmax(gmax, H[a][a]);
+            int rank = 0;
+            bool used[D];
+#pragma unroll
+            for (int a = 0; a < D; ++a) used[a] = false;
+            for (int st = 0; st < D && gmax > 0.0; ++st) {
+                int pv = -1;
+                double best = 1e-12 * gmax;
+#pragma unroll
+                for (int a = 0; a < D; ++a) if (!used[a] && H[a][a] > best) { best = H[a][a]; pv = a; }
+                if (pv < 0) break;
+                used[pv] = true;
+                ++rank;
+                double rowp[D];
+#pragma unroll
+                for (int b = 0; b < D; ++b) rowp[b] = 0.0;
+#pragma unroll
+                for (int a = 0; a < D; ++a)
+                    if (a == pv)
+#pragma unroll
+                        for (int b = 0; b < D; ++b) rowp[b] = H[a][b];
+                const double inv = 1.0 / best;
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    if (used[a]) continue;
+                    double hap = 0.0;
+#pragma unroll
+                    for (int b = 0; b < D; ++b) if (b == pv) hap = H[a][b];
+                    const double f = hap * inv;
+#pragma unroll
+                    for (int b = 0; b < D; ++b) if (!used[b]) H[a][b] -= f * rowp[b];
+                }
+            }
+            gE[N + q] = (double)max(0, m - rank);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kGrpThreads) k_lz_groups(const LzChain *chains, int nchains) {
     const int cid = blockIdx.x;
     if (cid >= nchains) return;
@@ -595,54 +684,16 @@ __global__ void __launch_bounds__(kGrpThreads) k_lz_groups(const LzChain *chains
         __syncthreads();
     }
     const int Q = s_base;
-    // availability per group, a warp per group
-    for (int q = warp; q < Q; q += kGrpThreads / 32) {
-        const int g0 = gInfo[1 + q];
-        const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
-        double G[8][8];
-#pragma unroll
-        for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int b = 0; b < 8; ++b) G[a][b] = 0.0;
-        for (int i = g0 + lane; i < g1; i += 32) {
-            double m[8];
-#pragma unroll
-            for (int a = 0; a < 8; ++a) m[a] = (a < D) ? C.M[(size_t)a * N + i] : 0.0;
-#pragma unroll
-            for (int a = 0; a < 8; ++a)
-#pragma unroll
-                for (int b = 0; b <= a; ++b) G[a][b] += m[a] * m[b];
-        }
-#pragma unroll
-        for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int b = 0; b <= a; ++b)
-                for (int o = 16; o > 0; o >>= 1) G[a][b] += __shfl_xor_sync(0xffffffffu, G[a][b], o);
-        __syncwarp();
-        if (lane == 0) {
-            for (int a = 0; a < 8; ++a) for (int b = a + 1; b < 8; ++b) G[a][b] = G[b][a];
-            double gmax = 0.0;
-            for (int a = 0; a < D; ++a) gmax = fmax(gmax, G[a][a]);
-            int rank = 0;
-            bool used[8] = {false, false, false, false, false, false, false, false};
-            for (int st = 0; st < D && gmax > 0.0; ++st) {
-                int pv = -1;
-                double best = 1e-12 * gmax;
-                for (int a = 0; a < D; ++a) if (!used[a] && G[a][a] > best) { best = G[a][a]; pv = a; }
-                if (pv < 0) break;
-                used[pv] = true;
-                ++rank;
-                const double inv = 1.0 / G[pv][pv];
-                for (int a = 0; a < D; ++a) {
-                    if (used[a]) continue;
-                    const double f = G[a][pv] * inv;
-                    for (int b = 0; b < D; ++b) if (!used[b]) G[a][b] -= f * G[pv][b];
-                }
-            }
-            const int m = g1 - g0;
-            // starts are still needed by the next warps' groups: write the count aside first
-            gE[N + q] = (double)max(0, m - rank);
-        }
+    // availability per group, a warp per group, with the Gram matrix sized for D
+    switch (D) {
+        case 1: group_counts<1>(C, Q, gE, gInfo, warp, lane); break;
+        case 2: group_counts<2>(C, Q, gE, gInfo, warp, lane); break;
+        case 3: group_counts<3>(C, Q, gE, gInfo, warp, lane); break;
+        case 4: group_counts<4>(C, Q, gE, gInfo, warp, lane); break;
+        case 5: group_counts<5>(C, Q, gE, gInfo, warp, lane); break;
+        case 6: group_counts<6>(C, Q, gE, gInfo, warp, lane); break;
+        case 7: group_counts<7>(C, Q, gE, gInfo, warp, lane); break;
+        default: group_counts<8>(C, Q, gE, gInfo, warp, lane); break;
     }
     __syncthreads();
     for (int q = tid; q < Q; q += kGrpThreads) gInfo[1 + q] = (int)gE[N + q];
