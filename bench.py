@@ -40,8 +40,8 @@ WORKLOAD = "nmax10_lanczos100"
 CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2, 3, 5, 6
 # Per-launch DRAM traffic of the FP32 Lanczos kernel on this workload, from the ncu
 # capture summarised in profiles/k_lanczos_float_nmax10_lanczos100_dram.md
-# (dram__bytes_read.sum 23 065 856 + dram__bytes_write.sum 7 211 008).
-LANCZOS_TRAFFIC_BYTES = 30_276_864
+# (dram__bytes_read.sum 22 365 184 + dram__bytes_write.sum 9 821 952).
+LANCZOS_TRAFFIC_BYTES = 32_187_136
 
 
 def parse():
