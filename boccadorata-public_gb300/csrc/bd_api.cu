@@ -18,6 +18,8 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <thread>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -89,6 +91,12 @@ struct bd_ctx {
     std::vector<DevBuf> bufs, sbufs;
     std::vector<DevBuf> *cur = nullptr;   // where dalloc records (nullptr: bufs)
     bool static_ok = false;
+    // interaction checks in flight: the segment scan's counters come back into a pinned
+    // buffer while the host plans the propagator (finish_static reads them)
+    bool static_pending = false;
+    int *h_segcheck = nullptr;
+    int2 *pending_rows = nullptr;
+    int pending_nJ = 0;
     // freed buffers kept for reuse by size: a repeated upload of a problem of the same
     // shape allocates nothing (cudaMalloc / cudaFree synchronise the device)
     std::multimap<size_t, void *> pool;
@@ -247,74 +255,124 @@ double seek_efermi(const bd_ctx *c, int I) {
 // Block enumeration in the loop order of Build_Dynamic_SlfEn_2ndOrder and the
 // all-poles counts of Count_2p1h_2h1p_poles (source/BcDor-Self_energy_ext_Op_c.cpp:47-111,380-394).
 void build_plan(bd_ctx *c) {
-    c->chans.assign(c->nsubsh, Chan());
-    c->blocks.clear();
-    c->blk_fw_first.clear(); c->blk_bk_first.clear();
-    long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
     const int ns = c->nsubsh;
+    c->chans.assign(ns, Chan());
     // (ia <= ib) pairs satisfying the Jab triangle, in the reference's (ia, ib) order, kept
     // only when they can carry 2p1h (particles in both) or 2h1p (holes in both) poles
-    std::vector<std::vector<int>> pairs(c->jmax + 1);
+    struct Pair { int ia, ib, chs, ips, nJab; bool pfw, pbk; };
+    std::vector<std::vector<Pair>> pairs(c->jmax + 1);
     for (int Jab = 0; Jab <= c->jmax; ++Jab)
         for (int ia = 0; ia < ns; ++ia)
             for (int ib = ia; ib < ns; ++ib) {
                 if (tri_fail(c->j2[ia], c->j2[ib], 2 * Jab)) continue;
-                if (!(c->np[ia] > 0 && c->np[ib] > 0) && !(c->nh[ia] > 0 && c->nh[ib] > 0)) continue;
-                pairs[Jab].push_back(ia * ns + ib);
+                const bool pfw = c->np[ia] > 0 && c->np[ib] > 0, pbk = c->nh[ia] > 0 && c->nh[ib] > 0;
+                if (!pfw && !pbk) continue;
+                pairs[Jab].push_back(Pair{ia, ib, c->ch[ia] + c->ch[ib], c->ip[ia] + c->ip[ib],
+                                          std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2, pfw, pbk});
             }
-    for (int I = 0; I < ns; ++I) {
-        Chan &C = c->chans[I];
-        C.D = c->no[I]; C.j2 = c->j2[I]; C.ch = c->ch[I];
-        C.fw_off = fw; C.bk_off = bk; C.mfw_off = mfw; C.mbk_off = mbk;
-        C.blk_first = (int)c->blocks.size(); C.vp_first = vp;
+    // partner-shell buckets by (charge, parity); a charge outside the shells' range has none
+    int chmin = INT_MAX, chmax = INT_MIN;
+    for (int s = 0; s < ns; ++s) { chmin = std::min(chmin, c->ch[s]); chmax = std::max(chmax, c->ch[s]); }
+    const int nkey = 2 * (chmax - chmin + 1);
+    auto gkey = [&](int ch, int ip) { return (ch < chmin || ch > chmax) ? -1 : 2 * (ch - chmin) + ((ip % 2) + 2) % 2; };
+
+    // Blocks of one channel, in the reference's (Jab, ia, ib, ig) order, with offsets
+    // relative to the channel (fw_first, bk_first, vp_first); the channels are
+    // independent and are enumerated on a few host threads.
+    std::vector<std::vector<S2Block>> cb(ns);
+    auto channel = [&](int I) {
+        std::vector<S2Block> &out = cb[I];
+        std::vector<std::vector<int>> gl(nkey), gh(nkey), gp(nkey);
+        const int D = c->no[I];
         int nfw = 0, nbk = 0;
+        long long vp = 0;
         for (int Jab = 0; Jab <= c->jmax; ++Jab) {
-            // triangle-valid ig for (I, Jab): all of them, those with holes (2p1h needs a
-            // hole in g) and those with particles (2h1p needs a particle in g)
-            std::vector<int> gl, gh, gp;
+            // triangle-valid ig for (I, Jab), in ascending order, bucketed by (charge,
+            // parity), since a pair (ia, ib) fixes both of its partner g: all of them,
+            // those with holes (2p1h needs a hole in g) and those with particles (2h1p
+            // needs a particle in g)
+            for (auto &v : gl) v.clear();
+            for (auto &v : gh) v.clear();
+            for (auto &v : gp) v.clear();
+            bool any = false;
             for (int ig = 0; ig < ns; ++ig) {
                 if (tri_fail(c->j2[ig], c->j2[I], 2 * Jab)) continue;
-                gl.push_back(ig);
-                if (c->nh[ig] > 0) gh.push_back(ig);
-                if (c->np[ig] > 0) gp.push_back(ig);
+                const int key = gkey(c->ch[ig], c->ip[ig]);
+                any = true;
+                gl[key].push_back(ig);
+                if (c->nh[ig] > 0) gh[key].push_back(ig);
+                if (c->np[ig] > 0) gp[key].push_back(ig);
             }
-            if (gl.empty()) continue;
-            for (int ab : pairs[Jab]) {
-                const int ia = ab / ns, ib = ab % ns;
-                const bool pfw = c->np[ia] > 0 && c->np[ib] > 0, pbk = c->nh[ia] > 0 && c->nh[ib] > 0;
-                const std::vector<int> &cand = (pfw && pbk) ? gl : (pfw ? gh : gp);
-                const int nJab = std::abs((c->j2[ia] + c->j2[ib]) / 2 - Jab + 1) % 2;
+            if (!any) continue;
+            const double x3 = std::sqrt((double)(Jab + Jab + 1) / (double)(1 + c->j2[I]));
+            for (const Pair &pr : pairs[Jab]) {
+                const int ia = pr.ia, ib = pr.ib, nJab = pr.nJab;
+                // charge and parity of g: ch_a + ch_b - ch_g = ch_I, pi_a + pi_b + pi_g + pi_I even
+                const int key = gkey(pr.chs - c->ch[I], pr.ips + c->ip[I]);
+                if (key < 0) continue;
+                const std::vector<int> &cand = (pr.pfw && pr.pbk) ? gl[key] : (pr.pfw ? gh[key] : gp[key]);
                 for (int ig : cand) {
-                    if (c->ch[ia] + c->ch[ib] - c->ch[ig] != c->ch[I]) continue;
-                    if ((c->ip[ia] + c->ip[ib] + c->ip[ig] + c->ip[I]) % 2 != 0) continue;
                     S2Block B{};
                     B.ch = I; B.Jab = Jab; B.ia = ia; B.ib = ib; B.ig = ig;
                     B.nJab = nJab;
                     B.nJgd = std::abs((c->j2[ig] + c->j2[I]) / 2 - Jab + 1) % 2;
-                    int na = c->np[ia], nb = c->np[ib], ng = c->nh[ig], s = na * nb * ng;
-                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
-                    B.nfw = s;
-                    na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; s = na * nb * ng;
-                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; s = (na * nb / 2) * ng; }
-                    B.nbk = s;
+                    int na = c->np[ia], nb = c->np[ib], ng = c->nh[ig], sz = na * nb * ng;
+                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; sz = (na * nb / 2) * ng; }
+                    B.nfw = sz;
+                    na = c->nh[ia]; nb = c->nh[ib]; ng = c->np[ig]; sz = na * nb * ng;
+                    if (ia == ib) { nb = na + 1; if (nJab == 1) nb -= 2; sz = (na * nb / 2) * ng; }
+                    B.nbk = sz;
                     // blocks without poles add nothing to either list
                     if (B.nfw <= 0 && B.nbk <= 0) continue;
-                    B.fw_first = (int)(fw + nfw); B.bk_first = (int)(bk + nbk);
+                    B.fw_first = nfw; B.bk_first = nbk;
                     B.vp_first = vp;
-                    B.nvp = C.D * c->no[ia] * c->no[ib] * c->no[ig];
-                    B.x3 = std::sqrt((double)(Jab + Jab + 1) / (double)(1 + c->j2[I]));
-                    c->blk_fw_first.push_back(fw + nfw);
-                    c->blk_bk_first.push_back(bk + nbk);
+                    B.nvp = D * c->no[ia] * c->no[ib] * c->no[ig];
+                    B.x3 = x3;
                     nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
-                    c->blocks.push_back(B);
+                    out.push_back(B);
                 }
             }
         }
-        C.nfw = nfw; C.nbk = nbk;
-        C.nblk = (int)c->blocks.size() - C.blk_first;
-        C.nvp = vp - C.vp_first;
-        fw += nfw; bk += nbk; mfw += (long long)nfw * C.D; mbk += (long long)nbk * C.D;
+        Chan &C = c->chans[I];
+        C.D = D; C.j2 = c->j2[I]; C.ch = c->ch[I];
+        C.nfw = nfw; C.nbk = nbk; C.nvp = vp;
+        C.nblk = (int)out.size();
         C.efermi = seek_efermi(c, I);
+    };
+    {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int nth = (int)std::min<unsigned>(std::min<unsigned>(hw, 8u), (unsigned)ns);
+        std::atomic<int> next(0);
+        auto worker = [&]() { for (int I; (I = next.fetch_add(1)) < ns;) channel(I); };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nth; ++t) th.emplace_back(worker);
+        worker();
+        for (auto &t : th) t.join();
+    }
+    // channel offsets, then the blocks at their global offsets
+    long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
+    size_t nb = 0;
+    for (int I = 0; I < ns; ++I) {
+        Chan &C = c->chans[I];
+        C.fw_off = fw; C.bk_off = bk; C.mfw_off = mfw; C.mbk_off = mbk;
+        C.blk_first = (int)nb; C.vp_first = vp;
+        fw += C.nfw; bk += C.nbk; mfw += (long long)C.nfw * C.D; mbk += (long long)C.nbk * C.D; vp += C.nvp;
+        nb += cb[I].size();
+    }
+    c->blocks.resize(nb);
+    c->blk_fw_first.resize(nb);
+    c->blk_bk_first.resize(nb);
+    for (int I = 0; I < ns; ++I) {
+        const Chan &C = c->chans[I];
+        for (size_t q = 0; q < cb[I].size(); ++q) {
+            S2Block B = cb[I][q];
+            B.fw_first += (int)C.fw_off;
+            B.bk_first += (int)C.bk_off;
+            B.vp_first += C.vp_first;
+            c->blocks[C.blk_first + q] = B;
+            c->blk_fw_first[C.blk_first + q] = B.fw_first;
+            c->blk_bk_first[C.blk_first + q] = B.bk_first;
+        }
     }
     c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
 }
@@ -499,9 +557,12 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     }
     if (ch.empty()) return BD_OK;
     if (2 + 7 + 7 > 32) return fail(ctx, BD_ERR_ARG, "too many scalars");
-    // largest chains first so the long ones start early
+    // Longest chains first so they start in the first wave: a chain's steps follow its
+    // row count L (the built vectors and the deflated tail), its step cost depends
+    // little on N (measured 1.81 -> 1.55 ms against ordering by N L^2)
     std::sort(ch.begin(), ch.end(), [](const LzChain &a, const LzChain &b) {
-        return (double)a.N * a.L * a.L > (double)b.N * b.L * b.L;
+        if (a.L != b.L) return a.L > b.L;
+        return a.N > b.N;
     });
     // The reference clears the output rows first (source/BcDor-Lanczos.cpp:88); the
     // kernel writes every element of every row itself (zeros where the reference's
@@ -796,17 +857,30 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
             CU(cudaGetLastError());
             ctx->launches += 1;
         }
-        std::vector<int> h(kSegTable + 3);
-        CU(cudaMemcpyAsync(h.data(), cnt, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, ctx->st));
-        CU(cudaStreamSynchronize(ctx->st));
-        if (h[kSegTable] != INT_MAX)
-            return fail(ctx, BD_ERR_ARG, "element %d: %s", h[kSegTable],
-                        h[kSegTable + 1] == 1 ? "orbit out of range" : "bad channel key");
-        for (int k = 0; k < kSegTable; ++k)
-            if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
-        P.rows = (rows && h[kSegTable + 2] == 0) ? rows : nullptr;
-        P.nJ = nJ;
+        if (!ctx->h_segcheck) CU(cudaMallocHost(&ctx->h_segcheck, sizeof(int) * (kSegTable + 3)));
+        CU(cudaMemcpyAsync(ctx->h_segcheck, cnt, sizeof(int) * (kSegTable + 3), cudaMemcpyDeviceToHost, ctx->st));
+        P.rows = nullptr;
+        ctx->pending_rows = rows;
+        ctx->pending_nJ = nJ;
+        ctx->static_pending = true;
     }
+    return BD_OK;
+}
+
+// Waits for the interaction's transfer and segment scan, then checks the list.
+int finish_static(bd_ctx *ctx) {
+    if (!ctx->static_pending) return BD_OK;
+    ctx->static_pending = false;
+    CU(cudaStreamSynchronize(ctx->st));
+    const int *h = ctx->h_segcheck;
+    if (h[kSegTable] != INT_MAX)
+        return fail(ctx, BD_ERR_ARG, "element %d: %s", h[kSegTable],
+                    h[kSegTable + 1] == 1 ? "orbit out of range" : "bad channel key");
+    for (int k = 0; k < kSegTable; ++k)
+        if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
+    ctx->dp.rows = (ctx->pending_rows && h[kSegTable + 2] == 0) ? ctx->pending_rows : nullptr;
+    ctx->dp.nJ = ctx->pending_nJ;
+    ctx->static_ok = true;
     return BD_OK;
 }
 
@@ -830,6 +904,7 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
     std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
     build_plan(ctx);
+    if (int rc0 = finish_static(ctx)) { ctx->static_ok = false; return rc0; }
     int rc;
     DevProblem &P = ctx->dp;
     P.nspb = ctx->nspb;
@@ -848,23 +923,34 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
     std::vector<ChanSig> cs(ns);
-    std::vector<int> seg_fw(ctx->tot_fw), seg_bk(ctx->tot_bk), segoff_fw(ns + 1), segoff_bk(ns + 1);
-    std::vector<int> idx_fw(ctx->tot_fw), idx_bk(ctx->tot_bk);
+    std::vector<int> segoff_fw(ns + 1), segoff_bk(ns + 1);
     for (int I = 0; I < ns; ++I) {
         const Chan &C = ctx->chans[I];
         cs[I] = ChanSig{C.D, C.nfw, C.nbk, (int)C.fw_off, (int)C.bk_off, C.mfw_off, C.mbk_off};
-        for (int k = 0; k < C.nfw; ++k) { seg_fw[C.fw_off + k] = I; idx_fw[C.fw_off + k] = (int)(C.fw_off + k); }
-        for (int k = 0; k < C.nbk; ++k) { seg_bk[C.bk_off + k] = I; idx_bk[C.bk_off + k] = (int)(C.bk_off + k); }
         segoff_fw[I] = (int)C.fw_off; segoff_bk[I] = (int)C.bk_off;
     }
-    segoff_fw[ns] = (int)ctx->tot_fw; segoff_bk[ns] = (int)ctx->tot_bk;  // scratch for per-range relative offsets
+    segoff_fw[ns] = (int)ctx->tot_fw; segoff_bk[ns] = (int)ctx->tot_bk;
     if ((rc = dupload(ctx, &ctx->d_cs, cs))) return rc;
-    if ((rc = dupload(ctx, &ctx->d_seg_fw, seg_fw))) return rc;
-    if ((rc = dupload(ctx, &ctx->d_seg_bk, seg_bk))) return rc;
-    if ((rc = dupload(ctx, &ctx->d_idx_fw, idx_fw))) return rc;
-    if ((rc = dupload(ctx, &ctx->d_idx_bk, idx_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_seg_fw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_seg_bk, ctx->tot_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_idx_fw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_idx_bk, ctx->tot_bk))) return rc;
+    // the channel of every pole and the identity order, on the device from the offsets
+    // (the sort's per-range offsets overwrite these arrays later)
     if ((rc = dupload(ctx, &ctx->d_segoff_fw, segoff_fw))) return rc;
     if ((rc = dupload(ctx, &ctx->d_segoff_bk, segoff_bk))) return rc;
+    if (ctx->tot_fw > 0) {
+        k_pole_index<<<(unsigned)((ctx->tot_fw + 255) / 256), 256, 0, ctx->st>>>(ctx->d_segoff_fw, ns, ctx->tot_fw,
+                                                                              ctx->d_seg_fw, ctx->d_idx_fw);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+    }
+    if (ctx->tot_bk > 0) {
+        k_pole_index<<<(unsigned)((ctx->tot_bk + 255) / 256), 256, 0, ctx->st>>>(ctx->d_segoff_bk, ns, ctx->tot_bk,
+                                                                              ctx->d_seg_bk, ctx->d_idx_bk);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+    }
     if ((rc = dalloc(ctx, &ctx->d_perm_fw, ctx->tot_fw))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_perm_bk, ctx->tot_bk))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_keys_tmp, std::max(ctx->tot_fw, ctx->tot_bk)))) return rc;
@@ -966,6 +1052,7 @@ void bd_destroy(bd_ctx *ctx) {
     if (ctx->d_dywork) cudaFree(ctx->d_dywork);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
     for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
+    if (ctx->h_segcheck) cudaFreeHost(ctx->h_segcheck);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -982,9 +1069,14 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     free_static(ctx);
     ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false; ctx->static_ok = false;
     int rc = upload_static(ctx, ms, vpp);
+    if (rc) { ctx->static_pending = false; cudaStreamSynchronize(ctx->st); return rc; }
+    ctx->static_ok = true;   // for upload_propagator; finish_static confirms it or fails
+    // the propagator's host plan runs while the interaction is in flight
+    rc = upload_propagator(ctx, prop);
+    const int rc2 = finish_static(ctx);   // no-op when upload_propagator already finished it
     if (rc) return rc;
-    ctx->static_ok = true;
-    return upload_propagator(ctx, prop);
+    if (rc2) { ctx->static_ok = false; ctx->uploaded = false; return rc2; }
+    return BD_OK;
 }
 
 int bd_upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {

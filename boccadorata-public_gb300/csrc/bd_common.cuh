@@ -169,6 +169,43 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
     return 0.0;
 }
 
+// FP64 division and square root are dependent chains of about ten FP64 instructions,
+// each of which holds an SM sub-partition's FP64 unit for ~64 cycles on this GPU; where
+// a few ulp suffice they are replaced by an FP32 seed refined by Newton's iteration
+// (the relative error squares at every step).
+//
+// 1/q to ~2^-48 (one step) from the FP32 reciprocal; plain division outside the FP32 range.
+__device__ inline double rcp_newton(double q) {
+    const double aq = fabs(q);
+    if (aq > 1e-36 && aq < 1e36) {
+        const double r = (double)__frcp_rn((float)q);
+        return fma(r, fma(-q, r, 1.0), r);
+    }
+    return 1.0 / q;
+}
+
+// 1/q to a few ulp (two steps)
+__device__ inline double rcp_newton2(double q) {
+    const double aq = fabs(q);
+    if (aq > 1e-36 && aq < 1e36) {
+        double r = (double)__frcp_rn((float)q);
+        r = fma(r, fma(-q, r, 1.0), r);
+        return fma(r, fma(-q, r, 1.0), r);
+    }
+    return 1.0 / q;
+}
+
+// 1/sqrt(x), x > 0, to a few ulp: the FP32 seed and two steps of y <- y (3/2 - x y^2 / 2)
+__device__ inline double rsqrt_newton(double x) {
+    if (x > 1e-36 && x < 1e36) {
+        const double hx = 0.5 * x;
+        double y = (double)__frsqrt_rn((float)x);
+        y = y * fma(-hx * y, y, 1.5);
+        return y * fma(-hx * y, y, 1.5);
+    }
+    return 1.0 / sqrt(x);
+}
+
 // Largest Dyson order (after deflation) reduced in one CTA's shared memory; larger
 // matrices go to the cluster kernel.
 constexpr int kTsMax = 160;

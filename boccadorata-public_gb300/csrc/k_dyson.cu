@@ -360,12 +360,13 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
 // stored element with every lane busy:
 //   - p = A v: thread i walks row i of the lower triangle and then column i below the
 //     diagonal, which is row i of the upper triangle: p_i = sum_q A(max(i,q), min(i,q)) v_q,
-//     split in two halves of q over two threads, no atomics and no shuffles;
-//   - A -= v w^T + w v^T on the lower triangle: a warp takes rows i and m-1-i together,
-//     m+1 elements, so the triangle's rows balance;
+//     split in four parts of q over four threads, no atomics and no shuffles;
+//   - A -= v w^T + w v^T on the lower triangle, two FMAs per element: a warp takes
+//     rows i and m-1-i together, m+1 elements, so the triangle's rows balance;
 //   - sums (column norm, R v, p.v) are single-warp reductions.
 // Step k (trailing order m = n-k-1) has six barriers.
 constexpr int kTsThreads = 256;
+constexpr int kTsParts = 4;   // threads per row of the symmetric product
 
 __device__ inline double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -383,8 +384,8 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     extern __shared__ double sm[];
     double *A = sm;                          // [n][ld], lower triangle
     double *v = A + (size_t)n * ld;          // [n]
-    double *ph = v + n;                      // [2][n] halves of A v
-    double *w = ph + 2 * n;                  // [n]
+    double *ph = v + n;                      // [kTsParts][n] parts of A v
+    double *w = ph + kTsParts * n;           // [n]
     double *R = w + n;                       // [D][n]
     double *scb = R + (size_t)D * n;         // [2][4] tau, scal, K, flag by step parity | s_d[8] | rx[8]
     for (int q = tid; q < n * n; q += kTsThreads) {
@@ -405,12 +406,16 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             for (int t = 1 + lane; t < m; t += 32) { const double x = col[(size_t)(b0 + t) * ld]; s2 += x * x; }
             s2 = warp_sum(s2);
             if (lane == 0) {
+                // beta = -sign(alpha) |x|, tau = (beta - alpha) / beta = 1 + |alpha| / |x|,
+                // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|): Newton
+                // reciprocals and square root instead of FP64 division and sqrt
                 const double alpha = col[(size_t)b0 * ld];
                 double tau = 0.0, beta = alpha, scal = 0.0;
                 if (s2 != 0.0) {
-                    beta = -copysign(sqrt(alpha * alpha + s2), alpha);
-                    tau = (beta - alpha) / beta;
-                    scal = 1.0 / (alpha - beta);
+                    const double x2 = fma(alpha, alpha, s2), r = rsqrt_newton(x2), nx = x2 * r;
+                    beta = -copysign(nx, alpha);
+                    tau = fma(fabs(alpha), r, 1.0);
+                    scal = copysign(rcp_newton2(fabs(alpha) + nx), alpha);
                 }
                 sc[0] = tau; sc[1] = scal; sc[3] = (s2 != 0.0) ? 1.0 : 0.0;
                 J.d[k] = A[(size_t)k * ld + k]; J.e[k] = beta; J.tau[k] = tau;
@@ -430,17 +435,24 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? 1.0 : col[(size_t)(b0 + t) * ld] * scal;
         if (tid < D) sd[tid] = R[(size_t)tid * n + b0] + scal * rx[tid];
         __syncthreads();
-        // 3. halves of A v (trailing block, local indices), and R <- R H_k
-        for (int u = tid; u < 2 * m; u += kTsThreads) {
-            const int i = u >> 1, h = u & 1;
-            const int q0 = h ? (m >> 1) : 0, q1 = h ? m : (m >> 1);
+        // 3. parts of A v (trailing block, local indices), and R <- R H_k.  Four parts
+        //    per row: 4m items over the CTA's eight warps leave the four FP64 units
+        //    evenly loaded for the orders met here (two parts left two of them idle).
+        for (int u = tid; u < kTsParts * m; u += kTsThreads) {
+            const int i = u / kTsParts, h = u - i * kTsParts;
+            const int q0 = (int)(((long long)m * h) / kTsParts), q1 = (int)(((long long)m * (h + 1)) / kTsParts);
             const double *Ai = A + (size_t)(b0 + i) * ld + b0;
-            double acc = 0.0;
-            for (int q = q0; q < q1; ++q) {
-                const double a = (q <= i) ? Ai[q] : A[(size_t)(b0 + q) * ld + b0 + i];
-                acc += a * v[q];
+            auto el = [&](int q) { return (q <= i) ? Ai[q] : A[(size_t)(b0 + q) * ld + b0 + i]; };
+            double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;   // four chains: FP64 latency
+            int q = q0;
+            for (; q + 3 < q1; q += 4) {
+                acc0 += el(q) * v[q];
+                acc1 += el(q + 1) * v[q + 1];
+                acc2 += el(q + 2) * v[q + 2];
+                acc3 += el(q + 3) * v[q + 3];
             }
-            ph[h * n + i] = acc;
+            for (; q < q1; ++q) acc0 += el(q) * v[q];
+            ph[h * n + i] = (acc0 + acc1) + (acc2 + acc3);
         }
         for (int u = tid; u < D * m; u += kTsThreads) {
             const int d = u / m, t = u - d * m;
@@ -451,7 +463,10 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         if (warp == 0) {
             double s = 0.0;
             for (int t = lane; t < m; t += 32) {
-                const double pt = tau * (ph[t] + ph[n + t]);
+                double pa = 0.0;
+#pragma unroll
+                for (int h = 0; h < kTsParts; ++h) pa += ph[h * n + t];
+                const double pt = tau * pa;
                 w[t] = pt;
                 s += pt * v[t];
             }
@@ -472,7 +487,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             for (int u = lane; u < len; u += 32) {
                 const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
                 double *a = A + (size_t)(b0 + r) * ld + b0 + c;
-                *a -= v[r] * w[c] + w[r] * v[c];
+                *a = fma(-w[r], v[c], fma(-v[r], w[c], *a));   // two FMAs per element
             }
         }
         __syncthreads();
@@ -492,7 +507,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
 
 size_t tridiag_small_smem_bytes(int nmax, int Dmax) {
     const size_t n = (size_t)std::min(nmax, kTsMax);
-    return sizeof(double) * (n * (n | 1) + 4 * n + (size_t)Dmax * n + 32);
+    return sizeof(double) * (n * (n | 1) + (size_t)(kTsParts + 2) * n + (size_t)Dmax * n + 32);
 }
 
 // Per-warp partial vectors that fit next to the other arrays (8 = one per warp).

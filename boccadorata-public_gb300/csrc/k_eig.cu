@@ -12,7 +12,7 @@
 //             max(1e-12 |W|, 1e-13 |T_b|)
 //   k_invit   y_k by inverse iteration on T_b - W_k I (tridiagonal LU with partial
 //             pivoting) over its block, one thread per eigenvalue, each from its own
-//             start vector
+//             start vector (k_invit_small: the factors in shared memory, orders <= 160)
 //   k_cluster_orth  eigenvalues of one block closer than 1e-6 |T_b| form a cluster;
 //             its vectors are orthonormalised together (the exactly degenerate
 //             groups of tens to hundreds of zero-strength solutions in the Dyson
@@ -214,30 +214,39 @@ __device__ inline EigTol eig_tol(double onenrm) {
     return t;
 }
 
-// 1/q to ~2^-48 relative: the FP32 reciprocal refined by one Newton step,
-// r <- r + r (1 - q r) (the error squares); plain division outside the FP32 range.
-// An FP64 division is a dependent chain of about ten FP64 instructions.
-__device__ inline double rcp_newton(double q) {
-    const double aq = fabs(q);
-    if (aq > 1e-36 && aq < 1e36) {
-        const double r = (double)__frcp_rn((float)q);
-        return fma(r, fma(-q, r, 1.0), r);
-    }
-    return 1.0 / q;
-}
+// Storage of one eigenvector's LU factors (first and second superdiagonal, pivots as
+// reciprocals, multipliers, interchanges) and of its iterate, element i of each.
+struct InvitGlobal {   // the job's work area and matrix region, column k at stride n
+    double *U1, *U2, *DD, *LL, *PV, *Y;
+    int n, k;
+    __device__ double &u1(int i) { return U1[(size_t)i * n + k]; }
+    __device__ double &u2(int i) { return U2[(size_t)i * n + k]; }
+    __device__ double &dd(int i) { return DD[(size_t)i * n + k]; }
+    __device__ double &ll(int i) { return LL[(size_t)i * n + k]; }
+    __device__ double &y(int i) { return Y[(size_t)i * n + k]; }
+    __device__ bool pv(int i) { return PV[(size_t)i * n + k] != 0.0; }
+    __device__ void set_pv(int i, bool b) { PV[(size_t)i * n + k] = b ? 1.0 : 0.0; }
+};
 
-__global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first, long long total, double *work,
-                        const long long *work_first) {
-    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (g >= total) return;
-    const int lo = job_of(row_first, njobs, g);
-    const DyJob J = jobs[lo];
-    const int k = (int)(g - row_first[lo]), n = J.nc, NS = 2 + J.D;
-    if (k >= n) return;
-    const int b0 = J.blk[k], b1 = J.blk[n + k];
+constexpr int kIvThreads = 16;   // eigenvectors per CTA of the shared-memory variant
+struct InvitShared {   // shared memory, element i of this thread at i * kIvThreads + lane
+    double *U1, *U2, *DD, *LL, *Y;
+    unsigned char *PV;
+    int lane;
+    __device__ double &u1(int i) { return U1[i * kIvThreads + lane]; }
+    __device__ double &u2(int i) { return U2[i * kIvThreads + lane]; }
+    __device__ double &dd(int i) { return DD[i * kIvThreads + lane]; }
+    __device__ double &ll(int i) { return LL[i * kIvThreads + lane]; }
+    __device__ double &y(int i) { return Y[i * kIvThreads + lane]; }
+    __device__ bool pv(int i) { return PV[i * kIvThreads + lane] != 0; }
+    __device__ void set_pv(int i, bool b) { PV[i * kIvThreads + lane] = b ? 1 : 0; }
+};
+
+// Eigenvector k of block [b0, b1] (b1 > b0) into a.y(b0 .. b1).
+template <class S>
+__device__ void invit_vector(const DyJob &J, int k, int b0, int b1, S &a) {
+    const int NS = 2 + J.D;
     const double *d = J.d, *e = J.e;
-    double *Y = J.A;
-    if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
     const EigTol tl = eig_tol(J.tau[k]);
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
     // shift: walk to the start of the cluster inside the block, then apply the separation rule forward
@@ -245,69 +254,105 @@ __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first
     while (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) --k0;
     double x = W(k0);
     for (int q = k0 + 1; q <= k; ++q) x = fmax(W(q), x + tl.pertol);
-    double *wk = work + work_first[lo];   // 5 arrays of n*n: super, super-super, diagonal, multipliers, interchanges
-    double *U1 = wk, *U2 = wk + (size_t)n * n, *DD = wk + 2 * (size_t)n * n, *LL = wk + 3 * (size_t)n * n,
-           *PV = wk + 4 * (size_t)n * n;
-    // LU with partial pivoting of T_b - x I; rows i and i+1 may swap (PV = 1)
+    // LU with partial pivoting of T_b - x I; rows i and i+1 may swap
     for (int i = b0; i <= b1; ++i) {
-        DD[(size_t)i * n + k] = d[i] - x;
-        U1[(size_t)i * n + k] = (i < b1) ? e[i] : 0.0;
-        LL[(size_t)i * n + k] = (i < b1) ? e[i] : 0.0;
-        U2[(size_t)i * n + k] = 0.0;
+        a.dd(i) = d[i] - x;
+        a.u1(i) = (i < b1) ? e[i] : 0.0;
+        a.ll(i) = (i < b1) ? e[i] : 0.0;
+        a.u2(i) = 0.0;
     }
     for (int i = b0; i < b1; ++i) {
-        const double di = DD[(size_t)i * n + k], li = LL[(size_t)i * n + k];
+        const double di = a.dd(i), li = a.ll(i);
         if (fabs(di) >= fabs(li)) {
-            PV[(size_t)i * n + k] = 0.0;
+            a.set_pv(i, false);
             const double f = (di != 0.0) ? li * rcp_newton(di) : 0.0;
-            LL[(size_t)i * n + k] = f;
-            DD[(size_t)(i + 1) * n + k] -= f * U1[(size_t)i * n + k];
+            a.ll(i) = f;
+            a.dd(i + 1) -= f * a.u1(i);
         } else {
-            PV[(size_t)i * n + k] = 1.0;
+            a.set_pv(i, true);
             const double f = di * rcp_newton(li);
-            DD[(size_t)i * n + k] = li;
-            LL[(size_t)i * n + k] = f;
-            const double tt = U1[(size_t)i * n + k];
-            U1[(size_t)i * n + k] = DD[(size_t)(i + 1) * n + k];
-            DD[(size_t)(i + 1) * n + k] = tt - f * DD[(size_t)(i + 1) * n + k];
+            a.dd(i) = li;
+            a.ll(i) = f;
+            const double tt = a.u1(i);
+            a.u1(i) = a.dd(i + 1);
+            a.dd(i + 1) = tt - f * a.dd(i + 1);
             if (i + 1 < b1) {
-                U2[(size_t)i * n + k] = U1[(size_t)(i + 1) * n + k];
-                U1[(size_t)(i + 1) * n + k] = -f * U1[(size_t)(i + 1) * n + k];
+                a.u2(i) = a.u1(i + 1);
+                a.u1(i + 1) = -f * a.u1(i + 1);
             }
         }
     }
     // pivots no smaller than pertol, kept as reciprocals for the solves
     for (int i = b0; i <= b1; ++i) {
-        double p = DD[(size_t)i * n + k];
+        double p = a.dd(i);
         if (fabs(p) < tl.pertol) p = (p < 0 ? -tl.pertol : tl.pertol);
-        DD[(size_t)i * n + k] = rcp_newton(p);
+        a.dd(i) = rcp_newton(p);
     }
     for (int i = b0; i <= b1; ++i)
-        Y[(size_t)i * n + k] = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
+        a.y(i) = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
     for (int it = 0; it < 3; ++it) {
         for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges
-            double bi = Y[(size_t)i * n + k], bi1 = Y[(size_t)(i + 1) * n + k];
-            const double f = LL[(size_t)i * n + k];
-            if (PV[(size_t)i * n + k] == 0.0) bi1 -= f * bi;
+            double bi = a.y(i), bi1 = a.y(i + 1);
+            const double f = a.ll(i);
+            if (!a.pv(i)) bi1 -= f * bi;
             else { const double tt = bi; bi = bi1; bi1 = tt - f * bi1; }
-            Y[(size_t)i * n + k] = bi; Y[(size_t)(i + 1) * n + k] = bi1;
+            a.y(i) = bi; a.y(i + 1) = bi1;
         }
         double y1 = 0.0, y2 = 0.0, nrm = 0.0;
         for (int i = b1; i >= b0; --i) {   // U y = b, two superdiagonals
-            double v = Y[(size_t)i * n + k];
-            if (i + 1 <= b1) v -= U1[(size_t)i * n + k] * y1;
-            if (i + 2 <= b1) v -= U2[(size_t)i * n + k] * y2;
-            v *= DD[(size_t)i * n + k];
-            Y[(size_t)i * n + k] = v;
+            double v = a.y(i);
+            if (i + 1 <= b1) v -= a.u1(i) * y1;
+            if (i + 2 <= b1) v -= a.u2(i) * y2;
+            v *= a.dd(i);
+            a.y(i) = v;
             y2 = y1; y1 = v;
             nrm = fmax(nrm, fabs(v));
         }
         const double sc = (nrm > 0.0) ? rcp_newton(nrm) : 1.0;
         double s2 = 0.0;
-        for (int i = b0; i <= b1; ++i) { const double v = Y[(size_t)i * n + k] * sc; Y[(size_t)i * n + k] = v; s2 += v * v; }
+        for (int i = b0; i <= b1; ++i) { const double v = a.y(i) * sc; a.y(i) = v; s2 += v * v; }
         const double inv = (s2 > 0.0) ? 1.0 / sqrt(s2) : 0.0;
-        for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] *= inv;
+        for (int i = b0; i <= b1; ++i) a.y(i) *= inv;
     }
+}
+
+// Matrices of order > kTsMax: one thread per position, factors in the job's work area.
+__global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first, long long total, double *work,
+                        const long long *work_first) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int lo = job_of(row_first, njobs, g);
+    const DyJob J = jobs[lo];
+    const int k = (int)(g - row_first[lo]), n = J.nc;
+    if (k >= n || n <= kTsMax) return;
+    const int b0 = J.blk[k], b1 = J.blk[n + k];
+    double *Y = J.A;
+    if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
+    double *wk = work + work_first[lo];   // 5 arrays of n*n
+    InvitGlobal a{wk, wk + (size_t)n * n, wk + 2 * (size_t)n * n, wk + 3 * (size_t)n * n, wk + 4 * (size_t)n * n, Y,
+                  n, k};
+    invit_vector(J, k, b0, b1, a);
+}
+
+// Orders <= kTsMax: CTA (job, chunk of kIvThreads positions), each thread's factors and
+// iterate in shared memory (the LU and the solves read back what they just wrote,
+// which from global memory is an L2 round trip per step); the iterate goes to the
+// matrix region at the end.
+__global__ void __launch_bounds__(kIvThreads) k_invit_small(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.nc, lane = threadIdx.x, k = blockIdx.y * kIvThreads + lane;
+    if (n > kTsMax || k >= n) return;
+    extern __shared__ double smi[];
+    const int cap = kTsMax * kIvThreads;
+    InvitShared a{smi, smi + cap, smi + 2 * cap, smi + 3 * cap, smi + 4 * cap,
+                  reinterpret_cast<unsigned char *>(smi + 5 * cap), lane};
+    const int b0 = J.blk[k], b1 = J.blk[n + k];
+    double *Y = J.A;
+    if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
+    invit_vector(J, k, b0, b1, a);
+    for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] = a.y(i);
 }
 
 // One CTA per position; the CTA of a cluster's first member (cluster of two or more,
@@ -509,6 +554,12 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
                                                                 d_work_first);
     k_invit<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
                                                                d_work_first);
+    {
+        const int smem = (int)(sizeof(double) * 5 * kTsMax * kIvThreads + kTsMax * kIvThreads);
+        cudaError_t e = cudaFuncSetAttribute(k_invit_small, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_invit_small<<<dim3(njobs, (kTsMax + kIvThreads - 1) / kIvThreads), kIvThreads, smem, st>>>(d_jobs, njobs);
+    }
     k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_post<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_place<<<njobs, 256, 0, st>>>(d_jobs, njobs);

@@ -303,6 +303,16 @@ __global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, co
     if (i + 1 == n || iabJ[i + 1] != iab) rw->y = i;
 }
 
+// Channel of every pole (offsets off[0..ns], off[ns] = n) and the identity order.
+__global__ void k_pole_index(const int *off, int ns, long long n, int *seg, int *idx) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    int lo = 0, hi = ns - 1;   // last channel whose offset is <= g
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (off[mid] <= g) lo = mid; else hi = mid - 1; }
+    seg[g] = lo;
+    idx[g] = (int)g;
+}
+
 // Gather rows in a given order into separate SoA arrays (used after the sort), plus an
 // FP32 copy of the couplings for the FP32-vector Lanczos form.
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
