@@ -491,8 +491,19 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
         int *perm = dir == 0 ? ctx->d_perm_fw : ctx->d_perm_bk;
         size_t bytes = ctx->cub_bytes;
         const int nseg = ch_hi - ch_lo;
+        int seg_max = 0;
+        for (int I = ch_lo; I < ch_hi; ++I) seg_max = std::max(seg_max, rel[I - ch_lo + 1] - rel[I - ch_lo]);
         cudaError_t e;
-        if (dir == 0)
+        if (seg_max <= kSortMax) {   // every segment fits one CTA's shared memory
+            int P = 32;
+            while (P < seg_max) P <<= 1;
+            const int smem = (int)((sizeof(unsigned long long) + sizeof(int)) * P);
+            e = cudaFuncSetAttribute(k_seg_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess) {
+                k_seg_sort<<<nseg, kSortThreads, smem, ctx->st>>>(E + n0, d_off, P, dir == 1, n0, perm + n0);
+                e = cudaGetLastError();
+            }
+        } else if (dir == 0)
             e = cub::DeviceSegmentedRadixSort::SortPairs(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp, idx + n0,
                                                          perm + n0, (int)n, nseg, d_off, d_off + 1, 0, 64, ctx->st);
         else

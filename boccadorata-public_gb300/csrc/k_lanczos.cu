@@ -39,8 +39,8 @@
 //
 // Work split: one thread-block cluster per chain; CTA r of the cluster owns the
 // pole rows [r*S, (r+1)*S) of every vector.  Partial sums are combined through
-// distributed shared memory; every CTA adds the peers' partials in rank order,
-// so all CTAs hold bit-identical totals and take identical branches.
+// distributed shared memory; every CTA adds the peers' partials in the same fixed
+// order, so all CTAs hold bit-identical totals and take identical branches.
 #include <climits>
 #include <cooperative_groups.h>
 #include "bd_common.cuh"
@@ -61,6 +61,12 @@ __device__ inline T warp_sum_ct(T v) {
     return v;
 }
 
+// Fixed pairwise sums: three (four) dependent FP64 adds instead of seven (fifteen).
+__device__ inline double tree_sum8(const double *x) {
+    return ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+}
+__device__ inline double tree_sum16(const double *x) { return tree_sum8(x) + tree_sum8(x + 8); }
+
 // Deterministic pseudo-random restart value of pole i at Lanczos index j, in [0.5, 1.5).
 __host__ __device__ inline double restart_value(int i, int j) {
     unsigned x = (unsigned)i * 2654435761u ^ ((unsigned)j * 40503u + 0x9e3779b9u);
@@ -70,6 +76,7 @@ __host__ __device__ inline double restart_value(int i, int j) {
 
 constexpr int kLzThreads = 256;
 constexpr int kLzWarps = kLzThreads / 32;
+static_assert(kLzWarps == 8, "the warp partials are summed by tree_sum8");
 constexpr int kMaxScal = 32;   // 1 + D + n_used <= 17 (D <= 8, at most 8 earlier pivots)
 
 // 16-byte vector of the storage type: 4 floats or 2 doubles
@@ -155,18 +162,21 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // such row is (E_q, 0, ..., 0), needs no vector, and deflates out of the Dyson matrix.
     const double thr_exh = (sizeof(VT) == 4) ? 1e-9 : 1e-20;
     const int Qg = C.gE ? C.gInfo[0] : 0;
-    int gq = 0, gused = 0;       // group cursor (identical in every CTA)
+    const int dtot = Qg > 0 ? C.gInfo[Qg] : 0;   // unreached directions of all groups
+    int dcur = 0;                // directions used so far (identical in every CTA)
+    auto group_of = [&](int d) {   // group holding direction d < dtot: first q with cum[q] > d
+        int lo = 0, hi = Qg - 1;
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if (C.gInfo[1 + mid] > d) hi = mid; else lo = mid + 1; }
+        return lo;
+    };
     int nvec = 0;                // vectors stored so far
     bool tail = false;           // rest of the current pivot chain deflated
     bool contaminated = false;   // a restart vector was stored: no deflation from here on
     int ndefl = 0;
-    auto next_slot = [&]() -> bool {   // advance to a group with an unused direction
-        while (gq < Qg && gused >= C.gInfo[1 + gq]) { ++gq; gused = 0; }
-        return gq < Qg;
-    };
+    auto next_slot = [&]() -> bool { return dcur < dtot; };   // an unused direction is left
     auto deflated_row = [&](int jr) {  // consume a direction and write its row
-        double a = (gq < Qg) ? C.gE[gq] : C.gE[Qg - 1];
-        if (gq < Qg) ++gused;
+        const double a = (dcur < dtot) ? C.gE[group_of(dcur)] : C.gE[Qg - 1];
+        if (dcur < dtot) ++dcur;
         if (rank == 0 && tid == 0) {
             double *row = C.out + (size_t)jr * NT;
             for (int q = 0; q < NT; ++q) row[q] = 0.0;
@@ -176,17 +186,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         ++ndefl;
     };
 
-    // Sum over the cluster of one value per CTA held at buf[t], in rank order (the
-    // loads first, then the adds: one DSMEM round trip instead of CL).
+    // Sum over the cluster of one value per CTA held at buf[t], a fixed pairwise tree
+    // over the ranks (the loads first, then four levels of adds: one DSMEM round trip
+    // and a short FP64 chain instead of CL of each).
     auto cluster_sum = [&](const double *buf, int t) -> double {
         double x[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r) x[r] = (r < CL) ? cluster.map_shared_rank(const_cast<double *>(buf), r)[t] : 0.0;
-        double s = 0.0;
-#pragma unroll
-        for (int r = 0; r < 16; ++r)
-            if (r < CL) s += x[r];
-        return s;
+        return tree_sum16(x);
     };
 
     // (b1) dots pass: <v_t, w> for the pass's vectors t < nl and |w|^2, summed over
@@ -198,33 +205,33 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     auto dots_pass = [&](bool loc, int nl) {
         double *Ap = A + (size_t)dpar * rmax2;
         dpar ^= 1;
-        for (int t = warp; t < nl; t += kLzWarps) {
-            const VT *vt = V + (size_t)(loc ? lt[t] : t) * C.ld + i0;
-            CT acc = 0, acc1 = 0, acc2 = 0, acc3 = 0;
-            int q = lane;
-            for (; q + 96 < nv; q += 128) {   // four 16-byte loads in flight per lane
-                VT x0[VW], x1[VW], x2[VW], x3[VW];
-                load16<VT>(vt + q * VW, x0);
-                load16<VT>(vt + (q + 32) * VW, x1);
-                load16<VT>(vt + (q + 64) * VW, x2);
-                load16<VT>(vt + (q + 96) * VW, x3);
+        // four vectors per warp at a time: four independent 16-byte loads in flight per
+        // lane (one vector's slice is only a few loads per lane, so a warp that took
+        // its vectors one after another would wait out the L2 latency per vector)
+        for (int t0 = warp; t0 < nl; t0 += 4 * kLzWarps) {
+            const VT *vp[4];
 #pragma unroll
-                for (int u = 0; u < VW; ++u) {
-                    acc += x0[u] * w[q * VW + u];
-                    acc1 += x1[u] * w[(q + 32) * VW + u];
-                    acc2 += x2[u] * w[(q + 64) * VW + u];
-                    acc3 += x3[u] * w[(q + 96) * VW + u];
-                }
+            for (int u = 0; u < 4; ++u) {
+                const int t = t0 + u * kLzWarps;
+                vp[u] = V + (size_t)(t < nl ? (loc ? lt[t] : t) : (loc ? lt[t0] : t0)) * C.ld + i0;
             }
-            for (; q < nv; q += 32) {
-                VT x[VW];
-                load16<VT>(vt + q * VW, x);
+            CT acc[4] = {0, 0, 0, 0};
+#pragma unroll 2
+            for (int q = lane; q < nv; q += 32) {
+                VT x[4][VW];
 #pragma unroll
-                for (int u = 0; u < VW; ++u) acc += x[u] * w[q * VW + u];
+                for (int u = 0; u < 4; ++u) load16<VT>(vp[u] + q * VW, x[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) acc[u] += x[u][e] * w[q * VW + e];
             }
-            acc += (acc1 + acc2) + acc3;
-            acc = warp_sum_ct(acc);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
-            if (lane == 0) Ap[t] = (double)acc;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                acc[u] = warp_sum_ct(acc[u]);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
+                const int t = t0 + u * kLzWarps;
+                if (lane == 0 && t < nl) Ap[t] = (double)acc[u];
+            }
         }
         CT nwp = 0;
         for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
@@ -232,9 +239,10 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         if (lane == 0) red[warp * kMaxScal] = (double)nwp;
         __syncthreads();
         if (tid == 0) {
-            double s = 0.0;
-            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal];
-            Ap[nl] = s;
+            double x[kLzWarps];
+#pragma unroll
+            for (int q = 0; q < kLzWarps; ++q) x[q] = red[q * kMaxScal];
+            Ap[nl] = tree_sum8(x);
         }
         cluster.sync();
         for (int t = tid; t <= nl; t += kLzThreads) {   // (b2) totals over the cluster
@@ -333,9 +341,10 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         __syncthreads();
         const int nsc = 2 + D + nq;
         if (tid < nsc) {
-            double s = 0.0;
-            for (int q = 0; q < kLzWarps; ++q) s += red[q * kMaxScal + tid];
-            Bs[tid] = s;
+            double x[kLzWarps];
+#pragma unroll
+            for (int q = 0; q < kLzWarps; ++q) x[q] = red[q * kMaxScal + tid];
+            Bs[tid] = tree_sum8(x);
         }
         cluster.sync();
         if (tid < nsc) tot[tid] = cluster_sum(Bs, tid);
@@ -349,8 +358,25 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         if (newv) { ++k; tail = false; }
         __syncthreads();
         if (tail) {
-            next_slot();
-            deflated_row(j);
+            // The rest of this pivot chain is deflated: rows j .. jend-1 take directions
+            // dcur, dcur + 1, ... (the last group's energy once none is left), as
+            // deflated_row would one at a time; each thread places rows by binary search
+            // in the cumulative counts.
+            const int jend = (k + 1 < C.n_used) ? min(L, (int)C.start[k + 1]) : L;
+            const int R = jend - j;
+            for (int r = tid; r < R; r += kLzThreads) {
+                const int d = dcur + r;
+                const double a = (d < dtot) ? C.gE[group_of(d)] : C.gE[Qg - 1];
+                if (rank == 0) {
+                    double *row = C.out + (size_t)(j + r) * NT;
+                    for (int e = 0; e < NT; ++e) row[e] = 0.0;
+                    row[0] = a;
+                }
+                rowslot[j + r] = -1;
+            }
+            dcur = min(dcur + R, dtot);
+            ndefl += R;
+            j = jend - 1;
             continue;
         }
         const int nq = k;   // earlier pivot chains
@@ -461,11 +487,12 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         if (done) continue;
         // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216);
-        // the scalars are formed once (FP64 division and square root are long FP64 chains)
+        // the scalars are formed once, by Newton's iteration instead of FP64 division and
+        // square root (long FP64 chains)
         if (tid == 0) {
-            const double xb = sqrt(n2);
-            s_xb = xb;
-            s_ixb = 1.0 / xb;
+            const double r = rsqrt_newton(n2);   // 1/sqrt(n2) to a few ulp
+            s_xb = n2 * r;
+            s_ixb = r;
         }
         __syncthreads();
         const double xb = s_xb, ixb = s_ixb;
@@ -481,7 +508,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         if (rank == 0 && tid < NT) {   // one output element per thread
             double *row = C.out + (size_t)j * NT;
             double x = 0.0;
-            if (tid == 0) x = tot[1] / n2;
+            if (tid == 0) x = tot[1] * ixb * ixb;   // <w|E|w> / |w|^2
             else if (tid == 1) x = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
             else if (tid < 2 + k) x = tot[2 + D + (tid - 2)] * ixb;
             else if (tid >= C.nden_out && tid < C.nden_out + D) x = tot[2 + (tid - C.nden_out)] * ixb;
@@ -572,7 +599,8 @@ constexpr int kGrpThreads = 256;
 // per group; the D(D+1)/2 entries of G are summed over the lanes.  A one-pole group
 // has rank 1 exactly when a coupling is non-zero (the elimination's second pivot is
 // rounding); it needs no Gram matrix.  The count is written to gE[N + q] (the starts
-// in gInfo are still read by other warps).
+// in gInfo are still read by other warps); the kernel then turns the counts into
+// cumulative counts in gInfo.
 template <int D>
 __device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gInfo, int warp, int lane) {
     constexpr int P = D * (D + 1) / 2;
@@ -696,7 +724,23 @@ __global__ void __launch_bounds__(kGrpThreads) k_lz_groups(const LzChain *chains
         default: group_counts<8>(C, Q, gE, gInfo, warp, lane); break;
     }
     __syncthreads();
-    for (int q = tid; q < Q; q += kGrpThreads) gInfo[1 + q] = (int)gE[N + q];
+    // inclusive cumulative counts: gInfo[1 + q] = directions of groups 0..q (a chunked
+    // block scan), so a direction index finds its group by binary search
+    if (tid == 0) s_base = 0;
+    __syncthreads();
+    for (int b = 0; b < Q; b += kGrpThreads) {
+        const int q = b + tid;
+        int x = (q < Q) ? (int)gE[N + q] : 0;
+        for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        int off = s_base;
+        for (int w2 = 0; w2 < warp; ++w2) off += wsum[w2];
+        if (q < Q) gInfo[1 + q] = off + x;
+        __syncthreads();
+        if (tid == kGrpThreads - 1) s_base = off + x;
+        __syncthreads();
+    }
     if (tid == 0) gInfo[0] = Q;
 }
 

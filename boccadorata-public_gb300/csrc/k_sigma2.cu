@@ -9,6 +9,7 @@
 // bit-identical to the reference's x86-64 build.
 #include "bd_common.cuh"
 #include "bd_kernels.h"
+#include <climits>
 
 namespace bd {
 
@@ -301,6 +302,48 @@ __global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, co
     if (i == 0 || iabJ[i - 1] != iab)
         if (atomicCAS(&rw->x, -1, i) != -1) bad[2] = 1;
     if (i + 1 == n || iabJ[i + 1] != iab) rw->y = i;
+}
+
+// Stable sort of each channel's poles by energy (ascending, or descending with desc),
+// one CTA per channel segment [off[s], off[s+1]) of at most P = 2^k poles, P a power of
+// two that fits in shared memory: a bitonic network over (key, index) pairs, the key
+// the order-preserving integer image of the double (sign bit set: all bits flipped,
+// else the sign bit set; the radix sort's mapping, -0 before +0) and the index as tie
+// break, which makes the order stable.  E, off and perm are relative to the range's
+// first pole; perm[g] = global index (base + relative) of the pole sorted to g.
+__global__ void __launch_bounds__(kSortThreads) k_seg_sort(const double *E, const int *off, int P, bool desc,
+                                                           long long base, int *perm) {
+    const int sgi = blockIdx.x;
+    const int g0 = off[sgi], n = off[sgi + 1] - g0;
+    if (n <= 0) return;
+    extern __shared__ unsigned long long skey[];
+    int *sidx = reinterpret_cast<int *>(skey + P);
+    for (int t = threadIdx.x; t < P; t += kSortThreads) {
+        unsigned long long k = ~0ull;
+        int ix = INT_MAX;
+        if (t < n) {
+            unsigned long long u = (unsigned long long)__double_as_longlong(E[g0 + t]);
+            u = (u >> 63) ? ~u : (u | (1ull << 63));
+            k = desc ? ~u : u;
+            ix = (int)(base + g0 + t);   // global pole index, as the radix sort's values
+        }
+        skey[t] = k;
+        sidx[t] = ix;
+    }
+    __syncthreads();
+    for (int kk = 2; kk <= P; kk <<= 1)
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int t = threadIdx.x; t < P; t += kSortThreads) {
+                const int u = t ^ j;
+                if (u <= t) continue;
+                const unsigned long long ka = skey[t], kb = skey[u];
+                const int ia = sidx[t], ib = sidx[u];
+                const bool gt = (ka > kb) || (ka == kb && ia > ib);
+                if (((t & kk) == 0) ? gt : !gt) { skey[t] = kb; skey[u] = ka; sidx[t] = ib; sidx[u] = ia; }
+            }
+            __syncthreads();
+        }
+    for (int t = threadIdx.x; t < n; t += kSortThreads) perm[g0 + t] = sidx[t];
 }
 
 // Channel of every pole (offsets off[0..ns], off[ns] = n) and the identity order.
