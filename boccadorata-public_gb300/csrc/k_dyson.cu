@@ -15,6 +15,7 @@
 #include <cooperative_groups.h>
 #include "bd_common.cuh"
 #include "bd_kernels.h"
+#include "df64.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -355,15 +356,17 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
 // Matrices of order nc <= kTsMax (after deflation nearly all: the N_max = 10 channels
 // reduce to 11..94) are reduced by one CTA with the lower triangle resident in shared
 // memory, and the first D rows of Q = H_0 ... H_{n-3} (what k_qrows forms for the
-// cluster path) are updated in the same pass.  The SM's FP64 rate (two FMAs a cycle)
-// is the bound, so the symmetric product and the rank-2 update each take one FMA per
-// stored element with every lane busy:
-//   - p = A v: thread i walks row i of the lower triangle and then column i below the
-//     diagonal, which is row i of the upper triangle: p_i = sum_q A(max(i,q), min(i,q)) v_q,
+// cluster path) are updated in the same pass.  The element arithmetic is double-float
+// (df64.cuh: hi + lo FP32 pairs, ~48 bits): on this GPU an FP64 FMA issues at 1/64 of
+// the FP32 rate.  The reflector's scalars are formed by one thread per column, also in
+// double-float (Newton's reciprocal and square root), since that thread's dependent
+// chain is the serial part of every column.
+//   - A -= v w^T + w v^T on the lower triangle, each result also stored at its mirror
+//     position: a warp takes rows i and m-1-i together, m+1 elements, so the
+//     triangle's rows balance;
+//   - p = A v over full rows (contiguous, the same trip count in every lane), each row
 //     split in four parts of q over four threads, no atomics and no shuffles;
-//   - A -= v w^T + w v^T on the lower triangle, two FMAs per element: a warp takes
-//     rows i and m-1-i together, m+1 elements, so the triangle's rows balance;
-//   - sums (column norm, R v, p.v) are single-warp reductions.
+//   - sums (column norm, R x, p.v) are single-warp reductions.
 // Step k (trailing order m = n-k-1) has six barriers.
 constexpr int kTsThreads = 256;
 constexpr int kTsParts = 4;   // threads per row of the symmetric product
@@ -374,6 +377,7 @@ __device__ inline double warp_sum(double v) {
 }
 
 __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs, int njobs) {
+    using dfm::df;
     const int jid = blockIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
@@ -382,102 +386,125 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     const int ld = n | 1;     // odd stride: column reads hit distinct bank pairs
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     extern __shared__ double sm[];
-    double *A = sm;                          // [n][ld], lower triangle
-    double *v = A + (size_t)n * ld;          // [n]
-    double *ph = v + n;                      // [kTsParts][n] parts of A v
-    double *w = ph + kTsParts * n;           // [n]
-    double *R = w + n;                       // [D][n]
-    double *scb = R + (size_t)D * n;         // [2][4] tau, scal, K, flag by step parity | s_d[8] | rx[8]
+    df *A = reinterpret_cast<df *>(sm);      // [n][ld], both triangles
+    df *v = A + (size_t)n * ld;              // [n]
+    df *ph = v + n;                          // [kTsParts][n] parts of A v
+    df *w = ph + kTsParts * n;               // [n]
+    df *R = w + n;                           // [D][n]
+    __shared__ df s_dfs[2][4];               // tau, scal, K, beta of the step, by parity
+    __shared__ int s_flag[2];                // the column has a reflector, by parity
+    __shared__ df s_rx[8];                   // R_d[b0+1:] . x[1:]
+    __shared__ df s_coef[8];                 // tau s_d, s_d = R_d[b0:] . v
     for (int q = tid; q < n * n; q += kTsThreads) {
         const int i = q / n, j = q - i * n;
-        if (j <= i) A[(size_t)i * ld + j] = __ldcg(J.A + q);
+        if (j <= i) {   // the assembled lower triangle, mirrored
+            const df x = dfm::from_double(__ldcg(J.A + q));
+            A[(size_t)i * ld + j] = x;
+            A[(size_t)j * ld + i] = x;
+        }
     }
-    for (int q = tid; q < D * n; q += kTsThreads) R[q] = ((q % n) == (q / n)) ? 1.0 : 0.0;
+    for (int q = tid; q < D * n; q += kTsThreads) R[q] = df{((q % n) == (q / n)) ? 1.0f : 0.0f, 0.0f};
     __syncthreads();
+    const df zero{0.0f, 0.0f};
     for (int k = 0; k + 2 < n; ++k) {
         const int b0 = k + 1, m = n - b0;
-        const double *col = A + k;           // A(b0 + t, k) = col[(b0 + t) * ld]
+        const df *col = A + k;               // A(b0 + t, k) = col[(b0 + t) * ld]
         // the step's scalars alternate between two slots: a warp that skips a step
         // (H_k = I) may write step k+1's while another still reads step k's
-        double *sc = scb + 4 * (k & 1), *sd = scb + 8, *rx = scb + 16;
+        df *sdf = s_dfs[k & 1];
         // 1. warp 0: sigma = |x_{1:}|^2 and the reflector; warps 1..D: rx_d = R_d[b0+1:] . x[1:]
         if (warp == 0) {
-            double s2 = 0.0;
-            for (int t = 1 + lane; t < m; t += 32) { const double x = col[(size_t)(b0 + t) * ld]; s2 += x * x; }
-            s2 = warp_sum(s2);
+            df s2 = zero;
+            for (int t = 1 + lane; t < m; t += 32) { const df x = col[(size_t)(b0 + t) * ld]; s2 = dfm::fma(x, x, s2); }
+            s2 = dfm::warp_sum(s2);
             if (lane == 0) {
                 // beta = -sign(alpha) |x|, tau = (beta - alpha) / beta = 1 + |alpha| / |x|,
-                // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|): Newton
-                // reciprocals and square root instead of FP64 division and sqrt
-                const double alpha = col[(size_t)b0 * ld];
-                double tau = 0.0, beta = alpha, scal = 0.0;
-                if (s2 != 0.0) {
-                    const double x2 = fma(alpha, alpha, s2), r = rsqrt_newton(x2), nx = x2 * r;
-                    beta = -copysign(nx, alpha);
-                    tau = fma(fabs(alpha), r, 1.0);
-                    scal = copysign(rcp_newton2(fabs(alpha) + nx), alpha);
+                // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|), in double-float
+                // with Newton's reciprocal and square root (FP64 only outside the FP32 range)
+                const df al = col[(size_t)b0 * ld];
+                const bool nz = (s2.h != 0.0f || s2.l != 0.0f);
+                const bool ng = signbit(al.h);
+                const df aa = ng ? dfm::neg(al) : al;
+                df tau = zero, scal = zero, beta = al;
+                if (nz) {
+                    const df x2 = dfm::fma(al, al, s2);
+                    if (x2.h > 1e-30f && x2.h < 1e30f) {
+                        const df r = dfm::rsqrt(x2), nx = dfm::mul(x2, r);
+                        beta = ng ? nx : dfm::neg(nx);
+                        tau = dfm::fma(aa, r, df{1.0f, 0.0f});
+                        scal = dfm::rcp(dfm::add(aa, nx));
+                        if (ng) scal = dfm::neg(scal);
+                    } else {
+                        const double a = dfm::to_double(al), x2d = dfm::to_double(x2);
+                        const double r = 1.0 / sqrt(x2d), nx = x2d * r;
+                        beta = dfm::from_double(-copysign(nx, a));
+                        tau = dfm::from_double(fma(fabs(a), r, 1.0));
+                        scal = dfm::from_double(copysign(1.0 / (fabs(a) + nx), a));
+                    }
                 }
-                sc[0] = tau; sc[1] = scal; sc[3] = (s2 != 0.0) ? 1.0 : 0.0;
-                J.d[k] = A[(size_t)k * ld + k]; J.e[k] = beta; J.tau[k] = tau;
+                sdf[0] = tau; sdf[1] = scal; sdf[3] = beta;
+                s_flag[k & 1] = nz;
             }
         } else {
             for (int d = warp - 1; d < D; d += kTsThreads / 32 - 1) {
-                double s = 0.0;
-                for (int t = 1 + lane; t < m; t += 32) s += R[(size_t)d * n + b0 + t] * col[(size_t)(b0 + t) * ld];
-                s = warp_sum(s);
-                if (lane == 0) rx[d] = s;
+                df s = zero;
+                for (int t = 1 + lane; t < m; t += 32) s = dfm::fma(R[(size_t)d * n + b0 + t], col[(size_t)(b0 + t) * ld], s);
+                s = dfm::warp_sum(s);
+                if (lane == 0) s_rx[d] = s;
             }
         }
         __syncthreads();
-        if (sc[3] == 0.0) continue;          // column already reduced: H_k = I
-        const double tau = sc[0], scal = sc[1];
-        // 2. v, and s_d = R_d[b0:] . v
-        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? 1.0 : col[(size_t)(b0 + t) * ld] * scal;
-        if (tid < D) sd[tid] = R[(size_t)tid * n + b0] + scal * rx[tid];
+        if (tid == kTsThreads - 1) {   // the step's d, e, tau in FP64, off the critical path
+            J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
+            J.e[k] = dfm::to_double(sdf[3]);
+            J.tau[k] = dfm::to_double(sdf[0]);
+        }
+        if (!s_flag[k & 1]) continue;        // column already reduced: H_k = I
+        const df taud = sdf[0], scald = sdf[1];
+        // 2. v, and s_d = R_d[b0:] . v (the R update's coefficient tau s_d)
+        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(col[(size_t)(b0 + t) * ld], scald);
+        if (tid < D) s_coef[tid] = dfm::mul(taud, dfm::fma(scald, s_rx[tid], R[(size_t)tid * n + b0]));
         __syncthreads();
         // 3. parts of A v (trailing block, local indices), and R <- R H_k.  Four parts
-        //    per row: 4m items over the CTA's eight warps leave the four FP64 units
-        //    evenly loaded for the orders met here (two parts left two of them idle).
+        //    per row keep all eight warps busy.
         for (int u = tid; u < kTsParts * m; u += kTsThreads) {
             const int i = u / kTsParts, h = u - i * kTsParts;
             const int q0 = (int)(((long long)m * h) / kTsParts), q1 = (int)(((long long)m * (h + 1)) / kTsParts);
-            const double *Ai = A + (size_t)(b0 + i) * ld + b0;
-            auto el = [&](int q) { return (q <= i) ? Ai[q] : A[(size_t)(b0 + q) * ld + b0 + i]; };
-            double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;   // four chains: FP64 latency
+            const df *Ai = A + (size_t)(b0 + i) * ld + b0;   // the full row (the update mirrors)
+            df acc0 = zero, acc1 = zero;   // two chains
             int q = q0;
-            for (; q + 3 < q1; q += 4) {
-                acc0 += el(q) * v[q];
-                acc1 += el(q + 1) * v[q + 1];
-                acc2 += el(q + 2) * v[q + 2];
-                acc3 += el(q + 3) * v[q + 3];
+            for (; q + 1 < q1; q += 2) {
+                acc0 = dfm::fma(Ai[q], v[q], acc0);
+                acc1 = dfm::fma(Ai[q + 1], v[q + 1], acc1);
             }
-            for (; q < q1; ++q) acc0 += el(q) * v[q];
-            ph[h * n + i] = (acc0 + acc1) + (acc2 + acc3);
+            if (q < q1) acc0 = dfm::fma(Ai[q], v[q], acc0);
+            ph[h * n + i] = dfm::add(acc0, acc1);
         }
         for (int u = tid; u < D * m; u += kTsThreads) {
             const int d = u / m, t = u - d * m;
-            R[(size_t)d * n + b0 + t] -= tau * sd[d] * v[t];
+            df &r = R[(size_t)d * n + b0 + t];
+            r = dfm::fma(dfm::neg(s_coef[d]), v[t], r);
         }
         __syncthreads();
         // 4. p = tau A v; K = (tau / 2) p . v
         if (warp == 0) {
-            double s = 0.0;
+            df s = zero;
             for (int t = lane; t < m; t += 32) {
-                double pa = 0.0;
+                df pa = ph[t];
 #pragma unroll
-                for (int h = 0; h < kTsParts; ++h) pa += ph[h * n + t];
-                const double pt = tau * pa;
+                for (int h = 1; h < kTsParts; ++h) pa = dfm::add(pa, ph[h * n + t]);
+                const df pt = dfm::mul(taud, pa);
                 w[t] = pt;
-                s += pt * v[t];
+                s = dfm::fma(pt, v[t], s);
             }
-            s = warp_sum(s);
-            if (lane == 0) sc[2] = 0.5 * tau * s;
+            s = dfm::warp_sum(s);
+            if (lane == 0) sdf[2] = dfm::mul(dfm::mul(df{0.5f, 0.0f}, taud), s);
         }
         __syncthreads();
         // 5. w = p - K v
         {
-            const double K = sc[2];
-            for (int t = tid; t < m; t += kTsThreads) w[t] -= K * v[t];
+            const df nK = dfm::neg(sdf[2]);
+            for (int t = tid; t < m; t += kTsThreads) w[t] = dfm::fma(nK, v[t], w[t]);
         }
         __syncthreads();
         // 6. A -= v w^T + w v^T on the trailing lower triangle, rows i and m-1-i per warp
@@ -486,23 +513,26 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             const int len = (i1 == i2) ? (i1 + 1) : (m + 1);
             for (int u = lane; u < len; u += 32) {
                 const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
-                double *a = A + (size_t)(b0 + r) * ld + b0 + c;
-                *a = fma(-w[r], v[c], fma(-v[r], w[c], *a));   // two FMAs per element
+                df *a = A + (size_t)(b0 + r) * ld + b0 + c;
+                const df t2 = dfm::fma(w[r], v[c], dfm::mul(v[r], w[c]));
+                const df x = dfm::add(*a, dfm::neg(t2));
+                *a = x;
+                A[(size_t)(b0 + c) * ld + b0 + r] = x;   // the mirror, read by the next product
             }
         }
         __syncthreads();
     }
     if (tid == 0) {
         if (n >= 2) {
-            J.d[n - 2] = A[(size_t)(n - 2) * ld + (n - 2)];
-            J.e[n - 2] = A[(size_t)(n - 1) * ld + (n - 2)];
+            J.d[n - 2] = dfm::to_double(A[(size_t)(n - 2) * ld + (n - 2)]);
+            J.e[n - 2] = dfm::to_double(A[(size_t)(n - 1) * ld + (n - 2)]);
             J.tau[n - 2] = 0.0;
         }
-        J.d[n - 1] = A[(size_t)(n - 1) * ld + (n - 1)];
+        J.d[n - 1] = dfm::to_double(A[(size_t)(n - 1) * ld + (n - 1)]);
         J.e[n - 1] = 0.0;
         J.tau[n - 1] = 0.0;
     }
-    for (int q = tid; q < D * n; q += kTsThreads) J.R[q] = R[q];
+    for (int q = tid; q < D * n; q += kTsThreads) J.R[q] = dfm::to_double(R[q]);
 }
 
 size_t tridiag_small_smem_bytes(int nmax, int Dmax) {
