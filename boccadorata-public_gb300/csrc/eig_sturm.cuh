@@ -17,8 +17,9 @@
 //     Once the bracket holds only the wanted eigenvalue, the double-float value of
 //     p_m(x) = det(T - x I) drives regula falsi with the Illinois modification
 //     (Dowell and Jarratt, BIT 11 (1971) 168), which converges superlinearly; else
-//     the step is a bisection.  Stopping rule: bracket width <= max(1e-12 |W|,
-//     1e-13 |T_b|), then W is the bracket's midpoint.
+//     the bracket is trisected.  Every pass evaluates several points at once (their
+//     recurrences interleave in one thread).  Stopping rule: bracket width
+//     <= max(1e-12 |W|, 1e-13 |T_b|), then W is the bracket's midpoint.
 //
 // Host- and device-compilable: the same arithmetic is checked on the CPU against
 // LAPACK.  The error-free transformations use explicitly rounded operations so the
@@ -215,72 +216,147 @@ BD_HD int count_df(const float *dh, const float *dl, const float *eh, const floa
     return c;
 }
 
+// Evaluators of four points per pass.  LaneEval4 (device): four lanes of a warp each
+// count one point and exchange the results by shuffles within their group.
+// SeqEval4 (host and device): one thread counts the four points one after another.
+// The bisection below is written against either, so the host check runs the same
+// driver as the device.
+struct SeqEval4 {
+    const float *dh, *dl, *eh, *el;
+    int m;
+    BD_HD void f(const float *x, int *c) const {
+        for (int j = 0; j < 4; ++j) c[j] = count_f(dh, eh, m, x[j]);
+    }
+    BD_HD void df(const double *x, int *c, float *fh, int *fe) const {
+        for (int j = 0; j < 4; ++j) {
+            float h, l;
+            split(x[j], h, l);
+            c[j] = count_df(dh, dl, eh, el, m, h, l, &fh[j], &fe[j]);
+        }
+    }
+};
+
+#if defined(__CUDACC__)
+struct LaneEval4 {
+    const float *dh, *dl, *eh, *el;
+    int m;
+    int sub;          // this lane's point, 0..3
+    int base;         // lane index of the group's first lane
+    unsigned mask;    // the group's four lanes
+    __device__ void f(const float *x, int *c) const {
+        const int mine = count_f(dh, eh, m, x[sub]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) c[j] = __shfl_sync(mask, mine, base + j);
+    }
+    __device__ void df(const double *x, int *c, float *fh, int *fe) const {
+        float h, l, f;
+        int e;
+        split(x[sub], h, l);
+        const int mine = count_df(dh, dl, eh, el, m, h, l, &f, &e);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            c[j] = __shfl_sync(mask, mine, base + j);
+            fh[j] = __shfl_sync(mask, f, base + j);
+            fe[j] = __shfl_sync(mask, e, base + j);
+        }
+    }
+};
+#endif
+
 // Eigenvalue k (0-based, ascending) of a block of order m >= 2 given scaled by
-// 2^-sexp: d = dh + dl, e2 = eh + el, Gershgorin bounds [glo, ghi] of the scaled
-// block (outward rounded).  Returns it unscaled; *nev counts the double-float Sturm
-// evaluations.
-BD_HD double bisect(const float *dh, const float *dl, const float *eh, const float *el, int m, int k, float glo,
-                    float ghi, int sexp, int *nev) {
+// 2^-sexp (the evaluator holds d = dh + dl and e2 = eh + el), Gershgorin bounds
+// [glo, ghi] of the scaled block (outward rounded).  Returns it unscaled; *nev counts
+// the double-float passes.
+//
+// Four points per pass.  FP32 stage: the bracket shrinks fivefold per pass, to 2^-20
+// of the scaled norm.  Double-float stage: fivefold sections until the bracket holds
+// eigenvalue k alone; then the regula falsi point x of the determinant with x -+ delta
+// and the bracket's midpoint, delta the last move of x (at first 1e-3 of the bracket;
+// at least tol / 2), so that the points usually straddle the root closely.  A pass
+// that moves one end only halves the other end's determinant (the Illinois rule).
+// Stopping rule: width <= max(1e-12 |W|, 1e-13 |T_b|); W is the bracket's midpoint.
+template <class Ev>
+BD_HD double bisect4(const Ev &ev, int k, float glo, float ghi, int sexp, int *nev) {
     const double tn = fmax(fabs((double)glo), fabs((double)ghi));
     const double g0 = (double)glo - 0x1p-45, g1 = (double)ghi + 0x1p-45;
-    // FP32 bracket to 2^-20 of the scaled norm; the FP32 rounding of the block moves
-    // its eigenvalues by ~1e-7
     float af = glo, bf = ghi;
-    for (int it = 0; it < 40 && bf - af > 0x1p-20f; ++it) {
-        const float mid = 0.5f * (af + bf);
-        if (mid <= af || mid >= bf) break;
-        if (count_f(dh, eh, m, mid) > k) bf = mid; else af = mid;
+    for (int it = 0; it < 20 && bf - af > 0x1p-20f; ++it) {
+        float xs[4];
+        int cs[4];
+        const float wd = bf - af;
+        for (int j = 0; j < 4; ++j) xs[j] = af + wd * (0.2f * (float)(j + 1));
+        ev.f(xs, cs);
+        float na = af, nb = bf;
+        for (int j = 0; j < 4; ++j) if (cs[j] <= k && xs[j] > na && xs[j] < bf) na = xs[j];
+        for (int j = 3; j >= 0; --j) if (cs[j] > k && xs[j] < nb && xs[j] > af) nb = xs[j];
+        if (!(na < nb) || (na == af && nb == bf)) break;   // FP32 rounding or no progress
+        af = na; bf = nb;
     }
-    const double margin = 4e-6;
-    double a = fmax(g0, (double)af - margin), b = fmin(g1, (double)bf + margin);
-    float fah, fbh, xh, xl;
-    int fae, fbe;
-    split(a, xh, xl);
-    int ca = count_df(dh, dl, eh, el, m, xh, xl, &fah, &fae);
-    split(b, xh, xl);
-    int cb = count_df(dh, dl, eh, el, m, xh, xl, &fbh, &fbe);
-    int ne = 2;
+    double a = fmax(g0, (double)af - 4e-6), b = fmin(g1, (double)bf + 4e-6);
+    float fah = 0.0f, fbh = 0.0f;
+    int fae = 0, fbe = 0, ca = 0, cb = 0;
+    double xs[4];
+    int c[4], fe[4];
+    float fh[4];
+    // both ends and the two trisection points in the first pass
+    auto first = [&](double lo, double hi) {
+        xs[0] = lo; xs[1] = lo + (hi - lo) / 3.0; xs[2] = lo + 2.0 * (hi - lo) / 3.0; xs[3] = hi;
+        ev.df(xs, c, fh, fe);
+        ca = c[0]; fah = fh[0]; fae = fe[0]; cb = c[3]; fbh = fh[3]; fbe = fe[3];
+    };
+    first(a, b);
+    int ne = 1;
     if (!(ca <= k && cb > k)) {   // the FP32 bracket missed: start over from Gershgorin
         a = g0; b = g1;
-        split(a, xh, xl);
-        ca = count_df(dh, dl, eh, el, m, xh, xl, &fah, &fae);
-        split(b, xh, xl);
-        cb = count_df(dh, dl, eh, el, m, xh, xl, &fbh, &fbe);
-        ne += 2;
+        first(a, b);
+        ++ne;
     }
-    int side = -1;   // endpoint replaced last: 0 = a, 1 = b
+    // the two interior points of the first pass
+    for (int j = 1; j <= 2; ++j) {
+        if (c[j] <= k && xs[j] > a) { a = xs[j]; ca = c[j]; fah = fh[j]; fae = fe[j]; }
+    }
+    for (int j = 2; j >= 1; --j) {
+        if (c[j] > k && xs[j] < b) { b = xs[j]; cb = c[j]; fbh = fh[j]; fbe = fe[j]; }
+    }
+    double xprev = 0.0;
+    bool have_prev = false;
     for (int it = 0; it < 200; ++it) {
         const double tol = fmax(1e-12 * fmax(fabs(a), fabs(b)), 1e-13 * tn);
         if (b - a <= tol) break;
         const double mid = 0.5 * (a + b);
         if (mid == a || mid == b) break;
-        double x = mid;
         const bool rf = (ca == k && cb == k + 1);
         if (rf) {
             // regula falsi: x = a + (b - a) f(a) / (f(a) - f(b)), f(b) / f(a) < 0
             int de = fbe - fae;
             de = de < -120 ? -120 : (de > 120 ? 120 : de);
             const float r = (fbh / fah) * pow2f(de);
-            const float w = 1.0f / (1.0f - r);
-            x = a + (double)w * (b - a);
+            const float wgt = 1.0f / (1.0f - r);
+            double x = a + (double)wgt * (b - a);
             if (!(x > a && x < b)) x = mid;
-            // a step closer than tol / 2 to an end moves to tol / 2, so the bracket
-            // either closes on the root or shrinks by at least that much
-            x = fmin(fmax(x, a + 0.5 * tol), b - 0.5 * tol);
-        }
-        float fxh;
-        int fxe;
-        split(x, xh, xl);
-        const int cx = count_df(dh, dl, eh, el, m, xh, xl, &fxh, &fxe);
-        ++ne;
-        if (cx > k) {
-            b = x; cb = cx; fbh = fxh; fbe = fxe;
-            if (rf && side == 1) fah *= 0.5f;   // Illinois: the stale end's value halves
-            side = rf ? 1 : -1;
+            const double lo = a + 0.5 * tol, hi = b - 0.5 * tol;
+            x = fmin(fmax(x, lo), hi);
+            const double delta = fmax(have_prev ? fabs(x - xprev) : 1e-3 * (b - a), 0.5 * tol);
+            xprev = x;
+            have_prev = true;
+            xs[0] = fmin(fmax(x - delta, lo), hi);
+            xs[1] = x;
+            xs[2] = fmin(fmax(x + delta, lo), hi);
+            xs[3] = mid;
         } else {
-            a = x; ca = cx; fah = fxh; fae = fxe;
-            if (rf && side == 0) fbh *= 0.5f;
-            side = rf ? 0 : -1;
+            for (int j = 0; j < 4; ++j) xs[j] = a + (b - a) * (0.2 * (double)(j + 1));
+            have_prev = false;
+        }
+        ev.df(xs, c, fh, fe);
+        ++ne;
+        const double a_old = a, b_old = b;
+        for (int j = 0; j < 4; ++j)
+            if (c[j] <= k && xs[j] > a && xs[j] < b_old) { a = xs[j]; ca = c[j]; fah = fh[j]; fae = fe[j]; }
+        for (int j = 0; j < 4; ++j)
+            if (c[j] > k && xs[j] < b && xs[j] > a_old) { b = xs[j]; cb = c[j]; fbh = fh[j]; fbe = fe[j]; }
+        if (rf) {   // one end moved only: the stale end's value halves (Illinois)
+            if (a == a_old && b != b_old) fah *= 0.5f;
+            if (b == b_old && a != a_old) fbh *= 0.5f;
         }
     }
     if (nev) *nev = ne;

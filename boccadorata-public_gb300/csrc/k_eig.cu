@@ -6,7 +6,7 @@
 //   k_qrows   R = first D rows of Q = H_0 H_1 ... H_{n-3} (reflectors kept in A's rows;
 //             matrices of order <= kTsMax get R from k_tridiag_small)
 //   k_bisect_prep  splits T into unreduced blocks at negligible off-diagonals
-//   k_bisect  W_k by bisection on Sturm counts over its block, one thread per
+//   k_bisect  W_k by bisection on Sturm counts over its block, four threads per
 //             eigenvalue (eig_sturm.cuh): an FP32 bracket, checked and finished in
 //             double-float arithmetic (FP64 issues at 1/64 of the FP32 rate) to
 //             max(1e-12 |W|, 1e-13 |T_b|)
@@ -168,11 +168,18 @@ __device__ inline int job_of(const long long *row_first, int njobs, long long g)
     return lo;
 }
 
-// One thread per position: the eigenvalue of its block with the position's local
-// index, by sturm::bisect (FP32 bracket, double-float finish; no FP64 in the counts).
-__global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_first, long long total,
-                         double *work, const long long *work_first) {
-    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// Four threads per position: the eigenvalue of its block with the position's local
+// index, by sturm::bisect4 (FP32 bracket, double-float finish, four points per pass,
+// one per lane; no FP64 in the counts).  A matrix's eigenvalues are few hundred at
+// most, so the per-eigenvalue chain is the latency that matters; four lanes shorten
+// it and still leave most of the GPU's sub-partitions idle.
+constexpr int kBisectThreads = 128;   // 32 positions per CTA
+
+__global__ void __launch_bounds__(kBisectThreads) k_bisect(const DyJob *jobs, int njobs, const long long *row_first,
+                                                           long long total, double *work, const long long *work_first) {
+    const long long g4 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long g = g4 >> 2;   // the group's position; its four lanes share every branch
+    const int sub = (int)(g4 & 3);
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
@@ -184,9 +191,11 @@ __global__ void k_bisect(const DyJob *jobs, int njobs, const long long *row_firs
         W = J.d[t];
     } else {
         const BisectTables T = bisect_tables(work + work_first[lo], n);
-        W = sturm::bisect(T.dh + b0, T.dl + b0, T.eh + b0, T.el + b0, m, k, T.glo[b0], T.ghi[b0], T.sx[b0], nullptr);
+        const int lane = threadIdx.x & 31, base = lane & ~3;
+        const sturm::LaneEval4 ev{T.dh + b0, T.dl + b0, T.eh + b0, T.el + b0, m, sub, base, 0xFu << base};
+        W = sturm::bisect4(ev, k, T.glo[b0], T.ghi[b0], T.sx[b0], nullptr);
     }
-    J.sol[(size_t)t * (2 + J.D)] = W;   // eigenvalue parked in the W slot of its position
+    if (sub == 0) J.sol[(size_t)t * (2 + J.D)] = W;   // eigenvalue parked in the W slot of its position
 }
 
 // ------------------------------------------------------------------ K4d
@@ -549,9 +558,9 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
     k_qrows<<<njobs, kEigThreads, 0, st>>>(d_jobs, njobs);
     k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs, work, d_work_first);
     const unsigned nb = (unsigned)((total_rows + 127) / 128);
-    // a warp per CTA: a matrix's few hundred eigenvalues spread over as many SMs
-    k_bisect<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
-                                                                d_work_first);
+    // four lanes per eigenvalue; a matrix's few hundred eigenvalues spread over many SMs
+    k_bisect<<<(unsigned)((total_rows * 4 + kBisectThreads - 1) / kBisectThreads), kBisectThreads, 0, st>>>(
+        d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
     k_invit<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
                                                                d_work_first);
     {

@@ -2,8 +2,9 @@
 // CPU check against LAPACK (tests/test_sturm_host.py).  The glue below follows the
 // device kernels k_bisect_prep / k_bisect: split at negligible off-diagonals, scale
 // each block by a power of two, split d and e^2 into FP32 pairs, bisect each
-// eigenvalue.  Built with -ffp-contract=off so no FMA is formed that the device code
-// does not form.
+// eigenvalue (the device's four-lane evaluator replaced by one that counts its four
+// points one after another).  Built with -ffp-contract=off so no FMA is formed that
+// the device code does not form.
 #include <math.h>
 #include <vector>
 #include "../boccadorata-public_gb300/csrc/eig_sturm.cuh"
@@ -38,7 +39,8 @@ extern "C" int bd_sturm_eigenvalues(const double *d, const double *e_in, int n, 
             blk_start[b0 + k] = b0;
             if (m == 1) { w[b0] = d[b0]; continue; }
             int ne = 0;
-            w[b0 + k] = bisect(&dh[b0], &dl[b0], &eh[b0], &el[b0], m, k, lo * (float)sc, hi * (float)sc, sx, &ne);
+            const SeqEval4 evl{&dh[b0], &dl[b0], &eh[b0], &el[b0], m};
+            w[b0 + k] = bisect4(evl, k, lo * (float)sc, hi * (float)sc, sx, &ne);
             ev += ne;
         }
         b0 = b1 + 1;
