@@ -113,6 +113,9 @@ struct bd_ctx {
         *d_perm_bk = nullptr;
     double *d_keys_tmp = nullptr;
     int *d_segoff_fw = nullptr, *d_segoff_bk = nullptr;
+    int4 *d_chunks_fw = nullptr, *d_chunks_bk = nullptr;   // chunk tables of the shared-memory sort
+    long long chunk_cap_fw = 0, chunk_cap_bk = 0;
+    int *d_sorti_fw = nullptr, *d_sorti_bk = nullptr;       // its sorted indices
     void *d_cub_tmp = nullptr;
     size_t cub_bytes = 0;
     double *d_sighf = nullptr, *d_sig1b = nullptr;  // per channel D*D at chan_dd_off
@@ -494,14 +497,24 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
         int seg_max = 0;
         for (int I = ch_lo; I < ch_hi; ++I) seg_max = std::max(seg_max, rel[I - ch_lo + 1] - rel[I - ch_lo]);
         cudaError_t e;
-        if (seg_max <= kSortMax) {   // every segment fits one CTA's shared memory
-            int P = 32;
-            while (P < seg_max) P <<= 1;
-            const int smem = (int)((sizeof(unsigned long long) + sizeof(int)) * P);
-            e = cudaFuncSetAttribute(k_seg_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (seg_max <= kSortMax) {   // chunks sorted in shared memory, then ranked
+            std::vector<int4> chunks;
+            for (int I = ch_lo; I < ch_hi; ++I) {
+                const int s0 = rel[I - ch_lo], sl = rel[I - ch_lo + 1] - s0;
+                for (int c0 = 0; c0 < sl; c0 += kSortChunk) chunks.push_back(make_int4(s0 + c0, std::min(kSortChunk, sl - c0), s0, sl));
+            }
+            int4 *dch = dir == 0 ? ctx->d_chunks_fw : ctx->d_chunks_bk;
+            if ((long long)chunks.size() > (dir == 0 ? ctx->chunk_cap_fw : ctx->chunk_cap_bk))
+                return fail(ctx, BD_ERR_STATE, "sort chunk table overflow");
+            e = cudaMemcpyAsync(dch, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, ctx->st);
+            unsigned long long *tk = reinterpret_cast<unsigned long long *>(ctx->d_keys_tmp);
+            int *ti = dir == 0 ? ctx->d_sorti_fw : ctx->d_sorti_bk;
             if (e == cudaSuccess) {
-                k_seg_sort<<<nseg, kSortThreads, smem, ctx->st>>>(E + n0, d_off, P, dir == 1, n0, perm + n0);
+                k_chunk_sort<<<(unsigned)chunks.size(), kSortThreads, 0, ctx->st>>>(E + n0, dch, dir == 1, n0, tk, ti);
+                k_chunk_place<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(tk, ti, dch, (int)chunks.size(), n, n0,
+                                                                              perm + n0);
                 e = cudaGetLastError();
+                ctx->launches += 1;
             }
         } else if (dir == 0)
             e = cub::DeviceSegmentedRadixSort::SortPairs(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp, idx + n0,
@@ -962,6 +975,12 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
+    ctx->chunk_cap_fw = ctx->tot_fw / kSortChunk + ns + 1;
+    ctx->chunk_cap_bk = ctx->tot_bk / kSortChunk + ns + 1;
+    if ((rc = dalloc(ctx, &ctx->d_chunks_fw, (size_t)ctx->chunk_cap_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_chunks_bk, (size_t)ctx->chunk_cap_bk))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_sorti_fw, ctx->tot_fw))) return rc;
+    if ((rc = dalloc(ctx, &ctx->d_sorti_bk, ctx->tot_bk))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_perm_fw, ctx->tot_fw))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_perm_bk, ctx->tot_bk))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_keys_tmp, std::max(ctx->tot_fw, ctx->tot_bk)))) return rc;

@@ -14,9 +14,13 @@ __global__ void k_ehf(DevProblem P, const int3 *entries, int nent, const long lo
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
                               const double *Ein, const double *Min, double *Eout, double *Mout, float *Mfout);
 __global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows);
-constexpr int kSortThreads = 1024;
-constexpr int kSortMax = 16384;   // longest channel segment sorted in shared memory
-__global__ void k_seg_sort(const double *E, const int *off, int P, bool desc, long long base, int *perm);
+constexpr int kSortThreads = 512;
+constexpr int kSortChunk = 2048;  // poles per chunk of the shared-memory sort
+constexpr int kSortMax = 16384;   // longest channel sorted by chunks (longer: radix sort)
+__global__ void k_chunk_sort(const double *E, const int4 *chunks, bool desc, long long base, unsigned long long *tk,
+                             int *ti);
+__global__ void k_chunk_place(const unsigned long long *tk, const int *ti, const int4 *chunks, int nchunks,
+                              long long n, long long base, int *perm);
 __global__ void k_pole_index(const int *off, int ns, long long n, int *seg, int *idx);
 __global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, const int *orb_sh, const int *ch,
                            const int *ip, int *seg_str, int *seg_end, int *seg_cnt, int *bad, int2 *rows, int nJ);

@@ -305,28 +305,36 @@ __global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, co
 }
 
 // Stable sort of each channel's poles by energy (ascending, or descending with desc),
-// one CTA per channel segment [off[s], off[s+1]) of at most P = 2^k poles, P a power of
-// two that fits in shared memory: a bitonic network over (key, index) pairs, the key
-// the order-preserving integer image of the double (sign bit set: all bits flipped,
-// else the sign bit set; the radix sort's mapping, -0 before +0) and the index as tie
-// break, which makes the order stable.  E, off and perm are relative to the range's
-// first pole; perm[g] = global index (base + relative) of the pole sorted to g.
-__global__ void __launch_bounds__(kSortThreads) k_seg_sort(const double *E, const int *off, int P, bool desc,
-                                                           long long base, int *perm) {
-    const int sgi = blockIdx.x;
-    const int g0 = off[sgi], n = off[sgi + 1] - g0;
-    if (n <= 0) return;
-    extern __shared__ unsigned long long skey[];
-    int *sidx = reinterpret_cast<int *>(skey + P);
+// for channels of at most kSortMax poles, in two kernels over chunks of kSortChunk
+// consecutive poles of one channel (the chunk table lists, per chunk, its first pole
+// and length and its channel's first pole and length, relative to the range):
+//   k_chunk_sort   one CTA per chunk sorts (key, index) pairs with a bitonic network
+//                  in shared memory, the key the order-preserving integer image of the
+//                  double (sign bit set: all bits flipped, else the sign bit set; the
+//                  radix sort's mapping, -0 before +0), complemented for descending
+//                  order, the index (the pole's global index) breaking ties;
+//   k_chunk_place  one thread per pole: its rank in the channel is the number of
+//                  pairs below its own in every chunk of the channel (binary searches
+//                  in the sorted chunks), so perm[rank] = its global index.
+// (key, index) pairs are distinct, so the order is the stable sort's.
+__device__ inline unsigned long long sort_key(double e, bool desc) {
+    unsigned long long u = (unsigned long long)__double_as_longlong(e);
+    u = (u >> 63) ? ~u : (u | (1ull << 63));
+    return desc ? ~u : u;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_chunk_sort(const double *E, const int4 *chunks, bool desc,
+                                                             long long base, unsigned long long *tk, int *ti) {
+    const int4 ch = chunks[blockIdx.x];   // first pole, length, channel's first pole, channel's length
+    __shared__ unsigned long long skey[kSortChunk];
+    __shared__ int sidx[kSortChunk];
+    const int n = ch.y;
+    int P = 32;
+    while (P < n) P <<= 1;
     for (int t = threadIdx.x; t < P; t += kSortThreads) {
         unsigned long long k = ~0ull;
         int ix = INT_MAX;
-        if (t < n) {
-            unsigned long long u = (unsigned long long)__double_as_longlong(E[g0 + t]);
-            u = (u >> 63) ? ~u : (u | (1ull << 63));
-            k = desc ? ~u : u;
-            ix = (int)(base + g0 + t);   // global pole index, as the radix sort's values
-        }
+        if (t < n) { k = sort_key(E[ch.x + t], desc); ix = (int)(base + ch.x + t); }
         skey[t] = k;
         sidx[t] = ix;
     }
@@ -343,7 +351,36 @@ __global__ void __launch_bounds__(kSortThreads) k_seg_sort(const double *E, cons
             }
             __syncthreads();
         }
-    for (int t = threadIdx.x; t < n; t += kSortThreads) perm[g0 + t] = sidx[t];
+    for (int t = threadIdx.x; t < n; t += kSortThreads) { tk[ch.x + t] = skey[t]; ti[ch.x + t] = sidx[t]; }
+}
+
+__global__ void k_chunk_place(const unsigned long long *tk, const int *ti, const int4 *chunks, int nchunks,
+                              long long n, long long base, int *perm) {
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    int lo = 0, hi = nchunks - 1;   // the chunk holding g
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (chunks[mid].x <= g) lo = mid; else hi = mid - 1; }
+    const int4 me = chunks[lo];
+    const unsigned long long key = tk[g];
+    const int idx = ti[g];
+    int rank = (int)(g - me.x);   // pairs below it in its own chunk
+    // the channel's other chunks (a channel's chunks are consecutive in the table)
+    int c0 = lo, c1 = lo;
+    while (c0 > 0 && chunks[c0 - 1].z == me.z) --c0;
+    while (c1 + 1 < nchunks && chunks[c1 + 1].z == me.z) ++c1;
+    for (int c = c0; c <= c1; ++c) {
+        if (c == lo) continue;
+        const int4 o = chunks[c];
+        int a = 0, b = o.y;   // first pair of chunk c not below (key, idx)
+        while (a < b) {
+            const int mid = (a + b) >> 1;
+            const unsigned long long km = tk[o.x + mid];
+            const bool below = km < key || (km == key && ti[o.x + mid] < idx);
+            if (below) a = mid + 1; else b = mid;
+        }
+        rank += a;
+    }
+    perm[me.z + rank] = idx;
 }
 
 // Channel of every pole (offsets off[0..ns], off[ns] = n) and the identity order.
