@@ -86,6 +86,7 @@ struct bd_ctx {
     std::vector<Chan> chans;
     std::vector<S2Block> blocks;
     std::vector<long long> blk_fw_first, blk_bk_first;
+    std::vector<int> vchunk_first, vchunk_blk;   // V' gather: 32-coefficient chunks of each block
     long long tot_fw = 0, tot_bk = 0, tot_mfw = 0, tot_mbk = 0, tot_vp = 0;
     // device: bufs follow the propagator, sbufs hold the model space and interaction
     std::vector<DevBuf> bufs, sbufs;
@@ -96,6 +97,7 @@ struct bd_ctx {
     bool static_pending = false;
     int *h_segcheck = nullptr;
     int2 *pending_rows = nullptr;
+    int *pending_prank = nullptr;
     int pending_nJ = 0;
     // freed buffers kept for reuse by size: a repeated upload of a problem of the same
     // shape allocates nothing (cudaMalloc / cudaFree synchronise the device)
@@ -103,6 +105,7 @@ struct bd_ctx {
     size_t pool_bytes = 0;
     DevProblem dp{};
     S2Block *d_blocks = nullptr;
+    int *d_vchunk_first = nullptr, *d_vchunk_blk = nullptr;
     long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr;
     ChanSig *d_cs = nullptr;
     double *d_vp = nullptr;
@@ -123,6 +126,11 @@ struct bd_ctx {
     long long *d_dd_off = nullptr;
     int3 *d_ehf_entries = nullptr;
     int n_ehf_entries = 0;
+    // static self-energy: per entry its first term, per channel its (iv, J2) list
+    std::vector<long long> ehf_term_first;
+    long long *d_ehf_term_first = nullptr;
+    int *d_ehf_cmb = nullptr, *d_ehf_toff = nullptr, *d_ehf_coff = nullptr, *d_ehf_ncomb = nullptr;
+    double *d_ehf_terms = nullptr;
     // Lanczos
     std::vector<long long> lz_v_off[2], lz_out_off[2];
     char *d_lzV = nullptr;
@@ -378,6 +386,17 @@ void build_plan(bd_ctx *c) {
         }
     }
     c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
+    // the V' gather's warps: one per 32 coefficients of a block
+    c->vchunk_first.resize(nb + 1);
+    c->vchunk_blk.clear();
+    int acc = 0;
+    for (size_t b = 0; b < nb; ++b) {
+        c->vchunk_first[b] = acc;
+        const int k = (c->blocks[b].nvp + 31) / 32;
+        c->vchunk_blk.insert(c->vchunk_blk.end(), (size_t)k, (int)b);
+        acc += k;
+    }
+    c->vchunk_first[nb] = acc;
 }
 
 // Lanczos sizes and pivot schedule of one direction (Reduce_SelfEn_Lncz
@@ -434,7 +453,9 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
     if (nb <= 0) return BD_OK;
     const long long vp0 = A.vp_first, nvp = Z.vp_first + Z.nvp - vp0;
     if (nvp > 0) {
-        k_vgather<<<(unsigned)((nb + 7) / 8), 256, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0, nb, ctx->d_vp);
+        const int w0 = ctx->vchunk_first[b0], nw = ctx->vchunk_first[b0 + nb] - w0;
+        k_vgather<<<(unsigned)((nw + 7) / 8), 256, 0, ctx->st>>>(ctx->dp, ctx->d_blocks, ctx->d_vchunk_blk,
+                                                                  ctx->d_vchunk_first, w0, nw, ctx->d_vp);
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
@@ -467,9 +488,16 @@ int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
         if (I == ch_hi - 1) e1 = acc;
     }
     if (e1 > e0) {
-        k_ehf<<<e1 - e0, 256, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries + e0, e1 - e0, ctx->d_dd_off, ctx->d_sighf);
+        const long long nt = ctx->ehf_term_first[e1] - ctx->ehf_term_first[e0];
+        if (nt > 0)
+            k_ehf_terms<<<(unsigned)((nt + 255) / 256), 256, 0, ctx->st>>>(
+                ctx->dp, ctx->d_ehf_entries, ctx->d_ehf_term_first, e0, e1, ctx->d_ehf_cmb, ctx->d_ehf_toff,
+                ctx->d_ehf_coff, ctx->d_ehf_ncomb, ctx->d_ehf_terms);
+        k_ehf_sum<<<e1 - e0, 256, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries, ctx->d_ehf_term_first, e0, ctx->d_ehf_cmb,
+                                                ctx->d_ehf_toff, ctx->d_ehf_coff, ctx->d_ehf_ncomb, ctx->d_ehf_terms,
+                                                ctx->d_dd_off, ctx->d_sighf);
         CU(cudaGetLastError());
-        ctx->launches += 1;
+        ctx->launches += 2;
     }
     return BD_OK;
 }
@@ -871,16 +899,26 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         int2 *rows = nullptr;
         const int nJ = ctx->jmax + 1;
         const size_t nrow = (size_t)ms->norb * ms->norb * nJ;
+        int *prank = nullptr;
         if (vpp->n_me > 0 && nrow * sizeof(int2) <= ((size_t)256 << 20)) {
             if ((rc = dalloc(ctx, &rows, nrow))) return rc;
+            if ((rc = dalloc(ctx, &prank, nrow))) return rc;
             CU(cudaMemsetAsync(rows, 0xff, sizeof(int2) * nrow, ctx->st));
+            CU(cudaMemsetAsync(prank, 0xff, sizeof(int) * nrow, ctx->st));
         }
         if (vpp->n_me > 0) {
             k_segments<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
                 P.iabJ, P.icdJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad, rows, nJ);
             CU(cudaGetLastError());
             ctx->launches += 1;
+            if (prank) {
+                k_pair_rank<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
+                    P.iabJ, P.icdJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, nJ, prank);
+                CU(cudaGetLastError());
+                ctx->launches += 1;
+            }
         }
+        ctx->pending_prank = prank;
         if (!ctx->h_segcheck) CU(cudaMallocHost(&ctx->h_segcheck, sizeof(int) * (kSegTable + 3)));
         CU(cudaMemcpyAsync(ctx->h_segcheck, cnt, sizeof(int) * (kSegTable + 3), cudaMemcpyDeviceToHost, ctx->st));
         P.rows = nullptr;
@@ -903,6 +941,7 @@ int finish_static(bd_ctx *ctx) {
     for (int k = 0; k < kSegTable; ++k)
         if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
     ctx->dp.rows = (ctx->pending_rows && h[kSegTable + 2] == 0) ? ctx->pending_rows : nullptr;
+    ctx->dp.prank = ctx->dp.rows ? ctx->pending_prank : nullptr;
     ctx->dp.nJ = ctx->pending_nJ;
     ctx->static_ok = true;
     return BD_OK;
@@ -944,6 +983,8 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &td, fqh))) return rc; P.fqh = td;
     // plan arrays
     if ((rc = dupload(ctx, &ctx->d_blocks, ctx->blocks))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_vchunk_first, ctx->vchunk_first))) return rc;
+    if ((rc = dupload(ctx, &ctx->d_vchunk_blk, ctx->vchunk_blk))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
     std::vector<ChanSig> cs(ns);
@@ -1026,6 +1067,35 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &ctx->d_dd_off, ctx->chan_dd_off))) return rc;
     if ((rc = dupload(ctx, &ctx->d_ehf_entries, ent))) return rc;
     ctx->n_ehf_entries = (int)ent.size();
+    {   // each channel's (iv, J2) combinations and the offsets of their no[iv]^2 terms
+        std::vector<int> cmb, toff, coff(ns), ncomb(ns);
+        std::vector<long long> terms_of(ns);
+        for (int I = 0; I < ns; ++I) {
+            coff[I] = (int)cmb.size();
+            int acc = 0, c = 0;
+            for (int iv = 0; iv < ns; ++iv) {
+                const int lo = std::abs(ctx->j2[I] - ctx->j2[iv]);
+                const int nJ2 = (ctx->j2[I] + ctx->j2[iv] - lo) / 2 + 1;
+                for (int cc = 0; cc < nJ2; ++cc, ++c) {
+                    cmb.push_back(iv | ((lo + 2 * cc) << 16));
+                    toff.push_back(acc);
+                    acc += ctx->no[iv] * ctx->no[iv];
+                }
+            }
+            cmb.push_back(0);
+            toff.push_back(acc);   // one past the last combination
+            ncomb[I] = c;
+            terms_of[I] = acc;
+        }
+        ctx->ehf_term_first.assign(ent.size() + 1, 0);
+        for (size_t e = 0; e < ent.size(); ++e) ctx->ehf_term_first[e + 1] = ctx->ehf_term_first[e] + terms_of[ent[e].x];
+        if ((rc = dupload(ctx, &ctx->d_ehf_term_first, ctx->ehf_term_first))) return rc;
+        if ((rc = dupload(ctx, &ctx->d_ehf_cmb, cmb))) return rc;
+        if ((rc = dupload(ctx, &ctx->d_ehf_toff, toff))) return rc;
+        if ((rc = dupload(ctx, &ctx->d_ehf_coff, coff))) return rc;
+        if ((rc = dupload(ctx, &ctx->d_ehf_ncomb, ncomb))) return rc;
+        if ((rc = dalloc(ctx, &ctx->d_ehf_terms, (size_t)std::max(1LL, ctx->ehf_term_first.back())))) return rc;
+    }
     // Dyson per-channel small outputs
     if ((rc = dalloc(ctx, &ctx->d_dynq, (size_t)2 * ns))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_dykol, (size_t)3 * ns))) return rc;

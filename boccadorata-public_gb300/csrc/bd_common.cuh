@@ -27,6 +27,11 @@ struct DevProblem {
     // the list is strictly sorted by (iabJ, icdJ) inside every segment (else null).
     const int2 *rows;
     int nJ;
+    // Rank of every pair index (a, b, J) among the elements of the first row of its
+    // segment (-1: not there); with a complete canonical list that row holds every
+    // pair of the segment, so row iab's element for pair icd sits at
+    // rows[iab].x + rank(icd) - rank(iab).  Set with rows.
+    const int *prank;
 };
 
 // One (Jab, ia, ib, ig) block of the Sigma(2) build of one channel.  Its poles
@@ -143,8 +148,17 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
         // of icdJ inside iab's run, when the run lies in this segment.
         if (J >= P.nJ) return 0.0;
         const int a = iab / (kJMult * kABMult), b = (iab / kJMult) % kABMult;
-        const int2 rw = P.rows[((size_t)a * P.norb + b) * P.nJ + J];
+        const size_t pa = ((size_t)a * P.norb + b) * P.nJ + J;
+        const int2 rw = P.rows[pa];
         if (rw.x < lo || rw.y > hi) return 0.0;
+        {   // the position a complete list puts it at; pairs are unique, so a match is it
+            const int c = icd / (kJMult * kABMult), d = (icd / kJMult) % kABMult;
+            const int r1 = P.prank[((size_t)c * P.norb + d) * P.nJ + J], r0 = P.prank[pa];
+            if (r1 >= 0 && r0 >= 0) {
+                const int pos = rw.x + (r1 - r0);
+                if (pos >= rw.x && pos <= rw.y && P.icdJ[pos] == icd) return __dmul_rn(P.V[pos], xph);
+            }
+        }
         int f = rw.x, l = rw.y;
         while (f <= l) {
             const int mid = (f + l) >> 1;

@@ -26,30 +26,32 @@ __device__ inline int find_block(const long long *first, int nblk, long long g) 
 }
 
 // K0: V'[d][alpha][beta][gamma] = sqrt((2Jab+1)/(2j_I+1)) * V^Jab_{ab,dg} (* sqrt2 if g == d),
-// source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One warp per (Jab, ia, ib, ig) block,
-// lanes over its coefficients: the block's descriptor is read once, and the lanes'
-// lookups of one (a, b) row share its first levels.  The prefactor comes with the
+// source/BcDor-Self_energy_ext_Op_c.cpp:396-421.  One warp per 32 consecutive
+// coefficients of a (Jab, ia, ib, ig) block (chunk w of the warp range; chunk_blk maps
+// it to its block, chunk_first[b] is the block's first chunk), a lane per coefficient:
+// every lookup of the launch is in flight at once.  The prefactor comes with the
 // block: FP64 division and square root take tens of FP64 instructions, each a full
 // warp slot on a pipe that issues at 1/64 of the FP32 rate.
-__global__ void k_vgather(DevProblem P, const S2Block *blk, int nblk, double *vp) {
-    const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (w >= nblk) return;
-    const S2Block B = blk[w];
+__global__ void k_vgather(DevProblem P, const S2Block *blk, const int *chunk_blk, const int *chunk_first, int w0,
+                          int nw, double *vp) {
+    const int wl = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (wl >= nw) return;
+    const int w = w0 + wl, b = chunk_blk[w];
+    const S2Block B = blk[b];
+    const int t = (w - chunk_first[b]) * 32 + lane;
+    if (t >= B.nvp) return;
     const int I = B.ch;
     const int na = P.no[B.ia], nb = P.no[B.ib], ng = P.no[B.ig];
-    const double x3 = B.x3;   // IEEE division and square root: the same bits on the host as here
-    for (int t = lane; t < B.nvp; t += 32) {
-        int ngs = t % ng, r = t / ng;
-        int nbs = r % nb; r /= nb;
-        int nas = r % na; int d = r / na;
-        if (B.ia == B.ib && nbs < nas + B.nJab) continue;
-        int iid = P.orb_start[I] + d, iig = P.orb_start[B.ig] + ngs;
-        if (iig == iid && B.nJgd) continue;
-        int iia = P.orb_start[B.ia] + nas, iib = P.orb_start[B.ib] + nbs;
-        double v = __dmul_rn(x3, vget(P, iia, iib, iid, iig, B.Jab));
-        if (iig == iid) v = __dmul_rn(v, kSqr2);
-        vp[B.vp_first + t] = v;
-    }
+    int ngs = t % ng, r = t / ng;
+    int nbs = r % nb; r /= nb;
+    int nas = r % na; int d = r / na;
+    if (B.ia == B.ib && nbs < nas + B.nJab) return;
+    int iid = P.orb_start[I] + d, iig = P.orb_start[B.ig] + ngs;
+    if (iig == iid && B.nJgd) return;
+    int iia = P.orb_start[B.ia] + nas, iib = P.orb_start[B.ib] + nbs;
+    double v = __dmul_rn(B.x3, vget(P, iia, iib, iid, iig, B.Jab));   // IEEE division and sqrt: the host's bits
+    if (iig == iid) v = __dmul_rn(v, kSqr2);
+    vp[B.vp_first + t] = v;
 }
 
 // K1: one thread per pole.  dir 0 = 2p1h (forward), 1 = 2h1p (backward);
@@ -175,82 +177,74 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
     S2[g] = s2;
 }
 
-// Static self-energy: one CTA per (channel, nr >= nc) entry.
+// Static self-energy, per (channel I, nr >= nc) entry:
 //   U = sum_c x1(c) x7(c),   x7(c) = sum_{nm, nv} (x2 x3) x6(nm, nv) V(...)
-// over the (iv, J2) combinations c.  The terms are independent of one another, so the
-// CTA's threads form them in parallel (their interaction lookups overlap); then one
-// thread per c adds its terms in the reference's (nm, nv) order and thread 0 adds the
-// c partials in the reference's (iv, J2) order: every sum keeps the reference's
-// sequence of roundings.  Terms go through shared memory in windows of whole c.
-constexpr int kEhfThreads = 256, kEhfComb = 2048, kEhfTerms = 1536;
-
+// over the (iv, J2) combinations c of channel I (their list and the offset of each
+// one's no[iv]^2 terms inside an entry come from the host, ctab_*).  The terms are
+// independent of one another: k_ehf_terms forms every term of every entry, a thread
+// each, so all interaction lookups are in flight together; k_ehf_sum, a CTA per entry,
+// adds each c's terms in the reference's (nm, nv) order and thread 0 adds the c
+// partials in the reference's (iv, J2) order: every sum keeps the reference's
+// sequence of roundings.
 __device__ inline bool ehf_skip(int iv, int I, int nm, int nv, int nr, int nc, int nJ) {
     return iv == I && nJ != 1 && (nm == nr || nv == nc);
 }
 
-__global__ void __launch_bounds__(kEhfThreads) k_ehf(DevProblem P, const int3 *entries, int nent,
-                                                     const long long *out_off, double *out) {
-    __shared__ double term[kEhfTerms];
+__global__ void k_ehf_terms(DevProblem P, const int3 *entries, const long long *term_first, int e0, int e1,
+                            const int *ctab_cmb, const int *ctab_toff, const int *ctab_off, const int *ncomb,
+                            double *terms) {
+    const long long g = term_first[e0] + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (g >= term_first[e1]) return;
+    int lo = e0, hi = e1 - 1;   // the entry of term g
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (term_first[mid] <= g) lo = mid; else hi = mid - 1; }
+    const int I = entries[lo].x, nr = entries[lo].y, nc = entries[lo].z;
+    const int u = (int)(g - term_first[lo]);
+    const int *toff = ctab_toff + ctab_off[I];
+    int cl = 0, ch = ncomb[I] - 1;   // the combination of term u
+    while (cl < ch) { const int mid = (cl + ch + 1) >> 1; if (toff[mid] <= u) cl = mid; else ch = mid - 1; }
+    const int cm = ctab_cmb[ctab_off[I] + cl], iv = cm & 0xffff, J2 = cm >> 16, no = P.no[iv];
+    const int r = u - toff[cl], nm = r / no, nv = r - nm * no;
+    const int j2I = P.j2[I], NS = P.nspb;
+    const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
+    if (ehf_skip(iv, I, nm, nv, nr, nc, nJ)) return;
+    const double x2 = (iv == I && nm == nr) ? kSqr2 : 1.0;
+    const double x3 = (iv == I && nv == nc) ? kSqr2 : 1.0;
+    const int ia = P.orb_start[I] + nr, im = P.orb_start[iv] + nm;
+    const int ib = P.orb_start[I] + nc, iu = P.orb_start[iv] + nv;
+    double x6 = 0.0;
+    const double *q = P.fqh + (size_t)P.h_start[iv] * NS;
+    for (int kg = 0; kg < P.nh[iv]; ++kg) { x6 = __dadd_rn(x6, __dmul_rn(q[nv], q[nm])); q += NS; }
+    terms[g] = __dmul_rn(__dmul_rn(__dmul_rn(x2, x3), x6), vget(P, ia, im, ib, iu, J2 / 2));
+}
+
+constexpr int kEhfThreads = 256, kEhfComb = 2048;
+
+__global__ void __launch_bounds__(kEhfThreads) k_ehf_sum(DevProblem P, const int3 *entries, const long long *term_first,
+                                                         int e0, const int *ctab_cmb, const int *ctab_toff,
+                                                         const int *ctab_off, const int *ncomb, const double *terms,
+                                                         const long long *out_off, double *out) {
     __shared__ double part[kEhfComb];
-    __shared__ int cmb[kEhfComb];        // iv | J2 << 16
-    __shared__ int toff[kEhfComb + 1];   // first term of each c
-    __shared__ int ncomb;
-    const int e = blockIdx.x;
-    if (e >= nent) return;
+    const int e = e0 + blockIdx.x;
     const int I = entries[e].x, nr = entries[e].y, nc = entries[e].z;
-    const int D = P.no[I], NS = P.nspb, j2I = P.j2[I];
-    if (threadIdx.x == 0) {
-        int c = 0, acc = 0;
-        for (int iv = 0; iv < P.nsubsh; ++iv) {
-            const int nJ2 = (j2I + P.j2[iv] - abs(j2I - P.j2[iv])) / 2 + 1;
-            for (int cc = 0; cc < nJ2; ++cc, ++c) {
-                if (c < kEhfComb) { cmb[c] = iv | ((abs(j2I - P.j2[iv]) + 2 * cc) << 16); toff[c] = acc; }
-                acc += P.no[iv] * P.no[iv];
-            }
-        }
-        if (c <= kEhfComb) toff[c] = acc;
-        ncomb = c;
+    const int D = P.no[I], j2I = P.j2[I], nco = ncomb[I];
+    if (nco > kEhfComb) return;
+    const int *cmb = ctab_cmb + ctab_off[I], *toff = ctab_toff + ctab_off[I];
+    const double *t0 = terms + term_first[e];
+    for (int c = threadIdx.x; c < nco; c += kEhfThreads) {
+        const int iv = cmb[c] & 0xffff, J2 = cmb[c] >> 16, no = P.no[iv];
+        const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
+        const double x1 = __ddiv_rn((double)(J2 + 1), (double)(j2I + 1));
+        double x7 = 0.0;
+        const double *t = t0 + toff[c];
+        for (int nm = 0; nm < no; ++nm)
+            for (int nv = 0; nv < no; ++nv)
+                if (!ehf_skip(iv, I, nm, nv, nr, nc, nJ)) x7 = __dadd_rn(x7, t[nm * no + nv]);
+        part[c] = __dmul_rn(x1, x7);
     }
     __syncthreads();
-    if (ncomb > kEhfComb) return;
-    for (int c0 = 0; c0 < ncomb;) {
-        int c1 = c0 + 1;
-        while (c1 < ncomb && toff[c1 + 1] - toff[c0] <= kEhfTerms) ++c1;
-        const int u0 = toff[c0], nu = toff[c1] - u0;
-        for (int u = threadIdx.x; u < nu; u += kEhfThreads) {
-            int lo = c0, hi = c1 - 1;   // c of term u0 + u
-            while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (toff[mid] <= u0 + u) lo = mid; else hi = mid - 1; }
-            const int iv = cmb[lo] & 0xffff, J2 = cmb[lo] >> 16, no = P.no[iv];
-            const int r = u0 + u - toff[lo], nm = r / no, nv = r - nm * no;
-            const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
-            if (ehf_skip(iv, I, nm, nv, nr, nc, nJ)) continue;
-            const double x2 = (iv == I && nm == nr) ? kSqr2 : 1.0;
-            const double x3 = (iv == I && nv == nc) ? kSqr2 : 1.0;
-            const int ia = P.orb_start[I] + nr, im = P.orb_start[iv] + nm;
-            const int ib = P.orb_start[I] + nc, iu = P.orb_start[iv] + nv;
-            double x6 = 0.0;
-            const double *q = P.fqh + (size_t)P.h_start[iv] * NS;
-            for (int kg = 0; kg < P.nh[iv]; ++kg) { x6 = __dadd_rn(x6, __dmul_rn(q[nv], q[nm])); q += NS; }
-            term[u] = __dmul_rn(__dmul_rn(__dmul_rn(x2, x3), x6), vget(P, ia, im, ib, iu, J2 / 2));
-        }
-        __syncthreads();
-        for (int c = c0 + threadIdx.x; c < c1; c += kEhfThreads) {
-            const int iv = cmb[c] & 0xffff, J2 = cmb[c] >> 16, no = P.no[iv];
-            const int nJ = ((j2I + P.j2[iv] + J2) / 2) % 2;
-            const double x1 = __ddiv_rn((double)(J2 + 1), (double)(j2I + 1));
-            double x7 = 0.0;
-            const double *t = term + (toff[c] - u0);
-            for (int nm = 0; nm < no; ++nm)
-                for (int nv = 0; nv < no; ++nv)
-                    if (!ehf_skip(iv, I, nm, nv, nr, nc, nJ)) x7 = __dadd_rn(x7, t[nm * no + nv]);
-            part[c] = __dmul_rn(x1, x7);
-        }
-        __syncthreads();
-        c0 = c1;
-    }
     if (threadIdx.x == 0) {
         double u = 0.0;
-        for (int c = 0; c < ncomb; ++c) u = __dadd_rn(u, part[c]);
+        for (int c = 0; c < nco; ++c) u = __dadd_rn(u, part[c]);
         double *U = out + out_off[I];
         U[nr * D + nc] = u;
         U[nc * D + nr] = u;
@@ -302,6 +296,23 @@ __global__ void k_segments(const int *iabJ, const int *icdJ, int n, int norb, co
     if (i == 0 || iabJ[i - 1] != iab)
         if (atomicCAS(&rw->x, -1, i) != -1) bad[2] = 1;
     if (i + 1 == n || iabJ[i + 1] != iab) rw->y = i;
+}
+
+// Pair ranks (DevProblem::prank): each element of the first row of its segment
+// records its position in the segment under its pair index icdJ.
+__global__ void k_pair_rank(const int *iabJ, const int *icdJ, int n, int norb, const int *orb_sh, const int *ch,
+                            const int *ip, const int *seg_str, int nJ, int *prank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int why = 0;
+    const int key = interaction_key(iabJ[i], norb, orb_sh, ch, ip, &why);
+    if (key < 0) return;
+    const int s0 = seg_str[key];
+    if (s0 < 0 || iabJ[i] != iabJ[s0]) return;   // not in the segment's first row
+    const int icd = icdJ[i];
+    const int J = icd % kJMult, c = icd / (kJMult * kABMult), d = (icd / kJMult) % kABMult;
+    if (J >= nJ || c >= norb || d >= norb || c < 0 || d < 0) return;
+    prank[((size_t)c * norb + d) * nJ + J] = i - s0;
 }
 
 // Stable sort of each channel's poles by energy (ascending, or descending with desc),
