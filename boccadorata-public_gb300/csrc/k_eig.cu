@@ -20,6 +20,7 @@
 //   k_post    x_k[0:D] = R y_k, Z_k = sum_d x_k[d]^2
 //   k_place   quasiparticle / quasihole split by E_F with both lists by descending W,
 //             Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
+#include <climits>
 #include "bd_common.cuh"
 #include "bd_kernels.h"
 #include "eig_sturm.cuh"
@@ -424,8 +425,13 @@ __global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs,
 }
 
 // ------------------------------------------------------------------ K5
+// Four lanes per position: each sums every fourth row of the block, the quad then
+// combines its partials (the FP64 dependent chains a quarter as long).
 __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first, long long total) {
-    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long g4 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long g = g4 >> 2;   // the quad's position; its lanes share every branch
+    const int sub = (int)(g4 & 3), lane = threadIdx.x & 31;
+    const unsigned qmask = 0xFu << (lane & ~3);
     if (g >= total) return;
     const int lo = job_of(row_first, njobs, g);
     const DyJob J = jobs[lo];
@@ -435,11 +441,17 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
     double x[8];
 #pragma unroll
     for (int dd = 0; dd < 8; ++dd) x[dd] = 0.0;
-    for (int i = b0; i <= b1; ++i) {
+    for (int i = b0 + sub; i <= b1; i += 4) {
         const double y = J.A[(size_t)i * n + k];
 #pragma unroll
         for (int dd = 0; dd < 8; ++dd) if (dd < D) x[dd] += J.R[(size_t)dd * n + i] * y;
     }
+#pragma unroll
+    for (int dd = 0; dd < 8; ++dd) {
+        x[dd] += __shfl_xor_sync(qmask, x[dd], 1);
+        x[dd] += __shfl_xor_sync(qmask, x[dd], 2);
+    }
+    if (sub != 0) return;
     // rows [W, Z, x] staged behind R, by position; k_place orders them
     double z = 0.0;
     for (int dd = 0; dd < D; ++dd) z += x[dd] * x[dd];
@@ -466,50 +478,80 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
     atomicAdd(&nbelow, c);
     __syncthreads();
     const int nqh = nbelow, nqp = n - nbelow;
-    // ascending rank of every staged row (ties by position): rows in tiles of eight per
-    // thread, compared against the energies staged in shared memory 2048 at a time.
-    // The energies are compared as order-preserving 64-bit integer keys (negative
-    // values bit-inverted, others with the sign bit set): FP64 compares would issue on
-    // the FP64 pipe, 1/64 of the integer rate here.
-    constexpr int kChunk = 2048, kPer = 8;
-    __shared__ unsigned long long wbuf[kChunk];
+    // ascending rank of every staged row (ties by position).  The energies are compared
+    // as order-preserving 64-bit integer keys (negative values bit-inverted, others with
+    // the sign bit set): FP64 compares would issue on the FP64 pipe, 1/64 of the
+    // integer rate here.  Up to kPlaceSort rows: a bitonic sort of (key, position) in
+    // shared memory gives every rank; beyond, each row counts the rows below it.
     auto key = [](double x) -> unsigned long long {
         const unsigned long long b = (unsigned long long)__double_as_longlong(x);
         return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
     };
-    const int tile = kPer * blockDim.x;
-    for (int k0 = 0; k0 < n; k0 += tile) {
-        int r[kPer];
-        unsigned long long w[kPer];
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int k = k0 + threadIdx.x + u * blockDim.x;
-            r[u] = 0;
-            w[u] = key((k < n) ? st[(size_t)k * NS] : 0.0);
+    auto put = [&](int k, int rank) {   // quasiparticles descending, then quasiholes descending
+        const int row = (rank >= nqh) ? (n - 1 - rank) : (nqp + (nqh - 1 - rank));
+        for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
+    };
+    constexpr int kPlaceSort = 2048;
+    __shared__ unsigned long long pkey[kPlaceSort];
+    __shared__ int pidx[kPlaceSort];
+    if (n <= kPlaceSort) {
+        int P = 32;
+        while (P < n) P <<= 1;
+        for (int t = threadIdx.x; t < P; t += blockDim.x) {
+            pkey[t] = (t < n) ? key(st[(size_t)t * NS]) : ~0ull;
+            pidx[t] = (t < n) ? t : INT_MAX;
         }
-        for (int q0 = 0; q0 < n; q0 += kChunk) {
-            const int qn = min(kChunk, n - q0);
-            __syncthreads();
-            for (int q = threadIdx.x; q < qn; q += blockDim.x) wbuf[q] = key(st[(size_t)(q0 + q) * NS]);
-            __syncthreads();
+        __syncthreads();
+        for (int kk = 2; kk <= P; kk <<= 1)
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int t = threadIdx.x; t < P; t += blockDim.x) {
+                    const int u = t ^ j;
+                    if (u <= t) continue;
+                    const unsigned long long ka = pkey[t], kb = pkey[u];
+                    const int ia = pidx[t], ib = pidx[u];
+                    const bool gt = (ka > kb) || (ka == kb && ia > ib);
+                    if (((t & kk) == 0) ? gt : !gt) { pkey[t] = kb; pkey[u] = ka; pidx[t] = ib; pidx[u] = ia; }
+                }
+                __syncthreads();
+            }
+        for (int r = threadIdx.x; r < n; r += blockDim.x) put(pidx[r], r);
+    } else {
+        // rows in tiles of eight per thread, compared against the energies staged in
+        // shared memory kPlaceSort at a time
+        constexpr int kPer = 8;
+        unsigned long long *wbuf = pkey;
+        const int tile = kPer * blockDim.x;
+        for (int k0 = 0; k0 < n; k0 += tile) {
+            int r[kPer];
+            unsigned long long w[kPer];
 #pragma unroll
             for (int u = 0; u < kPer; ++u) {
                 const int k = k0 + threadIdx.x + u * blockDim.x;
-                if (k >= n) continue;
-                int c2 = 0;
-                for (int q = 0; q < qn; ++q) {
-                    const unsigned long long wq = wbuf[q];
-                    c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
-                }
-                r[u] += c2;
+                r[u] = 0;
+                w[u] = key((k < n) ? st[(size_t)k * NS] : 0.0);
             }
-        }
+            for (int q0 = 0; q0 < n; q0 += kPlaceSort) {
+                const int qn = min(kPlaceSort, n - q0);
+                __syncthreads();
+                for (int q = threadIdx.x; q < qn; q += blockDim.x) wbuf[q] = key(st[(size_t)(q0 + q) * NS]);
+                __syncthreads();
 #pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int k = k0 + threadIdx.x + u * blockDim.x;
-            if (k >= n) continue;
-            const int row = (r[u] >= nqh) ? (n - 1 - r[u]) : (nqp + (nqh - 1 - r[u]));
-            for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
+                for (int u = 0; u < kPer; ++u) {
+                    const int k = k0 + threadIdx.x + u * blockDim.x;
+                    if (k >= n) continue;
+                    int c2 = 0;
+                    for (int q = 0; q < qn; ++q) {
+                        const unsigned long long wq = wbuf[q];
+                        c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
+                    }
+                    r[u] += c2;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) {
+                const int k = k0 + threadIdx.x + u * blockDim.x;
+                if (k < n) put(k, r[u]);
+            }
         }
     }
     __syncthreads();
@@ -557,7 +599,6 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
                        double *work, const long long *d_work_first, cudaStream_t st) {
     k_qrows<<<njobs, kEigThreads, 0, st>>>(d_jobs, njobs);
     k_bisect_prep<<<njobs, 256, 0, st>>>(d_jobs, njobs, work, d_work_first);
-    const unsigned nb = (unsigned)((total_rows + 127) / 128);
     // four lanes per eigenvalue; a matrix's few hundred eigenvalues spread over many SMs
     k_bisect<<<(unsigned)((total_rows * 4 + kBisectThreads - 1) / kBisectThreads), kBisectThreads, 0, st>>>(
         d_jobs, njobs, d_row_first, total_rows, work, d_work_first);
@@ -570,7 +611,7 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
         k_invit_small<<<dim3(njobs, (kTsMax + kIvThreads - 1) / kIvThreads), kIvThreads, smem, st>>>(d_jobs, njobs);
     }
     k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
-    k_post<<<nb, 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_post<<<(unsigned)((total_rows * 4 + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
     k_place<<<njobs, 256, 0, st>>>(d_jobs, njobs);
     return cudaGetLastError();
 }

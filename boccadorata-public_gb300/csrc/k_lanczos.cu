@@ -598,87 +598,93 @@ constexpr int kGrpThreads = 256;
 // by pivoted elimination (pivots above 1e-12 of the largest diagonal entry).  A warp
 // per group; the D(D+1)/2 entries of G are summed over the lanes.  A one-pole group
 // has rank 1 exactly when a coupling is non-zero (the elimination's second pivot is
-// rounding); it needs no Gram matrix.  The count is written to gE[N + q] (the starts
+// rounding); it needs no Gram matrix, and a warp settles 32 of them at once.  The count is written to gE[N + q] (the starts
 // in gInfo are still read by other warps); the kernel then turns the counts into
 // cumulative counts in gInfo.
 template <int D>
 __device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gInfo, int warp, int lane) {
     constexpr int P = D * (D + 1) / 2;
     const int N = C.N;
+    // one-pole groups: one thread each over the whole CTA; then the larger groups, a
+    // warp each, round robin (they cluster in energy, so windows would unbalance)
+    for (int q = warp * 32 + lane; q < Q; q += kGrpThreads) {
+        const int h0 = gInfo[1 + q];
+        const int mm = ((q + 1 < Q) ? gInfo[2 + q] : N) - h0;
+        if (mm == 1) {
+            bool any = false;
+#pragma unroll
+            for (int a = 0; a < D; ++a) any |= (C.M[(size_t)a * N + h0] != 0.0);
+            gE[N + q] = any ? 0.0 : 1.0;
+        }
+    }
     for (int q = warp; q < Q; q += kGrpThreads / 32) {
-        const int g0 = gInfo[1 + q];
-        const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
-        const int m = g1 - g0;
-        if (m == 1) {
-            if (lane == 0) {
-                bool any = false;
+        {
+            const int g0 = gInfo[1 + q];
+            const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
+            if (g1 - g0 <= 1) continue;
+            const int m = g1 - g0;
+            double G[P];
 #pragma unroll
-                for (int a = 0; a < D; ++a) any |= (C.M[(size_t)a * N + g0] != 0.0);
-                gE[N + q] = any ? 0.0 : 1.0;
-            }
-            continue;
-        }
-        double G[P];
+            for (int u = 0; u < P; ++u) G[u] = 0.0;
+            for (int i = g0 + lane; i < g1; i += 32) {
+                double mv[D];
 #pragma unroll
-        for (int u = 0; u < P; ++u) G[u] = 0.0;
-        for (int i = g0 + lane; i < g1; i += 32) {
-            double mv[D];
-#pragma unroll
-            for (int a = 0; a < D; ++a) mv[a] = C.M[(size_t)a * N + i];
-            int u = 0;
-#pragma unroll
-            for (int a = 0; a < D; ++a)
-#pragma unroll
-                for (int b = 0; b <= a; ++b) G[u++] += mv[a] * mv[b];
-        }
-#pragma unroll
-        for (int u = 0; u < P; ++u)
-            for (int o = 16; o > 0; o >>= 1) G[u] += __shfl_xor_sync(0xffffffffu, G[u], o);
-        if (lane == 0) {
-            double H[D][D];
-            {
+                for (int a = 0; a < D; ++a) mv[a] = C.M[(size_t)a * N + i];
                 int u = 0;
 #pragma unroll
                 for (int a = 0; a < D; ++a)
 #pragma unroll
-                    for (int b = 0; b <= a; ++b) { H[a][b] = G[u]; H[b][a] = G[u]; ++u; }
+                    for (int b = 0; b <= a; ++b) G[u++] += mv[a] * mv[b];
             }
-            double gmax = 0.0;
 #pragma unroll
-            for (int a = 0; a < D; ++a) gmax = fmax(gmax, H[a][a]);
-            int rank = 0;
-            bool used[D];
+            for (int u = 0; u < P; ++u)
+                for (int o = 16; o > 0; o >>= 1) G[u] += __shfl_xor_sync(0xffffffffu, G[u], o);
+            if (lane == 0) {
+                double H[D][D];
+                {
+                    int u = 0;
 #pragma unroll
-            for (int a = 0; a < D; ++a) used[a] = false;
-            for (int st = 0; st < D && gmax > 0.0; ++st) {
-                int pv = -1;
-                double best = 1e-12 * gmax;
+                    for (int a = 0; a < D; ++a)
 #pragma unroll
-                for (int a = 0; a < D; ++a) if (!used[a] && H[a][a] > best) { best = H[a][a]; pv = a; }
-                if (pv < 0) break;
-                used[pv] = true;
-                ++rank;
-                double rowp[D];
-#pragma unroll
-                for (int b = 0; b < D; ++b) rowp[b] = 0.0;
-#pragma unroll
-                for (int a = 0; a < D; ++a)
-                    if (a == pv)
-#pragma unroll
-                        for (int b = 0; b < D; ++b) rowp[b] = H[a][b];
-                const double inv = 1.0 / best;
-#pragma unroll
-                for (int a = 0; a < D; ++a) {
-                    if (used[a]) continue;
-                    double hap = 0.0;
-#pragma unroll
-                    for (int b = 0; b < D; ++b) if (b == pv) hap = H[a][b];
-                    const double f = hap * inv;
-#pragma unroll
-                    for (int b = 0; b < D; ++b) if (!used[b]) H[a][b] -= f * rowp[b];
+                        for (int b = 0; b <= a; ++b) { H[a][b] = G[u]; H[b][a] = G[u]; ++u; }
                 }
+                double gmax = 0.0;
+#pragma unroll
+                for (int a = 0; a < D; ++a) gmax = fmax(gmax, H[a][a]);
+                int rank = 0;
+                bool used[D];
+#pragma unroll
+                for (int a = 0; a < D; ++a) used[a] = false;
+                for (int st = 0; st < D && gmax > 0.0; ++st) {
+                    int pv = -1;
+                    double best = 1e-12 * gmax;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) if (!used[a] && H[a][a] > best) { best = H[a][a]; pv = a; }
+                    if (pv < 0) break;
+                    used[pv] = true;
+                    ++rank;
+                    double rowp[D];
+#pragma unroll
+                    for (int b = 0; b < D; ++b) rowp[b] = 0.0;
+#pragma unroll
+                    for (int a = 0; a < D; ++a)
+                        if (a == pv)
+#pragma unroll
+                            for (int b = 0; b < D; ++b) rowp[b] = H[a][b];
+                    const double inv = 1.0 / best;
+#pragma unroll
+                    for (int a = 0; a < D; ++a) {
+                        if (used[a]) continue;
+                        double hap = 0.0;
+#pragma unroll
+                        for (int b = 0; b < D; ++b) if (b == pv) hap = H[a][b];
+                        const double f = hap * inv;
+#pragma unroll
+                        for (int b = 0; b < D; ++b) if (!used[b]) H[a][b] -= f * rowp[b];
+                    }
+                }
+                gE[N + q] = (double)max(0, m - rank);
             }
-            gE[N + q] = (double)max(0, m - rank);
         }
     }
 }
