@@ -142,7 +142,7 @@ struct bd_ctx {
     long long lzout_total = 0;
     std::vector<long long> lz_int_off[2], lz_piv_off[2], lz_slice_off[2], lz_grp_off[2], lz_slot_off[2];
     char *d_lzslice = nullptr;
-    char *d_lzgrp = nullptr;     // per chain: energy groups (2N doubles, then N + 1 ints)
+    char *d_lzgrp = nullptr;     // per chain: energy groups and their Gram pieces (lz_group_bytes)
     int *d_lzslot = nullptr;     // per chain: vector slot of every row
     LzChain *d_chains = nullptr;
     int lz_two_pass = 0;
@@ -622,8 +622,10 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     // chain descriptors live in a small device array (one slot per chain of the range)
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
     CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
-    CU(launch_lz_groups(d_ch, (int)ch.size(), ctx->st));   // energy groups for the deflated tails
-    ctx->launches += 1;
+    long long gram_cap = 0;
+    for (const LzChain &z : ch) gram_cap += lz_gram_cap(z.N);
+    CU(launch_lz_groups(d_ch, (int)ch.size(), gram_cap, ctx->st));   // energy groups for the deflated tails
+    ctx->launches += 3;
     CU(cudaEventRecord(ctx->ev_lz[0], ctx->st));
     // chains whose slices do not fit next to the scalars keep them in global memory
     const bool gslices = ctx->lz_slices == 2 || (ctx->lz_slices == 0 && lanczos_smem_bytes(Smax, rmax) > kLanczosSmemSliceCap);
@@ -776,7 +778,7 @@ int alloc_lanczos(bd_ctx *ctx) {
             ctx->lz_slice_off[dir][I] = slices;
             if (P.L > 0) slices += lz_slice_bytes(P.N);
             ctx->lz_grp_off[dir][I] = groups;
-            if (P.L > 0) groups += ((long long)16 * P.N + 4 * ((long long)P.N + 1) + 255) / 256 * 256;
+            if (P.L > 0) groups += lz_group_bytes(P.N);
             ctx->lz_slot_off[dir][I] = slots;
             slots += std::max(P.L, 0);
             ctx->lz_int_off[dir][I] = ints;
@@ -1788,10 +1790,10 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     const int ld = lz_ld(N);
     const size_t vbytes = (size_t)P.L * (size_t)ld * (fp32 ? sizeof(float) : sizeof(double));
     // behind the vectors: an FP32 copy of M (FP32 form), the energy groups of the
-    // deflated tails (16 N + 4 (N + 1) bytes) and the row slots (4 L bytes)
+    // deflated tails (lz_group_bytes(N)) and the row slots (4 L bytes)
     const size_t mf_off = kNoallocVectors + (vbytes + 255) / 256 * 256;
     const size_t grp_off = mf_off + (fp32 ? (sizeof(float) * (size_t)D * (size_t)N + 255) / 256 * 256 : 0);
-    const size_t slot_off = grp_off + ((size_t)16 * N + 4 * ((size_t)N + 1) + 255) / 256 * 256;
+    const size_t slot_off = grp_off + (size_t)lz_group_bytes(N);
     const size_t need = slot_off + sizeof(int) * (size_t)P.L - kNoallocVectors;
     if (need > BD_NOALLOC_SCRATCH_BYTES - kNoallocVectors)
         return noalloc_fail(err, err_len, BD_ERR_CAPACITY,
@@ -1835,7 +1837,7 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     if (e == cudaSuccess) e = cudaMemsetAsync(d_rows, 0, row_bytes, st);   // the reference clears the rows
     if (e == cudaSuccess && fp32)
         e = launch_to_float(d_M, reinterpret_cast<float *>(base + mf_off), (long long)D * N, st);
-    if (e == cudaSuccess) e = launch_lz_groups(reinterpret_cast<const LzChain *>(base), 1, st);
+    if (e == cudaSuccess) e = launch_lz_groups(reinterpret_cast<const LzChain *>(base), 1, lz_gram_cap(N), st);
     if (e == cudaSuccess)
         e = launch_lanczos(reinterpret_cast<const LzChain *>(base), 1, S, P.L + 1, fp32, kNoallocCluster, kNoallocEta,
                            false, st);

@@ -87,6 +87,35 @@ struct LzChain {
     int *rowslot;           // [L] vector slot of every row, -1 for a deflated row (written at the end)
 };
 
+// Energy-group scratch of a chain of N poles, behind gE [2N doubles] and gInfo [N + 1
+// ints]: the Gram pieces of the groups of more than kGrpSmall poles (a piece is at most
+// kGrpPiece of a group's poles) -- the piece list {group, first pole, end pole}, every
+// group's first piece, the pieces' partial Gram matrices (up to 36 entries, the lower
+// triangle of 8 x 8) and the number of pieces.
+constexpr int kGrpSmall = 64;
+constexpr int kGrpPiece = 1024;
+constexpr int kGramEntries = 36;
+__host__ __device__ inline long long lz_gram_cap(long long N) { return N / (kGrpSmall + 1) + N / kGrpPiece + 2; }
+struct GrpScratch {
+    int *first;     // [N]   first piece of group q (groups of more than kGrpSmall poles)
+    int4 *list;     // [cap] pieces: group, first pole, end pole
+    double *part;   // [cap][kGramEntries] partial Gram matrices
+    int *count;     // [1]   pieces
+};
+__host__ __device__ inline long long lz_grp_first_off(long long N) { return (16 * N + 4 * (N + 1) + 15) / 16 * 16; }
+__host__ __device__ inline long long lz_grp_list_off(long long N) { return lz_grp_first_off(N) + (4 * N + 15) / 16 * 16; }
+__host__ __device__ inline long long lz_grp_part_off(long long N) { return lz_grp_list_off(N) + 16 * lz_gram_cap(N); }
+__host__ __device__ inline long long lz_grp_count_off(long long N) {
+    return lz_grp_part_off(N) + 8 * (long long)kGramEntries * lz_gram_cap(N);
+}
+// bytes of the whole group scratch, a multiple of 256
+__host__ __device__ inline long long lz_group_bytes(long long N) { return (lz_grp_count_off(N) + 16 + 255) / 256 * 256; }
+__host__ __device__ inline GrpScratch lz_grp_scratch(const double *gE, long long N) {
+    char *g = reinterpret_cast<char *>(const_cast<double *>(gE));
+    return GrpScratch{reinterpret_cast<int *>(g + lz_grp_first_off(N)), reinterpret_cast<int4 *>(g + lz_grp_list_off(N)),
+                      reinterpret_cast<double *>(g + lz_grp_part_off(N)), reinterpret_cast<int *>(g + lz_grp_count_off(N))};
+}
+
 // Global scratch of one chain's slices: enough for any cluster size up to 16 with FP64
 // slices (17 bytes per pole, each CTA's share rounded up to 256 bytes); a multiple of
 // 256 bytes, so consecutive chains' slices stay aligned.

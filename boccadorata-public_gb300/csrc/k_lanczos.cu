@@ -587,26 +587,268 @@ cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStrea
 }  // namespace bd
 
 namespace bd {
-// Energy groups of one chain's sorted poles (a CTA per chain): runs of bit-equal E,
-// and for each the dimension of its eigenvectors of E orthogonal to every coupling,
-// m_q - rank(M_q), M_q the group's rows of M.  The rank comes from the Gram matrix
-// M_q^T M_q by pivoted elimination, pivots above 1e-12 of the largest diagonal.
+// Energy groups of one chain's sorted poles: runs of bit-equal E, and for each the
+// dimension of its eigenvectors of E orthogonal to every coupling, m_q - rank(M_q), M_q
+// the D x m_q couplings of the group's poles.  The rank comes from the Gram matrix
+// G_q = M_q M_q^T by pivoted elimination (pivots above 1e-12 of the largest diagonal
+// entry).  Three launches:
+//   k_lz_gstart  a CTA per chain: the group starts, and the groups of more than
+//                kGrpSmall poles cut into Gram pieces of at most kGrpPiece poles;
+//   k_lz_gram    the pieces' partial Gram matrices, spread over the whole GPU (degenerate
+//                shells give a chain a few groups of thousands of poles, and their FP64
+//                sums on one SM would take tens of microseconds);
+//   k_lz_groups  a CTA per chain: one-pole groups, the small groups (a warp each), the
+//                sums of the pieces, the eliminations and the cumulative counts.
 constexpr int kGrpThreads = 256;
+constexpr int kGstartThreads = 512;
+constexpr int kGramThreads = 128;
+constexpr int kGramCtas = 608;   // four per SM
 
-// Directions of energy group q (poles [g0, g1) of equal E) that no coupling reaches:
-// m - rank(M_q), M_q the D x m couplings, the rank from the Gram matrix G = M_q M_q^T
-// by pivoted elimination (pivots above 1e-12 of the largest diagonal entry).  A warp
-// per group; the D(D+1)/2 entries of G are summed over the lanes.  A one-pole group
-// has rank 1 exactly when a coupling is non-zero (the elimination's second pivot is
-// rounding); it needs no Gram matrix, and a warp settles 32 of them at once.  The count is written to gE[N + q] (the starts
-// in gInfo are still read by other warps); the kernel then turns the counts into
-// cumulative counts in gInfo.
+// Block-wide exclusive scan of one int per thread (T threads, a multiple of 32): returns
+// the thread's exclusive prefix and sets total.  ws holds T / 32 ints.
+template <int T>
+__device__ __forceinline__ int block_excl_scan(int x, int &total, int *ws) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) ws[warp] = v;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < T / 32; ++w) {
+        const int s = ws[w];
+        if (w < warp) off += s;
+        tot += s;
+    }
+    __syncthreads();   // ws is free for the next scan
+    total = tot;
+    return off + v - x;
+}
+
+// Group starts (gInfo[1 + q], with gE[q] = the group's energy, gInfo[0] = the number of
+// groups) and the Gram pieces of the groups of more than kGrpSmall poles.  Each thread
+// flags eight consecutive poles per pass.
+__global__ void __launch_bounds__(kGstartThreads) k_lz_gstart(const LzChain *chains, int nchains) {
+    const int cid = blockIdx.x;
+    if (cid >= nchains) return;
+    const LzChain C = chains[cid];
+    if (!C.gE) return;
+    double *gE = const_cast<double *>(C.gE);
+    int *gInfo = const_cast<int *>(C.gInfo);
+    const GrpScratch S = lz_grp_scratch(C.gE, C.N);
+    const int N = C.N, tid = threadIdx.x;
+    __shared__ int ws[kGstartThreads / 32];
+    int base = 0;
+    for (int b = 0; b < N; b += 8 * kGstartThreads) {
+        const int i0 = b + 8 * tid;
+        double e[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const int i = i0 - 1 + k;
+            e[k] = (i >= 0 && i < N) ? C.E[i] : 0.0;
+        }
+        unsigned fl = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int i = i0 + k;
+            if (i < N && (i == 0 || e[k + 1] != e[k])) fl |= 1u << k;
+        }
+        int tot;
+        int q = base + block_excl_scan<kGstartThreads>(__popc(fl), tot, ws);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (fl >> k & 1u) {
+                gInfo[1 + q] = i0 + k;
+                gE[q] = e[k + 1];
+                ++q;
+            }
+        base += tot;
+    }
+    const int Q = base;
+    __syncthreads();   // the starts are read back below
+    int pbase = 0;
+    for (int b = 0; b < Q; b += kGstartThreads) {
+        const int q = b + tid;
+        int g0 = 0, m = 0, np = 0;
+        if (q < Q) {
+            g0 = gInfo[1 + q];
+            m = ((q + 1 < Q) ? gInfo[2 + q] : N) - g0;
+            np = m > kGrpSmall ? (m + kGrpPiece - 1) / kGrpPiece : 0;
+        }
+        int tot;
+        const int p0 = pbase + block_excl_scan<kGstartThreads>(np, tot, ws);
+        if (q < Q) S.first[q] = p0;
+        for (int k = 0; k < np; ++k)
+            S.list[p0 + k] = make_int4(q, g0 + k * kGrpPiece, min(g0 + m, g0 + (k + 1) * kGrpPiece), 0);
+        pbase += tot;
+    }
+    if (tid == 0) {
+        gInfo[0] = Q;
+        *S.count = pbase;
+    }
+}
+
+// One piece's partial Gram matrix (the lower triangle, D(D+1)/2 entries): each thread
+// sums its poles' products, each warp's 32 partial sums of an entry are added by one
+// lane, and the warps' sums in warp order; the order is fixed, so the sums repeat.
 template <int D>
-__device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gInfo, int warp, int lane) {
+__device__ void gram_piece(const LzChain &C, int4 pc, double *out, double (*red)[kGramEntries][33],
+                           double (*wtot)[kGramEntries]) {
+    constexpr int P = D * (D + 1) / 2;
+    const int N = C.N, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double G[P];
+#pragma unroll
+    for (int u = 0; u < P; ++u) G[u] = 0.0;
+    for (int i = pc.y + tid; i < pc.z; i += kGramThreads) {
+        double mv[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) mv[a] = C.M[(size_t)a * N + i];
+        int u = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b = 0; b <= a; ++b) { G[u] = fma(mv[a], mv[b], G[u]); ++u; }
+    }
+#pragma unroll
+    for (int u = 0; u < P; ++u) red[warp][u][lane] = G[u];
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < (P + 31) / 32; ++h) {
+        const int u = lane + 32 * h;
+        if (u < P) {
+            double s = 0.0;
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) s += red[warp][u][k];
+            wtot[warp][u] = s;
+        }
+    }
+    __syncthreads();
+    if (tid < P) {
+        double s = wtot[0][tid];
+#pragma unroll
+        for (int w = 1; w < kGramThreads / 32; ++w) s += wtot[w][tid];
+        out[tid] = s;
+    }
+    __syncthreads();   // red and wtot are reused by the next piece
+}
+
+// The pieces of all chains, numbered chain by chain, CTA k taking pieces k, k + grid, ...
+__global__ void __launch_bounds__(kGramThreads) k_lz_gram(const LzChain *chains, int nchains) {
+    __shared__ double red[kGramThreads / 32][kGramEntries][33];
+    __shared__ double wtot[kGramThreads / 32][kGramEntries];
+    __shared__ int pre[kGramThreads + 1];
+    __shared__ int ws[kGramThreads / 32];
+    const int G = gridDim.x;
+    int base = 0;
+    for (int c0 = 0; c0 < nchains; c0 += kGramThreads) {
+        const int c = c0 + threadIdx.x, nc = min(kGramThreads, nchains - c0);
+        int cnt = 0;
+        if (c < nchains && chains[c].gE) cnt = *lz_grp_scratch(chains[c].gE, chains[c].N).count;
+        int tot;
+        pre[threadIdx.x] = base + block_excl_scan<kGramThreads>(cnt, tot, ws);
+        __syncthreads();
+        // the first piece w >= base with w = blockIdx.x (mod G)
+        int w = base + (((int)blockIdx.x - base) % G + G) % G;
+        for (; w < base + tot; w += G) {
+            int lo = 0, hi = nc - 1;   // the last chain whose first piece is <= w
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (pre[mid] <= w) lo = mid; else hi = mid - 1;
+            }
+            const LzChain &C = chains[c0 + lo];
+            const GrpScratch S = lz_grp_scratch(C.gE, C.N);
+            const int k = w - pre[lo];
+            const int4 pc = S.list[k];
+            double *out = S.part + (size_t)k * kGramEntries;
+            switch (C.D) {
+                case 1: gram_piece<1>(C, pc, out, red, wtot); break;
+                case 2: gram_piece<2>(C, pc, out, red, wtot); break;
+                case 3: gram_piece<3>(C, pc, out, red, wtot); break;
+                case 4: gram_piece<4>(C, pc, out, red, wtot); break;
+                case 5: gram_piece<5>(C, pc, out, red, wtot); break;
+                case 6: gram_piece<6>(C, pc, out, red, wtot); break;
+                case 7: gram_piece<7>(C, pc, out, red, wtot); break;
+                default: gram_piece<8>(C, pc, out, red, wtot); break;
+            }
+        }
+        base += tot;
+        __syncthreads();   // pre is rewritten for the next chains
+    }
+}
+
+// Rank of a D x D Gram matrix (lower triangle in tri) by pivoted elimination, pivots
+// above 1e-12 of the largest diagonal entry, a warp over the D^2 entries (two a lane, in
+// H, D^2 doubles of shared memory).  The matrix is first scaled by a power of two (exact)
+// that brings the largest diagonal entry into [1, 2), so the pivots' reciprocals come
+// from an FP32 seed and one FP64 Newton step; diagonal entries (never negative before
+// the elimination, and compared only against a positive threshold) are compared as
+// integers, which the FP64-starved SM does on its integer pipe.
+template <int D>
+__device__ int warp_rank(const double *tri, double *H, int lane) {
+    constexpr int DD = D * D;
+    auto tidx = [](int a, int b) { return a >= b ? a * (a + 1) / 2 + b : b * (b + 1) / 2 + a; };
+    const int e1 = lane + 32;
+    const int a0 = lane / D, b0 = lane % D, a1 = e1 / D, b1 = e1 % D;
+    const bool has0 = lane < DD, has1 = e1 < DD;
+    long long gbits = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) gbits = max(gbits, __double_as_longlong(tri[tidx(a, a)]));
+    if (gbits <= 0 || gbits >= 0x7ff0000000000000LL) return 0;   // zero couplings (or not finite)
+    const int ex = (int)(gbits >> 52);                               // biased exponent of the largest entry
+    const double scale = __longlong_as_double((long long)max(1, 2046 - ex) << 52);
+    double h0 = has0 ? tri[tidx(a0, b0)] * scale : 0.0;
+    double h1 = has1 ? tri[tidx(a1, b1)] * scale : 0.0;
+    if (has0) H[lane] = h0;
+    if (has1) H[e1] = h1;
+    const long long thr = __double_as_longlong(1e-12 * (__longlong_as_double(gbits) * scale));
+    __syncwarp();
+    unsigned used = 0;
+    int rank = 0;
+    for (int st = 0; st < D; ++st) {
+        long long best = thr;
+        int pv = -1;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+            const long long v = __double_as_longlong(H[a * D + a]);
+            if (!(used >> a & 1u) && v > best && v < 0x7ff0000000000000LL) { best = v; pv = a; }
+        }
+        if (pv < 0) break;
+        used |= 1u << pv;
+        ++rank;
+        const double p = __longlong_as_double(best);
+        double inv = (double)__frcp_rn((float)p);
+        inv = fma(inv, fma(-p, inv, 1.0), inv);
+        __syncwarp();   // the diagonal is read before any entry changes
+        // Schur complement on the remaining rows and columns; the pivot row and column
+        // are only read
+        if (has0 && !(used >> a0 & 1u) && !(used >> b0 & 1u)) {
+            h0 = fma(-H[a0 * D + pv] * inv, H[pv * D + b0], h0);
+            H[lane] = h0;
+        }
+        if (has1 && !(used >> a1 & 1u) && !(used >> b1 & 1u)) {
+            h1 = fma(-H[a1 * D + pv] * inv, H[pv * D + b1], h1);
+            H[e1] = h1;
+        }
+        __syncwarp();
+    }
+    return rank;
+}
+
+// Directions of group q that no coupling reaches, m - rank(M_q), written to gE[N + q].
+// One-pole groups: rank 1 exactly when a coupling is non-zero (the elimination's second
+// pivot is rounding), one thread each over the whole CTA.  Larger groups a warp each,
+// round robin: up to kGrpSmall poles the Gram entries are summed here (lanes over the
+// entries, one FP64 instruction per pole for all of them, when they fit in a warp),
+// beyond that from the pieces' partial sums in piece order; then warp_rank.
+template <int D>
+__device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gInfo, const GrpScratch &S, int warp,
+                             int lane, double *tri, double *H) {
     constexpr int P = D * (D + 1) / 2;
     const int N = C.N;
-    // one-pole groups: one thread each over the whole CTA; then the larger groups, a
-    // warp each, round robin (they cluster in energy, so windows would unbalance)
     for (int q = warp * 32 + lane; q < Q; q += kGrpThreads) {
         const int h0 = gInfo[1 + q];
         const int mm = ((q + 1 < Q) ? gInfo[2 + q] : N) - h0;
@@ -618,11 +860,30 @@ __device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gIn
         }
     }
     for (int q = warp; q < Q; q += kGrpThreads / 32) {
-        {
-            const int g0 = gInfo[1 + q];
-            const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
-            if (g1 - g0 <= 1) continue;
-            const int m = g1 - g0;
+        const int g0 = gInfo[1 + q];
+        const int g1 = (q + 1 < Q) ? gInfo[2 + q] : N;
+        const int m = g1 - g0;
+        if (m <= 1) continue;
+        if (m > kGrpSmall) {
+            const double *pp = S.part + (size_t)S.first[q] * kGramEntries;
+            const int np = (m + kGrpPiece - 1) / kGrpPiece;
+            double a0 = 0.0, a1 = 0.0;
+            for (int k = 0; k < np; ++k, pp += kGramEntries) {
+                if (lane < P) a0 += pp[lane];
+                if (lane + 32 < P) a1 += pp[lane + 32];
+            }
+            if (lane < P) tri[lane] = a0;
+            if (lane + 32 < P) tri[lane + 32] = a1;
+        } else if (P <= 32) {
+            if (lane < P) {
+                int a = 0, b = lane;
+                while (b > a) { b -= a + 1; ++a; }   // entry (a, b) of the lower triangle
+                const double *ma = C.M + (size_t)a * N, *mb = C.M + (size_t)b * N;
+                double acc = 0.0;
+                for (int i = g0; i < g1; ++i) acc += ma[i] * mb[i];
+                tri[lane] = acc;
+            }
+        } else {
             double G[P];
 #pragma unroll
             for (int u = 0; u < P; ++u) G[u] = 0.0;
@@ -639,53 +900,13 @@ __device__ void group_counts(const LzChain &C, int Q, double *gE, const int *gIn
 #pragma unroll
             for (int u = 0; u < P; ++u)
                 for (int o = 16; o > 0; o >>= 1) G[u] += __shfl_xor_sync(0xffffffffu, G[u], o);
-            if (lane == 0) {
-                double H[D][D];
-                {
-                    int u = 0;
+            if (lane == 0)
 #pragma unroll
-                    for (int a = 0; a < D; ++a)
-#pragma unroll
-                        for (int b = 0; b <= a; ++b) { H[a][b] = G[u]; H[b][a] = G[u]; ++u; }
-                }
-                double gmax = 0.0;
-#pragma unroll
-                for (int a = 0; a < D; ++a) gmax = fmax(gmax, H[a][a]);
-                int rank = 0;
-                bool used[D];
-#pragma unroll
-                for (int a = 0; a < D; ++a) used[a] = false;
-                for (int st = 0; st < D && gmax > 0.0; ++st) {
-                    int pv = -1;
-                    double best = 1e-12 * gmax;
-#pragma unroll
-                    for (int a = 0; a < D; ++a) if (!used[a] && H[a][a] > best) { best = H[a][a]; pv = a; }
-                    if (pv < 0) break;
-                    used[pv] = true;
-                    ++rank;
-                    double rowp[D];
-#pragma unroll
-                    for (int b = 0; b < D; ++b) rowp[b] = 0.0;
-#pragma unroll
-                    for (int a = 0; a < D; ++a)
-                        if (a == pv)
-#pragma unroll
-                            for (int b = 0; b < D; ++b) rowp[b] = H[a][b];
-                    const double inv = 1.0 / best;
-#pragma unroll
-                    for (int a = 0; a < D; ++a) {
-                        if (used[a]) continue;
-                        double hap = 0.0;
-#pragma unroll
-                        for (int b = 0; b < D; ++b) if (b == pv) hap = H[a][b];
-                        const double f = hap * inv;
-#pragma unroll
-                        for (int b = 0; b < D; ++b) if (!used[b]) H[a][b] -= f * rowp[b];
-                    }
-                }
-                gE[N + q] = (double)max(0, m - rank);
-            }
+                for (int u = 0; u < P; ++u) tri[u] = G[u];
         }
+        __syncwarp();
+        const int rank = warp_rank<D>(tri, H, lane);
+        if (lane == 0) gE[N + q] = (double)max(0, m - rank);
     }
 }
 
@@ -696,62 +917,41 @@ __global__ void __launch_bounds__(kGrpThreads) k_lz_groups(const LzChain *chains
     if (!C.gE) return;
     double *gE = const_cast<double *>(C.gE);
     int *gInfo = const_cast<int *>(C.gInfo);
+    const GrpScratch S = lz_grp_scratch(C.gE, C.N);
     const int N = C.N, D = C.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __shared__ int wsum[kGrpThreads / 32];
-    __shared__ int s_base;
-    // group starts by a chunked block scan of the "new energy" flags; gInfo[1 + q] holds
-    // the start of group q until the counts replace it
-    if (tid == 0) s_base = 0;
-    __syncthreads();
-    for (int b = 0; b < N; b += kGrpThreads) {
-        const int i = b + tid;
-        const int f = (i < N) && (i == 0 || C.E[i] != C.E[i - 1]);
-        int x = f;
-        for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
-        if (lane == 31) wsum[warp] = x;
-        __syncthreads();
-        int off = s_base;
-        for (int q = 0; q < warp; ++q) off += wsum[q];
-        if (f) { gInfo[1 + off + x - 1] = i; gE[off + x - 1] = C.E[i]; }
-        __syncthreads();
-        if (tid == kGrpThreads - 1) s_base = off + x;
-        __syncthreads();
-    }
-    const int Q = s_base;
-    // availability per group, a warp per group, with the Gram matrix sized for D
+    __shared__ int ws[kGrpThreads / 32];
+    __shared__ double s_tri[kGrpThreads / 32][kGramEntries];
+    __shared__ double s_h[kGrpThreads / 32][64];
+    const int Q = gInfo[0];
     switch (D) {
-        case 1: group_counts<1>(C, Q, gE, gInfo, warp, lane); break;
-        case 2: group_counts<2>(C, Q, gE, gInfo, warp, lane); break;
-        case 3: group_counts<3>(C, Q, gE, gInfo, warp, lane); break;
-        case 4: group_counts<4>(C, Q, gE, gInfo, warp, lane); break;
-        case 5: group_counts<5>(C, Q, gE, gInfo, warp, lane); break;
-        case 6: group_counts<6>(C, Q, gE, gInfo, warp, lane); break;
-        case 7: group_counts<7>(C, Q, gE, gInfo, warp, lane); break;
-        default: group_counts<8>(C, Q, gE, gInfo, warp, lane); break;
+        case 1: group_counts<1>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 2: group_counts<2>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 3: group_counts<3>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 4: group_counts<4>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 5: group_counts<5>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 6: group_counts<6>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        case 7: group_counts<7>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
+        default: group_counts<8>(C, Q, gE, gInfo, S, warp, lane, s_tri[warp], s_h[warp]); break;
     }
     __syncthreads();
-    // inclusive cumulative counts: gInfo[1 + q] = directions of groups 0..q (a chunked
-    // block scan), so a direction index finds its group by binary search
-    if (tid == 0) s_base = 0;
-    __syncthreads();
+    // inclusive cumulative counts: gInfo[1 + q] = directions of groups 0..q, so a
+    // direction index finds its group by binary search
+    int base = 0;
     for (int b = 0; b < Q; b += kGrpThreads) {
         const int q = b + tid;
-        int x = (q < Q) ? (int)gE[N + q] : 0;
-        for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
-        if (lane == 31) wsum[warp] = x;
-        __syncthreads();
-        int off = s_base;
-        for (int w2 = 0; w2 < warp; ++w2) off += wsum[w2];
-        if (q < Q) gInfo[1 + q] = off + x;
-        __syncthreads();
-        if (tid == kGrpThreads - 1) s_base = off + x;
-        __syncthreads();
+        const int x = (q < Q) ? (int)gE[N + q] : 0;
+        int tot;
+        const int ex = block_excl_scan<kGrpThreads>(x, tot, ws);
+        if (q < Q) gInfo[1 + q] = base + ex + x;
+        base += tot;
     }
-    if (tid == 0) gInfo[0] = Q;
 }
 
-cudaError_t launch_lz_groups(const LzChain *d_chains, int nchains, cudaStream_t st) {
+cudaError_t launch_lz_groups(const LzChain *d_chains, int nchains, long long gram_cap, cudaStream_t st) {
     if (nchains <= 0) return cudaSuccess;
+    k_lz_gstart<<<nchains, kGstartThreads, 0, st>>>(d_chains, nchains);
+    const int grid = (int)(gram_cap < 1 ? 1 : (gram_cap < kGramCtas ? gram_cap : kGramCtas));
+    k_lz_gram<<<grid, kGramThreads, 0, st>>>(d_chains, nchains);
     k_lz_groups<<<nchains, kGrpThreads, 0, st>>>(d_chains, nchains);
     return cudaGetLastError();
 }
