@@ -19,7 +19,10 @@
 #include <limits>
 #include <map>
 #include <thread>
+#include <unistd.h>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -61,6 +64,159 @@ struct Chan {
     int state = ST_NONE;
 };
 
+// Host array in page-locked memory (grown by reallocation, contents not kept), so a
+// cudaMemcpyAsync from it neither blocks the host nor waits for the stream.  It is
+// only regrown while no copy from it is pending.
+template <typename T>
+struct PinnedArray {
+    T *p = nullptr;
+    size_t n = 0, cap = 0;
+    PinnedArray() = default;
+    PinnedArray(const PinnedArray &) = delete;
+    PinnedArray &operator=(const PinnedArray &) = delete;
+    ~PinnedArray() {
+        if (p) cudaFreeHost(p);
+    }
+    bool resize(size_t m) {
+        if (m > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            const size_t c = std::max(m, cap + cap / 2);
+            cap = 0;
+            n = 0;
+            void *q = nullptr;
+            if (cudaMallocHost(&q, sizeof(T) * c) != cudaSuccess) return false;
+            p = static_cast<T *>(q);
+            cap = c;
+        }
+        n = m;
+        return true;
+    }
+    size_t size() const { return n; }
+    T &operator[](size_t i) { return p[i]; }
+    const T &operator[](size_t i) const { return p[i]; }
+};
+
+// Page-locked staging of the small uploads: dupload copies a vector here and sends it
+// with cudaMemcpyAsync, so the host runs on while the interaction is in flight (a copy
+// from pageable memory waits for the stream).  Space is handed out between stream
+// synchronisations and reclaimed after one; a full buffer is set aside (freed at the
+// next reclaim) for a larger one.
+struct HostStage {
+    char *p = nullptr;
+    size_t cap = 0, used = 0;
+    std::vector<char *> retired;
+    HostStage() = default;
+    HostStage(const HostStage &) = delete;
+    HostStage &operator=(const HostStage &) = delete;
+    ~HostStage() {
+        reclaim();
+        if (p) cudaFreeHost(p);
+    }
+    void *take(size_t bytes) {
+        const size_t b = (bytes + 255) / 256 * 256;
+        if (used + b > cap) {
+            if (p) retired.push_back(p);
+            p = nullptr;
+            const size_t c = std::max<size_t>(std::max(b, (size_t)1 << 20), 2 * cap);
+            cap = 0;
+            used = 0;
+            void *q = nullptr;
+            if (cudaMallocHost(&q, c) != cudaSuccess) return nullptr;
+            p = static_cast<char *>(q);
+            cap = c;
+        }
+        void *r = p + used;
+        used += b;
+        return r;
+    }
+    void reclaim() {   // every copy from the stage has completed
+        used = 0;
+        for (char *q : retired) cudaFreeHost(q);
+        retired.clear();
+    }
+};
+
+// A few host threads kept for the plan's per-channel passes (started on first use,
+// joined with the context): run(n, fn) calls fn(i) for every i < n on the workers and
+// the calling thread, and returns when all calls are done.  A forked child has none of
+// the workers and runs the calls itself.
+class HostPool {
+public:
+    ~HostPool() {
+        if (getpid() != pid_) {
+            for (auto &t : th_) t.detach();
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    void run(int n, const std::function<void(int)> &fn) {
+        if (n <= 0) return;
+        if (started_ && getpid() != pid_) {
+            for (int i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        if (!started_) {
+            started_ = true;
+            pid_ = getpid();
+            const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+            const int nw = (int)std::min(hw, 8u) - 1;
+            for (int t = 0; t < nw; ++t) th_.emplace_back([this] { worker(); });
+        }
+        if (th_.empty() || n == 1) {
+            for (int i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            job_ = &fn;
+            n_ = n;
+            next_.store(0);
+            active_ = (int)th_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (int i; (i = next_.fetch_add(1)) < n;) fn(i);
+        std::unique_lock<std::mutex> lk(m_);
+        done_.wait(lk, [this] { return active_ == 0; });
+        job_ = nullptr;
+    }
+
+private:
+    void worker() {
+        unsigned seen = 0;
+        for (;;) {
+            const std::function<void(int)> *job;
+            int n;
+            {
+                std::unique_lock<std::mutex> lk(m_);
+                cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+                if (quit_) return;
+                seen = gen_;
+                job = job_;
+                n = n_;
+            }
+            for (int i; (i = next_.fetch_add(1)) < n;) (*job)(i);
+            std::lock_guard<std::mutex> lk(m_);
+            if (--active_ == 0) done_.notify_one();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    int n_ = 0, active_ = 0;
+    std::atomic<int> next_{0};
+    unsigned gen_ = 0;
+    bool quit_ = false, started_ = false;
+    pid_t pid_ = 0;
+};
+
 }  // namespace
 
 struct bd_ctx {
@@ -84,9 +240,13 @@ struct bd_ctx {
     std::vector<double> piv_vec;
     // plan
     std::vector<Chan> chans;
-    std::vector<S2Block> blocks;
-    std::vector<long long> blk_fw_first, blk_bk_first;
-    std::vector<int> vchunk_first, vchunk_blk;   // V' gather: 32-coefficient chunks of each block
+    PinnedArray<S2Block> blocks;
+    std::vector<std::vector<S2Block>> chan_blocks;   // per channel, before placement (kept for their capacity)
+    std::vector<int> chan_chunks;
+    HostPool pool_threads;
+    PinnedArray<long long> blk_fw_first, blk_bk_first;
+    PinnedArray<int> vchunk_first, vchunk_blk;   // V' gather: 32-coefficient chunks of each block
+    HostStage stage;
     long long tot_fw = 0, tot_bk = 0, tot_mfw = 0, tot_mbk = 0, tot_vp = 0;
     // device: bufs follow the propagator, sbufs hold the model space and interaction
     std::vector<DevBuf> bufs, sbufs;
@@ -222,13 +382,34 @@ template <typename T>
 int dupload(bd_ctx *ctx, T **p, const std::vector<T> &h) {
     int rc = dalloc(ctx, p, h.size());
     if (rc) return rc;
-    if (!h.empty()) CU(cudaMemcpyAsync(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    if (h.empty()) return BD_OK;
+    const size_t bytes = sizeof(T) * h.size();
+    void *st = ctx->stage.take(bytes);
+    if (!st) return fail(ctx, BD_ERR_CUDA, "page-locked staging of %zu bytes", bytes);
+    std::memcpy(st, h.data(), bytes);
+    CU(cudaMemcpyAsync(*p, st, bytes, cudaMemcpyHostToDevice, ctx->st));
+    return BD_OK;
+}
+
+template <typename T>
+int dupload(bd_ctx *ctx, T **p, const PinnedArray<T> &h) {
+    int rc = dalloc(ctx, p, h.size());
+    if (rc) return rc;
+    if (h.size()) CU(cudaMemcpyAsync(*p, h.p, sizeof(T) * h.size(), cudaMemcpyHostToDevice, ctx->st));
+    return BD_OK;
+}
+
+// Waits for the stream; the staging space is free again.
+int sync_stream(bd_ctx *ctx) {
+    CU(cudaStreamSynchronize(ctx->st));
+    ctx->stage.reclaim();
     return BD_OK;
 }
 
 // Buffers of a list go back to the pool (beyond kPoolCap idle bytes: to the driver).
 void release(bd_ctx *ctx, std::vector<DevBuf> &list) {
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    ctx->stage.reclaim();
     for (auto &b : list) {
         if (ctx->pool_bytes + b.bytes <= kPoolCap) {
             ctx->pool.emplace(b.bytes, b.p);
@@ -265,7 +446,7 @@ double seek_efermi(const bd_ctx *c, int I) {
 
 // Block enumeration in the loop order of Build_Dynamic_SlfEn_2ndOrder and the
 // all-poles counts of Count_2p1h_2h1p_poles (source/BcDor-Self_energy_ext_Op_c.cpp:47-111,380-394).
-void build_plan(bd_ctx *c) {
+int build_plan(bd_ctx *c) {
     const int ns = c->nsubsh;
     c->chans.assign(ns, Chan());
     // (ia <= ib) pairs satisfying the Jab triangle, in the reference's (ia, ib) order, kept
@@ -290,9 +471,12 @@ void build_plan(bd_ctx *c) {
     // Blocks of one channel, in the reference's (Jab, ia, ib, ig) order, with offsets
     // relative to the channel (fw_first, bk_first, vp_first); the channels are
     // independent and are enumerated on a few host threads.
-    std::vector<std::vector<S2Block>> cb(ns);
+    c->chan_blocks.resize(ns);
+    c->chan_chunks.assign(ns, 0);
     auto channel = [&](int I) {
-        std::vector<S2Block> &out = cb[I];
+        std::vector<S2Block> &out = c->chan_blocks[I];
+        out.clear();
+        int chunks = 0;
         std::vector<std::vector<int>> gl(nkey), gh(nkey), gp(nkey);
         const int D = c->no[I];
         int nfw = 0, nbk = 0;
@@ -340,6 +524,7 @@ void build_plan(bd_ctx *c) {
                     B.nvp = D * c->no[ia] * c->no[ib] * c->no[ig];
                     B.x3 = x3;
                     nfw += B.nfw; nbk += B.nbk; vp += B.nvp;
+                    chunks += (B.nvp + 31) / 32;
                     out.push_back(B);
                 }
             }
@@ -349,54 +534,50 @@ void build_plan(bd_ctx *c) {
         C.nfw = nfw; C.nbk = nbk; C.nvp = vp;
         C.nblk = (int)out.size();
         C.efermi = seek_efermi(c, I);
+        c->chan_chunks[I] = chunks;
     };
-    {
-        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-        const int nth = (int)std::min<unsigned>(std::min<unsigned>(hw, 8u), (unsigned)ns);
-        std::atomic<int> next(0);
-        auto worker = [&]() { for (int I; (I = next.fetch_add(1)) < ns;) channel(I); };
-        std::vector<std::thread> th;
-        for (int t = 1; t < nth; ++t) th.emplace_back(worker);
-        worker();
-        for (auto &t : th) t.join();
-    }
-    // channel offsets, then the blocks at their global offsets
+    c->pool_threads.run(ns, channel);
+    // channel offsets (blocks, poles, couplings, coefficients and the V' gather's warps,
+    // one per 32 coefficients of a block)
     long long fw = 0, bk = 0, mfw = 0, mbk = 0, vp = 0;
     size_t nb = 0;
+    int nchunk = 0;
+    std::vector<int> chunk_first(ns);
     for (int I = 0; I < ns; ++I) {
         Chan &C = c->chans[I];
         C.fw_off = fw; C.bk_off = bk; C.mfw_off = mfw; C.mbk_off = mbk;
         C.blk_first = (int)nb; C.vp_first = vp;
+        chunk_first[I] = nchunk;
         fw += C.nfw; bk += C.nbk; mfw += (long long)C.nfw * C.D; mbk += (long long)C.nbk * C.D; vp += C.nvp;
-        nb += cb[I].size();
+        nb += c->chan_blocks[I].size();
+        nchunk += c->chan_chunks[I];
     }
-    c->blocks.resize(nb);
-    c->blk_fw_first.resize(nb);
-    c->blk_bk_first.resize(nb);
-    for (int I = 0; I < ns; ++I) {
+    if (!c->blocks.resize(nb) || !c->blk_fw_first.resize(nb) || !c->blk_bk_first.resize(nb) ||
+        !c->vchunk_first.resize(nb + 1) || !c->vchunk_blk.resize((size_t)nchunk))
+        return fail(c, BD_ERR_CUDA, "page-locked plan arrays of %zu blocks", nb);
+    // the blocks at their global offsets, a channel per task
+    c->pool_threads.run(ns, [&](int I) {
         const Chan &C = c->chans[I];
-        for (size_t q = 0; q < cb[I].size(); ++q) {
-            S2Block B = cb[I][q];
+        const std::vector<S2Block> &cb = c->chan_blocks[I];
+        int acc = chunk_first[I];
+        for (size_t q = 0; q < cb.size(); ++q) {
+            S2Block B = cb[q];
             B.fw_first += (int)C.fw_off;
             B.bk_first += (int)C.bk_off;
             B.vp_first += C.vp_first;
-            c->blocks[C.blk_first + q] = B;
-            c->blk_fw_first[C.blk_first + q] = B.fw_first;
-            c->blk_bk_first[C.blk_first + q] = B.bk_first;
+            const size_t b = (size_t)C.blk_first + q;
+            c->blocks[b] = B;
+            c->blk_fw_first[b] = B.fw_first;
+            c->blk_bk_first[b] = B.bk_first;
+            c->vchunk_first[b] = acc;
+            const int k = (B.nvp + 31) / 32;
+            std::fill(c->vchunk_blk.p + acc, c->vchunk_blk.p + acc + k, (int)b);
+            acc += k;
         }
-    }
+    });
+    c->vchunk_first[nb] = nchunk;
     c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
-    // the V' gather's warps: one per 32 coefficients of a block
-    c->vchunk_first.resize(nb + 1);
-    c->vchunk_blk.clear();
-    int acc = 0;
-    for (size_t b = 0; b < nb; ++b) {
-        c->vchunk_first[b] = acc;
-        const int k = (c->blocks[b].nvp + 31) / 32;
-        c->vchunk_blk.insert(c->vchunk_blk.end(), (size_t)k, (int)b);
-        acc += k;
-    }
-    c->vchunk_first[nb] = acc;
+    return BD_OK;
 }
 
 // Lanczos sizes and pivot schedule of one direction (Reduce_SelfEn_Lncz
@@ -830,7 +1011,7 @@ int plan_pivots(bd_ctx *ctx) {
     }
     int rc = alloc_lanczos(ctx);
     if (rc) return rc;
-    CU(cudaStreamSynchronize(ctx->st));
+    if ((rc = sync_stream(ctx))) return rc;
     ctx->have_pivots = true;
     return BD_OK;
 }
@@ -968,9 +1149,8 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
     std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
     std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
-    build_plan(ctx);
-    if (int rc0 = finish_static(ctx)) { ctx->static_ok = false; return rc0; }
     int rc;
+    if ((rc = build_plan(ctx))) return rc;
     DevProblem &P = ctx->dp;
     P.nspb = ctx->nspb;
     int *t;
@@ -1108,7 +1288,9 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dalloc(ctx, &ctx->d_work_first, (size_t)ns))) return rc;
     ctx->dy_sol_off.assign(ns, 0);
     ctx->res_nq.assign(2 * ns, 0);
-    CU(cudaStreamSynchronize(ctx->st));
+    // everything above was queued behind the interaction's transfer; its checks now
+    if (int rc0 = finish_static(ctx)) { ctx->static_ok = false; return rc0; }
+    if ((rc = sync_stream(ctx))) return rc;
     ctx->uploaded = true;
     if (ctx->have_pivots) {
         ctx->have_pivots = false;
