@@ -224,6 +224,11 @@ struct bd_ctx {
     cudaStream_t st = nullptr;
     cudaEvent_t ev[6] = {};
     cudaEvent_t ev_lz[2] = {};
+    // the interaction's matrix elements go over on a second stream, after the index
+    // lists, so the segment scan and the plan's uploads overlap their transfer
+    cudaStream_t st_aux = nullptr;
+    cudaEvent_t ev_up[2] = {};
+    bool v_pending = false;
     bool lz_timed = false;
     double lz_kernel_ms = 0.0;
     long long launches = 0;   // kernels of this library launched since creation
@@ -399,6 +404,14 @@ int dupload(bd_ctx *ctx, T **p, const PinnedArray<T> &h) {
     return BD_OK;
 }
 
+// The main stream waits for the matrix elements' transfer.
+int join_interaction(bd_ctx *ctx) {
+    if (!ctx->v_pending) return BD_OK;
+    ctx->v_pending = false;
+    CU(cudaStreamWaitEvent(ctx->st, ctx->ev_up[1], 0));
+    return BD_OK;
+}
+
 // Waits for the stream; the staging space is free again.
 int sync_stream(bd_ctx *ctx) {
     CU(cudaStreamSynchronize(ctx->st));
@@ -408,6 +421,8 @@ int sync_stream(bd_ctx *ctx) {
 
 // Buffers of a list go back to the pool (beyond kPoolCap idle bytes: to the driver).
 void release(bd_ctx *ctx, std::vector<DevBuf> &list) {
+    if (ctx->st_aux) cudaStreamSynchronize(ctx->st_aux);
+    ctx->v_pending = false;
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     ctx->stage.reclaim();
     for (auto &b : list) {
@@ -1064,7 +1079,11 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         if (vpp->n_me > 0) {
             CU(cudaMemcpyAsync(a, vpp->iabJ, sizeof(int) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
             CU(cudaMemcpyAsync(b, vpp->icdJ, sizeof(int) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
-            CU(cudaMemcpyAsync(v, vpp->V, sizeof(double) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st));
+            CU(cudaEventRecord(ctx->ev_up[0], ctx->st));
+            CU(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_up[0], 0));
+            CU(cudaMemcpyAsync(v, vpp->V, sizeof(double) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st_aux));
+            CU(cudaEventRecord(ctx->ev_up[1], ctx->st_aux));
+            ctx->v_pending = true;
         }
         P.iabJ = a; P.icdJ = b; P.V = v;
     }
@@ -1116,6 +1135,7 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
 int finish_static(bd_ctx *ctx) {
     if (!ctx->static_pending) return BD_OK;
     ctx->static_pending = false;
+    if (int rc = join_interaction(ctx)) return rc;
     CU(cudaStreamSynchronize(ctx->st));
     const int *h = ctx->h_segcheck;
     if (h[kSegTable] != INT_MAX)
@@ -1319,6 +1339,11 @@ int bd_create(bd_ctx **out, int device) {
     }
     for (auto &e : ctx->ev) cudaEventCreate(&e);
     for (auto &e : ctx->ev_lz) cudaEventCreate(&e);
+    for (auto &e : ctx->ev_up) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (cudaStreamCreateWithFlags(&ctx->st_aux, cudaStreamNonBlocking) != cudaSuccess) {
+        bd_destroy(ctx);
+        return BD_ERR_CUDA;
+    }
     *out = ctx;
     return BD_OK;
 }
@@ -1336,7 +1361,9 @@ void bd_destroy(bd_ctx *ctx) {
     if (ctx->d_dywork) cudaFree(ctx->d_dywork);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
     for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->ev_up) if (e) cudaEventDestroy(e);
     if (ctx->h_segcheck) cudaFreeHost(ctx->h_segcheck);
+    if (ctx->st_aux) cudaStreamDestroy(ctx->st_aux);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -1353,7 +1380,12 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     free_static(ctx);
     ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false; ctx->static_ok = false;
     int rc = upload_static(ctx, ms, vpp);
-    if (rc) { ctx->static_pending = false; cudaStreamSynchronize(ctx->st); return rc; }
+    if (rc) {
+        ctx->static_pending = false;
+        join_interaction(ctx);
+        cudaStreamSynchronize(ctx->st);
+        return rc;
+    }
     ctx->static_ok = true;   // for upload_propagator; finish_static confirms it or fails
     // the propagator's host plan runs while the interaction is in flight
     rc = upload_propagator(ctx, prop);
