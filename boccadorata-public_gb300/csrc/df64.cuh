@@ -104,9 +104,10 @@ DF_HD df fma(df a, df b, df c) {
     return renorm(s, f);
 }
 
-// 1/sqrt(x), x > 0 in the FP32 range: the FP32 seed and two Newton steps
-// y <- y + y (1 - x y^2) / 2 in double-float (the relative error squares each step)
-DF_HD df rsqrt(df x) {
+// 1/sqrt(x), x > 0 in the FP32 range: the FP32 seed and `its` Newton steps
+// y <- y + y (1 - x y^2) / 2 in double-float (the relative error squares each step:
+// one step from a seed within 2 ulp leaves about 2^-43, two reach double-float rounding)
+DF_HD df rsqrt(df x, int its = 2) {
 #if defined(__CUDA_ARCH__)
     const float y0 = rsqrtf(x.h);
 #else
@@ -114,7 +115,7 @@ DF_HD df rsqrt(df x) {
 #endif
     df y{y0, 0.0f};
     const df half{0.5f, 0.0f};
-    for (int it = 0; it < 2; ++it) {
+    for (int it = 0; it < its; ++it) {
         const df t = mul(x, mul(y, y));              // x y^2
         const df c = fma(neg(half), t, half);         // (1 - x y^2) / 2
         y = fma(y, c, y);
@@ -122,11 +123,11 @@ DF_HD df rsqrt(df x) {
     return y;
 }
 
-// 1/d, d in the FP32 range: the FP32 seed and two Newton steps r <- r + r (1 - d r)
-DF_HD df rcp(df d) {
+// 1/d, d in the FP32 range: the FP32 seed and `its` Newton steps r <- r + r (1 - d r)
+DF_HD df rcp(df d, int its = 2) {
     df r{1.0f / d.h, 0.0f};
     const df one{1.0f, 0.0f};
-    for (int it = 0; it < 2; ++it) r = fma(r, fma(neg(d), r, one), r);
+    for (int it = 0; it < its; ++it) r = fma(r, fma(neg(d), r, one), r);
     return r;
 }
 

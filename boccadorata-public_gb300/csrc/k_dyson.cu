@@ -365,9 +365,13 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
 //     position: a warp takes rows i and m-1-i together, m+1 elements, so the
 //     triangle's rows balance;
 //   - p = A v over full rows (contiguous, the same trip count in every lane), each row
-//     split in four parts of q over four threads, no atomics and no shuffles;
-//   - sums (column norm, R x, p.v) are single-warp reductions.
-// Step k (trailing order m = n-k-1) has six barriers.
+//     split in four parts of q over four threads, no atomics and no shuffles, with v
+//     read as the scaled column in place (so no barrier between the reflector and it);
+//   - sums (column norm, R x, p.v) are single-warp reductions, and the warp that forms
+//     p.v also forms w = p - K v.
+// Step k (trailing order m = n-k-1) has four barriers.  The reflector's square root and
+// reciprocal take one Newton step each from their FP32 seeds (about 2^-43, far inside
+// the eigenvalue tolerance).
 constexpr int kTsThreads = 256;
 constexpr int kTsParts = 4;   // threads per row of the symmetric product
 
@@ -391,7 +395,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     df *ph = v + n;                          // [kTsParts][n] parts of A v
     df *w = ph + kTsParts * n;               // [n]
     df *R = w + n;                           // [D][n]
-    __shared__ df s_dfs[2][4];               // tau, scal, K, beta of the step, by parity
+    __shared__ df s_dfs[2][4];               // tau, scal, -, beta of the step, by parity
     __shared__ int s_flag[2];                // the column has a reflector, by parity
     __shared__ df s_rx[8];                   // R_d[b0+1:] . x[1:]
     __shared__ df s_coef[8];                 // tau s_d, s_d = R_d[b0:] . v
@@ -429,10 +433,10 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
                 if (nz) {
                     const df x2 = dfm::fma(al, al, s2);
                     if (x2.h > 1e-30f && x2.h < 1e30f) {
-                        const df r = dfm::rsqrt(x2), nx = dfm::mul(x2, r);
+                        const df r = dfm::rsqrt(x2, 1), nx = dfm::mul(x2, r);
                         beta = ng ? nx : dfm::neg(nx);
                         tau = dfm::fma(aa, r, df{1.0f, 0.0f});
-                        scal = dfm::rcp(dfm::add(aa, nx));
+                        scal = dfm::rcp(dfm::add(aa, nx), 1);
                         if (ng) scal = dfm::neg(scal);
                     } else {
                         const double a = dfm::to_double(al), x2d = dfm::to_double(x2);
@@ -461,32 +465,29 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         }
         if (!s_flag[k & 1]) continue;        // column already reduced: H_k = I
         const df taud = sdf[0], scald = sdf[1];
-        // 2. v, and s_d = R_d[b0:] . v (the R update's coefficient tau s_d)
-        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(col[(size_t)(b0 + t) * ld], scald);
-        if (tid < D) s_coef[tid] = dfm::mul(taud, dfm::fma(scald, s_rx[tid], R[(size_t)tid * n + b0]));
-        __syncthreads();
-        // 3. parts of A v (trailing block, local indices), and R <- R H_k.  Four parts
-        //    per row keep all eight warps busy.
+        // 2. parts of A v (trailing block, local indices) with v = (1, scal x[1:]), the
+        //    column read in place, four parts per row so all eight warps are busy; v
+        //    itself, and the R update's coefficients tau s_d, s_d = R_d[b0:] . v
         for (int u = tid; u < kTsParts * m; u += kTsThreads) {
             const int i = u / kTsParts, h = u - i * kTsParts;
             const int q0 = (int)(((long long)m * h) / kTsParts), q1 = (int)(((long long)m * (h + 1)) / kTsParts);
             const df *Ai = A + (size_t)(b0 + i) * ld + b0;   // the full row (the update mirrors)
             df acc0 = zero, acc1 = zero;   // two chains
-            int q = q0;
+            int q = q0 > 0 ? q0 : 1;
             for (; q + 1 < q1; q += 2) {
-                acc0 = dfm::fma(Ai[q], v[q], acc0);
-                acc1 = dfm::fma(Ai[q + 1], v[q + 1], acc1);
+                acc0 = dfm::fma(Ai[q], col[(size_t)(b0 + q) * ld], acc0);
+                acc1 = dfm::fma(Ai[q + 1], col[(size_t)(b0 + q + 1) * ld], acc1);
             }
-            if (q < q1) acc0 = dfm::fma(Ai[q], v[q], acc0);
-            ph[h * n + i] = dfm::add(acc0, acc1);
+            if (q < q1) acc0 = dfm::fma(Ai[q], col[(size_t)(b0 + q) * ld], acc0);
+            df r = dfm::mul(scald, dfm::add(acc0, acc1));
+            if (q0 == 0 && q1 > 0) r = dfm::add(Ai[0], r);   // the part holding v_0 = 1
+            ph[h * n + i] = r;
         }
-        for (int u = tid; u < D * m; u += kTsThreads) {
-            const int d = u / m, t = u - d * m;
-            df &r = R[(size_t)d * n + b0 + t];
-            r = dfm::fma(dfm::neg(s_coef[d]), v[t], r);
-        }
+        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(col[(size_t)(b0 + t) * ld], scald);
+        if (tid < D) s_coef[tid] = dfm::mul(taud, dfm::fma(scald, s_rx[tid], R[(size_t)tid * n + b0]));
         __syncthreads();
-        // 4. p = tau A v; K = (tau / 2) p . v
+        // 3. warp 0: p = tau A v, K = (tau / 2) p . v and w = p - K v (each lane its own
+        //    entries); the other warps: R <- R H_k
         if (warp == 0) {
             df s = zero;
             for (int t = lane; t < m; t += 32) {
@@ -498,16 +499,17 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
                 s = dfm::fma(pt, v[t], s);
             }
             s = dfm::warp_sum(s);
-            if (lane == 0) sdf[2] = dfm::mul(dfm::mul(df{0.5f, 0.0f}, taud), s);
+            const df nK = dfm::neg(dfm::mul(dfm::mul(df{0.5f, 0.0f}, taud), s));
+            for (int t = lane; t < m; t += 32) w[t] = dfm::fma(nK, v[t], w[t]);
+        } else {
+            for (int u = tid - 32; u < D * m; u += kTsThreads - 32) {
+                const int d = u / m, t = u - d * m;
+                df &r = R[(size_t)d * n + b0 + t];
+                r = dfm::fma(dfm::neg(s_coef[d]), v[t], r);
+            }
         }
         __syncthreads();
-        // 5. w = p - K v
-        {
-            const df nK = dfm::neg(sdf[2]);
-            for (int t = tid; t < m; t += kTsThreads) w[t] = dfm::fma(nK, v[t], w[t]);
-        }
-        __syncthreads();
-        // 6. A -= v w^T + w v^T on the trailing lower triangle, rows i and m-1-i per warp
+        // 4. A -= v w^T + w v^T on the trailing lower triangle, rows i and m-1-i per warp
         for (int i1 = warp; i1 < (m + 1) / 2; i1 += kTsThreads / 32) {
             const int i2 = m - 1 - i1;
             const int len = (i1 == i2) ? (i1 + 1) : (m + 1);

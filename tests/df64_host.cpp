@@ -20,7 +20,10 @@ extern "C" double bd_df64_sumsq(const double *a, int n) {
     return to_double(s);
 }
 
-// op 0: 1/sqrt(a), 1: 1/a, on the double-float images of the inputs
+// op 0: 1/sqrt(a), 1: 1/a, on the double-float images of the inputs; ops 2, 3: the
+// same with one Newton step
 extern "C" void bd_df64_fun(int op, const double *a, int n, double *out) {
-    for (int i = 0; i < n; ++i) out[i] = to_double(op == 0 ? rsqrt(from_double(a[i])) : rcp(from_double(a[i])));
+    const int its = op < 2 ? 2 : 1;
+    for (int i = 0; i < n; ++i)
+        out[i] = to_double(op % 2 == 0 ? rsqrt(from_double(a[i]), its) : rcp(from_double(a[i]), its));
 }
