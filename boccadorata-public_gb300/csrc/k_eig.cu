@@ -300,7 +300,10 @@ __device__ void invit_vector(const DyJob &J, int k, int b0, int b1, S &a) {
     }
     for (int i = b0; i <= b1; ++i)
         a.y(i) = 0.5 + (double)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0;
-    for (int it = 0; it < 3; ++it) {
+    // two sweeps: the shift is within 1e-13 |T_b| of W_k and eigenvalues of a block
+    // closer than 1e-6 |T_b| are clustered (orthonormalised together), so each sweep
+    // scales the other eigenvectors' share by at most 1e-7 against this one's
+    for (int it = 0; it < 2; ++it) {
         for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges
             double bi = a.y(i), bi1 = a.y(i + 1);
             const double f = a.ll(i);
