@@ -41,7 +41,6 @@ struct DevBuf {
 };
 
 enum ChanState { ST_NONE = 0, ST_SIGMA = 1, ST_LANCZOS = 2 };
-constexpr int kDysonKernels = 9;   // assemble, tridiag, qrows, bisect_prep, bisect, invit, cluster_orth, post, place
 
 struct ChainPlan {     // one Lanczos direction of one channel
     int N = 0, L = 0, n_used = 0, nden_out = 0, n_pvt = 0;
@@ -113,8 +112,12 @@ struct HostStage {
         reclaim();
         if (p) cudaFreeHost(p);
     }
-    void *take(size_t bytes) {
+    void *take(size_t bytes, cudaStream_t st) {
         const size_t b = (bytes + 255) / 256 * 256;
+        if (used + b > cap && cap >= ((size_t)64 << 20)) {   // a long run without a synchronisation
+            cudaStreamSynchronize(st);
+            reclaim();
+        }
         if (used + b > cap) {
             if (p) retired.push_back(p);
             p = nullptr;
@@ -389,7 +392,7 @@ int dupload(bd_ctx *ctx, T **p, const std::vector<T> &h) {
     if (rc) return rc;
     if (h.empty()) return BD_OK;
     const size_t bytes = sizeof(T) * h.size();
-    void *st = ctx->stage.take(bytes);
+    void *st = ctx->stage.take(bytes, ctx->st);
     if (!st) return fail(ctx, BD_ERR_CUDA, "page-locked staging of %zu bytes", bytes);
     std::memcpy(st, h.data(), bytes);
     CU(cudaMemcpyAsync(*p, st, bytes, cudaMemcpyHostToDevice, ctx->st));
@@ -730,16 +733,14 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
             int4 *dch = dir == 0 ? ctx->d_chunks_fw : ctx->d_chunks_bk;
             if ((long long)chunks.size() > (dir == 0 ? ctx->chunk_cap_fw : ctx->chunk_cap_bk))
                 return fail(ctx, BD_ERR_STATE, "sort chunk table overflow");
-            e = cudaMemcpyAsync(dch, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, ctx->st);
+            CU(cudaMemcpyAsync(dch, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, ctx->st));
             unsigned long long *tk = reinterpret_cast<unsigned long long *>(ctx->d_keys_tmp);
             int *ti = dir == 0 ? ctx->d_sorti_fw : ctx->d_sorti_bk;
-            if (e == cudaSuccess) {
-                k_chunk_sort<<<(unsigned)chunks.size(), kSortThreads, 0, ctx->st>>>(E + n0, dch, dir == 1, n0, tk, ti);
-                k_chunk_place<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(tk, ti, dch, (int)chunks.size(), n, n0,
-                                                                              perm + n0);
-                e = cudaGetLastError();
-                ctx->launches += 1;
-            }
+            k_chunk_sort<<<(unsigned)chunks.size(), kSortThreads, 0, ctx->st>>>(E + n0, dch, dir == 1, n0, tk, ti);
+            k_chunk_place<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(tk, ti, dch, (int)chunks.size(), n, n0,
+                                                                          perm + n0);
+            e = cudaGetLastError();
+            ctx->launches += 2;
         } else if (dir == 0)
             e = cub::DeviceSegmentedRadixSort::SortPairs(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp, idx + n0,
                                                          perm + n0, (int)n, nseg, d_off, d_off + 1, 0, 64, ctx->st);
@@ -942,7 +943,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
                        cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(ctx->d_jobs + ch_lo, (int)jobs.size(), ctx->d_row_first + ch_lo, rows, nmax, Dmax,
                     dy_cluster_for(ctx, ch_hi - ch_lo), ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
-    ctx->launches += kDysonKernels;
+    ctx->launches += dyson_launch_count(nmax);
     return BD_OK;
 }
 
@@ -1630,7 +1631,7 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     CU(cudaMemcpyAsync(dwf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(cudaMemcpyAsync(drf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(dj, 1, drf, n, n, D, dy_cluster_for(ctx, 1), dwork, dwf, ctx->st));
-    ctx->launches += kDysonKernels;
+    ctx->launches += dyson_launch_count(n);
     int nq[2] = {0, 0};
     double kol[3];
     CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof nq, cudaMemcpyDeviceToHost, ctx->st));
@@ -1729,7 +1730,7 @@ int bd_run_all(bd_ctx *ctx, int flags) {
 int bd_sync(bd_ctx *ctx) {
     if (!ctx) return BD_ERR_ARG;
     CU(cudaSetDevice(ctx->device));
-    CU(cudaStreamSynchronize(ctx->st));
+    if (int rc = sync_stream(ctx)) return rc;
     if (ctx->results_valid) {
         std::vector<int> st(ctx->nsubsh, 0);
         CU(cudaMemcpy(ctx->res_nq.data(), ctx->d_dynq, sizeof(int) * 2 * ctx->nsubsh, cudaMemcpyDeviceToHost));

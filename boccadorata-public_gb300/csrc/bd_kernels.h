@@ -40,6 +40,7 @@ constexpr size_t kLanczosSmemSliceCap = 100 * 1024;   // above this the slices g
 cudaError_t launch_to_float(const double *in, float *out, long long n, cudaStream_t st);
 cudaError_t launch_lz_groups(const LzChain *d_chains, int nchains, long long gram_cap, cudaStream_t st);
 
+int dyson_launch_count(int nmax);
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                          int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st);
 cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,

@@ -555,6 +555,10 @@ size_t tridiag_smem_bytes(int nmax, int cluster) {
     return sizeof(double) * ((size_t)(3 + tridiag_npriv(nmax, cluster)) * nmax + (size_t)(nmax / cluster + 1) + 32);
 }
 
+// Kernels launch_dyson starts for matrices of order up to nmax: deflate, assemble, the
+// small-matrix reduction (and the cluster one beyond kTsMax), then launch_eig's eight.
+int dyson_launch_count(int nmax) { return (nmax <= kTsMax ? 3 : 4) + 8; }
+
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                          int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st) {
     if (njobs <= 0) return cudaSuccess;
