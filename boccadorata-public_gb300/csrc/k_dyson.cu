@@ -365,15 +365,15 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
 //     position: a warp takes rows i and m-1-i together, m+1 elements, so the
 //     triangle's rows balance;
 //   - p = A v over full rows (contiguous, the same trip count in every lane), each row
-//     split in four parts of q over four threads, no atomics and no shuffles, with v
+//     split in eight parts of q over eight threads, no atomics and no shuffles, with v
 //     read as the scaled column in place (so no barrier between the reflector and it);
 //   - sums (column norm, R x, p.v) are single-warp reductions, and the warp that forms
 //     p.v also forms w = p - K v.
 // Step k (trailing order m = n-k-1) has four barriers.  The reflector's square root and
 // reciprocal take one Newton step each from their FP32 seeds (about 2^-43, far inside
 // the eigenvalue tolerance).
-constexpr int kTsThreads = 256;
-constexpr int kTsParts = 4;   // threads per row of the symmetric product
+constexpr int kTsThreads = 512;
+constexpr int kTsParts = 8;   // threads per row of the symmetric product
 
 __device__ inline double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         if (!s_flag[k & 1]) continue;        // column already reduced: H_k = I
         const df taud = sdf[0], scald = sdf[1];
         // 2. parts of A v (trailing block, local indices) with v = (1, scal x[1:]), the
-        //    column read in place, four parts per row so all eight warps are busy; v
+        //    column read in place, eight parts per row so all sixteen warps are busy; v
         //    itself, and the R update's coefficients tau s_d, s_d = R_d[b0:] . v
         for (int u = tid; u < kTsParts * m; u += kTsThreads) {
             const int i = u / kTsParts, h = u - i * kTsParts;
