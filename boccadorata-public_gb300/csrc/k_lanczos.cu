@@ -43,6 +43,7 @@
 // order, so all CTAs hold bit-identical totals and take identical branches.
 #include <climits>
 #include <cooperative_groups.h>
+#include "df64.cuh"
 #include "bd_common.cuh"
 #include "bd_kernels.h"
 
@@ -61,11 +62,42 @@ __device__ inline T warp_sum_ct(T v) {
     return v;
 }
 
-// Fixed pairwise sums: three (four) dependent FP64 adds instead of seven (fifteen).
-__device__ inline double tree_sum8(const double *x) {
-    return ((x[0] + x[1]) + (x[2] + x[3])) + ((x[4] + x[5]) + (x[6] + x[7]));
+// Sums across warps and CTAs.  FP64 vectors: FP64 adds.  FP32 vectors: the partials
+// are FP32 values, summed in double-float (df64.cuh) on the FP32 pipe -- an FP64 add
+// holds the SM sub-partition's FP64 unit for about 64 cycles, and the trees below are
+// on every step's critical path -- and kept as (hi, lo) pairs in the 8 bytes of a
+// double slot.  Both are exact for the first level and far inside FP32 vectors'
+// rounding after it.
+template <typename CT> struct LzSum {
+    using T = double;
+    static __device__ __forceinline__ T zero() { return 0.0; }
+    static __device__ __forceinline__ T from_ct(CT x) { return (double)x; }
+    static __device__ __forceinline__ void put(double *slot, T x) { *slot = x; }
+    static __device__ __forceinline__ T get(const double *slot) { return *slot; }
+    static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+    static __device__ __forceinline__ double value(T x) { return x; }
+};
+template <> struct LzSum<float> {
+    using T = dfm::df;
+    static __device__ __forceinline__ T zero() { return T{0.0f, 0.0f}; }
+    static __device__ __forceinline__ T from_ct(float x) { return T{x, 0.0f}; }
+    static __device__ __forceinline__ void put(double *slot, T x) {
+        *reinterpret_cast<float2 *>(slot) = make_float2(x.h, x.l);
+    }
+    static __device__ __forceinline__ T get(const double *slot) {
+        const float2 f = *reinterpret_cast<const float2 *>(slot);
+        return T{f.x, f.y};
+    }
+    static __device__ __forceinline__ T add(T a, T b) { return dfm::add(a, b); }
+    static __device__ __forceinline__ double value(T x) { return dfm::to_double(x); }
+};
+
+// Fixed pairwise sums: three (four) dependent adds instead of seven (fifteen).
+template <class Sum>
+__device__ inline typename Sum::T tree_sum8(const typename Sum::T *x) {
+    return Sum::add(Sum::add(Sum::add(x[0], x[1]), Sum::add(x[2], x[3])),
+                    Sum::add(Sum::add(x[4], x[5]), Sum::add(x[6], x[7])));
 }
-__device__ inline double tree_sum16(const double *x) { return tree_sum8(x) + tree_sum8(x + 8); }
 
 // Deterministic pseudo-random restart value of pole i at Lanczos index j, in [0.5, 1.5).
 __host__ __device__ inline double restart_value(int i, int j) {
@@ -105,12 +137,14 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 //
 // Arithmetic: with FP64 vectors everything is FP64.  With FP32 vectors every
 // per-pole operation (products, the update, the per-thread partial sums of the dot
-// products, norms and scalars) is FP32, and only the sums across threads, warps and
-// CTAs are FP64: on this GPU FP64 issues at 1/64 of the FP32 rate, and a per-pole
-// FP64 operation would cost more than the whole FP32 sweep.
+// products, norms and scalars) is FP32, and only the sums across warps and CTAs are
+// wider, in double-float (LzSum): on this GPU FP64 issues at 1/64 of the FP32 rate, and
+// a per-pole FP64 operation would cost more than the whole FP32 sweep.
 template <typename VT, bool kGlobalSlices>
 __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
     using CT = typename LzTraits<VT>::CT;
+    using Sum = LzSum<CT>;
+    using ST = typename Sum::T;
     constexpr int VW = Vec16<VT>::n;
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
@@ -190,10 +224,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // over the ranks (the loads first, then four levels of adds: one DSMEM round trip
     // and a short FP64 chain instead of CL of each).
     auto cluster_sum = [&](const double *buf, int t) -> double {
-        double x[16];
+        ST x[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) x[r] = (r < CL) ? cluster.map_shared_rank(const_cast<double *>(buf), r)[t] : 0.0;
-        return tree_sum16(x);
+        for (int r = 0; r < 16; ++r)
+            x[r] = (r < CL) ? Sum::get(cluster.map_shared_rank(const_cast<double *>(buf), r) + t) : Sum::zero();
+        return Sum::value(Sum::add(tree_sum8<Sum>(x), tree_sum8<Sum>(x + 8)));
     };
 
     // (b1) dots pass: <v_t, w> for the pass's vectors t < nl and |w|^2, summed over
@@ -230,19 +265,19 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             for (int u = 0; u < 4; ++u) {
                 acc[u] = warp_sum_ct(acc[u]);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
                 const int t = t0 + u * kLzWarps;
-                if (lane == 0 && t < nl) Ap[t] = (double)acc[u];
+                if (lane == 0 && t < nl) Sum::put(Ap + t, Sum::from_ct(acc[u]));
             }
         }
         CT nwp = 0;
         for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
         nwp = warp_sum_ct(nwp);
-        if (lane == 0) red[warp * kMaxScal] = (double)nwp;
+        if (lane == 0) Sum::put(red + warp * kMaxScal, Sum::from_ct(nwp));
         __syncthreads();
         if (tid == 0) {
-            double x[kLzWarps];
+            ST x[kLzWarps];
 #pragma unroll
-            for (int q = 0; q < kLzWarps; ++q) x[q] = red[q * kMaxScal];
-            Ap[nl] = tree_sum8(x);
+            for (int q = 0; q < kLzWarps; ++q) x[q] = Sum::get(red + q * kMaxScal);
+            Sum::put(Ap + nl, tree_sum8<Sum>(x));
         }
         cluster.sync();
         for (int t = tid; t <= nl; t += kLzThreads) {   // (b2) totals over the cluster
@@ -325,26 +360,26 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         pn = warp_sum_ct(pn);
         sa = warp_sum_ct(sa);
-        if (lane == 0) { red[warp * kMaxScal] = (double)pn; red[warp * kMaxScal + 1] = (double)sa; }
+        if (lane == 0) { Sum::put(red + warp * kMaxScal, Sum::from_ct(pn)); Sum::put(red + warp * kMaxScal + 1, Sum::from_ct(sa)); }
 #pragma unroll
         for (int d = 0; d < 8; ++d)
             if (d < D) {
                 const CT x = warp_sum_ct(sm_[d]);
-                if (lane == 0) red[warp * kMaxScal + 2 + d] = (double)x;
+                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + d, Sum::from_ct(x));
             }
 #pragma unroll
         for (int g = 0; g < 8; ++g)
             if (g < nq) {
                 const CT x = warp_sum_ct(sg[g]);
-                if (lane == 0) red[warp * kMaxScal + 2 + D + g] = (double)x;
+                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + D + g, Sum::from_ct(x));
             }
         __syncthreads();
         const int nsc = 2 + D + nq;
         if (tid < nsc) {
-            double x[kLzWarps];
+            ST x[kLzWarps];
 #pragma unroll
-            for (int q = 0; q < kLzWarps; ++q) x[q] = red[q * kMaxScal + tid];
-            Bs[tid] = tree_sum8(x);
+            for (int q = 0; q < kLzWarps; ++q) x[q] = Sum::get(red + q * kMaxScal + tid);
+            Sum::put(Bs + tid, tree_sum8<Sum>(x));
         }
         cluster.sync();
         if (tid < nsc) tot[tid] = cluster_sum(Bs, tid);
