@@ -26,7 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbd_gb300.so")
 
 BD_OK, BD_ERR_ARG, BD_ERR_CUDA, BD_ERR_CAPACITY, BD_ERR_STATE, BD_ERR_NUMERIC, BD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
-BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL = 1, 2, 4
+BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL, BD_RUN_STABLE_SORT, BD_RUN_GRAPH = 1, 2, 4, 8, 16
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -59,7 +59,11 @@ EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload
             "bd_count_poles", "bd_ehf", "bd_sigma2_build", "bd_lanczos_reduce", "bd_dyson_solve", "bd_run_all",
             "bd_sync", "bd_result_counts", "bd_result_fetch", "bd_result_koltun_all", "bd_last_timings",
             "bd_dyson_rows", "bd_lanczos_vectors", "bd_upload_propagator", "bd_dressed_propagator",
-            "bd_result_fetch_all"]
+            "bd_result_fetch_all", "bd_sigma2_sorted", "bd_files_open", "bd_files_close", "bd_files_error",
+            "bd_files_read_propagator", "bd_files_read_pivots", "bd_files_read_interaction", "bd_files_modspace",
+            "bd_files_propagator", "bd_files_pivots", "bd_files_interaction_lines", "bd_upload_files",
+            "bd_interaction_fetch", "bd_files_write_propagator", "bd_files_write_pivots", "bd_write_interaction_bin",
+            "bd_files_save_selfenergy", "bd_files_load_selfenergy", "bd_files_selfenergy_name"]
 
 
 def load_library(path: str = LIB_PATH):
@@ -75,6 +79,7 @@ def load_library(path: str = LIB_PATH):
     lib.bd_count_poles.argtypes = [vp, C.c_int, _ip, _ip]
     lib.bd_ehf.argtypes = [vp, C.c_int, _dp]
     lib.bd_sigma2_build.argtypes = [vp, C.c_int, _dp, C.c_int, _ip, _dp, C.c_int, _ip]
+    lib.bd_sigma2_sorted.argtypes = [vp, C.c_int, _dp, C.c_int, _dp, C.c_int]
     lib.bd_lanczos_reduce.argtypes = [vp, C.c_int, C.c_int, _dp, _ip, _ip, _dp, C.c_int, _ip, _ip,
                                       _dp, C.c_int, _ip, _ip, C.c_int]
     lib.bd_dyson_solve.argtypes = [vp, C.c_int, _dp, _dp, C.c_double, _dp, C.c_int, _ip, _dp, C.c_int, _ip, _dp]
@@ -93,10 +98,31 @@ def load_library(path: str = LIB_PATH):
     lib.bd_last_timings.argtypes = [vp, _dp]
     lib.bd_diag_two_pass.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+    lib.bd_autotune.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.bd_set_lanczos_slices.argtypes = [vp, C.c_int]
     lib.bd_lanczos_stored.argtypes = [vp, _ip]
     lib.bd_lanczos_kernel_ms.argtypes = [vp]; lib.bd_lanczos_kernel_ms.restype = C.c_double
     lib.bd_launch_count.argtypes = [vp]; lib.bd_launch_count.restype = C.c_longlong
+    cp = C.c_char_p
+    lp = C.POINTER(C.c_longlong)
+    lib.bd_files_open.argtypes = [C.POINTER(vp), cp]
+    lib.bd_files_close.argtypes = [vp]; lib.bd_files_close.restype = None
+    lib.bd_files_error.argtypes = [vp]; lib.bd_files_error.restype = cp
+    lib.bd_files_read_propagator.argtypes = [vp, cp]
+    lib.bd_files_read_pivots.argtypes = [vp, cp]
+    lib.bd_files_read_interaction.argtypes = [vp, cp, C.c_int]
+    lib.bd_files_modspace.argtypes = [vp, C.POINTER(_ModSpace), C.POINTER(_ip), C.POINTER(C.POINTER(cp))]
+    lib.bd_files_propagator.argtypes = [vp, C.POINTER(_Propagator), C.POINTER(_dp), C.POINTER(_dp)]
+    lib.bd_files_pivots.argtypes = [vp, C.POINTER(_Pivots)]
+    lib.bd_files_interaction_lines.argtypes = [vp, lp, lp, lp]
+    lib.bd_upload_files.argtypes = [vp, vp]
+    lib.bd_interaction_fetch.argtypes = [vp, _ip, _ip, _dp, C.c_longlong, lp, lp]
+    lib.bd_files_write_propagator.argtypes = [vp, cp, C.POINTER(_Propagator), _dp, _dp]
+    lib.bd_files_write_pivots.argtypes = [vp, cp, C.POINTER(_Propagator), _dp, _dp, C.c_int, C.c_int, C.c_double]
+    lib.bd_write_interaction_bin.argtypes = [cp, C.POINTER(_Interaction), C.c_longlong]
+    lib.bd_files_save_selfenergy.argtypes = [vp, cp, C.c_int, C.c_int, C.c_int, _dp, _ip, C.c_int, _dp, _ip, C.c_int]
+    lib.bd_files_load_selfenergy.argtypes = [vp, cp, C.c_int, _ip, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip]
+    lib.bd_files_selfenergy_name.argtypes = [vp, cp, cp, C.c_int, C.c_char_p, C.c_int]
     return lib
 
 
@@ -174,6 +200,21 @@ class Context:
         if with_pivots and prob.piv is not None:
             self.upload_pivots(prob.piv)
         return self
+
+    def upload_files(self, files: "Files", prob=None):
+        """The problem of a Files object (bd_upload_files); prob (optional) is kept for the
+        helpers that read model-space sizes."""
+        self._chk(self.lib.bd_upload_files(self.h, files.h))
+        self.prob = prob
+        return self
+
+    def interaction(self):
+        """The resident interaction list (iabJ, icdJ, V) and the repeated pairs left out."""
+        n, r = C.c_longlong(), C.c_longlong()
+        self._chk(self.lib.bd_interaction_fetch(self.h, None, None, None, 0, C.byref(n), C.byref(r)))
+        a, b, v = np.zeros(max(n.value, 1), np.int32), np.zeros(max(n.value, 1), np.int32), np.zeros(max(n.value, 1))
+        self._chk(self.lib.bd_interaction_fetch(self.h, _pi(a), _pi(b), _pd(v), len(v), C.byref(n), C.byref(r)))
+        return a[:n.value], b[:n.value], v[:n.value], r.value
 
     def upload_propagator(self, prop):
         """Replace the input propagator; model space, interaction and pivots stay."""
@@ -255,7 +296,16 @@ class Context:
             return None, None
         return fw[:a.value], bk[:b.value]
 
-    def lanczos_reduce(self, ish, pivots, nitr_fw, nitr_bk, mixed: bool = False):
+    def sigma2_sorted(self, ish):
+        """Rows of the resident Sigma(2) in the order the last reduction visited them
+        (the reference's in-place sort of Reduce_SelfEn_Lncz)."""
+        nfw, nbk = self.count_poles(ish)
+        D = self.D(ish)
+        fw, bk = np.zeros((max(nfw, 1), 2 + D)), np.zeros((max(nbk, 1), 2 + D))
+        self._chk(self.lib.bd_sigma2_sorted(self.h, ish, _pd(fw), max(nfw, 1), _pd(bk), max(nbk, 1)))
+        return fw[:nfw], bk[:nbk]
+
+    def lanczos_reduce(self, ish, pivots, nitr_fw, nitr_bk, mixed: bool = False, stable_sort: bool = False):
         D = self.D(ish)
         piv = _d(np.array(pivots, np.float64).reshape(-1, D)).copy()
         nf, nb = _i(nitr_fw).copy(), _i(nitr_bk).copy()
@@ -268,7 +318,7 @@ class Context:
         Lf, Lb = C.c_int(), C.c_int()
         self._chk(self.lib.bd_lanczos_reduce(self.h, ish, npv, _pd(piv), _pi(nf), _pi(nb), _pd(lf), capf, C.byref(Lf),
                                              _pi(ipf), _pd(lb), capb, C.byref(Lb), _pi(ipb),
-                                             BD_RUN_MIXED if mixed else 0))
+                                             (BD_RUN_MIXED if mixed else 0) | (BD_RUN_STABLE_SORT if stable_sort else 0)))
         return dict(lz_fw=lf[:Lf.value], lz_bk=lb[:Lb.value], ipiv_fw=ipf, ipiv_bk=ipb, NDEN=npv + 1,
                     n_piv_fw=int(ipf[0]) if Lf.value else 0, n_piv_bk=int(ipb[0]) if Lb.value else 0,
                     pivots=piv, nitr_fw=nf, nitr_bk=nb)
@@ -309,8 +359,19 @@ class Context:
         return dict(qp=qp[:a.value], qh=qh[:b.value], koltun=kol)
 
     # ---------------------------------------------------------------- all channels
-    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True):
+    @staticmethod
+    def _flags(lanczos=True, mixed=False, per_channel=False, stable_sort=False, graph=False):
         flags = (BD_RUN_LANCZOS if lanczos else 0) | (BD_RUN_MIXED if mixed else 0) | (BD_RUN_PER_CHANNEL if per_channel else 0)
+        return flags | (BD_RUN_STABLE_SORT if stable_sort else 0) | (BD_RUN_GRAPH if graph else 0)
+
+    def autotune(self, reps=3, **kw):
+        """bd_autotune: the fastest Lanczos / Dyson cluster sizes for the batched step."""
+        a, b = C.c_int(), C.c_int()
+        self._chk(self.lib.bd_autotune(self.h, self._flags(**kw), reps, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True, stable_sort=False, graph=False):
+        flags = self._flags(lanczos, mixed, per_channel, stable_sort, graph)
         self._chk(self.lib.bd_run_all(self.h, flags))
         if sync:
             self.sync()
@@ -363,6 +424,140 @@ class Context:
         qp, qh, kol = np.zeros((max(a.value, 1), 2 + D)), np.zeros((max(b.value, 1), 2 + D)), np.zeros(3)
         self._chk(self.lib.bd_result_fetch(self.h, ish, _pd(qp), max(a.value, 1), _pd(qh), max(b.value, 1), _pd(kol)))
         return dict(qp=qp[:a.value], qh=qh[:b.value], koltun=kol)
+
+
+class Files:
+    """A problem read from the reference's own files, on the host (bd_files_*): model space,
+    propagator, Lanczos pivots and interaction, and the reference's writers.  No GPU is
+    needed until it is uploaded with Context.upload_files."""
+
+    def __init__(self, modspace_path: str):
+        self.lib = lib()
+        h = C.c_void_p()
+        rc = self.lib.bd_files_open(C.byref(h), os.fsencode(modspace_path))
+        self.h = h
+        self._chk(rc)
+
+    def _chk(self, rc):
+        if rc != BD_OK:
+            raise BDError(rc, self.lib.bd_files_error(self.h).decode() if self.h else "bd_files_open")
+        return rc
+
+    def close(self):
+        if self.h:
+            self.lib.bd_files_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def read_propagator(self, path):
+        self._chk(self.lib.bd_files_read_propagator(self.h, os.fsencode(path)))
+        return self
+
+    def read_pivots(self, path):
+        self._chk(self.lib.bd_files_read_pivots(self.h, os.fsencode(path)))
+        return self
+
+    def read_interaction(self, path, threads: int = 0):
+        self._chk(self.lib.bd_files_read_interaction(self.h, os.fsencode(path), threads))
+        return self
+
+    def modspace(self):
+        m = _ModSpace()
+        on = _ip()
+        names = C.POINTER(C.c_char_p)()
+        self._chk(self.lib.bd_files_modspace(self.h, C.byref(m), C.byref(on), C.byref(names)))
+        ns, no_ = m.nsubsh, m.norb
+        arr = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy()
+        return dict(nsubsh=ns, norb=no_, l=arr(m.l, ns), j2=arr(m.j2, ns), ip=arr(m.ip, ns), ch=arr(m.ch, ns),
+                    no=arr(m.no, ns), orb_sh=arr(m.orb_sh, no_), orb_xe=arr(m.orb_xe, no_), orb_n=arr(on, no_),
+                    names=[names[i].decode() for i in range(ns)])
+
+    def propagator(self):
+        p = _Propagator()
+        zp, zh = _dp(), _dp()
+        self._chk(self.lib.bd_files_propagator(self.h, C.byref(p), C.byref(zp), C.byref(zh)))
+        ns = self.modspace()["nsubsh"]
+        npa = np.ctypeslib.as_array(p.np, shape=(ns,)).copy(); nha = np.ctypeslib.as_array(p.nh, shape=(ns,)).copy()
+        a, b = int(npa.sum()), int(nha.sum())
+        g = lambda q, n: np.ctypeslib.as_array(q, shape=(n,)).copy() if n else np.zeros(0)
+        return dict(nspb=p.nspb, np=npa, nh=nha, ep=g(p.ep, a), eh=g(p.eh, b), zp=g(zp, a), zh=g(zh, b),
+                    fqp=g(p.fqp, a * p.nspb).reshape(a, p.nspb), fqh=g(p.fqh, b * p.nspb).reshape(b, p.nspb))
+
+    def pivots(self):
+        pv = _Pivots()
+        self._chk(self.lib.bd_files_pivots(self.h, C.byref(pv)))
+        ms = self.modspace()
+        npvt = np.ctypeslib.as_array(pv.npvt, shape=(ms["nsubsh"],)).copy()
+        tot = int(npvt.sum()); vt = int((npvt * ms["no"]).sum())
+        g = lambda q, n, t: np.ctypeslib.as_array(q, shape=(n,)).copy() if n else np.zeros(0, t)
+        return dict(npvt=npvt, n_fw=g(pv.n_itr_fw, tot, np.int32), n_bk=g(pv.n_itr_bk, tot, np.int32),
+                    vec=g(pv.vec, vt, np.float64))
+
+    def lines(self):
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self._chk(self.lib.bd_files_interaction_lines(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return dict(kept=a.value, outside=b.value, pauli=c.value)
+
+    @staticmethod
+    def _prop_struct(prop):
+        arrs = dict(np=_i(prop["np"]), nh=_i(prop["nh"]), ep=_d(prop["ep"] if len(prop["ep"]) else np.zeros(1)),
+                    eh=_d(prop["eh"] if len(prop["eh"]) else np.zeros(1)),
+                    fqp=_d(np.asarray(prop["fqp"]).reshape(-1) if len(prop["ep"]) else np.zeros(prop["nspb"])),
+                    fqh=_d(np.asarray(prop["fqh"]).reshape(-1) if len(prop["eh"]) else np.zeros(prop["nspb"])))
+        st = _Propagator(prop["nspb"], _pi(arrs["np"]), _pi(arrs["nh"]), _pd(arrs["ep"]), _pd(arrs["eh"]),
+                         _pd(arrs["fqp"]), _pd(arrs["fqh"]))
+        return st, arrs
+
+    def write_propagator(self, path, prop, zp=None, zh=None):
+        st, keep = self._prop_struct(prop)
+        zpa = _d(zp) if zp is not None else None
+        zha = _d(zh) if zh is not None else None
+        self._chk(self.lib.bd_files_write_propagator(self.h, os.fsencode(path), C.byref(st), _pd(zpa), _pd(zha)))
+
+    def write_pivots(self, path, prop, n_fw, n_bk, z_cut=60.0, zp=None, zh=None):
+        st, keep = self._prop_struct(prop)
+        zpa = _d(zp) if zp is not None else None
+        zha = _d(zh) if zh is not None else None
+        self._chk(self.lib.bd_files_write_pivots(self.h, os.fsencode(path), C.byref(st), _pd(zpa), _pd(zha), n_fw,
+                                                 n_bk, z_cut))
+
+    def selfenergy_name(self, folder, ish, label="SelfEn"):
+        buf = C.create_string_buffer(1024)
+        self._chk(self.lib.bd_files_selfenergy_name(self.h, os.fsencode(folder), label.encode(), ish, buf, len(buf)))
+        return buf.value.decode()
+
+    def save_selfenergy(self, path, ish, nden, fw, bk, ipiv_fw=None, ipiv_bk=None, fwbk=0):
+        fw = _d(np.asarray(fw).reshape(-1)); bk = _d(np.asarray(bk).reshape(-1))
+        D = int(self.modspace()["no"][ish]); nt = nden + D
+        ipf = _i(ipiv_fw) if ipiv_fw is not None else None
+        ipb = _i(ipiv_bk) if ipiv_bk is not None else None
+        self._chk(self.lib.bd_files_save_selfenergy(self.h, os.fsencode(path), ish, nden, len(fw) // nt, _pd(fw),
+                                                    _pi(ipf), len(bk) // nt, _pd(bk), _pi(ipb), fwbk))
+
+    def load_selfenergy(self, path, ish):
+        nden, nf, nb = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self.lib.bd_files_load_selfenergy(self.h, os.fsencode(path), ish, C.byref(nden), C.byref(nf), None, 0,
+                                                    None, C.byref(nb), None, 0, None))
+        D = int(self.modspace()["no"][ish]); nt = nden.value + D
+        fw, bk = np.zeros((max(nf.value, 1), nt)), np.zeros((max(nb.value, 1), nt))
+        ipf, ipb = np.zeros(nt, np.int32), np.zeros(nt, np.int32)
+        self._chk(self.lib.bd_files_load_selfenergy(self.h, os.fsencode(path), ish, C.byref(nden), C.byref(nf), _pd(fw),
+                                                    len(fw), _pi(ipf), C.byref(nb), _pd(bk), len(bk), _pi(ipb)))
+        return dict(nden=nden.value, fw=fw[:nf.value], bk=bk[:nb.value], ipiv_fw=ipf, ipiv_bk=ipb)
+
+
+def write_interaction_bin(path, iabJ, icdJ, V, n_alloc: int = 0):
+    """VppInt_t::write_bin of one interaction list."""
+    a, b, v = _i(iabJ), _i(icdJ), _d(V)
+    st = _Interaction(len(v), _pi(a), _pi(b), _pd(v))
+    rc = lib().bd_write_interaction_bin(os.fsencode(path), C.byref(st), n_alloc)
+    if rc != BD_OK:
+        raise BDError(rc, f"writing {path}")
 
 
 def koltun_totals(kol_per_channel, ch):

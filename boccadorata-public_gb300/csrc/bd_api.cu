@@ -8,7 +8,6 @@
 //   * per channel (bd_sigma2_build / bd_lanczos_reduce / bd_dyson_solve), the
 //     drop-in for the reference's three calls, one channel per launch;
 //   * all channels at once (bd_run_all), one launch per phase over every channel.
-#include <cub/cub.cuh>
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -114,7 +113,7 @@ struct HostStage {
     }
     void *take(size_t bytes, cudaStream_t st) {
         const size_t b = (bytes + 255) / 256 * 256;
-        if (used + b > cap && cap >= ((size_t)64 << 20)) {   // a long run without a synchronisation
+        if (st && used + b > cap && cap >= ((size_t)64 << 20)) {   // a long run without a synchronisation
             cudaStreamSynchronize(st);
             reclaim();
         }
@@ -232,6 +231,8 @@ struct bd_ctx {
     cudaStream_t st_aux = nullptr;
     cudaEvent_t ev_up[2] = {};
     bool v_pending = false;
+    bool v_checked = false;   // h_vcheck holds the check of the last interaction upload
+    long long vpp_repeated = 0;   // repeated pairs left out of the last interaction read from a file
     bool lz_timed = false;
     double lz_kernel_ms = 0.0;
     long long launches = 0;   // kernels of this library launched since creation
@@ -264,6 +265,7 @@ struct bd_ctx {
     // buffer while the host plans the propagator (finish_static reads them)
     bool static_pending = false;
     int *h_segcheck = nullptr;
+    int *h_vcheck = nullptr;   // non-finite matrix elements found where they landed (index + 1, 0: none)
     int2 *pending_rows = nullptr;
     int *pending_prank = nullptr;
     int pending_nJ = 0;
@@ -287,8 +289,9 @@ struct bd_ctx {
     int4 *d_chunks_fw = nullptr, *d_chunks_bk = nullptr;   // chunk tables of the shared-memory sort
     long long chunk_cap_fw = 0, chunk_cap_bk = 0;
     int *d_sorti_fw = nullptr, *d_sorti_bk = nullptr;       // its sorted indices
-    void *d_cub_tmp = nullptr;
-    size_t cub_bytes = 0;
+    unsigned long long *d_rkey[2] = {nullptr, nullptr};   // radix sort ping-pong buffers (long channels)
+    unsigned *d_rval[2] = {nullptr, nullptr};
+    void *d_rscratch = nullptr;
     double *d_sighf = nullptr, *d_sig1b = nullptr;  // per channel D*D at chan_dd_off
     std::vector<long long> chan_dd_off;
     long long *d_dd_off = nullptr;
@@ -328,6 +331,14 @@ struct bd_ctx {
     bool results_valid = false;
     std::vector<int> res_nq;  // after run_all: 2 per channel
     double timings[5] = {0, 0, 0, 0, 0};
+    // CUDA graphs of the batched step, one per run-flag combination: captured on first use,
+    // replayed after; every change of the plan, the buffers or the tuning drops them.  While
+    // a step is captured, the host tables it copies come from gstage (page-locked, kept as
+    // long as the graphs: a replay reads them again).
+    bool capturing = false;
+    HostStage gstage;
+    cudaGraphExec_t gexec[32] = {};
+    long long glaunches[32] = {};
 };
 
 namespace {
@@ -422,8 +433,32 @@ int sync_stream(bd_ctx *ctx) {
     return BD_OK;
 }
 
+// A host table to the device on the context's stream.  While a step is being captured the
+// source is first copied into the graphs' page-locked stage, which outlives the capture.
+int h2d_table(bd_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return BD_OK;
+    if (ctx->capturing) {
+        void *p = ctx->gstage.take(bytes, nullptr);
+        if (!p) return fail(ctx, BD_ERR_CUDA, "page-locked staging of %zu bytes", bytes);
+        std::memcpy(p, src, bytes);
+        src = p;
+    }
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->st));
+    return BD_OK;
+}
+
+// Drops the captured steps (their nodes hold buffer addresses and table contents).
+void graph_invalidate(bd_ctx *ctx) {
+    bool any = false;
+    for (auto &g : ctx->gexec)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; any = true; }
+    if (any && ctx->st) cudaStreamSynchronize(ctx->st);
+    ctx->gstage.reclaim();
+}
+
 // Buffers of a list go back to the pool (beyond kPoolCap idle bytes: to the driver).
 void release(bd_ctx *ctx, std::vector<DevBuf> &list) {
+    graph_invalidate(ctx);
     if (ctx->st_aux) cudaStreamSynchronize(ctx->st_aux);
     ctx->v_pending = false;
     if (ctx->st) cudaStreamSynchronize(ctx->st);
@@ -701,10 +736,12 @@ int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
     return BD_OK;
 }
 
-// Stable sort of each channel's poles by energy: forward ascending, backward descending
-// (the orders Reduce_SelfEn_Lncz establishes, source/BcDor-Self_energy_ext_Op_e.cpp:119-130),
-// then gather E and M into the sorted copies.
-int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
+// Sort of each channel's poles by energy: forward ascending, backward descending (the
+// orders Reduce_SelfEn_Lncz establishes, source/BcDor-Self_energy_ext_Op_e.cpp:119-130),
+// then gather E and M into the sorted copies.  A stable sort runs first; with ref_order
+// (the FP64 path) k_heap_order then puts equal energies in the order the reference's
+// heap sorts leave them (source/BcDor-Utilities.cpp:25-94).
+int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi, bool ref_order) {
     for (int dir = 0; dir < 2; ++dir) {
         const Chan &A = ctx->chans[ch_lo], &Z = ctx->chans[ch_hi - 1];
         const long long n0 = dir == 0 ? A.fw_off : A.bk_off;
@@ -715,11 +752,9 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
             rel[I - ch_lo] = (int)((dir == 0 ? ctx->chans[I].fw_off : ctx->chans[I].bk_off) - n0);
         rel[ch_hi - ch_lo] = (int)n;
         int *d_off = dir == 0 ? ctx->d_segoff_fw : ctx->d_segoff_bk;
-        CU(cudaMemcpyAsync(d_off, rel.data(), sizeof(int) * rel.size(), cudaMemcpyHostToDevice, ctx->st));
+        if (int rc = h2d_table(ctx, d_off, rel.data(), sizeof(int) * rel.size())) return rc;
         double *E = dir == 0 ? ctx->d_Efw : ctx->d_Ebk;
-        int *idx = dir == 0 ? ctx->d_idx_fw : ctx->d_idx_bk;
         int *perm = dir == 0 ? ctx->d_perm_fw : ctx->d_perm_bk;
-        size_t bytes = ctx->cub_bytes;
         const int nseg = ch_hi - ch_lo;
         int seg_max = 0;
         for (int I = ch_lo; I < ch_hi; ++I) seg_max = std::max(seg_max, rel[I - ch_lo + 1] - rel[I - ch_lo]);
@@ -733,7 +768,7 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
             int4 *dch = dir == 0 ? ctx->d_chunks_fw : ctx->d_chunks_bk;
             if ((long long)chunks.size() > (dir == 0 ? ctx->chunk_cap_fw : ctx->chunk_cap_bk))
                 return fail(ctx, BD_ERR_STATE, "sort chunk table overflow");
-            CU(cudaMemcpyAsync(dch, chunks.data(), sizeof(int4) * chunks.size(), cudaMemcpyHostToDevice, ctx->st));
+            if (int rc = h2d_table(ctx, dch, chunks.data(), sizeof(int4) * chunks.size())) return rc;
             unsigned long long *tk = reinterpret_cast<unsigned long long *>(ctx->d_keys_tmp);
             int *ti = dir == 0 ? ctx->d_sorti_fw : ctx->d_sorti_bk;
             k_chunk_sort<<<(unsigned)chunks.size(), kSortThreads, 0, ctx->st>>>(E + n0, dch, dir == 1, n0, tk, ti);
@@ -741,14 +776,18 @@ int launch_sort(bd_ctx *ctx, int ch_lo, int ch_hi) {
                                                                           perm + n0);
             e = cudaGetLastError();
             ctx->launches += 2;
-        } else if (dir == 0)
-            e = cub::DeviceSegmentedRadixSort::SortPairs(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp, idx + n0,
-                                                         perm + n0, (int)n, nseg, d_off, d_off + 1, 0, 64, ctx->st);
-        else
-            e = cub::DeviceSegmentedRadixSort::SortPairsDescending(ctx->d_cub_tmp, bytes, E + n0, ctx->d_keys_tmp,
-                                                                   idx + n0, perm + n0, (int)n, nseg, d_off,
-                                                                   d_off + 1, 0, 64, ctx->st);
+        } else {   // a channel beyond shared memory: radix sorts over the range
+            int nl = 0;
+            e = launch_pole_radix(E, dir == 0 ? ctx->d_seg_fw : ctx->d_seg_bk, ch_lo, nseg, n0, n, dir == 1,
+                                  ctx->d_rkey[0], ctx->d_rval[0], ctx->d_rkey[1], ctx->d_rval[1], ctx->d_rscratch,
+                                  perm, &nl, ctx->st);
+            ctx->launches += nl;
+        }
         CU(e);
+        if (ref_order) {
+            CU(launch_heap_order(E, d_off, nseg, seg_max, n0, perm, ctx->st));
+            ctx->launches += 1;
+        }
         k_permute_soa<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(
             perm, n0, n, dir == 0 ? ctx->d_seg_fw : ctx->d_seg_bk, ctx->d_cs, dir, E, dir == 0 ? ctx->d_Mfw : ctx->d_Mbk,
             dir == 0 ? ctx->d_Efw_s : ctx->d_Ebk_s, dir == 0 ? ctx->d_Mfw_s : ctx->d_Mbk_s,
@@ -818,7 +857,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     // stay), so no clearing pass is needed.
     // chain descriptors live in a small device array (one slot per chain of the range)
     LzChain *d_ch = ctx->d_chains + 2 * ch_lo;   // this range's own slots
-    CU(cudaMemcpyAsync(d_ch, ch.data(), sizeof(LzChain) * ch.size(), cudaMemcpyHostToDevice, ctx->st));
+    if (int rc = h2d_table(ctx, d_ch, ch.data(), sizeof(LzChain) * ch.size())) return rc;
     long long gram_cap = 0;
     for (const LzChain &z : ch) gram_cap += lz_gram_cap(z.N);
     CU(launch_lz_groups(d_ch, (int)ch.size(), gram_cap, ctx->st));   // energy groups for the deflated tails
@@ -856,6 +895,7 @@ int ensure_dyson(bd_ctx *ctx, bool lanczos) {
     }
     if (a > (size_t)2 << 30) return fail(ctx, BD_ERR_CAPACITY, "Dyson matrices need %.1f GB", a * 8.0 / 1e9);
     if (a > ctx->dyA_cap || v > ctx->dyvec_cap || s > ctx->dysol_cap || r > ctx->dyR_cap || w > ctx->dywork_cap) {
+        graph_invalidate(ctx);
         CU(cudaStreamSynchronize(ctx->st));
         if (r > ctx->dyR_cap) {
             if (ctx->d_dyR) cudaFree(ctx->d_dyR);
@@ -936,11 +976,11 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
     }
     if (Dmax > 8) return fail(ctx, BD_ERR_CAPACITY, "more than 8 orbitals in a channel");
     // descriptors at the channel's slot so per-channel launches never overwrite queued ones
-    CU(cudaMemcpyAsync(ctx->d_jobs + ch_lo, jobs.data(), sizeof(DyJob) * jobs.size(), cudaMemcpyHostToDevice, ctx->st));
-    CU(cudaMemcpyAsync(ctx->d_row_first + ch_lo, row_first.data(), sizeof(long long) * row_first.size(),
-                       cudaMemcpyHostToDevice, ctx->st));
-    CU(cudaMemcpyAsync(ctx->d_work_first + ch_lo, ctx->dy_work_off.data() + ch_lo, sizeof(long long) * jobs.size(),
-                       cudaMemcpyHostToDevice, ctx->st));
+    int rct;
+    if ((rct = h2d_table(ctx, ctx->d_jobs + ch_lo, jobs.data(), sizeof(DyJob) * jobs.size()))) return rct;
+    if ((rct = h2d_table(ctx, ctx->d_row_first + ch_lo, row_first.data(), sizeof(long long) * row_first.size()))) return rct;
+    if ((rct = h2d_table(ctx, ctx->d_work_first + ch_lo, ctx->dy_work_off.data() + ch_lo, sizeof(long long) * jobs.size())))
+        return rct;
     CU(launch_dyson(ctx->d_jobs + ch_lo, (int)jobs.size(), ctx->d_row_first + ch_lo, rows, nmax, Dmax,
                     dy_cluster_for(ctx, ch_hi - ch_lo), ctx->d_dywork, ctx->d_work_first + ch_lo, ctx->st));
     ctx->launches += dyson_launch_count(nmax);
@@ -1014,6 +1054,7 @@ int alloc_lanczos(bd_ctx *ctx) {
 // Chain schedules of every channel from the stored pivots (pole counts may have
 // changed with the propagator), then the Lanczos buffers.
 int plan_pivots(bd_ctx *ctx) {
+    graph_invalidate(ctx);
     size_t vo = 0;
     for (int I = 0; I < ctx->nsubsh; ++I) {
         const int D = ctx->no[I], npv = ctx->piv_npvt[I], p0 = ctx->piv_first[I];
@@ -1034,8 +1075,115 @@ int plan_pivots(bd_ctx *ctx) {
 
 // Model space and interaction: resident until the next bd_upload_problem (the
 // Wide_self_energy_t's MdSp and Vpp, which Run_itrs keeps across iterations).
-int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp) {
+// Index of the first non-finite value of x[0 .. n), or -1.
+long long first_nonfinite(const double *x, long long n) {
+    if (!x) return -1;
+    for (long long i = 0; i < n; ++i)
+        if (!std::isfinite(x[i])) return i;
+    return -1;
+}
+
+// Interaction lines read from a file (orbits, J, V in file order) on the host.
+struct FileLines {
+    const int4 *abcd = nullptr;
+    const int *J = nullptr;
+    const double *V = nullptr;
+    long long n = 0;
+};
+
+// The canonical, sorted list of VppInt_t after Load_interaction (read_ascii's canonical
+// pairs, prepare_for_reading's order, check_for_double_entries' first of each repeated
+// pair; source/BcDor-Initialize.cpp:110-117) built on the device from file lines: a
+// kernel forms each line's canonical keys and phase, the radix sort orders them (stable,
+// so among repeated pairs the first in the file is kept), a scan places the kept ones.
+// The model space must already be on the device (ctx->dp).  *pa / *pb / *pv are new
+// resident arrays of *pn elements; *n_rep counts the repeated pairs left out.
+int build_canonical(bd_ctx *ctx, const FileLines &fl, int **pa, int **pb, double **pv, long long *pn, long long *n_rep) {
+    const long long n = fl.n;
+    const DevProblem &P = ctx->dp;
+    *pa = nullptr; *pb = nullptr; *pv = nullptr; *pn = 0; *n_rep = 0;
+    if (n > (long long)INT_MAX / 2) return fail(ctx, BD_ERR_CAPACITY, "%lld interaction lines (at most %d)", n, INT_MAX / 2);
+    if (ctx->norb > 1024) return fail(ctx, BD_ERR_CAPACITY, "%d orbits (the canonical keys hold 1024)", ctx->norb);
+    std::vector<DevBuf> tmp;
+    long long kept = 0;
+    int rc;
+    unsigned long long *k0 = nullptr;
+    unsigned *v0 = nullptr, *pos = nullptr, *keep = nullptr;
+    signed char *sg = nullptr;
+    double *dV = nullptr;
+    {
+        BufScope scope(ctx, &tmp);
+        int4 *dabcd;
+        int *dJ, *bad;
+        unsigned long long *k1;
+        unsigned *v1;
+        char *scratch;
+        if ((rc = dalloc(ctx, &dabcd, (size_t)n)) || (rc = dalloc(ctx, &dJ, (size_t)n)) || (rc = dalloc(ctx, &dV, (size_t)n)) ||
+            (rc = dalloc(ctx, &k0, (size_t)n)) || (rc = dalloc(ctx, &k1, (size_t)n)) || (rc = dalloc(ctx, &v0, (size_t)n)) ||
+            (rc = dalloc(ctx, &v1, (size_t)n)) || (rc = dalloc(ctx, &sg, (size_t)n)) || (rc = dalloc(ctx, &keep, (size_t)n)) ||
+            (rc = dalloc(ctx, &pos, (size_t)n)) || (rc = dalloc(ctx, &bad, 1)) ||
+            (rc = dalloc(ctx, &scratch, std::max(radix_scratch_bytes(n), scan_scratch_bytes(n))))) {
+            release(ctx, tmp);
+            return rc;
+        }
+        if (n > 0) {
+            CU(cudaMemcpyAsync(dabcd, fl.abcd, sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->st));
+            CU(cudaMemcpyAsync(dJ, fl.J, sizeof(int) * n, cudaMemcpyHostToDevice, ctx->st));
+            CU(cudaMemcpyAsync(dV, fl.V, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
+        }
+        CU(cudaMemsetAsync(bad, 0, sizeof(int), ctx->st));
+        const unsigned nb = (unsigned)std::max<long long>(1, (n + 255) / 256);
+        if (n > 0) {
+            k_vpp_canon<<<nb, 256, 0, ctx->st>>>(dabcd, dJ, n, P.orb_sh, P.j2, P.ip, P.ch, k0, v0, sg, bad);
+            CU(cudaGetLastError());
+            ctx->launches += 1;
+        }
+        int passes = 0;
+        CU(radix_sort_pairs(k0, v0, k1, v1, n, 0, 51, true, scratch, &passes, ctx->st));
+        ctx->launches += radix_launches(passes, true);
+        if (n > 0) {
+            k_vpp_first<<<nb, 256, 0, ctx->st>>>(k0, n, keep);
+            CU(cudaGetLastError());
+            CU(cudaMemcpyAsync(pos, keep, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, ctx->st));
+            CU(exclusive_scan_u32(pos, n, scratch, ctx->st));
+            ctx->launches += 4;
+        }
+        int hbad = 0;
+        unsigned last[2] = {0u, 0u};
+        CU(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        if (n > 0) {
+            CU(cudaMemcpyAsync(&last[0], pos + n - 1, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+            CU(cudaMemcpyAsync(&last[1], keep + n - 1, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+        }
+        CU(cudaStreamSynchronize(ctx->st));
+        if (hbad) {
+            release(ctx, tmp);
+            return fail(ctx, BD_ERR_ARG, "interaction line %d: charge, parity or J differ between its two pairs", hbad - 1);
+        }
+        kept = n > 0 ? (long long)last[0] + last[1] : 0;
+        // the sorted pairs: k0 / v0 point at them after the sort (ping-pong buffers)
+    }
+    int *a, *b;
+    double *v;
+    if ((rc = dalloc(ctx, &a, (size_t)kept)) || (rc = dalloc(ctx, &b, (size_t)kept)) || (rc = dalloc(ctx, &v, (size_t)kept))) {
+        release(ctx, tmp);
+        return rc;
+    }
+    if (n > 0) {
+        k_vpp_place<<<(unsigned)((n + 255) / 256), 256, 0, ctx->st>>>(k0, v0, pos, keep, n, dV, sg, a, b, v);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+    }
+    release(ctx, tmp);   // waits for the stream
+    *pa = a; *pb = b; *pv = v; *pn = kept; *n_rep = n - kept;
+    return BD_OK;
+}
+
+int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp, const FileLines *fl = nullptr) {
     const int ns = ms->nsubsh;
+    ctx->v_checked = false;
+    if (long long k = first_nonfinite(ms->orb_xe, ms->norb); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "model space: xe of orbit %lld is not finite", k);
     ctx->nsubsh = ns; ctx->norb = ms->norb;
     ctx->l.assign(ms->l, ms->l + ns); ctx->j2.assign(ms->j2, ms->j2 + ns); ctx->ip.assign(ms->ip, ms->ip + ns);
     ctx->ch.assign(ms->ch, ms->ch + ns); ctx->no.assign(ms->no, ms->no + ns);
@@ -1060,7 +1208,7 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
     int rc;
     DevProblem &P = ctx->dp;
     BufScope scope(ctx, &ctx->sbufs);   // resident buffers
-    P.nsubsh = ns; P.norb = ctx->norb; P.jmax = ctx->jmax; P.n_me = vpp->n_me;
+    P.nsubsh = ns; P.norb = ctx->norb; P.jmax = ctx->jmax; P.n_me = fl ? 0 : vpp->n_me;
     int *t;
     double *td;
     if ((rc = dupload(ctx, &t, ctx->l))) return rc; P.l = t;
@@ -1071,7 +1219,25 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
     if ((rc = dupload(ctx, &t, ctx->orb_start))) return rc; P.orb_start = t;
     if ((rc = dupload(ctx, &t, ctx->orb_sh))) return rc; P.orb_sh = t;
     if ((rc = dupload(ctx, &td, ctx->orb_xe))) return rc; P.orb_xe = td;
-    {
+    ctx->vpp_repeated = 0;
+    if (fl) {   // from file lines: the canonical list is built on the device
+        int *a, *b;
+        double *v;
+        long long nk = 0, nrep = 0;
+        if ((rc = build_canonical(ctx, *fl, &a, &b, &v, &nk, &nrep))) return rc;
+        P.iabJ = a; P.icdJ = b; P.V = v; P.n_me = (int)nk;
+        ctx->vpp_repeated = nrep;
+        if (nk > 0) {
+            int *vbad = nullptr;
+            if ((rc = dalloc(ctx, &vbad, 1))) return rc;
+            if (!ctx->h_vcheck) CU(cudaMallocHost(&ctx->h_vcheck, sizeof(int)));
+            CU(cudaMemsetAsync(vbad, 0, sizeof(int), ctx->st));
+            CU(launch_nonfinite(v, nk, vbad, ctx->st));
+            ctx->launches += 1;
+            CU(cudaMemcpyAsync(ctx->h_vcheck, vbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+            ctx->v_checked = true;
+        }
+    } else {
         int *a, *b;
         double *v;
         if ((rc = dalloc(ctx, &a, vpp->n_me))) return rc;
@@ -1083,11 +1249,22 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
             CU(cudaEventRecord(ctx->ev_up[0], ctx->st));
             CU(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_up[0], 0));
             CU(cudaMemcpyAsync(v, vpp->V, sizeof(double) * vpp->n_me, cudaMemcpyHostToDevice, ctx->st_aux));
+            // finiteness of the matrix elements, checked on the device where they land (a
+            // host pass over them would cost more than their transfer)
+            int *vbad = nullptr;
+            if ((rc = dalloc(ctx, &vbad, 1))) return rc;
+            if (!ctx->h_vcheck) CU(cudaMallocHost(&ctx->h_vcheck, sizeof(int)));
+            CU(cudaMemsetAsync(vbad, 0, sizeof(int), ctx->st_aux));
+            CU(launch_nonfinite(v, vpp->n_me, vbad, ctx->st_aux));
+            ctx->launches += 1;
+            CU(cudaMemcpyAsync(ctx->h_vcheck, vbad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st_aux));
             CU(cudaEventRecord(ctx->ev_up[1], ctx->st_aux));
+            ctx->v_checked = true;
             ctx->v_pending = true;
         }
         P.iabJ = a; P.icdJ = b; P.V = v;
     }
+    const int n_me = P.n_me;
     // segment table of the sorted interaction, on the device (k_segments)
     {
         const std::vector<int> init(kSegTable, -10), zero(kSegTable + 3, 0);
@@ -1103,20 +1280,20 @@ int upload_static(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *vpp)
         const int nJ = ctx->jmax + 1;
         const size_t nrow = (size_t)ms->norb * ms->norb * nJ;
         int *prank = nullptr;
-        if (vpp->n_me > 0 && nrow * sizeof(int2) <= ((size_t)256 << 20)) {
+        if (n_me > 0 && nrow * sizeof(int2) <= ((size_t)256 << 20)) {
             if ((rc = dalloc(ctx, &rows, nrow))) return rc;
             if ((rc = dalloc(ctx, &prank, nrow))) return rc;
             CU(cudaMemsetAsync(rows, 0xff, sizeof(int2) * nrow, ctx->st));
             CU(cudaMemsetAsync(prank, 0xff, sizeof(int) * nrow, ctx->st));
         }
-        if (vpp->n_me > 0) {
-            k_segments<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
-                P.iabJ, P.icdJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad, rows, nJ);
+        if (n_me > 0) {
+            k_segments<<<(unsigned)((n_me + 255) / 256), 256, 0, ctx->st>>>(
+                P.iabJ, P.icdJ, n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, send, cnt, bad, rows, nJ);
             CU(cudaGetLastError());
             ctx->launches += 1;
             if (prank) {
-                k_pair_rank<<<(unsigned)((vpp->n_me + 255) / 256), 256, 0, ctx->st>>>(
-                    P.iabJ, P.icdJ, vpp->n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, nJ, prank);
+                k_pair_rank<<<(unsigned)((n_me + 255) / 256), 256, 0, ctx->st>>>(
+                    P.iabJ, P.icdJ, n_me, ms->norb, P.orb_sh, P.ch, P.ip, sstr, nJ, prank);
                 CU(cudaGetLastError());
                 ctx->launches += 1;
             }
@@ -1144,6 +1321,8 @@ int finish_static(bd_ctx *ctx) {
                     h[kSegTable + 1] == 1 ? "orbit out of range" : "bad channel key");
     for (int k = 0; k < kSegTable; ++k)
         if (h[k] > 1) return fail(ctx, BD_ERR_ARG, "interaction list not sorted by (ch, ip, J)");
+    if (ctx->v_checked && *ctx->h_vcheck != 0)
+        return fail(ctx, BD_ERR_NUMERIC, "interaction: matrix element %d is not finite", *ctx->h_vcheck - 1);
     ctx->dp.rows = (ctx->pending_rows && h[kSegTable + 2] == 0) ? ctx->pending_rows : nullptr;
     ctx->dp.prank = ctx->dp.rows ? ctx->pending_prank : nullptr;
     ctx->dp.nJ = ctx->pending_nJ;
@@ -1167,6 +1346,14 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
         if (ctx->np[s] < 0 || ctx->nh[s] < 0) return fail(ctx, BD_ERR_ARG, "negative fragment count");
         ctx->p_start[s] = nqp; ctx->h_start[s] = nqh; nqp += ctx->np[s]; nqh += ctx->nh[s];
     }
+    if (long long k = first_nonfinite(prop->ep, nqp); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "propagator: quasiparticle energy %lld is not finite", k);
+    if (long long k = first_nonfinite(prop->eh, nqh); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "propagator: quasihole energy %lld is not finite", k);
+    if (long long k = first_nonfinite(prop->fqp, (long long)nqp * prop->nspb); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "propagator: quasiparticle amplitude %lld is not finite", k);
+    if (long long k = first_nonfinite(prop->fqh, (long long)nqh * prop->nspb); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "propagator: quasihole amplitude %lld is not finite", k);
     ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
     std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
     std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
@@ -1241,17 +1428,15 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dalloc(ctx, &ctx->d_Mbk_s, ctx->tot_mbk))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_Mfw_f, ctx->tot_mfw))) return rc;
     if ((rc = dalloc(ctx, &ctx->d_Mbk_f, ctx->tot_mbk))) return rc;
-    {   // CUB scratch for the largest segmented sort
-        size_t b1 = 0, b2 = 0;
-        const int nmax = (int)std::max<long long>(1, std::max(ctx->tot_fw, ctx->tot_bk));
-        CU(cub::DeviceSegmentedRadixSort::SortPairs(nullptr, b1, ctx->d_Efw, ctx->d_keys_tmp, ctx->d_idx_fw,
-                                                    ctx->d_perm_fw, nmax, ns, ctx->d_segoff_fw, ctx->d_segoff_fw + 1,
-                                                    0, 64, ctx->st));
-        CU(cub::DeviceSegmentedRadixSort::SortPairsDescending(nullptr, b2, ctx->d_Efw, ctx->d_keys_tmp,
-                                                              ctx->d_idx_fw, ctx->d_perm_fw, nmax, ns,
-                                                              ctx->d_segoff_fw, ctx->d_segoff_fw + 1, 0, 64, ctx->st));
-        ctx->cub_bytes = std::max(b1, b2);
-        if ((rc = dalloc(ctx, reinterpret_cast<char **>(&ctx->d_cub_tmp), ctx->cub_bytes))) return rc;
+    {   // radix sort buffers, used when a channel exceeds the shared-memory chunk sort
+        long long seg_max = 0;
+        for (int I = 0; I < ns; ++I) seg_max = std::max<long long>(seg_max, std::max(ctx->chans[I].nfw, ctx->chans[I].nbk));
+        const long long nr = seg_max > kSortMax ? std::max<long long>(1, std::max(ctx->tot_fw, ctx->tot_bk)) : 1;
+        for (int b = 0; b < 2; ++b) {
+            if ((rc = dalloc(ctx, &ctx->d_rkey[b], (size_t)nr))) return rc;
+            if ((rc = dalloc(ctx, &ctx->d_rval[b], (size_t)nr))) return rc;
+        }
+        if ((rc = dalloc(ctx, reinterpret_cast<char **>(&ctx->d_rscratch), radix_scratch_bytes(nr)))) return rc;
     }
     // one-body (diag xe, Trel=7 ExtU1=1) and static self-energy, per channel D x D
     ctx->chan_dd_off.assign(ns, 0);
@@ -1352,6 +1537,7 @@ int bd_create(bd_ctx **out, int device) {
 void bd_destroy(bd_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    graph_invalidate(ctx);
     free_all(ctx);
     free_static(ctx);
     drain_pool(ctx);
@@ -1364,6 +1550,7 @@ void bd_destroy(bd_ctx *ctx) {
     for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
     for (auto &e : ctx->ev_up) if (e) cudaEventDestroy(e);
     if (ctx->h_segcheck) cudaFreeHost(ctx->h_segcheck);
+    if (ctx->h_vcheck) cudaFreeHost(ctx->h_vcheck);
     if (ctx->st_aux) cudaStreamDestroy(ctx->st_aux);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -1396,6 +1583,57 @@ int bd_upload_problem(bd_ctx *ctx, const bd_modspace *ms, const bd_interaction *
     return BD_OK;
 }
 
+// bd_upload_problem from a files object: the interaction's canonical list is built on
+// the device from the file's lines (build_canonical), then as bd_upload_problem; the
+// pivots too when the object holds them.
+int bd_upload_files(bd_ctx *ctx, const bd_files *f) {
+    if (!ctx || !f) return BD_ERR_ARG;
+    bd_modspace ms;
+    bd_propagator prop;
+    if (bd_files_modspace(f, &ms, nullptr, nullptr) != BD_OK) return fail(ctx, BD_ERR_STATE, "files: no model space");
+    if (bd_files_propagator(f, &prop, nullptr, nullptr) != BD_OK) return fail(ctx, BD_ERR_STATE, "files: no propagator read");
+    FileLines fl;
+    if (!files_interaction(f, &fl.abcd, &fl.J, &fl.V, &fl.n)) return fail(ctx, BD_ERR_STATE, "files: no interaction read");
+    CU(cudaSetDevice(ctx->device));
+    free_all(ctx);
+    free_static(ctx);
+    ctx->uploaded = false; ctx->have_pivots = false; ctx->results_valid = false; ctx->static_ok = false;
+    const bd_interaction none{0, nullptr, nullptr, nullptr};
+    int rc = upload_static(ctx, &ms, &none, &fl);
+    if (rc) {
+        ctx->static_pending = false;
+        join_interaction(ctx);
+        cudaStreamSynchronize(ctx->st);
+        return rc;
+    }
+    ctx->static_ok = true;
+    rc = upload_propagator(ctx, &prop);
+    const int rc2 = finish_static(ctx);
+    if (rc) return rc;
+    if (rc2) { ctx->static_ok = false; ctx->uploaded = false; return rc2; }
+    bd_pivots piv;
+    if (bd_files_pivots(f, &piv) == BD_OK) return bd_upload_pivots(ctx, &piv);
+    return BD_OK;
+}
+
+int bd_interaction_fetch(bd_ctx *ctx, int *iabJ, int *icdJ, double *V, long long cap, long long *n_me,
+                         long long *n_repeated) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->static_ok) return fail(ctx, BD_ERR_STATE, "no interaction uploaded");
+    CU(cudaSetDevice(ctx->device));
+    const long long n = ctx->dp.n_me;
+    if (n_me) *n_me = n;
+    if (n_repeated) *n_repeated = ctx->vpp_repeated;
+    if ((iabJ || icdJ || V) && cap < n) return fail(ctx, BD_ERR_CAPACITY, "%lld elements, room for %lld", n, cap);
+    CU(cudaStreamSynchronize(ctx->st));
+    if (n > 0) {
+        if (iabJ) CU(cudaMemcpy(iabJ, ctx->dp.iabJ, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        if (icdJ) CU(cudaMemcpy(icdJ, ctx->dp.icdJ, sizeof(int) * n, cudaMemcpyDeviceToHost));
+        if (V) CU(cudaMemcpy(V, ctx->dp.V, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+    return BD_OK;
+}
+
 int bd_upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if (!ctx || !prop) return BD_ERR_ARG;
     if (!ctx->static_ok) return fail(ctx, BD_ERR_STATE, "no model space / interaction uploaded");
@@ -1420,6 +1658,8 @@ int bd_upload_pivots(bd_ctx *ctx, const bd_pivots *piv) {
         ctx->piv_first[s] = tot; tot += ctx->piv_npvt[s]; vtot += (size_t)ctx->piv_npvt[s] * ctx->no[s];
     }
     ctx->piv_first[ctx->nsubsh] = tot;
+    if (long long k = first_nonfinite(piv->vec, (long long)vtot); k >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "pivots: element %lld is not finite", k);
     ctx->piv_nfw.assign(piv->n_itr_fw, piv->n_itr_fw + tot);
     ctx->piv_nbk.assign(piv->n_itr_bk, piv->n_itr_bk + tot);
     ctx->piv_vec.assign(piv->vec, piv->vec + vtot);
@@ -1478,6 +1718,34 @@ int bd_sigma2_build(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, int *n_fw,
     return BD_OK;
 }
 
+int bd_sigma2_sorted(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, double *sig_bk, int cap_bk) {
+    int rc = check_chan(ctx, ish);
+    if (rc) return rc;
+    CU(cudaSetDevice(ctx->device));
+    Chan &C = ctx->chans[ish];
+    if (C.state < ST_LANCZOS) return fail(ctx, BD_ERR_STATE, "channel %d: no Lanczos reduction (no sorted poles)", ish);
+    if (sig_fw && cap_fw < C.nfw) return fail(ctx, BD_ERR_CAPACITY, "sig_fw holds %d rows, %d needed", cap_fw, C.nfw);
+    if (sig_bk && cap_bk < C.nbk) return fail(ctx, BD_ERR_CAPACITY, "sig_bk holds %d rows, %d needed", cap_bk, C.nbk);
+    for (int dir = 0; dir < 2; ++dir) {
+        double *host = dir == 0 ? sig_fw : sig_bk;
+        const int N = dir == 0 ? C.nfw : C.nbk;
+        if (!host || N == 0) continue;
+        const long long off = dir == 0 ? C.fw_off : C.bk_off;
+        double *tmp = nullptr;
+        CU(cudaMallocAsync(&tmp, sizeof(double) * (size_t)N * (2 + C.D), ctx->st));
+        k_rows_aos_perm<<<(N + 255) / 256, 256, 0, ctx->st>>>(
+            dir == 0 ? ctx->d_perm_fw : ctx->d_perm_bk, off, (dir == 0 ? ctx->d_Efw : ctx->d_Ebk) + off,
+            (dir == 0 ? ctx->d_S2fw : ctx->d_S2bk) + off, (dir == 0 ? ctx->d_Mfw + C.mfw_off : ctx->d_Mbk + C.mbk_off),
+            N, C.D, tmp);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+        CU(cudaMemcpyAsync(host, tmp, sizeof(double) * (size_t)N * (2 + C.D), cudaMemcpyDeviceToHost, ctx->st));
+        CU(cudaFreeAsync(tmp, ctx->st));
+    }
+    CU(cudaStreamSynchronize(ctx->st));
+    return BD_OK;
+}
+
 int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_itr_fw, int *n_itr_bk,
                       double *lz_fw, int cap_fw, int *L_fw, int *ipiv_fw,
                       double *lz_bk, int cap_bk, int *L_bk, int *ipiv_bk, int flags) {
@@ -1488,6 +1756,9 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
     if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no Sigma(2) built", ish);
     if (n_pvt < 0 || (n_pvt > 0 && (!pivots || !n_itr_fw || !n_itr_bk))) return fail(ctx, BD_ERR_ARG, "pivots");
     if (n_pvt > 9) return fail(ctx, BD_ERR_ARG, "too many pivots (%d, at most 9)", n_pvt);
+    if (flags & ~(BD_RUN_MIXED | BD_RUN_STABLE_SORT)) return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
+    if (n_pvt > 0 && first_nonfinite(pivots, (long long)n_pvt * C.D) >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "channel %d: a pivot element is not finite", ish);
     // (re)plan this channel with the caller's pivots; same side effects as the reference:
     // started pivots normalised in place, iteration counts rescaled in place
     ChainPlan F, B;
@@ -1504,6 +1775,7 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
         C.lz[0].n_used != F.n_used || C.lz[1].n_used != B.n_used)
         return fail(ctx, BD_ERR_STATE, "channel %d: pivots differ in shape from the uploaded ones", ish);
     C.lz[0] = F; C.lz[1] = B;
+    graph_invalidate(ctx);
     // refresh this channel's schedule / pivots on the device
     for (int dir = 0; dir < 2; ++dir) {
         const ChainPlan &P = C.lz[dir];
@@ -1517,8 +1789,9 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
             CU(cudaMemcpyAsync(ctx->d_lzpiv + ctx->lz_piv_off[dir][ish], P.piv.data(), sizeof(double) * P.piv.size(),
                                cudaMemcpyHostToDevice, ctx->st));
     }
-    if ((rc = launch_sort(ctx, ish, ish + 1))) return rc;
-    if ((rc = launch_lanczos_range(ctx, ish, ish + 1, (flags & BD_RUN_MIXED) != 0))) return rc;
+    const bool fp32 = (flags & BD_RUN_MIXED) != 0;
+    if ((rc = launch_sort(ctx, ish, ish + 1, !fp32 && !(flags & BD_RUN_STABLE_SORT)))) return rc;
+    if ((rc = launch_lanczos_range(ctx, ish, ish + 1, fp32))) return rc;
     for (int dir = 0; dir < 2; ++dir) {
         const ChainPlan &P = C.lz[dir];
         double *host = dir == 0 ? lz_fw : lz_bk;
@@ -1541,6 +1814,8 @@ int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_
     Chan &C = ctx->chans[ish];
     if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no self-energy", ish);
     const int D = C.D;
+    if (first_nonfinite(sig1b, (long long)D * D) >= 0 || first_nonfinite(sig_hf, (long long)D * D) >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "channel %d: a one-body or static self-energy entry is not finite", ish);
     if (sig1b)
         CU(cudaMemcpyAsync(ctx->d_sig1b + ctx->chan_dd_off[ish], sig1b, sizeof(double) * D * D, cudaMemcpyHostToDevice,
                            ctx->st));
@@ -1590,6 +1865,10 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     const int D = C.D, NT = nden + D;
     if (nden < 2 || n_fw < 0 || n_bk < 0 || (n_fw > 0 && !fw_rows) || (n_bk > 0 && !bk_rows))
         return fail(ctx, BD_ERR_ARG, "self-energy rows");
+    if (first_nonfinite(fw_rows, (long long)n_fw * NT) >= 0 || first_nonfinite(bk_rows, (long long)n_bk * NT) >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "channel %d: a self-energy row element is not finite", ish);
+    if (first_nonfinite(sig1b, (long long)D * D) >= 0 || first_nonfinite(sig_hf, (long long)D * D) >= 0)
+        return fail(ctx, BD_ERR_NUMERIC, "channel %d: a one-body or static self-energy entry is not finite", ish);
     const int n = D + n_fw + n_bk;
     const size_t nip = (size_t)nden + D;
     double *dfw = nullptr, *dbk = nullptr, *dA = nullptr, *dv = nullptr, *dR = nullptr, *dsol = nullptr, *dwork = nullptr;
@@ -1685,17 +1964,17 @@ int bd_lanczos_vectors(bd_ctx *ctx, int ish, int dir, int fp32, double *out, lon
     return BD_OK;
 }
 
-int bd_run_all(bd_ctx *ctx, int flags) {
-    if (!ctx) return BD_ERR_ARG;
-    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+}  // extern "C"
+
+namespace {
+
+// The whole chain for every channel, queued on the context's stream (between the
+// events ev[0] .. ev[4] that time its phases).
+int enqueue_step(bd_ctx *ctx, int flags) {
     const bool lanczos = (flags & BD_RUN_LANCZOS) != 0, fp32 = (flags & BD_RUN_MIXED) != 0;
-    if (lanczos && !ctx->have_pivots) return fail(ctx, BD_ERR_STATE, "no pivots uploaded");
-    CU(cudaSetDevice(ctx->device));
+    const bool ref_order = !fp32 && !(flags & BD_RUN_STABLE_SORT);
     const int ns = ctx->nsubsh;
     int rc;
-    ctx->results_valid = false;
-    ctx->lz_timed = false;
-    if ((rc = ensure_dyson(ctx, lanczos))) return rc;
     if (ctx->d_lzstat) CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
     CU(cudaEventRecord(ctx->ev[0], ctx->st));
     if (flags & BD_RUN_PER_CHANNEL) {
@@ -1705,7 +1984,7 @@ int bd_run_all(bd_ctx *ctx, int flags) {
             if ((rc = launch_sigma2(ctx, I, I + 1))) return rc;
         }
         CU(cudaEventRecord(ctx->ev[1], ctx->st));
-        if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_sort(ctx, I, I + 1))) return rc;
+        if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_sort(ctx, I, I + 1, ref_order))) return rc;
         CU(cudaEventRecord(ctx->ev[2], ctx->st));
         if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_lanczos_range(ctx, I, I + 1, fp32))) return rc;
         CU(cudaEventRecord(ctx->ev[3], ctx->st));
@@ -1714,16 +1993,113 @@ int bd_run_all(bd_ctx *ctx, int flags) {
         if ((rc = launch_ehf(ctx, 0, ns))) return rc;
         if ((rc = launch_sigma2(ctx, 0, ns))) return rc;
         CU(cudaEventRecord(ctx->ev[1], ctx->st));
-        if (lanczos && (rc = launch_sort(ctx, 0, ns))) return rc;
+        if (lanczos && (rc = launch_sort(ctx, 0, ns, ref_order))) return rc;
         CU(cudaEventRecord(ctx->ev[2], ctx->st));
         if (lanczos && (rc = launch_lanczos_range(ctx, 0, ns, fp32))) return rc;
         CU(cudaEventRecord(ctx->ev[3], ctx->st));
         if ((rc = launch_dyson_range(ctx, 0, ns, lanczos))) return rc;
     }
     CU(cudaEventRecord(ctx->ev[4], ctx->st));
+    return BD_OK;
+}
+
+// The step captured once per flag combination into a CUDA graph, then replayed: one
+// launch of the whole chain instead of one per kernel from the host.
+int graph_step(bd_ctx *ctx, int flags) {
+    const int key = flags & 15;
+    if (!ctx->gexec[key]) {
+        CU(cudaStreamSynchronize(ctx->st));
+        ctx->capturing = true;
+        const long long l0 = ctx->launches;
+        cudaError_t e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            ctx->capturing = false;
+            return fail(ctx, BD_ERR_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+        }
+        const int rc = enqueue_step(ctx, flags);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(ctx->st, &g);
+        ctx->capturing = false;
+        if (rc || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            if (rc) return rc;
+            return fail(ctx, BD_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&ctx->gexec[key], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ctx->gexec[key] = nullptr;
+            return fail(ctx, BD_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        }
+        ctx->glaunches[key] = ctx->launches - l0;
+        ctx->launches = l0;
+    }
+    CU(cudaGraphLaunch(ctx->gexec[key], ctx->st));
+    ctx->launches += ctx->glaunches[key];
+    return BD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bd_run_all(bd_ctx *ctx, int flags) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+    if (flags & ~(BD_RUN_LANCZOS | BD_RUN_MIXED | BD_RUN_PER_CHANNEL | BD_RUN_STABLE_SORT | BD_RUN_GRAPH))
+        return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
+    const bool lanczos = (flags & BD_RUN_LANCZOS) != 0;
+    if (lanczos && !ctx->have_pivots) return fail(ctx, BD_ERR_STATE, "no pivots uploaded");
+    CU(cudaSetDevice(ctx->device));
+    const int ns = ctx->nsubsh;
+    int rc;
+    ctx->results_valid = false;
+    ctx->lz_timed = false;
+    if ((rc = ensure_dyson(ctx, lanczos))) return rc;
+    const bool graph = (flags & BD_RUN_GRAPH) && !(flags & BD_RUN_PER_CHANNEL);
+    rc = graph ? graph_step(ctx, flags & ~BD_RUN_GRAPH) : enqueue_step(ctx, flags & ~BD_RUN_GRAPH);
+    if (rc) return rc;
+    if (graph && lanczos) ctx->lz_timed = true;
     for (int I = 0; I < ns; ++I) ctx->chans[I].state = lanczos ? ST_LANCZOS : ST_SIGMA;
     ctx->last_lanczos_flags = flags;
     ctx->results_valid = true;
+    return BD_OK;
+}
+
+// Cluster sizes of the Lanczos kernel (and of the Dyson reduction beyond order 160) for
+// this problem: each candidate runs the batched step (after one warm-up) `reps` times
+// and the fastest by device time is kept.  Returns the chosen sizes.
+int bd_autotune(bd_ctx *ctx, int flags, int reps, int *lz_cluster, int *dy_cluster) {
+    if (!ctx) return BD_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
+    flags &= ~(BD_RUN_PER_CHANNEL | BD_RUN_GRAPH);
+    reps = std::max(1, std::min(reps, 20));
+    int nmax = 0;
+    for (int I = 0; I < ctx->nsubsh; ++I) nmax = std::max(nmax, dyson_order(ctx, I, (flags & BD_RUN_LANCZOS) != 0));
+    const int lz_c[3] = {4, 8, 16};
+    const int dy_c[3] = {4, 8, 16};
+    const int ndy = nmax > kTsMax ? 3 : 1;   // the cluster reduction runs only beyond kTsMax
+    double best = 1e300;
+    int bl = ctx->lz_cluster, bdc = ctx->dy_cluster;
+    for (int a = 0; a < ((flags & BD_RUN_LANCZOS) ? 3 : 1); ++a)
+        for (int b = 0; b < ndy; ++b) {
+            ctx->lz_cluster = lz_c[a];
+            ctx->dy_cluster = ndy > 1 ? dy_c[b] : ctx->dy_cluster;
+            double tot = 0.0;
+            for (int r = 0; r <= reps; ++r) {
+                int rc = bd_run_all(ctx, flags);
+                if (!rc) rc = bd_sync(ctx);
+                if (rc) return rc;
+                if (r > 0) tot += ctx->timings[4];
+            }
+            if (tot < best) { best = tot; bl = ctx->lz_cluster; bdc = ctx->dy_cluster; }
+        }
+    ctx->lz_cluster = bl;
+    ctx->dy_cluster = bdc;
+    graph_invalidate(ctx);
+    if (lz_cluster) *lz_cluster = bl;
+    if (dy_cluster) *dy_cluster = bdc;
     return BD_OK;
 }
 
@@ -1901,6 +2277,7 @@ int bd_set_lanczos_slices(bd_ctx *ctx, int mode) {
     if (!ctx) return BD_ERR_ARG;
     if (mode < 0 || mode > 2) return fail(ctx, BD_ERR_ARG, "slice mode %d", mode);
     ctx->lz_slices = mode;
+    graph_invalidate(ctx);
     return BD_OK;
 }
 
@@ -1912,6 +2289,7 @@ int bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta) {
         return fail(ctx, BD_ERR_ARG, "cluster size");
     if (!(eta > 0.0 && eta < 1.0)) return fail(ctx, BD_ERR_ARG, "eta");
     ctx->lz_cluster = lz_cluster; ctx->dy_cluster = dy_cluster; ctx->eta = eta;
+    graph_invalidate(ctx);
     return BD_OK;
 }
 
@@ -1939,7 +2317,6 @@ static __device__ __align__(256) unsigned char g_lz_scratch[BD_NOALLOC_SCRATCH_B
 
 namespace {
 
-constexpr int kNoallocDevices = 64;
 // scratch layout: [0, 256) descriptor | [256, 272) counters | [512, 1024) chain starts
 // and ends | [1024, 2048) pivots | [4096, end) Lanczos vectors
 constexpr size_t kNoallocCounters = 256, kNoallocInts = 512, kNoallocPiv = 1024, kNoallocStage = 2048;
@@ -1947,9 +2324,6 @@ constexpr size_t kNoallocVectors = 4096;
 constexpr int kNoallocCluster = 16;                      // as for a channel launched alone
 constexpr double kNoallocEta = 0.70710678118654752;      // the context's DGKS threshold
 static_assert(sizeof(LzChain) <= kNoallocCounters, "descriptor slot");
-
-std::mutex g_noalloc_mu;
-void *g_noalloc_base[kNoallocDevices];
 
 int noalloc_fail(char *err, int err_len, int code, const char *fmt, ...) {
     if (err && err_len > 0) {
@@ -1961,22 +2335,20 @@ int noalloc_fail(char *err, int err_len, int code, const char *fmt, ...) {
     return code;
 }
 
-// Device address of the scratch array on the current device, looked up once per
-// device (the first call on a device does this set-up).
+// Device address of the scratch array on the current device.  It is looked up on every
+// call (a host-side lookup, no synchronisation): an address kept from an earlier call
+// would go stale if the host program reset the device or its primary context was torn
+// down and created again, since the module and its array are then loaded anew.
 int noalloc_scratch(char **base, char *err, int err_len) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(err, err_len, BD_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-    if (dev < 0 || dev >= kNoallocDevices) return noalloc_fail(err, err_len, BD_ERR_ARG, "device %d", dev);
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_base[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_lz_scratch);
-        if (e != cudaSuccess || !p)
-            return noalloc_fail(err, err_len, BD_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-        g_noalloc_base[dev] = p;
-    }
-    *base = static_cast<char *>(g_noalloc_base[dev]);
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_lz_scratch);
+    if (e != cudaSuccess || !p)
+        return noalloc_fail(err, err_len, BD_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev,
+                            cudaGetErrorString(e));
+    *base = static_cast<char *>(p);
     return BD_OK;
 }
 
@@ -1991,6 +2363,8 @@ extern "C" int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, in
     if (n_pvt < 1 || n_pvt > 9 || !pivots || !n_itr)
         return noalloc_fail(err, err_len, BD_ERR_ARG, "pivots: n_pvt = %d (1..9), pivots and n_itr required", n_pvt);
     if ((flags & ~BD_RUN_MIXED) != 0) return noalloc_fail(err, err_len, BD_ERR_ARG, "flags 0x%x", flags);
+    for (long long i = 0; i < (long long)n_pvt * D; ++i)
+        if (!std::isfinite(pivots[i])) return noalloc_fail(err, err_len, BD_ERR_NUMERIC, "pivot element %lld is not finite", i);
     ChainPlan P;
     plan_chain(P, N, D, n_pvt, n_itr, pivots);
     if (P.L > 0)

@@ -4,7 +4,12 @@
 #include <cstddef>
 #include "bd_common.cuh"
 
+struct bd_files;
+
 namespace bd {
+
+// the interaction lines of a files object (orbits, J, V in file order); false if none
+bool files_interaction(const bd_files *f, const int4 **abcd, const int **J, const double **V, long long *n);
 
 __global__ void k_vgather(DevProblem P, const S2Block *blk, const int *chunk_blk, const int *chunk_first, int w0,
                           int nw, double *vp);
@@ -20,11 +25,36 @@ __global__ void k_ehf_sum(DevProblem P, const int3 *entries, const long long *te
 __global__ void k_permute_soa(const int *perm, long long n0, long long n, const int *seg_of, const ChanSig *cs, int dir,
                               const double *Ein, const double *Min, double *Eout, double *Mout, float *Mfout);
 __global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows);
+__global__ void k_rows_aos_perm(const int *perm, long long off, const double *E, const double *S2, const double *M,
+                                int N, int D, double *rows);
 constexpr int kSortThreads = 512;
 constexpr int kSortChunk = 2048;  // poles per chunk of the shared-memory sort
 constexpr int kSortMax = 16384;   // longest channel sorted by chunks (longer: radix sort)
 __global__ void k_chunk_sort(const double *E, const int4 *chunks, bool desc, long long base, unsigned long long *tk,
                              int *ti);
+// Stable LSD radix sort of (key, value) pairs over key bits [bit0, bit1), eight per pass
+// (k_sort.cu).  keys / vals and ktmp / vtmp are ping-pong buffers of n entries: on
+// return keys / vals point at the sorted pairs.  scratch: radix_scratch_bytes(n).
+size_t radix_scratch_bytes(long long n);
+int radix_launches(int passes, bool skip_constant);
+cudaError_t radix_sort_pairs(unsigned long long *&keys, unsigned *&vals, unsigned long long *&ktmp, unsigned *&vtmp,
+                             long long n, int bit0, int bit1, bool skip_constant, void *scratch, int *passes_out,
+                             cudaStream_t st);
+size_t scan_scratch_bytes(long long m);
+cudaError_t exclusive_scan_u32(unsigned *data, long long m, void *scratch, cudaStream_t st);
+__global__ void k_vpp_canon(const int4 *abcd, const int *Jv, long long n, const int *orb_sh, const int *j2,
+                            const int *ip, const int *ch, unsigned long long *key, unsigned *val, signed char *sign,
+                            int *bad);
+__global__ void k_vpp_first(const unsigned long long *key, long long n, unsigned *keep);
+__global__ void k_vpp_place(const unsigned long long *key, const unsigned *val, const unsigned *pos, const unsigned *keep,
+                            long long n, const double *Vin, const signed char *sign, int *iabJ, int *icdJ, double *V);
+cudaError_t launch_pole_radix(const double *E, const int *seg_of, int ch_lo, int nseg, long long n0, long long n,
+                              bool desc, unsigned long long *k0, unsigned *v0, unsigned long long *k1, unsigned *v1,
+                              void *scratch, int *perm, int *launches, cudaStream_t st);
+cudaError_t launch_nonfinite(const double *x, long long n, int *bad, cudaStream_t st);
+constexpr int kHeapMax = 49152;  // longest channel put in the reference's heap-sort order
+cudaError_t launch_heap_order(const double *E, const int *d_off, int nseg, int max_len, long long n0, int *perm,
+                              cudaStream_t st);
 __global__ void k_chunk_place(const unsigned long long *tk, const int *ti, const int4 *chunks, int nchunks,
                               long long n, long long base, int *perm);
 __global__ void k_pair_rank(const int *iabJ, const int *icdJ, int n, int norb, const int *orb_sh, const int *ch,

@@ -41,6 +41,7 @@
 // pole rows [r*S, (r+1)*S) of every vector.  Partial sums are combined through
 // distributed shared memory; every CTA adds the peers' partials in the same fixed
 // order, so all CTAs hold bit-identical totals and take identical branches.
+#include <algorithm>
 #include <climits>
 #include <cooperative_groups.h>
 #include "df64.cuh"
@@ -109,7 +110,10 @@ __host__ __device__ inline double restart_value(int i, int j) {
 constexpr int kLzThreads = 256;
 constexpr int kLzWarps = kLzThreads / 32;
 static_assert(kLzWarps == 8, "the warp partials are summed by tree_sum8");
-constexpr int kMaxScal = 32;   // 1 + D + n_used <= 17 (D <= 8, at most 8 earlier pivots)
+constexpr int kMaxScal = 32;   // 3 + D + n_used <= 19 (D <= 8, at most 8 earlier pivots)
+// Dynamic shared memory of a launch at least this large (two CTAs per SM), the room
+// behind the slices holding the basis cache.
+constexpr size_t kLzSmemCache = 108 * 1024;
 
 // 16-byte vector of the storage type: 4 floats or 2 doubles
 template <typename VT> struct Vec16;
@@ -126,6 +130,17 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
     const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
     o[0] = v.x; o[1] = v.y;
 }
+// the same through a generic address (shared or global memory)
+template <typename VT>
+__device__ inline void load16g(const VT *p, VT *out);
+template <> __device__ inline void load16g<float>(const float *p, float *o) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+template <> __device__ inline void load16g<double>(const double *p, double *o) {
+    const double2 v = *reinterpret_cast<const double2 *>(p);
+    o[0] = v.x; o[1] = v.y;
+}
 
 // Slice of a CTA: S pole rows starting at rank*S, S a multiple of 4; rows past N are
 // zero in every vector (E, w, V), so the vector loads need no tail handling.
@@ -133,7 +148,14 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // Shared-memory layout: doubles A[2][rmax] (dot partials of alternate passes) |
 // c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | red[kLzWarps * kMaxScal],
 // then CT (the vectors' arithmetic type) cf[rmax rounded up to 4] (totals in CT) |
-// Es[S] | w[S], then touched[S] bytes.
+// Es[S] | w[S], then touched[S] bytes, then the basis cache up to smem_bytes.
+//
+// Basis cache: a CTA reads and writes only its own slice of every stored vector (the
+// dot products, the updates and the step scalars are slice-local; CTAs meet only in
+// the cluster sums), so the first ccap vectors' slices are kept in the CTA's shared
+// memory as well as in V: ccap = the room left behind the slices divided by S values.
+// The reads of those vectors then cost shared-memory latency instead of L2's.  V keeps
+// every vector (the host reads the basis back from it).
 //
 // Arithmetic: with FP64 vectors everything is FP64.  With FP32 vectors every
 // per-pole operation (products, the update, the per-thread partial sums of the dot
@@ -141,7 +163,8 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // wider, in double-float (LzSum): on this GPU FP64 issues at 1/64 of the FP32 rate, and
 // a per-pole FP64 operation would cost more than the whole FP32 sweep.
 template <typename VT, bool kGlobalSlices>
-__global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2) {
+__global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains, int nchains, int rmax, double eta2,
+                                                          int smem_bytes) {
     using CT = typename LzTraits<VT>::CT;
     using Sum = LzSum<CT>;
     using ST = typename Sum::T;
@@ -178,7 +201,21 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         w = Es + S;
         touched = reinterpret_cast<unsigned char *>(w + S);
     }
+    // the basis cache behind the slices
+    VT *cache;
+    int ccap;
+    {
+        const char *end = kGlobalSlices ? reinterpret_cast<const char *>(cf + (rmax + 3) / 4 * 4)
+                                        : reinterpret_cast<const char *>(touched + S);
+        const uintptr_t e = (reinterpret_cast<uintptr_t>(end) + 15) & ~static_cast<uintptr_t>(15);
+        const uintptr_t lim = reinterpret_cast<uintptr_t>(sm) + static_cast<uintptr_t>(smem_bytes);
+        cache = reinterpret_cast<VT *>(e);
+        ccap = (e < lim && S > 0) ? (int)((lim - e) / ((uintptr_t)S * sizeof(VT))) : 0;
+    }
     __shared__ double tot[kMaxScal];
+    __shared__ double prow[kMaxScal];   // the last built row, [alpha, beta, g..., m...] (every CTA)
+    __shared__ double lc[16];           // coefficients of a recurrence step's local vectors
+    __shared__ double s_e2v;            // |E v|^2 of the last built vector
     __shared__ double s_xb, s_ixb;
     __shared__ int s_kmin;
     __shared__ int lt[16];       // vectors of a local pass
@@ -186,6 +223,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int lslot[8];     // slots of the earlier chains' last vectors (-1: deflated)
 
     VT *V = reinterpret_cast<VT *>(C.V);
+    // this CTA's slice of stored vector t: in the cache, or in V
+    auto vslice = [&](int t) -> VT * { return t < ccap ? cache + (size_t)t * S : V + (size_t)t * C.ld + i0; };
     const CT *Mc = reinterpret_cast<const CT *>(sizeof(CT) == 4 ? static_cast<const void *>(C.Mf)
                                                                   : static_cast<const void *>(C.M));
     for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? (CT)C.E[i0 + i] : (CT)0; touched[i] = 0; }
@@ -248,14 +287,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int t = t0 + u * kLzWarps;
-                vp[u] = V + (size_t)(t < nl ? (loc ? lt[t] : t) : (loc ? lt[t0] : t0)) * C.ld + i0;
+                vp[u] = vslice(t < nl ? (loc ? lt[t] : t) : (loc ? lt[t0] : t0));
             }
             CT acc[4] = {0, 0, 0, 0};
 #pragma unroll 2
             for (int q = lane; q < nv; q += 32) {
                 VT x[4][VW];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) load16<VT>(vp[u] + q * VW, x[u]);
+                for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -295,12 +334,12 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             CT acc[VW];
 #pragma unroll
             for (int u = 0; u < VW; ++u) acc[u] = 0;
-            const VT *base = V + i0 + q * VW;
+            const int qo = q * VW;
             int t = 0;
             for (; t + 7 < nl; t += 8) {
                 VT x[8][VW];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) load16<VT>(base + (size_t)(loc ? lt[t + r] : t + r) * C.ld, x[r]);
+                for (int r = 0; r < 8; ++r) load16g<VT>(vslice(loc ? lt[t + r] : t + r) + qo, x[r]);
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
                     const CT cr = cf[t + r];
@@ -310,17 +349,17 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             }
             for (; t + 3 < nl; t += 4) {
                 VT x0[VW], x1[VW], x2[VW], x3[VW];
-                load16<VT>(base + (size_t)(loc ? lt[t] : t) * C.ld, x0);
-                load16<VT>(base + (size_t)(loc ? lt[t + 1] : t + 1) * C.ld, x1);
-                load16<VT>(base + (size_t)(loc ? lt[t + 2] : t + 2) * C.ld, x2);
-                load16<VT>(base + (size_t)(loc ? lt[t + 3] : t + 3) * C.ld, x3);
+                load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
+                load16g<VT>(vslice(loc ? lt[t + 1] : t + 1) + qo, x1);
+                load16g<VT>(vslice(loc ? lt[t + 2] : t + 2) + qo, x2);
+                load16g<VT>(vslice(loc ? lt[t + 3] : t + 3) + qo, x3);
                 const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
 #pragma unroll
                 for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
             }
             for (; t < nl; ++t) {
                 VT x0[VW];
-                load16<VT>(base + (size_t)(loc ? lt[t] : t) * C.ld, x0);
+                load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
                 const CT c0 = cf[t];
 #pragma unroll
                 for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
@@ -337,7 +376,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // back only the groups it updated, so no barrier separates this from the update.
     // When another sweep follows, these sums are simply recomputed.
     auto scalar_pass = [&](int nq) {
-        CT pn = 0, sa = 0, sm_[8], sg[8];
+        CT pn = 0, sa = 0, se = 0, sm_[8], sg[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) { sm_[q] = 0; sg[q] = 0; }
         for (int q = tid; q < nv; q += kLzThreads) {
@@ -349,18 +388,24 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (i < ns) {
                     const CT e = Es[i];
                     sa += e * wi * wi;
+                    se += e * e * wi * wi;
 #pragma unroll
                     for (int d = 0; d < 8; ++d)
                         if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
 #pragma unroll
                     for (int g = 0; g < 8; ++g)
-                        if (g < nq && lslot[g] >= 0) sg[g] += e * (CT)V[(size_t)lslot[g] * C.ld + i0 + i] * wi;
+                        if (g < nq && lslot[g] >= 0) sg[g] += e * (CT)vslice(lslot[g])[i] * wi;
                 }
             }
         }
         pn = warp_sum_ct(pn);
         sa = warp_sum_ct(sa);
-        if (lane == 0) { Sum::put(red + warp * kMaxScal, Sum::from_ct(pn)); Sum::put(red + warp * kMaxScal + 1, Sum::from_ct(sa)); }
+        se = warp_sum_ct(se);
+        if (lane == 0) {
+            Sum::put(red + warp * kMaxScal, Sum::from_ct(pn));
+            Sum::put(red + warp * kMaxScal + 1, Sum::from_ct(sa));
+            Sum::put(red + warp * kMaxScal + 2 + D + nq, Sum::from_ct(se));
+        }
 #pragma unroll
         for (int d = 0; d < 8; ++d)
             if (d < D) {
@@ -374,7 +419,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + D + g, Sum::from_ct(x));
             }
         __syncthreads();
-        const int nsc = 2 + D + nq;
+        const int nsc = 3 + D + nq;   // |w|^2, <w|E|w>, m_d, g_q, |E w|^2
         if (tid < nsc) {
             ST x[kLzWarps];
 #pragma unroll
@@ -388,6 +433,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
     int k = -1;           // current pivot chain
     int extra = 0;        // sweeps beyond the first
+    bool prow_ok = false; // prow holds row j - 1, a vector this chain built (identical in every CTA)
     for (int j = 0; j < L; ++j) {
         const bool newv = (k + 1 < C.n_used) && (j == C.start[k + 1]);
         if (newv) { ++k; tail = false; }
@@ -416,6 +462,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         const int nq = k;   // earlier pivot chains
         if (tid < nq) lslot[tid] = rowslot[C.last[tid]];
+        // A continuing step's E v_{j-1} has large components only on v_{j-1}, v_{j-2} and
+        // the last vector of every earlier chain, with the coefficients row j - 1 already
+        // holds: <v_{j-1}|E|v_{j-1}> = alpha_{j-1}, <v_{j-2}|E|v_{j-1}> = beta_{j-1} (the
+        // previous chain's g on a chain's first row), <v_last(q)|E|v_{j-1}> = g_q.  After a
+        // built row the step removes those with the row's values (the three-term
+        // recurrence and its fishbone terms), so no reduction is needed before the full
+        // sweep; after anything else it measures them (the local pass below).
+        const bool rec = !newv && j > 0 && prow_ok;
         // (a) w = M.p  or  w = v_{j-1} * E   (source/BcDor-Lanczos.cpp:137-150)
         if (newv) {
             const double *p = C.piv + (size_t)k * D;
@@ -425,8 +479,25 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     for (int d = 0; d < D; ++d) s = __dadd_rn(s, __dmul_rn(C.M[(size_t)d * N + i0 + i], p[d]));
                 w[i] = (CT)s;
             }
+        } else if (rec) {
+            if (tid == 0) {   // v_{j-1}, v_{j-2} and the earlier chains' last vectors, with their coefficients
+                int n = 0;
+                lt[n] = rowslot[j - 1]; lc[n++] = prow[0];
+                if (j >= 2 && rowslot[j - 2] >= 0) { lt[n] = rowslot[j - 2]; lc[n++] = prow[1]; }
+                for (int q = 0; q < k; ++q)
+                    if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) { lt[n] = rowslot[C.last[q]]; lc[n++] = prow[2 + q]; }
+                s_nl = n;
+            }
+            __syncthreads();
+            const int nl0 = s_nl;
+            const VT *vp = vslice(lt[0]);
+            for (int i = tid; i < S; i += kLzThreads) {
+                CT x = (CT)vp[i] * Es[i];
+                for (int t = 0; t < nl0; ++t) x -= (CT)lc[t] * (CT)vslice(lt[t])[i];
+                w[i] = x;
+            }
         } else {
-            const VT *vp = V + (size_t)rowslot[j - 1] * C.ld + i0;
+            const VT *vp = vslice(rowslot[j - 1]);
             for (int i = tid; i < S; i += kLzThreads) w[i] = (CT)vp[i] * Es[i];
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
@@ -438,7 +509,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             // and the last vector of every earlier chain (the fishbone couplings); everything
             // else is rounding.  The first pass projects out just those few vectors, then
             // full sweeps follow (at least one), each repeated under the DGKS criterion.
-            bool local = !newv && attempt == 0 && j > 0;
+            bool local = !newv && attempt == 0 && j > 0 && !rec;
             if (local && tid == 0) {   // slots of v_{j-1}, v_{j-2} and the earlier chains' last vectors
                 int n = 0;
                 lt[n++] = rowslot[j - 1];
@@ -450,8 +521,9 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             __syncthreads();
             int nl = local ? s_nl : nvec;
             dots_pass(local, nl);
-            const double wn2_first = c[nl];
-            double wn2_before = wn2_first;
+            // |w|^2 before any projection: E v_{j-1}'s, from row j - 1's sums, after the recurrence
+            const double wn2_first = (rec && attempt == 0) ? s_e2v : c[nl];
+            double wn2_before = c[nl];
             for (;;) {
                 update_pass(local, nl);
                 if (local) {   // the full sweep's dot products follow the local update directly
@@ -477,6 +549,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 deflated_row(j);   // this chain's Krylov space is exhausted
                 tail = true;
                 done = true;
+                prow_ok = false;
                 break;
             }
             if (attempt > 0 || !(n2 <= tau * wn2_first || n2 == 0.0)) break;
@@ -500,9 +573,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
             if (kmin != INT_MAX) {
                 VT *vj = V + (size_t)nvec * C.ld + i0;
+                VT *vc = nvec < ccap ? cache + (size_t)nvec * S : nullptr;
                 for (int i = tid; i < S; i += kLzThreads) {
                     const bool hit = (i0 + i == kmin);
                     vj[i] = hit ? (VT)1 : (VT)0;
+                    if (vc) vc[i] = hit ? (VT)1 : (VT)0;
                     if (hit) touched[i] = 1;
                 }
                 if (rank == 0 && tid == 0) {
@@ -514,6 +589,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (tid == 0) rowslot[j] = nvec;
                 ++nvec;
                 done = true;
+                prow_ok = false;
             } else {
                 for (int i = tid; i < S; i += kLzThreads) w[i] = (i < ns) ? (CT)restart_value(i0 + i, j) : (CT)0;
                 injected = true;
@@ -533,25 +609,31 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         const double xb = s_xb, ixb = s_ixb;
         VT *vj = V + (size_t)nvec * C.ld + i0;
         {
+            VT *vc = nvec < ccap ? cache + (size_t)nvec * S : nullptr;
             const CT inv = (CT)ixb;
             for (int i = tid; i < S; i += kLzThreads) {
                 const VT v = (VT)(w[i] * inv);
                 vj[i] = v;
+                if (vc) vc[i] = v;
                 touched[i] |= (v != (VT)0);
             }
         }
-        if (rank == 0 && tid < NT) {   // one output element per thread
-            double *row = C.out + (size_t)j * NT;
+        if (tid < NT) {   // one output element per thread; every CTA keeps the row for the next step
             double x = 0.0;
             if (tid == 0) x = tot[1] * ixb * ixb;   // <w|E|w> / |w|^2
             else if (tid == 1) x = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
             else if (tid < 2 + k) x = tot[2 + D + (tid - 2)] * ixb;
             else if (tid >= C.nden_out && tid < C.nden_out + D) x = tot[2 + (tid - C.nden_out)] * ixb;
             if (newv && tid == 1) x = (k >= 1) ? tot[2 + D + (k - 1)] * ixb : x;
-            if (tid < 2 + k || tid >= C.nden_out) row[tid] = x;
-            else if (tid < C.nden_out) row[tid] = 0.0;
+            if (!(tid < 2 + k || tid >= C.nden_out)) x = 0.0;
+            prow[tid] = x;
+            if (rank == 0) C.out[(size_t)j * NT + tid] = x;
         }
-        if (tid == 0) rowslot[j] = nvec;
+        if (tid == 0) {
+            rowslot[j] = nvec;
+            s_e2v = tot[2 + D + k] * ixb * ixb;   // |E v_j|^2
+        }
+        prow_ok = !injected;
         ++nvec;
         __syncthreads();
     }
@@ -574,18 +656,20 @@ size_t lanczos_smem_bytes(int S, int rmax, bool global_slices) {
 template <typename VT, bool G>
 static cudaError_t launch_lz(const cudaLaunchConfig_t &cfg, int cluster, const LzChain *d_chains, int nchains, int rmax,
                              double eta2) {
+    const int smem_bytes = (int)cfg.dynamicSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)cfg.dynamicSmemBytes);
     if (e == cudaSuccess && cluster > 8)
         e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_lanczos<VT, G>, d_chains, nchains, rmax, eta2);
+    return cudaLaunchKernelEx(&cfg, k_lanczos<VT, G>, d_chains, nchains, rmax, eta2, smem_bytes);
 }
 
 cudaError_t launch_lanczos(const LzChain *d_chains, int nchains, int S_max, int rmax, bool fp32, int cluster,
                            double eta, bool global_slices, cudaStream_t st) {
     if (nchains <= 0) return cudaSuccess;
-    const size_t smem = lanczos_smem_bytes(S_max, rmax, global_slices);
+    // what the slices and scalars need, raised to kLzSmemCache so the rest holds the basis cache
+    const size_t smem = std::max(lanczos_smem_bytes(S_max, rmax, global_slices), kLzSmemCache);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nchains * cluster, 1, 1);
     cfg.blockDim = dim3(kLzThreads, 1, 1);

@@ -9,6 +9,7 @@
 // bit-identical to the reference's x86-64 build.
 #include "bd_common.cuh"
 #include "bd_kernels.h"
+#include <algorithm>
 #include <climits>
 
 namespace bd {
@@ -433,6 +434,255 @@ __global__ void k_rows_aos(const double *E, const double *S2, const double *M, i
     double *r = rows + (size_t)k * (2 + D);
     r[0] = E[k]; r[1] = S2[k];
     for (int d = 0; d < D; ++d) r[2 + d] = M[(size_t)d * N + k];
+}
+
+// The same rows in the order of a sort: row k is pole perm[off + k] (a global index of
+// the channel, whose first pole is off; E, S2 and M are the channel's unsorted arrays).
+__global__ void k_rows_aos_perm(const int *perm, long long off, const double *E, const double *S2, const double *M,
+                                int N, int D, double *rows) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    long long src = (long long)perm[off + k] - off;
+    if (src < 0 || src >= N) src = k;   // a permutation of the channel by construction
+    double *r = rows + (size_t)k * (2 + D);
+    r[0] = E[src]; r[1] = S2[src];
+    for (int d = 0; d < D; ++d) r[2 + d] = M[(size_t)d * N + src];
+}
+
+// The reference's order of equal energies.  Sort_u_double2dim / Sort_d_double2dim
+// (source/BcDor-Utilities.cpp:25-94) are heap sorts, so rows of equal energy end in
+// the order the heap's moves leave them, not in their input order.  k_heap_order
+// runs that heap sort again on every channel's poles, one CTA per channel, starting
+// from the stable order a previous sort left in perm (perm[off + r] = global index of
+// the pole of rank r; off[b] .. off[b + 1] is channel b's range relative to n0):
+//   * each pole gets the dense rank of its energy, from the runs of equal energies in
+//     the stable order.  The heap sort compares nothing but energies, so ranks give it
+//     the same moves (-0 and +0 compare equal, as doubles do).  Rank and position in
+//     the channel are packed into one 32-bit word, rank << 16 | position, in shared
+//     memory (position p at word p + 1, so a node's two children are one 8-byte load);
+//   * the heap is built level by level: the reference sifts nodes n/2 - 1 .. 0 in turn,
+//     and the nodes of one depth own disjoint subtrees, so they sift at once, the
+//     deepest level first;
+//   * the n - 1 extractions are one serial chain, each sift done by a warp five heap
+//     levels at a time (heap_sift_root_warp);
+//   * perm receives the result.  Sort_d's descending heap sort is Sort_u's on the
+//     ranks of the descending stable order, so one routine serves both.
+// A channel without equal energies keeps the stable order, which is then the heap
+// sort's; channels of more than kHeapMax poles keep the stable order.
+__device__ __forceinline__ void heap_sift(unsigned *a, int i, unsigned tmp, int ir) {
+    const unsigned kt = tmp >> 16;
+    int j = 2 * i + 1;
+    while (j <= ir) {
+        unsigned cj = a[j];
+        if (j < ir) {
+            const unsigned cj1 = a[j + 1];
+            if ((cj >> 16) < (cj1 >> 16)) { ++j; cj = cj1; }
+        }
+        if (kt < (cj >> 16)) { a[i] = cj; i = j; j = 2 * j + 1; }
+        else break;
+    }
+    a[i] = tmp;
+}
+
+// One extraction's sift from the root, by a whole warp, five levels per round: lane l
+// holds node r = l + 1 of the five-level subtree below the hole v (r's global index
+// g(r) = (v + 1) 2^t + r - 2^t - 1 at relative depth t) and loads its two children in
+// one 8-byte load; ballots give, for every such node, whether it has children and
+// whether the right one is the larger (the reference's tie rule: right only if
+// strictly larger).  Every lane then follows the path of larger children through the
+// ballot bits (no memory), the lanes on the path test tmp against their chosen child,
+// and the first that does not exceed tmp is where the sift stops: the parents above it
+// take their chosen child, the stop (or the node without children the path reached)
+// takes tmp.  Otherwise the hole moves five levels down and the next round starts.
+__device__ __forceinline__ void heap_sift_root_warp(unsigned *hs, unsigned tmp, int ir, int lane) {
+    unsigned *a = hs + 1;
+    const unsigned kt = tmp >> 16;
+    const int r = lane + 1;
+    const int t = 31 - __clz(r);
+    int v = 0;
+    for (;;) {
+        const int gr = ((v + 1) << t) + (r - (1 << t)) - 1;
+        const int c0 = 2 * gr + 1;
+        const bool ok = lane < 31 && c0 <= ir;
+        uint2 w = make_uint2(0u, 0u);
+        if (ok) w = *reinterpret_cast<const uint2 *>(hs + c0 + 1);
+        const bool right = ok && c0 + 1 <= ir && (w.x >> 16) < (w.y >> 16);
+        const unsigned big = right ? w.y : w.x;
+        const unsigned mh = __ballot_sync(0xffffffffu, ok), mr = __ballot_sync(0xffffffffu, right);
+        unsigned pm = 0u;
+        int rr = 1, depth = 0;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+            if (!((mh >> (rr - 1)) & 1u)) break;
+            pm |= 1u << (rr - 1);
+            rr = 2 * rr + (int)((mr >> (rr - 1)) & 1u);
+            ++depth;
+        }
+        const unsigned ms = __ballot_sync(0xffffffffu, ((pm >> lane) & 1u) && !(kt < (big >> 16)));
+        const unsigned mv = ms ? (pm & ((ms & (0u - ms)) - 1u)) : pm;
+        if ((mv >> lane) & 1u) a[gr] = big;
+        __syncwarp();
+        if (ms || depth < 5) {
+            const int hr = ms ? __ffs(ms) : rr;
+            const int th = 31 - __clz(hr);
+            if (lane == 0) a[((v + 1) << th) + (hr - (1 << th)) - 1] = tmp;
+            __syncwarp();
+            return;
+        }
+        v = ((v + 1) << 5) + (rr - 32) - 1;
+    }
+}
+
+constexpr int kHeapThreads = 1024;
+static_assert(kHeapMax < 65536, "positions are packed into 16 bits");
+__global__ void __launch_bounds__(kHeapThreads) k_heap_order(const double *E, const int *off, long long n0, int *perm) {
+    const int s0 = off[blockIdx.x], n = off[blockIdx.x + 1] - s0;
+    if (n < 2 || n > kHeapMax) return;
+    extern __shared__ __align__(16) unsigned hs[];   // position p at hs[p + 1]
+    unsigned *a = hs + 1;
+    __shared__ int wsum[kHeapThreads / 32];
+    int *pm = perm + n0 + s0;
+    const long long gbase = n0 + s0;   // global index of the channel's first pole
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // 1. dense ranks along the stable order; thread t takes positions [p0, p1)
+    const int c = (n + kHeapThreads - 1) / kHeapThreads;
+    const int p0 = min(n, tid * c), p1 = min(n, p0 + c);
+    int cnt = 0;
+    {
+        double pv = (p0 > 0 && p0 < n) ? E[pm[p0 - 1]] : 0.0;
+        for (int p = p0; p < p1; ++p) {
+            const double e = E[pm[p]];
+            cnt += (p == 0 || e != pv);
+            pv = e;
+        }
+    }
+    int x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int v = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        wsum[lane] = v;
+    }
+    __syncthreads();
+    const int ndist = wsum[kHeapThreads / 32 - 1];
+    if (ndist == n) return;   // no equal energies: the stable order is the heap sort's
+    {
+        int run = x - cnt + (wid > 0 ? wsum[wid - 1] : 0);   // rank runs before p0
+        double pv = (p0 > 0 && p0 < n) ? E[pm[p0 - 1]] : 0.0;
+        for (int p = p0; p < p1; ++p) {
+            const int g = pm[p];
+            const double e = E[g];
+            run += (p == 0 || e != pv);
+            pv = e;
+            const long long loc = (long long)g - gbase;
+            if (loc >= 0 && loc < n) a[loc] = ((unsigned)(run - 1) << 16) | (unsigned)loc;
+        }
+    }
+    __syncthreads();
+    // 2. the heap: nodes n/2 - 1 .. 0 sifted over [0, n - 1], one depth at a time
+    const int lastl = n / 2 - 1;
+    for (int d = 31 - __clz(lastl + 1); d >= 0; --d) {
+        const int lo = (1 << d) - 1, hi = min((2 << d) - 2, lastl);
+        for (int l = lo + tid; l <= hi; l += kHeapThreads) heap_sift(a, l, a[l], n - 1);
+        __syncthreads();
+    }
+    // 3. extractions by warp 0: the largest to the end of the shrinking heap, the last
+    //    node sifted from the root
+    if (wid == 0) {
+        for (int ir = n - 1; ir > 0;) {
+            const unsigned tmp = a[ir];
+            __syncwarp();
+            if (lane == 0) a[ir] = a[0];
+            --ir;
+            __syncwarp();
+            if (ir == 0) {
+                if (lane == 0) a[0] = tmp;
+                break;
+            }
+            heap_sift_root_warp(hs, tmp, ir, lane);
+        }
+    }
+    __syncthreads();
+    for (int p = tid; p < n; p += kHeapThreads) {
+        int loc = (int)(a[p] & 0xffffu);
+        if (loc >= n) loc = p;   // a permutation of the channel by construction
+        pm[p] = (int)(gbase + loc);
+    }
+}
+
+// Channels longer than kSortMax poles: a stable radix sort of the range by the energies'
+// integer images (k_sort.cu), then a stable one by channel, so each channel's poles end
+// in energy order and equal energies keep their build order.
+__global__ void k_pole_keys(const double *E, long long n0, long long n, bool desc, unsigned long long *key,
+                            unsigned *val) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    key[i] = sort_key(E[n0 + i], desc);
+    val[i] = (unsigned)(n0 + i);
+}
+__global__ void k_pole_chan(const unsigned *val, const int *seg_of, int ch_lo, long long n, unsigned long long *key) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    key[i] = (unsigned long long)(seg_of[val[i]] - ch_lo);
+}
+__global__ void k_perm_out(const unsigned *val, long long n0, long long n, int *perm) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    perm[n0 + i] = (int)val[i];
+}
+
+cudaError_t launch_pole_radix(const double *E, const int *seg_of, int ch_lo, int nseg, long long n0, long long n,
+                              bool desc, unsigned long long *k0, unsigned *v0, unsigned long long *k1, unsigned *v1,
+                              void *scratch, int *perm, int *launches, cudaStream_t st) {
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    k_pole_keys<<<nb, 256, 0, st>>>(E, n0, n, desc, k0, v0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int p1 = 0, p2 = 0;
+    if ((e = radix_sort_pairs(k0, v0, k1, v1, n, 0, 64, false, scratch, &p1, st)) != cudaSuccess) return e;
+    k_pole_chan<<<nb, 256, 0, st>>>(v0, seg_of, ch_lo, n, k0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int cbits = nseg <= 256 ? 8 : 16;
+    if ((e = radix_sort_pairs(k0, v0, k1, v1, n, 0, cbits, false, scratch, &p2, st)) != cudaSuccess) return e;
+    k_perm_out<<<nb, 256, 0, st>>>(v0, n0, n, perm);
+    if (launches) *launches += 3 + radix_launches(p1, false) + radix_launches(p2, false);
+    return cudaGetLastError();
+}
+
+// Finiteness of n doubles: bad receives 1 + the index of a non-finite one (any, when
+// there are several), and stays as it was when all are finite.
+__global__ void k_nonfinite(const double *x, long long n, int *bad) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long u = (unsigned long long)__double_as_longlong(x[i]);
+        if (((u >> 52) & 0x7ff) == 0x7ff) atomicMax(bad, (int)min(i + 1, (long long)INT_MAX));
+    }
+}
+
+cudaError_t launch_nonfinite(const double *x, long long n, int *bad, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152 * 8);
+    k_nonfinite<<<(unsigned)blocks, 256, 0, st>>>(x, n, bad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_heap_order(const double *E, const int *d_off, int nseg, int max_len, long long n0, int *perm,
+                              cudaStream_t st) {
+    if (nseg <= 0 || max_len < 2) return cudaSuccess;
+    const size_t smem = sizeof(unsigned) * (size_t)(std::min(max_len, kHeapMax) + 4);
+    cudaError_t e = cudaFuncSetAttribute(k_heap_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_heap_order<<<nseg, kHeapThreads, smem, st>>>(E, d_off, n0, perm);
+    return cudaGetLastError();
 }
 
 }  // namespace bd

@@ -332,6 +332,63 @@ def write_interaction_bcd(ms: ModelSpace, vpp: Interaction, path: str) -> None:
             f.write("".join(lines))
 
 
+def write_interaction_bcd_scrambled(ms: ModelSpace, vpp: Interaction, path: str, seed: int = 0,
+                                    repeat: float = 0.03, pauli: int = 5, outside: int = 5) -> dict:
+    """The same interaction as a ``.bcd`` a reader must put in canonical form: each line's
+    pairs in random order (a <-> b and c <-> d with the exchange phase (-1)^(j_a + j_b - J + 1)
+    folded into V, bra <-> ket), the lines shuffled, a fraction repeated (same value), and
+    a few lines a reader must drop -- Pauli-forbidden pairs (a == b at odd J) and orbits
+    outside the model space.  Returns the counts written."""
+    rng = np.random.default_rng(seed)
+    iab = vpp.iabJ.astype(np.int64); icd = vpp.icdJ.astype(np.int64)
+    J = iab % JMULT
+    a = (iab // JMULT) // ABMULT; b = (iab // JMULT) % ABMULT
+    c = (icd // JMULT) // ABMULT; d = (icd // JMULT) % ABMULT
+    V = vpp.V.copy()
+    sh = ms.orb_sh
+    j2 = ms.j2[sh]
+    n = len(V)
+    rep = rng.random(n) < repeat
+    idx = np.concatenate([np.arange(n), np.nonzero(rep)[0]])
+    a, b, c, d, J, V = a[idx], b[idx], c[idx], d[idx], J[idx], V[idx]
+    m = len(V)
+    s1 = rng.random(m) < 0.5
+    ph1 = np.where((((j2[a] + j2[b]) // 2 - J + 1) % 2) != 0, -1.0, 1.0)
+    a, b = np.where(s1, b, a), np.where(s1, a, b)
+    V = np.where(s1, V * ph1, V)
+    s2 = rng.random(m) < 0.5
+    ph2 = np.where((((j2[c] + j2[d]) // 2 - J + 1) % 2) != 0, -1.0, 1.0)
+    c, d = np.where(s2, d, c), np.where(s2, c, d)
+    V = np.where(s2, V * ph2, V)
+    s3 = rng.random(m) < 0.5
+    a, c = np.where(s3, c, a), np.where(s3, a, c)
+    b, d = np.where(s3, d, b), np.where(s3, b, d)
+    q = lambda o: np.stack([ms.orb_n[o], ms.j2[sh[o]], ms.ip[sh[o]], ms.ch[sh[o]]], 1)
+    cols = np.concatenate([q(a), q(b), q(c), q(d), J[:, None]], 1)
+    extra, vals = [], []
+    for k in range(pauli):                       # a == b at odd J
+        o = int(rng.integers(ms.norb)); Jo = 2 * int(rng.integers(0, (ms.j2[sh[o]] + 1) // 2)) + 1
+        if Jo > ms.j2[sh[o]]:
+            Jo -= 2
+        extra.append(np.concatenate([q(np.array([o]))[0], q(np.array([o]))[0], q(np.array([o]))[0],
+                                     q(np.array([o]))[0], [Jo]]))
+        vals.append(float(rng.normal()))
+    for k in range(outside):                      # a principal number beyond the model space
+        o = int(rng.integers(ms.norb))
+        row = np.concatenate([q(np.array([o]))[0]] * 4 + [[0]])
+        row[0] = ms.nmax + 7
+        extra.append(row); vals.append(float(rng.normal()))
+    if extra:
+        cols = np.concatenate([cols, np.array(extra, np.int64)], 0)
+        V = np.concatenate([V, np.array(vals)])
+    order = rng.permutation(len(V))
+    cols, V = cols[order], V[order]
+    with open(path, "w") as f:
+        f.write(f" {len(V)}  {len(V)}  # tot number of mtx el.\n")
+        f.write("".join(" ".join(map(str, r)) + f" {x:.17e}\n" for r, x in zip(cols.tolist(), V.tolist())))
+    return dict(lines=len(V), repeated=int(rep.sum()), pauli=pauli, outside=outside)
+
+
 def write_pivots(ms: ModelSpace, piv: Pivots, path: str) -> None:
     with open(path, "w") as f:
         f.write("#   Template pivots file\n#\n")

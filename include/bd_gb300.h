@@ -13,6 +13,8 @@
  *                      source/BcDor-SlfEn_classes.hh:83, source/BcDor-Self_energy_ext_Op_c.cpp:35
  *   bd_sigma2_build    Wide_self_energy_t::Build_Dynamic_SlfEn_2ndOrder
  *                      source/BcDor-SlfEn_classes.hh:84, source/BcDor-Self_energy_ext_Op_c.cpp:323
+ *   bd_sigma2_sorted   the in-place sort of Reduce_SelfEn_Lncz (Sort_u/d_double2dim)
+ *                      source/BcDor-Self_energy_ext_Op_e.cpp:116-130, source/BcDor-Utilities.cpp:25-94
  *   bd_ehf             Wide_self_energy_t::Build_ExtendedHartreeFock -> SpProp_t::ExtendedHartreeFock_Pot
  *                      source/BcDor-Self_energy_ext_Op_b.cpp:71, source/BcDor-Sp_Propagator_a.cpp:39
  *   bd_lanczos_reduce  Wide_self_energy_t::Reduce_SelfEn_Lncz + Reduce_Mtx_Lncz
@@ -47,6 +49,11 @@ extern "C" {
 #define BD_RUN_LANCZOS   1   /* Lanczos-reduce Sigma(2) before Dyson (else full Dyson)  */
 #define BD_RUN_MIXED     2   /* FP32 Lanczos vectors / reorthogonalisation              */
 #define BD_RUN_PER_CHANNEL 4 /* launch channel by channel (the drop-in call pattern)   */
+#define BD_RUN_STABLE_SORT 8 /* FP64: equal pole energies in their build order instead of
+                                the reference's heap-sort order (the FP32 form always is) */
+#define BD_RUN_GRAPH     16  /* batched: capture the step in a CUDA graph on first use (per
+                                flag combination) and replay it; any change of the problem,
+                                the pivots or the tuning captures it again */
 
 typedef struct bd_ctx bd_ctx;
 
@@ -117,10 +124,22 @@ int bd_sigma2_build(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, int *n_fw,
  * the pole count (as the reference does).  Output rows have (n_pvt + 1) + D
  * doubles [alpha, beta, g_0 .., m_0 .. m_{D-1}]; ipiv_* receive
  * [n_used_pivots, 1, start_1, ...] and must hold n_pvt + 1 + D ints.
- * flags: 0 = FP64, BD_RUN_MIXED = FP32 vectors. */
+ * flags: 0 = FP64 (poles sorted as the reference sorts them, bd_sigma2_sorted),
+ * BD_RUN_MIXED = FP32 vectors, BD_RUN_STABLE_SORT = FP64 with the build order kept
+ * among equal energies. */
 int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_itr_fw, int *n_itr_bk,
                       double *lz_fw, int cap_fw, int *L_fw, int *ipiv_fw,
                       double *lz_bk, int cap_bk, int *L_bk, int *ipiv_bk, int flags);
+
+/* Rows [E, sum_d M_d^2, M_0 .. M_{D-1}] of channel ish's resident Sigma(2) in the order
+ * the last Lanczos reduction visited them: the reference sorts the self-energy's poles
+ * in place before reducing them (Reduce_SelfEn_Lncz, source/BcDor-Self_energy_ext_Op_e.cpp:
+ * 116-130; forward ascending, backward descending, by the heap sorts of
+ * source/BcDor-Utilities.cpp:25-94).  The FP64 form reproduces that order, equal
+ * energies included, for channels of up to 49 152 poles; the FP32 form (and longer
+ * channels) keeps equal energies in their build order.  Capacities in rows; either
+ * buffer may be NULL.  BD_ERR_STATE before any reduction of the channel. */
+int bd_sigma2_sorted(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, double *sig_bk, int cap_bk);
 
 /* Dyson eigensolve of channel ish with the most recent resident self-energy
  * (Lanczos-reduced if bd_lanczos_reduce was called after bd_sigma2_build).
@@ -195,6 +214,11 @@ int       bd_diag_two_pass(bd_ctx *ctx);
 double    bd_lanczos_kernel_ms(bd_ctx *ctx);
 long long bd_launch_count(bd_ctx *ctx);
 int       bd_set_tuning(bd_ctx *ctx, int lz_cluster, int dy_cluster, double eta);
+/* Autotuner: runs the batched step (flags as bd_run_all) for each candidate cluster size
+ * of the Lanczos kernel (4, 8, 16) and, when a Dyson matrix exceeds order 160, of the
+ * cluster Householder reduction (4, 8, 16), reps timed runs each after a warm-up, and
+ * keeps the fastest by device time; the chosen sizes are returned. */
+int       bd_autotune(bd_ctx *ctx, int flags, int reps, int *lz_cluster, int *dy_cluster);
 /* stored[2 * ish + dir]: Lanczos vectors the last reduction of each chain actually
  * built (the other rows are the deflated tail of an exhausted Krylov space). */
 int       bd_lanczos_stored(bd_ctx *ctx, int *stored);
@@ -202,6 +226,76 @@ int       bd_lanczos_stored(bd_ctx *ctx, int *stored);
  * working vector: 0 = shared memory unless it would exceed 100 KB (default),
  * 1 = shared memory, 2 = global memory (for chains of any length). */
 int       bd_set_lanczos_slices(bd_ctx *ctx, int mode);
+
+/* ------------------------------------------------------------------------------
+ * The reference's files.  A bd_files object holds, on the host, a problem read from
+ * the reference's own input files; bd_upload_files puts it on a context.  Readers keep
+ * what the reference's keep and report what it would warn about; a malformed file is
+ * a status code (bd_files_error gives the message), never an exit.  The functions
+ * below that take no context touch no GPU. */
+typedef struct bd_files bd_files;
+
+/* Model space file: ModSpace_t::ModSpace_t(char*), source/BcDor-Mod_Space.cpp:415-505.
+ * *f is set (and must be closed) even when the file is refused. */
+int  bd_files_open(bd_files **f, const char *modspace_path);
+void bd_files_close(bd_files *f);
+const char *bd_files_error(const bd_files *f);
+/* Propagator file: SpProp_t::SpProp_t(char*, ModSpace_t*), source/BcDor-Sp_Propagator.cpp:
+ * 387-610 (optional n1 / n2 / d1 columns read and dropped; amplitude rows of the model
+ * space's largest subshell size, missing amplitudes zero; Z = the file's percentage / 100). */
+int  bd_files_read_propagator(bd_files *f, const char *path);
+/* Lanczos pivots file for every subshell: Make_LancPivots, source/BcDor-Miscellanea.cpp:334-390. */
+int  bd_files_read_pivots(bd_files *f, const char *path);
+/* Interaction: VppInt_t::read, source/BcDor-Vpp_potential.cpp:205-215 -- read_bin (:406-438)
+ * for a name containing ".bin", else read_ascii (:281-375) on `threads` host threads
+ * (0 = all): lines with an orbit outside the model space are skipped, Pauli-forbidden
+ * ones (a == b or c == d at odd J) discarded; the kept lines stay in file order until
+ * bd_upload_files puts them in canonical form on the device. */
+int  bd_files_read_interaction(bd_files *f, const char *path, int threads);
+/* Views of what was read (pointers into the object, valid until it is closed). */
+int  bd_files_modspace(const bd_files *f, bd_modspace *ms, const int **orb_n, const char *const **names);
+int  bd_files_propagator(const bd_files *f, bd_propagator *prop, const double **zp, const double **zh);
+int  bd_files_pivots(const bd_files *f, bd_pivots *piv);
+int  bd_files_interaction_lines(const bd_files *f, long long *kept, long long *outside, long long *pauli);
+
+/* bd_upload_problem (and bd_upload_pivots, when pivots were read) from a files object.
+ * The interaction becomes the list VppInt_t holds after Load_interaction
+ * (source/BcDor-Initialize.cpp:110-117): read_ascii's canonical pairs and phases
+ * (source/BcDor-Vpp_potential.cpp:330-356), prepare_for_reading's order (:440-501) and,
+ * of repeated pairs, the first (check_for_double_entries, :663-702) -- built on the
+ * device: one kernel per line forms the keys, a radix sort orders them, a scan places
+ * the kept ones.  Among repeated pairs the reference keeps the one its heap sort puts
+ * first; this build keeps the first in the file. */
+int  bd_upload_files(bd_ctx *ctx, const bd_files *f);
+/* The context's resident interaction list (cap elements per array; NULL arrays: counts
+ * only); *n_repeated = repeated pairs left out of the last bd_upload_files. */
+int  bd_interaction_fetch(bd_ctx *ctx, int *iabJ, int *icdJ, double *V, long long cap, long long *n_me,
+                          long long *n_repeated);
+
+/* Writers, in the reference's formats (subshell names from the model space file).
+ * Propagator: SpProp_t::write with wcode 0, source/BcDor-Sp_Propagator.cpp:613-680;
+ * zp / zh NULL: Z = sum of the squared amplitudes (what add_qp / add_qh store). */
+int  bd_files_write_propagator(const bd_files *f, const char *path, const bd_propagator *prop, const double *zp,
+                               const double *zh);
+/* Pivots: SpProp_t::DysPivots(fname, n_bk, n_fw, z_cut), source/BcDor-Sp_Propagator.cpp:1225-1290. */
+int  bd_files_write_pivots(const bd_files *f, const char *path, const bd_propagator *prop, const double *zp,
+                           const double *zh, int n_fw, int n_bk, double z_cut);
+/* Interaction: VppInt_t::write_bin, source/BcDor-Vpp_potential.cpp:377-404 (one interaction;
+ * n_alloc = the allocation recorded in the header, <= 0: n_me). */
+int  bd_write_interaction_bin(const char *path, const bd_interaction *vpp, long long n_alloc);
+/* Self-energy of channel ish in binary form: Wide_self_energy_t::save_SelfEn_bin (fwbk > 0
+ * forward only, < 0 backward only) and load_SelfEn_bin for one file,
+ * source/BcDor-Self_energy_ext_Op_d.cpp:55-133,136-255.  Rows of nden + D doubles (nden = 2
+ * for a plain Sigma(2), n_pvt + 1 for Lanczos rows with their i_piv arrays; NULL ipiv =
+ * plain rows), as bd_dyson_rows takes them; the loader checks the header against the
+ * model space and fills NULL-free buffers (ipiv: nden + D ints), sizes always. */
+int  bd_files_save_selfenergy(const bd_files *f, const char *path, int ish, int nden, int n_fw, const double *fw_rows,
+                              const int *ipiv_fw, int n_bk, const double *bk_rows, const int *ipiv_bk, int fwbk);
+int  bd_files_load_selfenergy(const bd_files *f, const char *path, int ish, int *nden, int *n_fw, double *fw_rows,
+                              int cap_fw, int *ipiv_fw, int *n_bk, double *bk_rows, int cap_bk, int *ipiv_bk);
+/* The reference's name of that file: dir/label_Dyn_J2pi=<2j><+|->_dt=<charge>.bin
+ * (Wide_self_energy_t::get_filename, source/BcDor-Self_energy_ext_Op_d.cpp:43-52). */
+int  bd_files_selfenergy_name(const bd_files *f, const char *dir, const char *label, int ish, char *buf, int len);
 
 /* Allocation-free Lanczos reduction of one pole set.  This entry point has no
  * counterpart in the reference.  It is for host programs that cannot let a
@@ -223,14 +317,14 @@ int       bd_set_lanczos_slices(bd_ctx *ctx, int mode);
  * device that loads the library until the process exits.  The Lanczos vectors
  * must fit in it with their companions: L * ld * 8 bytes (L * ld * 4 with
  * BD_RUN_MIXED, plus an FP32 copy of M, D * N * 4 bytes), ld = N + 64 rounded up to a
- * multiple of 32, plus 20 N + 4 L bytes for the energy groups and row slots of the
- * deflated tails, each part rounded up to 256 bytes, at most
- * BD_NOALLOC_SCRATCH_BYTES - 4096 in all.  Larger chains are rejected with
- * BD_ERR_CAPACITY.  D <= 8 and n_pvt <= 9.
- * The first call on each device looks up the array's device address; make that
- * first call before any stream capture on that device.  All calls share the
- * array, so calls that overlap on the GPU (two streams, two host threads) race.
- * The call itself allocates no device or pinned memory. */
+ * multiple of 32; the energy-group tables of the deflated tails, at most
+ * 29 N + 1024 bytes; and the row slots, 4 L bytes; each part rounded up to 256
+ * bytes, at most BD_NOALLOC_SCRATCH_BYTES - 4096 in all.  Larger chains are rejected
+ * with BD_ERR_CAPACITY before anything is launched.  D <= 8 and n_pvt <= 9.
+ * Every call looks up the array's device address on the current device (no set-up
+ * call is needed).  All calls share the array, so calls that overlap on the GPU
+ * (two streams, two host threads) race.  The call is synchronous and itself
+ * allocates no device or pinned memory. */
 #define BD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int bd_lanczos_chain_noalloc(const double *d_E, const double *d_M, int N, int D, int n_pvt,
                              double *pivots, int *n_itr, double *d_rows, int cap_rows, int *L_out,

@@ -39,9 +39,13 @@ def build() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
 
 
+# The reference's source folder (BD_REFERENCE_SOURCE overrides the mount point).
+REF_SOURCE = os.environ.get("BD_REFERENCE_SOURCE", "/root/reference/source")
+
+
 def build_ref() -> bool:
-    """Builds oracle/_ref from the reference sources when they are mounted (here only)."""
-    if not os.path.isdir("/root/reference/source"):
+    """Builds oracle/_ref from the reference sources when they are mounted."""
+    if not os.path.isdir(REF_SOURCE):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8"], check=True, stdout=subprocess.DEVNULL)
     return os.path.exists(REF_BIN)
@@ -155,6 +159,15 @@ class Oracle:
 
     def efermi(self, ish):
         return self.lib.bdo_seek_efermi(C.byref(self._P), ish)
+
+    def sort_perm(self, key, desc: bool):
+        """Row permutation of Sort_u_double2dim (ascending) / Sort_d_double2dim (descending),
+        source/BcDor-Utilities.cpp:25-94: sorted row r is input row perm[r]."""
+        key = np.ascontiguousarray(key, np.float64)
+        perm = np.zeros(len(key), np.int32)
+        if len(key):
+            self.lib.bdo_sort_perm(len(key), key, 1 if desc else 0, perm)
+        return perm
 
     def reduce_lanczos(self, ish, fw, bk, pivots, nitr_fw, nitr_bk, passes: int = 1):
         """Reduce_SelfEn_Lncz (source/BcDor-Self_energy_ext_Op_e.cpp:55-232): sorts fw ascending and

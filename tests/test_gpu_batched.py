@@ -129,3 +129,88 @@ def test_results_all_in_one_copy(bdmod, problems):
         for k in ("qp", "qh", "koltun"):
             assert np.array_equal(allr[ish][k], r[k]), (ish, k)
     ctx.close()
+
+
+def test_non_finite_inputs_are_refused(bdmod, problems):
+    """A NaN or an infinity planted (on the host) in any input gives BD_ERR_NUMERIC naming
+    the input, before any kernel reads it; the context stays usable."""
+    import copy
+    import dataclasses
+    p = problems(4, 20.0, 0, 20)
+    ctx = bdmod.Context()
+    cases = []
+    v = p.vpp
+    V = v.V.copy(); V[v.n // 2] = np.nan
+    cases.append((dataclasses.replace(p, vpp=dataclasses.replace(v, V=V)), "matrix element"))
+    V = v.V.copy(); V[-1] = np.inf
+    cases.append((dataclasses.replace(p, vpp=dataclasses.replace(v, V=V)), "matrix element"))
+    pr = copy.deepcopy(p.prop); pr.eh[0] = np.nan
+    cases.append((dataclasses.replace(p, prop=pr), "quasihole energy"))
+    pr = copy.deepcopy(p.prop); pr.fqp.reshape(-1)[3] = -np.inf
+    cases.append((dataclasses.replace(p, prop=pr), "quasiparticle amplitude"))
+    for bad, msg in cases:
+        with pytest.raises(bdmod.BDError) as e:
+            ctx.upload(bad)
+        assert e.value.code == bdmod.BD_ERR_NUMERIC and msg in str(e.value), str(e.value)
+    ctx.upload(p)
+    piv = copy.deepcopy(p.piv)
+    piv.vec[0] = piv.vec[0].copy(); piv.vec[0][0, 0] = np.nan
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.upload_pivots(piv)
+    assert e.value.code == bdmod.BD_ERR_NUMERIC and "pivots" in str(e.value)
+    ctx.upload_pivots(p.piv)
+    ctx.sigma2_build(0, copy=False)
+    bad = p.piv.vec[0].copy(); bad[0, 0] = np.inf
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.lanczos_reduce(0, bad, p.piv.n_fw[0], p.piv.n_bk[0])
+    assert e.value.code == bdmod.BD_ERR_NUMERIC
+    D = p.ms.no[0]
+    s1 = np.eye(D); s1[0, 0] = np.nan
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.dyson_solve(0, s1)
+    assert e.value.code == bdmod.BD_ERR_NUMERIC
+    fw, bk = ctx.sigma2_build(0)
+    fw[1, 2] = np.nan
+    with pytest.raises(bdmod.BDError) as e:
+        ctx.dyson_rows(0, 2, fw, bk, sig1b=np.eye(D))
+    assert e.value.code == bdmod.BD_ERR_NUMERIC
+    ctx.run_all(lanczos=True)                                # the context stays usable
+    assert np.isfinite(ctx.koltun_all()).all()
+    ctx.close()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_graph_replay_equals_stream_launches(bdmod, problems, mixed):
+    """The batched step captured in a CUDA graph and replayed gives the stream launches'
+    results bit for bit, repeatedly, and its phase timings."""
+    p = problems(6, 20.0, 1, 50)
+    ctx = bdmod.Context().upload(p)
+    ctx.run_all(lanczos=True, mixed=mixed)
+    want = ctx.results_all()
+    l0 = ctx.launch_count()
+    for rep in range(3):
+        ctx.run_all(lanczos=True, mixed=mixed, graph=True)
+        got = ctx.results_all()
+        for a, b in zip(want, got):
+            for k in ("qp", "qh", "koltun"):
+                assert np.array_equal(a[k], b[k]), (rep, k)
+        t = ctx.timings()
+        assert t["total"] > 0 and t["lanczos"] > 0
+    assert ctx.launch_count() - l0 >= 3 * 20          # every replay counts its kernels
+    ctx.set_tuning(lz_cluster=4)                      # a new tuning: captured again
+    ctx.run_all(lanczos=True, mixed=mixed, graph=True)
+    for a, b in zip(want, ctx.results_all()):
+        for tag in ("qp", "qh"):
+            e, z = strong_diffs(a[tag], b[tag], zmin=1e-4)
+            assert e < (1e-5 if mixed else 1e-10) and z < (1e-5 if mixed else 1e-10)
+    ctx.close()
+
+
+def test_autotune_picks_a_cluster_size(bdmod, problems):
+    p = problems(6, 20.0, 1, 50)
+    ctx = bdmod.Context().upload(p)
+    lz, dy = ctx.autotune(reps=2, lanczos=True, mixed=True)
+    assert lz in (4, 8, 16) and dy in (4, 8, 16)
+    ctx.run_all(lanczos=True, mixed=True, graph=True)
+    assert np.isfinite(ctx.koltun_all()).all()
+    ctx.close()

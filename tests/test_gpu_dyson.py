@@ -87,3 +87,39 @@ def test_sum_rules(bdmod, problems):
         A += r["koltun"][2]
     assert 15.0 < A < 17.5
     ctx.close()
+
+
+def test_dressed_orders_near_1000_against_lapack(bdmod, problems, oracle):
+    """The eigensolver where the dressed spectra put it: N_max=10 second iteration (Z >= 1e-3,
+    two fragments per side), whose chains build every vector, so the Dyson matrices keep
+    orders near 1 000 (Householder in FP64 on a cluster, Sturm bisection in double-float,
+    inverse iteration in FP64).  The same Lanczos rows go to bd_dyson_rows and to the
+    oracle's DysonMatrix with LAPACK dsyevd: every solution with Z > 1e-6 within 1e-8
+    relative in energy and 1e-8 in Z, Koltun sums within 1e-7 relative."""
+    p = problems(10, 16.0, 2, 100)
+    orc = oracle(10, 16.0, 2, 100)
+    ctx = bdmod.Context().upload(p)
+    ctx.run_all(lanczos=True)
+    ctx.dressed_propagator(1e-3, 2)
+    pv = p.piv
+    orders = []
+    for ish in (0, 21, 9):
+        ctx.sigma2_build(ish, copy=False)
+        lz = ctx.lanczos_reduce(ish, pv.vec[ish].copy(), pv.n_fw[ish], pv.n_bk[ish])
+        D = int(p.ms.no[ish])
+        n = D + len(lz["lz_fw"]) + len(lz["lz_bk"])
+        orders.append(n)
+        s1 = np.diag(p.ms.orb_xe[p.ms.orb_start[ish]:p.ms.orb_start[ish] + D])
+        sh = ctx.ehf(ish)
+        ef = orc.efermi(ish)
+        got = ctx.dyson_rows(ish, lz["NDEN"], lz["lz_fw"], lz["lz_bk"], lz["ipiv_fw"], lz["ipiv_bk"], sig1b=s1,
+                             sighf=sh, efermi=ef)
+        ref = orc.dyson(ish, s1, sh, lz["NDEN"], lz["lz_fw"], lz["lz_bk"], lz["n_piv_fw"], lz["ipiv_fw"],
+                        lz["n_piv_bk"], lz["ipiv_bk"])
+        for tag in ("qp", "qh"):
+            assert len(got[tag]) == len(ref[tag]), (ish, tag)
+            e, z = strong_diffs(ref[tag], got[tag])
+            assert e < 1e-8 and z < 1e-8, (ish, tag, n, e, z)
+        np.testing.assert_allclose(got["koltun"], ref["koltun"], rtol=1e-7, atol=1e-9)
+    assert max(orders) > 800, orders
+    ctx.close()

@@ -61,3 +61,20 @@ print("ok", err)
 """
     r = subprocess.run([sys.executable, "-c", code, oracle_mod.PORT_SO], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stderr + r.stdout
+
+
+def test_oracle_fixtures_of_bench_workloads(golden, oracle):
+    """The bench-size oracle fixtures (tests/golden/make_oracle_fixtures.py) are what the
+    oracle gives now: a few of the smaller channels recomputed."""
+    from helpers import strong_diffs
+    for name, key, chans in (("nmax8_lanczos100_oracle", (8, 20.0, 1, 100), (16, 33)),
+                             ("nmax10_lanczos100_oracle", (10, 16.0, 2, 100), (20, 41))):
+        g = golden(name)
+        orc = oracle(*key)
+        for ish in chans:
+            r = orc.run_channel(ish, True, passes=2)
+            assert (len(r["sig_fw"]), len(r["sig_bk"])) == tuple(g[f"c{ish}_counts"])
+            np.testing.assert_array_equal(r["koltun"], g[f"c{ish}_koltun"])
+            for tag in ("qp", "qh"):
+                e, z = strong_diffs(g[f"c{ish}_{tag}_strong"], r[tag][:, :2])
+                assert e == 0.0 and z == 0.0, (name, ish, tag)

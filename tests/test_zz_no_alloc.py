@@ -10,11 +10,9 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _sorted_poles(rows, descending):
-    """The device sort's order: stable by energy, ascending (forward) or descending (backward)."""
-    E = rows[:, 0]
-    order = np.argsort(-E if descending else E, kind="stable")
-    return E[order].copy(), np.ascontiguousarray(rows[order, 2:].T)
+def _poles(rows):
+    """Energies [N] and couplings [D][N] of rows already in the order the chain visits."""
+    return np.ascontiguousarray(rows[:, 0]), np.ascontiguousarray(rows[:, 2:].T)
 
 
 @pytest.mark.parametrize("mixed,tol", [(False, 1e-10), (True, 1e-5)])
@@ -25,13 +23,14 @@ def test_noalloc_matches_lanczos_reduce(bdmod, problems, mixed, tol):
     pv = p.piv
     cases = []
     for ish in (0, 12, 0):
-        fw, bk = ctx.sigma2_build(ish)
+        ctx.sigma2_build(ish, copy=False)
         want = ctx.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish], mixed=mixed)
+        fw, bk = ctx.sigma2_sorted(ish)     # the poles in the order that reduction visited them
         for d, rows, tag, ip, nit in ((0, fw, "lz_fw", "ipiv_fw", pv.n_fw[ish]),
                                       (1, bk, "lz_bk", "ipiv_bk", pv.n_bk[ish])):
             cases.append((ish, d, rows, want[tag], want[ip], nit))
     for ish, d, rows, ref, ref_ipiv, nit in cases:
-        E, M = _sorted_poles(rows, descending=(d == 1))
+        E, M = _poles(rows)
         D = M.shape[0]
         N = len(E)
         tE = torch.from_numpy(E).to(dev)
@@ -53,8 +52,17 @@ def test_noalloc_matches_lanczos_reduce(bdmod, problems, mixed, tol):
 
 
 def test_noalloc_rejects_chains_beyond_its_scratch(bdmod):
-    """More Lanczos vectors than the scratch array holds: a clear error, nothing launched."""
-    N, D = 40000, 1
+    """More Lanczos vectors than the scratch array holds: a clear error, nothing launched.
+    The buffers are real device buffers of the sizes given, so a regression of the size
+    check would show as a wrong status or wrong rows, not as a stray device access."""
+    N, D, L = 40000, 1, 200
+    dev = torch.device("cuda", 0)
+    tE = torch.linspace(-1.0, 1.0, N, dtype=torch.float64, device=dev)
+    tM = torch.ones((D, N), dtype=torch.float64, device=dev)
+    tout = torch.zeros((L, 2 + D), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
     with pytest.raises(bdmod.BDError) as ei:
-        bdmod.lanczos_chain_noalloc(16, 16, N, D, np.ones((1, 1)), np.array([200], np.int32), 16, 200)
+        bdmod.lanczos_chain_noalloc(tE.data_ptr(), tM.data_ptr(), N, D, np.ones((1, 1)), np.array([L], np.int32),
+                                    tout.data_ptr(), L)
     assert ei.value.code == bdmod.BD_ERR_CAPACITY and "scratch" in str(ei.value)
+    assert torch.count_nonzero(tout).item() == 0
