@@ -26,7 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbd_gb300.so")
 
 BD_OK, BD_ERR_ARG, BD_ERR_CUDA, BD_ERR_CAPACITY, BD_ERR_STATE, BD_ERR_NUMERIC, BD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
-BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL, BD_RUN_STABLE_SORT, BD_RUN_GRAPH = 1, 2, 4, 8, 16
+BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL, BD_RUN_REF_ORDER, BD_RUN_GRAPH = 1, 2, 4, 8, 16
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -63,7 +63,8 @@ EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload
             "bd_files_read_propagator", "bd_files_read_pivots", "bd_files_read_interaction", "bd_files_modspace",
             "bd_files_propagator", "bd_files_pivots", "bd_files_interaction_lines", "bd_upload_files",
             "bd_interaction_fetch", "bd_files_write_propagator", "bd_files_write_pivots", "bd_write_interaction_bin",
-            "bd_files_save_selfenergy", "bd_files_load_selfenergy", "bd_files_selfenergy_name"]
+            "bd_files_save_selfenergy", "bd_files_load_selfenergy", "bd_files_selfenergy_name", "bd_autotune",
+            "bd_dressed_on_device"]
 
 
 def load_library(path: str = LIB_PATH):
@@ -97,6 +98,7 @@ def load_library(path: str = LIB_PATH):
     lib.bd_result_fetch_all.argtypes = [vp, _dp, C.c_longlong, _ip, _dp]
     lib.bd_last_timings.argtypes = [vp, _dp]
     lib.bd_diag_two_pass.argtypes = [vp]
+    lib.bd_dressed_on_device.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
     lib.bd_autotune.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.bd_set_lanczos_slices.argtypes = [vp, C.c_int]
@@ -297,15 +299,15 @@ class Context:
         return fw[:a.value], bk[:b.value]
 
     def sigma2_sorted(self, ish):
-        """Rows of the resident Sigma(2) in the order the last reduction visited them
-        (the reference's in-place sort of Reduce_SelfEn_Lncz)."""
+        """Rows of the resident Sigma(2) as the reference's in-place sort of
+        Reduce_SelfEn_Lncz leaves them (heap-sort order of equal energies)."""
         nfw, nbk = self.count_poles(ish)
         D = self.D(ish)
         fw, bk = np.zeros((max(nfw, 1), 2 + D)), np.zeros((max(nbk, 1), 2 + D))
         self._chk(self.lib.bd_sigma2_sorted(self.h, ish, _pd(fw), max(nfw, 1), _pd(bk), max(nbk, 1)))
         return fw[:nfw], bk[:nbk]
 
-    def lanczos_reduce(self, ish, pivots, nitr_fw, nitr_bk, mixed: bool = False, stable_sort: bool = False):
+    def lanczos_reduce(self, ish, pivots, nitr_fw, nitr_bk, mixed: bool = False, ref_order: bool = False):
         D = self.D(ish)
         piv = _d(np.array(pivots, np.float64).reshape(-1, D)).copy()
         nf, nb = _i(nitr_fw).copy(), _i(nitr_bk).copy()
@@ -318,7 +320,7 @@ class Context:
         Lf, Lb = C.c_int(), C.c_int()
         self._chk(self.lib.bd_lanczos_reduce(self.h, ish, npv, _pd(piv), _pi(nf), _pi(nb), _pd(lf), capf, C.byref(Lf),
                                              _pi(ipf), _pd(lb), capb, C.byref(Lb), _pi(ipb),
-                                             (BD_RUN_MIXED if mixed else 0) | (BD_RUN_STABLE_SORT if stable_sort else 0)))
+                                             (BD_RUN_MIXED if mixed else 0) | (BD_RUN_REF_ORDER if ref_order else 0)))
         return dict(lz_fw=lf[:Lf.value], lz_bk=lb[:Lb.value], ipiv_fw=ipf, ipiv_bk=ipb, NDEN=npv + 1,
                     n_piv_fw=int(ipf[0]) if Lf.value else 0, n_piv_bk=int(ipb[0]) if Lb.value else 0,
                     pivots=piv, nitr_fw=nf, nitr_bk=nb)
@@ -360,9 +362,9 @@ class Context:
 
     # ---------------------------------------------------------------- all channels
     @staticmethod
-    def _flags(lanczos=True, mixed=False, per_channel=False, stable_sort=False, graph=False):
+    def _flags(lanczos=True, mixed=False, per_channel=False, ref_order=False, graph=False):
         flags = (BD_RUN_LANCZOS if lanczos else 0) | (BD_RUN_MIXED if mixed else 0) | (BD_RUN_PER_CHANNEL if per_channel else 0)
-        return flags | (BD_RUN_STABLE_SORT if stable_sort else 0) | (BD_RUN_GRAPH if graph else 0)
+        return flags | (BD_RUN_REF_ORDER if ref_order else 0) | (BD_RUN_GRAPH if graph else 0)
 
     def autotune(self, reps=3, **kw):
         """bd_autotune: the fastest Lanczos / Dyson cluster sizes for the batched step."""
@@ -370,8 +372,8 @@ class Context:
         self._chk(self.lib.bd_autotune(self.h, self._flags(**kw), reps, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True, stable_sort=False, graph=False):
-        flags = self._flags(lanczos, mixed, per_channel, stable_sort, graph)
+    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True, ref_order=False, graph=False):
+        flags = self._flags(lanczos, mixed, per_channel, ref_order, graph)
         self._chk(self.lib.bd_run_all(self.h, flags))
         if sync:
             self.sync()
@@ -383,6 +385,10 @@ class Context:
         t = np.zeros(5)
         self._chk(self.lib.bd_last_timings(self.h, _pd(t)))
         return dict(sigma2=t[0], sort=t[1], lanczos=t[2], dyson=t[3], total=t[4])
+
+    def dressed_on_device(self):
+        """Whether the last dressed_propagator stayed on the device (no re-planning)."""
+        return bool(self.lib.bd_dressed_on_device(self.h))
 
     def two_pass_steps(self):
         return int(self.lib.bd_diag_two_pass(self.h))

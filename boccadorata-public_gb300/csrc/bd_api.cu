@@ -60,6 +60,7 @@ struct Chan {
     ChainPlan lz[2];
     // resident results of the per-channel API
     int state = ST_NONE;
+    bool ref_sorted = false;   // the sort permutation holds the reference's order of equal energies
 };
 
 // Host array in page-locked memory (grown by reallocation, contents not kept), so a
@@ -293,6 +294,9 @@ struct bd_ctx {
     unsigned *d_rval[2] = {nullptr, nullptr};
     void *d_rscratch = nullptr;
     double *d_sighf = nullptr, *d_sig1b = nullptr;  // per channel D*D at chan_dd_off
+    double *d_efermi = nullptr;   // per channel: the Fermi energy of the input propagator (Seek_EFermi)
+    bool ef_override = false;     // a per-channel Dyson call with the caller's Fermi energy
+    bool last_update_on_device = false;
     std::vector<long long> chan_dd_off;
     long long *d_dd_off = nullptr;
     int3 *d_ehf_entries = nullptr;
@@ -353,11 +357,16 @@ int fail(bd_ctx *c, int code, const char *fmt, ...) {
     return code;
 }
 
+// A failed runtime call is reported and the thread's last-error state cleared, so a
+// non-sticky failure does not resurface in a later, unrelated call.
 #define CU(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess) return fail(ctx, BD_ERR_CUDA, "%s: %s (%s:%d)", #call,              \
-                                           cudaGetErrorString(e_), __FILE__, __LINE__);            \
+        if (e_ != cudaSuccess) {                                                                   \
+            cudaGetLastError();                                                                    \
+            return fail(ctx, BD_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                 \
+        }                                                                                          \
     } while (0)
 
 constexpr size_t kPoolCap = (size_t)16 << 30;   // idle bytes the pool may hold
@@ -445,6 +454,12 @@ int h2d_table(bd_ctx *ctx, void *dst, const void *src, size_t bytes) {
     }
     CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->st));
     return BD_OK;
+}
+
+// A timing event on the context's stream; during a capture it becomes an event-record
+// node of the graph (recorded again at every replay), not a capture-internal marker.
+cudaError_t record(bd_ctx *ctx, cudaEvent_t ev) {
+    return cudaEventRecordWithFlags(ev, ctx->st, ctx->capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
 }
 
 // Drops the captured steps (their nodes hold buffer addresses and table contents).
@@ -862,13 +877,13 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
     for (const LzChain &z : ch) gram_cap += lz_gram_cap(z.N);
     CU(launch_lz_groups(d_ch, (int)ch.size(), gram_cap, ctx->st));   // energy groups for the deflated tails
     ctx->launches += 3;
-    CU(cudaEventRecord(ctx->ev_lz[0], ctx->st));
+    CU(record(ctx, ctx->ev_lz[0]));
     // chains whose slices do not fit next to the scalars keep them in global memory
     const bool gslices = ctx->lz_slices == 2 || (ctx->lz_slices == 0 && lanczos_smem_bytes(Smax, rmax) > kLanczosSmemSliceCap);
     if (!gslices && lanczos_smem_bytes(Smax, rmax) > (size_t)227 * 1024)
         return fail(ctx, BD_ERR_CAPACITY, "Lanczos slices of %d poles do not fit in shared memory", Smax);
     CU(launch_lanczos(d_ch, (int)ch.size(), Smax, rmax, fp32, CL, ctx->eta, gslices, ctx->st));
-    CU(cudaEventRecord(ctx->ev_lz[1], ctx->st));
+    CU(record(ctx, ctx->ev_lz[1]));
     ctx->lz_timed = true;
     ctx->launches += 1;
     return BD_OK;
@@ -960,6 +975,7 @@ int launch_dyson_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool lanczos) {
         J.sighf = ctx->d_sighf + ctx->chan_dd_off[I];
         J.sig1b = ctx->d_sig1b + ctx->chan_dd_off[I];
         J.efermi = C.efermi;
+        J.efp = ctx->ef_override ? nullptr : ctx->d_efermi + I;
         J.A = ctx->d_dyA + ctx->dy_A_off[I];
         J.d = ctx->d_dyvec + ctx->dy_vec_off[I]; J.e = J.d + J.n; J.tau = J.e + J.n;
         J.blk = reinterpret_cast<int *>(J.tau + J.n);
@@ -1451,6 +1467,11 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
             for (int nr = nc; nr < D; ++nr) ent.push_back(make_int3(I, nr, nc));
     }
     if ((rc = dupload(ctx, &ctx->d_sig1b, s1b))) return rc;
+    {
+        std::vector<double> ef(ns);
+        for (int I = 0; I < ns; ++I) ef[I] = ctx->chans[I].efermi;
+        if ((rc = dupload(ctx, &ctx->d_efermi, ef))) return rc;
+    }
     if ((rc = dalloc(ctx, &ctx->d_sighf, s1b.size()))) return rc;
     if ((rc = dupload(ctx, &ctx->d_dd_off, ctx->chan_dd_off))) return rc;
     if ((rc = dupload(ctx, &ctx->d_ehf_entries, ent))) return rc;
@@ -1724,6 +1745,10 @@ int bd_sigma2_sorted(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, double *s
     CU(cudaSetDevice(ctx->device));
     Chan &C = ctx->chans[ish];
     if (C.state < ST_LANCZOS) return fail(ctx, BD_ERR_STATE, "channel %d: no Lanczos reduction (no sorted poles)", ish);
+    if (!C.ref_sorted) {   // the reference's order of this channel's equal energies, on demand
+        if ((rc = launch_sort(ctx, ish, ish + 1, true))) return rc;
+        C.ref_sorted = true;
+    }
     if (sig_fw && cap_fw < C.nfw) return fail(ctx, BD_ERR_CAPACITY, "sig_fw holds %d rows, %d needed", cap_fw, C.nfw);
     if (sig_bk && cap_bk < C.nbk) return fail(ctx, BD_ERR_CAPACITY, "sig_bk holds %d rows, %d needed", cap_bk, C.nbk);
     for (int dir = 0; dir < 2; ++dir) {
@@ -1756,7 +1781,7 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
     if (C.state < ST_SIGMA) return fail(ctx, BD_ERR_STATE, "channel %d: no Sigma(2) built", ish);
     if (n_pvt < 0 || (n_pvt > 0 && (!pivots || !n_itr_fw || !n_itr_bk))) return fail(ctx, BD_ERR_ARG, "pivots");
     if (n_pvt > 9) return fail(ctx, BD_ERR_ARG, "too many pivots (%d, at most 9)", n_pvt);
-    if (flags & ~(BD_RUN_MIXED | BD_RUN_STABLE_SORT)) return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
+    if (flags & ~(BD_RUN_MIXED | BD_RUN_REF_ORDER)) return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
     if (n_pvt > 0 && first_nonfinite(pivots, (long long)n_pvt * C.D) >= 0)
         return fail(ctx, BD_ERR_NUMERIC, "channel %d: a pivot element is not finite", ish);
     // (re)plan this channel with the caller's pivots; same side effects as the reference:
@@ -1790,7 +1815,9 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
                                cudaMemcpyHostToDevice, ctx->st));
     }
     const bool fp32 = (flags & BD_RUN_MIXED) != 0;
-    if ((rc = launch_sort(ctx, ish, ish + 1, !fp32 && !(flags & BD_RUN_STABLE_SORT)))) return rc;
+    const bool ref_order = !fp32 && (flags & BD_RUN_REF_ORDER);
+    if ((rc = launch_sort(ctx, ish, ish + 1, ref_order))) return rc;
+    C.ref_sorted = ref_order;
     if ((rc = launch_lanczos_range(ctx, ish, ish + 1, fp32))) return rc;
     for (int dir = 0; dir < 2; ++dir) {
         const ChainPlan &P = C.lz[dir];
@@ -1825,10 +1852,11 @@ int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_
     else if ((rc = launch_ehf(ctx, ish, ish + 1)))
         return rc;
     const double saved_ef = C.efermi;
-    if (!std::isnan(e_fermi)) C.efermi = e_fermi;
+    if (!std::isnan(e_fermi)) { C.efermi = e_fermi; ctx->ef_override = true; }
     rc = ensure_dyson(ctx, C.state == ST_LANCZOS);
     if (!rc) rc = launch_dyson_range(ctx, ish, ish + 1, C.state == ST_LANCZOS);
     C.efermi = saved_ef;
+    ctx->ef_override = false;
     if (rc) return rc;
     int nq[2] = {0, 0}, st = 0;
     CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx->st));
@@ -1972,34 +2000,34 @@ namespace {
 // events ev[0] .. ev[4] that time its phases).
 int enqueue_step(bd_ctx *ctx, int flags) {
     const bool lanczos = (flags & BD_RUN_LANCZOS) != 0, fp32 = (flags & BD_RUN_MIXED) != 0;
-    const bool ref_order = !fp32 && !(flags & BD_RUN_STABLE_SORT);
+    const bool ref_order = !fp32 && (flags & BD_RUN_REF_ORDER);
     const int ns = ctx->nsubsh;
     int rc;
     if (ctx->d_lzstat) CU(cudaMemsetAsync(ctx->d_lzstat, 0, sizeof(int) * 4, ctx->st));
-    CU(cudaEventRecord(ctx->ev[0], ctx->st));
+    CU(record(ctx, ctx->ev[0]));
     if (flags & BD_RUN_PER_CHANNEL) {
         // the drop-in call pattern: every phase launched channel by channel
         for (int I = 0; I < ns; ++I) {
             if ((rc = launch_ehf(ctx, I, I + 1))) return rc;
             if ((rc = launch_sigma2(ctx, I, I + 1))) return rc;
         }
-        CU(cudaEventRecord(ctx->ev[1], ctx->st));
+        CU(record(ctx, ctx->ev[1]));
         if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_sort(ctx, I, I + 1, ref_order))) return rc;
-        CU(cudaEventRecord(ctx->ev[2], ctx->st));
+        CU(record(ctx, ctx->ev[2]));
         if (lanczos) for (int I = 0; I < ns; ++I) if ((rc = launch_lanczos_range(ctx, I, I + 1, fp32))) return rc;
-        CU(cudaEventRecord(ctx->ev[3], ctx->st));
+        CU(record(ctx, ctx->ev[3]));
         for (int I = 0; I < ns; ++I) if ((rc = launch_dyson_range(ctx, I, I + 1, lanczos))) return rc;
     } else {
         if ((rc = launch_ehf(ctx, 0, ns))) return rc;
         if ((rc = launch_sigma2(ctx, 0, ns))) return rc;
-        CU(cudaEventRecord(ctx->ev[1], ctx->st));
+        CU(record(ctx, ctx->ev[1]));
         if (lanczos && (rc = launch_sort(ctx, 0, ns, ref_order))) return rc;
-        CU(cudaEventRecord(ctx->ev[2], ctx->st));
+        CU(record(ctx, ctx->ev[2]));
         if (lanczos && (rc = launch_lanczos_range(ctx, 0, ns, fp32))) return rc;
-        CU(cudaEventRecord(ctx->ev[3], ctx->st));
+        CU(record(ctx, ctx->ev[3]));
         if ((rc = launch_dyson_range(ctx, 0, ns, lanczos))) return rc;
     }
-    CU(cudaEventRecord(ctx->ev[4], ctx->st));
+    CU(record(ctx, ctx->ev[4]));
     return BD_OK;
 }
 
@@ -2047,7 +2075,7 @@ extern "C" {
 int bd_run_all(bd_ctx *ctx, int flags) {
     if (!ctx) return BD_ERR_ARG;
     if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
-    if (flags & ~(BD_RUN_LANCZOS | BD_RUN_MIXED | BD_RUN_PER_CHANNEL | BD_RUN_STABLE_SORT | BD_RUN_GRAPH))
+    if (flags & ~(BD_RUN_LANCZOS | BD_RUN_MIXED | BD_RUN_PER_CHANNEL | BD_RUN_REF_ORDER | BD_RUN_GRAPH))
         return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
     const bool lanczos = (flags & BD_RUN_LANCZOS) != 0;
     if (lanczos && !ctx->have_pivots) return fail(ctx, BD_ERR_STATE, "no pivots uploaded");
@@ -2061,7 +2089,10 @@ int bd_run_all(bd_ctx *ctx, int flags) {
     rc = graph ? graph_step(ctx, flags & ~BD_RUN_GRAPH) : enqueue_step(ctx, flags & ~BD_RUN_GRAPH);
     if (rc) return rc;
     if (graph && lanczos) ctx->lz_timed = true;
-    for (int I = 0; I < ns; ++I) ctx->chans[I].state = lanczos ? ST_LANCZOS : ST_SIGMA;
+    for (int I = 0; I < ns; ++I) {
+        ctx->chans[I].state = lanczos ? ST_LANCZOS : ST_SIGMA;
+        ctx->chans[I].ref_sorted = lanczos && (flags & BD_RUN_REF_ORDER) && !(flags & BD_RUN_MIXED);
+    }
     ctx->last_lanczos_flags = flags;
     ctx->results_valid = true;
     return BD_OK;
@@ -2188,6 +2219,80 @@ int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_curr
     if (!ctx->results_valid) return fail(ctx, BD_ERR_STATE, "no results (run bd_run_all and bd_sync)");
     CU(cudaSetDevice(ctx->device));
     const int ns = ctx->nsubsh, NSP = ctx->nspb;
+    ctx->last_update_on_device = false;
+    if (!keep_current && max_frag > 0 && max_frag <= 32) {
+        // On the device when the truncated propagator keeps the current fragment counts
+        // (from the second iteration on, as a rule): the fragments are selected and
+        // written over the resident propagator in place, and the block plan, the pole
+        // counts and the chain schedules stay as they are -- nothing is planned again.
+        const int cap = max_frag;
+        int *dcnt = nullptr, *dsel = nullptr, *ddof = nullptr;
+        long long *doff = nullptr;
+        std::vector<int> dof(ns);
+        for (int I = 0; I < ns; ++I) dof[I] = ctx->chans[I].D;
+        CU(cudaMallocAsync(&dcnt, sizeof(int) * 2 * ns, ctx->st));
+        CU(cudaMallocAsync(&dsel, sizeof(int) * 2 * ns * cap, ctx->st));
+        CU(cudaMallocAsync(&ddof, sizeof(int) * ns, ctx->st));
+        CU(cudaMallocAsync(&doff, sizeof(long long) * ns, ctx->st));
+        CU(cudaMemcpyAsync(ddof, dof.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, ctx->st));
+        CU(cudaMemcpyAsync(doff, ctx->dy_sol_off.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice, ctx->st));
+        k_dressed_select<<<(unsigned)((2 * ns * 32 + 255) / 256), 256, 0, ctx->st>>>(
+            ctx->d_dysol, doff, ctx->d_dynq, ddof, ns, z_cut, max_frag, cap, dcnt, dsel);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+        std::vector<int> cnt(2 * ns);
+        CU(cudaMemcpyAsync(cnt.data(), dcnt, sizeof(int) * 2 * ns, cudaMemcpyDeviceToHost, ctx->st));
+        CU(cudaStreamSynchronize(ctx->st));
+        bool same = true;
+        for (int I = 0; I < ns; ++I) same = same && cnt[2 * I] == ctx->np[I] && cnt[2 * I + 1] == ctx->nh[I];
+        if (same) {
+            DevProblem &P = ctx->dp;
+            k_dressed_write<<<2 * ns, 128, 0, ctx->st>>>(ctx->d_dysol, doff, ctx->d_dynq, ddof, P.p_start, P.h_start, ns,
+                                                       NSP, cap, dcnt, dsel, const_cast<double *>(P.ep),
+                                                       const_cast<double *>(P.eh), const_cast<double *>(P.fqp),
+                                                       const_cast<double *>(P.fqh));
+            CU(cudaGetLastError());
+            ctx->launches += 1;
+            // the new energies back to the host copies: the Fermi energies and the difference
+            // between the two propagators follow from them as on the host path
+            std::vector<double> ep(ctx->ep.size()), eh(ctx->eh.size());
+            if (!ep.empty()) CU(cudaMemcpyAsync(ep.data(), P.ep, sizeof(double) * ep.size(), cudaMemcpyDeviceToHost, ctx->st));
+            if (!eh.empty()) CU(cudaMemcpyAsync(eh.data(), P.eh, sizeof(double) * eh.size(), cudaMemcpyDeviceToHost, ctx->st));
+            CU(cudaStreamSynchronize(ctx->st));
+            if (diff) {
+                double d = 0.0;
+                for (size_t i = 0; i < ep.size(); ++i) d += std::fabs(ep[i] - ctx->ep[i]);
+                for (size_t i = 0; i < eh.size(); ++i) d += std::fabs(eh[i] - ctx->eh[i]);
+                *diff = d;
+            }
+            ctx->ep.swap(ep);
+            ctx->eh.swap(eh);
+            std::vector<double> ef(ns);
+            for (int I = 0; I < ns; ++I) ef[I] = ctx->chans[I].efermi = seek_efermi(ctx, I);
+            CU(cudaMemcpyAsync(ctx->d_efermi, ef.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, ctx->st));
+            if (np_out) std::memcpy(np_out, ctx->np.data(), sizeof(int) * ns);
+            if (nh_out) std::memcpy(nh_out, ctx->nh.data(), sizeof(int) * ns);
+            int rc = BD_OK;
+            if ((ep_out && cap_p < (int)ctx->ep.size()) || (eh_out && cap_h < (int)ctx->eh.size()))
+                rc = fail(ctx, BD_ERR_CAPACITY, "propagator buffers hold %d / %d fragments, %zu / %zu needed", cap_p,
+                          cap_h, ctx->ep.size(), ctx->eh.size());
+            else {
+                if (ep_out && !ctx->ep.empty()) std::memcpy(ep_out, ctx->ep.data(), sizeof(double) * ctx->ep.size());
+                if (eh_out && !ctx->eh.empty()) std::memcpy(eh_out, ctx->eh.data(), sizeof(double) * ctx->eh.size());
+                if (fqp_out && !ctx->ep.empty())
+                    CU(cudaMemcpyAsync(fqp_out, P.fqp, sizeof(double) * ctx->ep.size() * NSP, cudaMemcpyDeviceToHost, ctx->st));
+                if (fqh_out && !ctx->eh.empty())
+                    CU(cudaMemcpyAsync(fqh_out, P.fqh, sizeof(double) * ctx->eh.size() * NSP, cudaMemcpyDeviceToHost, ctx->st));
+            }
+            for (void *q : {(void *)dcnt, (void *)dsel, (void *)ddof, (void *)doff}) CU(cudaFreeAsync(q, ctx->st));
+            CU(cudaStreamSynchronize(ctx->st));
+            ctx->results_valid = false;
+            for (int I = 0; I < ns; ++I) ctx->chans[I].state = ST_NONE;
+            ctx->last_update_on_device = true;
+            return rc;
+        }
+        for (void *q : {(void *)dcnt, (void *)dsel, (void *)ddof, (void *)doff}) CU(cudaFreeAsync(q, ctx->st));
+    }
     std::vector<int> np(ns, 0), nh(ns, 0);
     std::vector<double> ep, eh, fqp, fqh;
     std::vector<double> rows;
@@ -2253,6 +2358,7 @@ int bd_last_timings(bd_ctx *ctx, double *ms5) {
 /* Not part of the public header: number of Lanczos steps that took a second
  * reorthogonalisation sweep in the last bd_run_all, and tuning knobs. */
 int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
+int bd_dressed_on_device(bd_ctx *ctx) { return ctx ? (ctx->last_update_on_device ? 1 : 0) : -1; }
 double bd_lanczos_kernel_ms(bd_ctx *ctx) { return ctx ? ctx->lz_kernel_ms : -1.0; }
 long long bd_launch_count(bd_ctx *ctx) { return ctx ? ctx->launches : -1; }
 int bd_lanczos_stored(bd_ctx *ctx, int *stored) {

@@ -138,6 +138,8 @@ struct DyJob {
     const double *sighf;     // [D][D] static self-energy
     const double *sig1b;     // [D][D]
     double efermi;
+    const double *efp;       // the Fermi energy in device memory (it follows device-side updates
+                             // of the propagator), or nullptr: efermi
     double *A;               // [n][n] scratch (row-major)
     double *d, *e, *tau;     // [n] tridiagonal diagonal, off-diagonal, reflector scalars
     int *blk;                // [2n] first and last position of each position's tridiagonal block

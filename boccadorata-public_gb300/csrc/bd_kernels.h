@@ -51,6 +51,11 @@ __global__ void k_vpp_place(const unsigned long long *key, const unsigned *val, 
 cudaError_t launch_pole_radix(const double *E, const int *seg_of, int ch_lo, int nseg, long long n0, long long n,
                               bool desc, unsigned long long *k0, unsigned *v0, unsigned long long *k1, unsigned *v1,
                               void *scratch, int *perm, int *launches, cudaStream_t st);
+__global__ void k_dressed_select(const double *sol, const long long *sol_off, const int *nq, const int *D_of, int ns,
+                                 double z_cut, int max_frag, int cap, int *cnt, int *sel);
+__global__ void k_dressed_write(const double *sol, const long long *sol_off, const int *nq, const int *D_of,
+                                const int *p_start, const int *h_start, int ns, int nspb, int cap, const int *cnt,
+                                const int *sel, double *ep, double *eh, double *fqp, double *fqh);
 cudaError_t launch_nonfinite(const double *x, long long n, int *bad, cudaStream_t st);
 constexpr int kHeapMax = 49152;  // longest channel put in the reference's heap-sort order
 cudaError_t launch_heap_order(const double *E, const int *d_off, int nseg, int max_len, long long n0, int *perm,

@@ -477,7 +477,8 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
     if (threadIdx.x == 0) nbelow = 0;
     __syncthreads();
     int c = 0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) c += !(st[(size_t)k * NS] > J.efermi);
+    const double ef = J.efp ? *J.efp : J.efermi;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) c += !(st[(size_t)k * NS] > ef);
     atomicAdd(&nbelow, c);
     __syncthreads();
     const int nqh = nbelow, nqp = n - nbelow;

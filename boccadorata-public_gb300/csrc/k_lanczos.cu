@@ -93,6 +93,24 @@ template <> struct LzSum<float> {
     static __device__ __forceinline__ double value(T x) { return dfm::to_double(x); }
 };
 
+// A thread's partial sum of many terms.  Plain: in the arithmetic type.  Compensated
+// (FP32 vectors on long chains, whose slices hold tens of thousands of poles): in
+// double-float, each term (or chunk of four FP32 products) added exactly, so a partial
+// over hundreds of terms keeps FP64-class accuracy; then the warp combines the pairs.
+// Long chains stream their bases from HBM, so the FP32 pipe has the room.
+template <typename CT, bool kComp> struct PSum {
+    using A = CT;
+    static __device__ __forceinline__ A zero() { return (CT)0; }
+    static __device__ __forceinline__ void add(A &a, CT x) { a += x; }
+    static __device__ __forceinline__ typename LzSum<CT>::T finish(A a) { return LzSum<CT>::from_ct(warp_sum_ct(a)); }
+};
+template <> struct PSum<float, true> {
+    using A = dfm::df;
+    static __device__ __forceinline__ A zero() { return A{0.0f, 0.0f}; }
+    static __device__ __forceinline__ void add(A &a, float x) { a = dfm::add(a, A{x, 0.0f}); }
+    static __device__ __forceinline__ A finish(A a) { return dfm::warp_sum(a); }
+};
+
 // Fixed pairwise sums: three (four) dependent adds instead of seven (fifteen).
 template <class Sum>
 __device__ inline typename Sum::T tree_sum8(const typename Sum::T *x) {
@@ -168,6 +186,9 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     using CT = typename LzTraits<VT>::CT;
     using Sum = LzSum<CT>;
     using ST = typename Sum::T;
+    constexpr bool kComp = kGlobalSlices && sizeof(VT) == 4;   // compensated partial sums
+    using PS = PSum<CT, kComp>;
+    using PA = typename PS::A;
     constexpr int VW = Vec16<VT>::n;
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
@@ -201,12 +222,19 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         w = Es + S;
         touched = reinterpret_cast<unsigned char *>(w + S);
     }
-    // the basis cache behind the slices
+    // this CTA's slice of the couplings M (CT, [d][S]) behind the slices, then the basis cache
+    CT *Msl = nullptr;
+    if constexpr (!kGlobalSlices) {
+        const uintptr_t mb = (reinterpret_cast<uintptr_t>(touched + S) + 15) & ~static_cast<uintptr_t>(15);
+        const uintptr_t me = mb + sizeof(CT) * (size_t)D * S;
+        if (me <= reinterpret_cast<uintptr_t>(sm) + static_cast<uintptr_t>(smem_bytes)) Msl = reinterpret_cast<CT *>(mb);
+    }
     VT *cache;
     int ccap;
     {
         const char *end = kGlobalSlices ? reinterpret_cast<const char *>(cf + (rmax + 3) / 4 * 4)
-                                        : reinterpret_cast<const char *>(touched + S);
+                                        : (Msl ? reinterpret_cast<const char *>(Msl + (size_t)D * S)
+                                               : reinterpret_cast<const char *>(touched + S));
         const uintptr_t e = (reinterpret_cast<uintptr_t>(end) + 15) & ~static_cast<uintptr_t>(15);
         const uintptr_t lim = reinterpret_cast<uintptr_t>(sm) + static_cast<uintptr_t>(smem_bytes);
         cache = reinterpret_cast<VT *>(e);
@@ -221,6 +249,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int lt[16];       // vectors of a local pass
     __shared__ int s_nl;
     __shared__ int lslot[8];     // slots of the earlier chains' last vectors (-1: deflated)
+    __shared__ int s_start[10], s_last[10];   // the chain schedule (read every step: kept on chip)
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
@@ -228,6 +257,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     const CT *Mc = reinterpret_cast<const CT *>(sizeof(CT) == 4 ? static_cast<const void *>(C.Mf)
                                                                   : static_cast<const void *>(C.M));
     for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? (CT)C.E[i0 + i] : (CT)0; touched[i] = 0; }
+    if (Msl)
+        for (int q = tid; q < D * S; q += kLzThreads) {
+            const int d = q / S, i = q - d * S;
+            Msl[q] = (i < ns) ? Mc[(size_t)d * N + i0 + i] : (CT)0;
+        }
+    if (tid <= C.n_used && tid < 10) s_start[tid] = C.start[tid];
+    if (tid < C.n_used && tid < 10) s_last[tid] = C.last[tid];
+    __syncthreads();   // the schedule is read at the top of the first step, before its barrier
     const double tau = (sizeof(VT) == 4) ? 1e-22 : 1e-48;
     // Exhausted Krylov space: the squared residual after the sweeps at rounding level
     // relative to its value before them.  The chain's remaining rows then continue with
@@ -289,28 +326,53 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 const int t = t0 + u * kLzWarps;
                 vp[u] = vslice(t < nl ? (loc ? lt[t] : t) : (loc ? lt[t0] : t0));
             }
-            CT acc[4] = {0, 0, 0, 0};
+            if constexpr (kComp) {   // each 16-byte group's four products, then exactly into the pair
+                PA acc[4] = {PS::zero(), PS::zero(), PS::zero(), PS::zero()};
 #pragma unroll 2
-            for (int q = lane; q < nv; q += 32) {
-                VT x[4][VW];
+                for (int q = lane; q < nv; q += 32) {
+                    VT x[4][VW];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
+                    for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < 4; ++u) {
+                        CT g = (CT)0;
 #pragma unroll
-                    for (int e = 0; e < VW; ++e) acc[u] += x[u][e] * w[q * VW + e];
-            }
+                        for (int e = 0; e < VW; ++e) g += x[u][e] * w[q * VW + e];
+                        PS::add(acc[u], g);
+                    }
+                }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                acc[u] = warp_sum_ct(acc[u]);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
-                const int t = t0 + u * kLzWarps;
-                if (lane == 0 && t < nl) Sum::put(Ap + t, Sum::from_ct(acc[u]));
+                for (int u = 0; u < 4; ++u) {
+                    const ST r = PS::finish(acc[u]);
+                    const int t = t0 + u * kLzWarps;
+                    if (lane == 0 && t < nl) Sum::put(Ap + t, r);
+                }
+            } else {
+                CT acc[4] = {0, 0, 0, 0};
+#pragma unroll 2
+                for (int q = lane; q < nv; q += 32) {
+                    VT x[4][VW];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int e = 0; e < VW; ++e) acc[u] += x[u][e] * w[q * VW + e];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    acc[u] = warp_sum_ct(acc[u]);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
+                    const int t = t0 + u * kLzWarps;
+                    if (lane == 0 && t < nl) Sum::put(Ap + t, Sum::from_ct(acc[u]));
+                }
             }
         }
-        CT nwp = 0;
-        for (int i = tid; i < S; i += kLzThreads) nwp += w[i] * w[i];
-        nwp = warp_sum_ct(nwp);
-        if (lane == 0) Sum::put(red + warp * kMaxScal, Sum::from_ct(nwp));
+        PA nwp = PS::zero();
+        for (int i = tid; i < S; i += kLzThreads) PS::add(nwp, w[i] * w[i]);
+        {
+            const ST r = PS::finish(nwp);
+            if (lane == 0) Sum::put(red + warp * kMaxScal, r);
+        }
         __syncthreads();
         if (tid == 0) {
             ST x[kLzWarps];
@@ -376,47 +438,47 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // back only the groups it updated, so no barrier separates this from the update.
     // When another sweep follows, these sums are simply recomputed.
     auto scalar_pass = [&](int nq) {
-        CT pn = 0, sa = 0, se = 0, sm_[8], sg[8];
+        PA pn = PS::zero(), sa = PS::zero(), se = PS::zero(), sm_[8], sg[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { sm_[q] = 0; sg[q] = 0; }
+        for (int q = 0; q < 8; ++q) { sm_[q] = PS::zero(); sg[q] = PS::zero(); }
         for (int q = tid; q < nv; q += kLzThreads) {
 #pragma unroll
             for (int u = 0; u < VW; ++u) {
                 const int i = q * VW + u;
                 const CT wi = w[i];
-                pn += wi * wi;
+                PS::add(pn, wi * wi);
                 if (i < ns) {
                     const CT e = Es[i];
-                    sa += e * wi * wi;
-                    se += e * e * wi * wi;
+                    PS::add(sa, e * wi * wi);
+                    PS::add(se, e * e * wi * wi);
 #pragma unroll
                     for (int d = 0; d < 8; ++d)
-                        if (d < D) sm_[d] += Mc[(size_t)d * N + i0 + i] * wi;
+                        if (d < D) PS::add(sm_[d], (Msl ? Msl[d * S + i] : Mc[(size_t)d * N + i0 + i]) * wi);
 #pragma unroll
                     for (int g = 0; g < 8; ++g)
-                        if (g < nq && lslot[g] >= 0) sg[g] += e * (CT)vslice(lslot[g])[i] * wi;
+                        if (g < nq && lslot[g] >= 0) PS::add(sg[g], e * (CT)vslice(lslot[g])[i] * wi);
                 }
             }
         }
-        pn = warp_sum_ct(pn);
-        sa = warp_sum_ct(sa);
-        se = warp_sum_ct(se);
-        if (lane == 0) {
-            Sum::put(red + warp * kMaxScal, Sum::from_ct(pn));
-            Sum::put(red + warp * kMaxScal + 1, Sum::from_ct(sa));
-            Sum::put(red + warp * kMaxScal + 2 + D + nq, Sum::from_ct(se));
+        {
+            const ST a = PS::finish(pn), b = PS::finish(sa), c2 = PS::finish(se);
+            if (lane == 0) {
+                Sum::put(red + warp * kMaxScal, a);
+                Sum::put(red + warp * kMaxScal + 1, b);
+                Sum::put(red + warp * kMaxScal + 2 + D + nq, c2);
+            }
         }
 #pragma unroll
         for (int d = 0; d < 8; ++d)
             if (d < D) {
-                const CT x = warp_sum_ct(sm_[d]);
-                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + d, Sum::from_ct(x));
+                const ST x = PS::finish(sm_[d]);
+                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + d, x);
             }
 #pragma unroll
         for (int g = 0; g < 8; ++g)
             if (g < nq) {
-                const CT x = warp_sum_ct(sg[g]);
-                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + D + g, Sum::from_ct(x));
+                const ST x = PS::finish(sg[g]);
+                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + D + g, x);
             }
         __syncthreads();
         const int nsc = 3 + D + nq;   // |w|^2, <w|E|w>, m_d, g_q, |E w|^2
@@ -435,7 +497,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     int extra = 0;        // sweeps beyond the first
     bool prow_ok = false; // prow holds row j - 1, a vector this chain built (identical in every CTA)
     for (int j = 0; j < L; ++j) {
-        const bool newv = (k + 1 < C.n_used) && (j == C.start[k + 1]);
+        const bool newv = (k + 1 < C.n_used) && (j == s_start[k + 1]);
         if (newv) { ++k; tail = false; }
         __syncthreads();
         if (tail) {
@@ -443,7 +505,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             // dcur, dcur + 1, ... (the last group's energy once none is left), as
             // deflated_row would one at a time; each thread places rows by binary search
             // in the cumulative counts.
-            const int jend = (k + 1 < C.n_used) ? min(L, (int)C.start[k + 1]) : L;
+            const int jend = (k + 1 < C.n_used) ? min(L, s_start[k + 1]) : L;
             const int R = jend - j;
             for (int r = tid; r < R; r += kLzThreads) {
                 const int d = dcur + r;
@@ -461,7 +523,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             continue;
         }
         const int nq = k;   // earlier pivot chains
-        if (tid < nq) lslot[tid] = rowslot[C.last[tid]];
+        if (tid < nq) lslot[tid] = rowslot[s_last[tid]];
         // A continuing step's E v_{j-1} has large components only on v_{j-1}, v_{j-2} and
         // the last vector of every earlier chain, with the coefficients row j - 1 already
         // holds: <v_{j-1}|E|v_{j-1}> = alpha_{j-1}, <v_{j-2}|E|v_{j-1}> = beta_{j-1} (the
@@ -485,7 +547,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 lt[n] = rowslot[j - 1]; lc[n++] = prow[0];
                 if (j >= 2 && rowslot[j - 2] >= 0) { lt[n] = rowslot[j - 2]; lc[n++] = prow[1]; }
                 for (int q = 0; q < k; ++q)
-                    if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) { lt[n] = rowslot[C.last[q]]; lc[n++] = prow[2 + q]; }
+                    if (s_last[q] < j - 2 && rowslot[s_last[q]] >= 0) { lt[n] = rowslot[s_last[q]]; lc[n++] = prow[2 + q]; }
                 s_nl = n;
             }
             __syncthreads();
@@ -515,7 +577,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 lt[n++] = rowslot[j - 1];
                 if (j >= 2 && rowslot[j - 2] >= 0) lt[n++] = rowslot[j - 2];
                 for (int q = 0; q < k; ++q)
-                    if (C.last[q] < j - 2 && rowslot[C.last[q]] >= 0) lt[n++] = rowslot[C.last[q]];
+                    if (s_last[q] < j - 2 && rowslot[s_last[q]] >= 0) lt[n++] = rowslot[s_last[q]];
                 s_nl = n;
             }
             __syncthreads();

@@ -659,6 +659,91 @@ cudaError_t launch_pole_radix(const double *E, const int *seg_of, int ch_lo, int
     return cudaGetLastError();
 }
 
+// The next iteration's propagator on the device (bd_dressed_propagator): one warp per
+// (subshell, side) picks, of that channel's Dyson solutions (rows [W, Z, x..]: the
+// quasiparticles, then the quasiholes, each by descending W), those with Z >= z_cut, at
+// most max_frag of them (max_frag <= 0: all) by largest Z, ties to the earlier row, and
+// lists them in row order: cnt[2 I + side], sel[(2 I + side) * cap + r].
+__global__ void k_dressed_select(const double *sol, const long long *sol_off, const int *nq, const int *D_of, int ns,
+                                 double z_cut, int max_frag, int cap, int *cnt, int *sel) {
+    const int wg = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (wg >= 2 * ns) return;
+    const int I = wg >> 1, side = wg & 1, NS = 2 + D_of[I];
+    const int n = nq[2 * I + side];
+    const double *rows = sol + sol_off[I] + (side ? (size_t)nq[2 * I] * NS : 0);
+    int *out = sel + (size_t)wg * cap;
+    int m = 0;   // candidates
+    for (int b = 0; b < n; b += 32) {
+        const int k = b + lane;
+        const bool c = k < n && rows[(size_t)k * NS + 1] >= z_cut;
+        const unsigned bal = __ballot_sync(0xffffffffu, c);
+        if (max_frag <= 0 && c) {
+            const int r = m + __popc(bal & ((1u << lane) - 1u));
+            if (r < cap) out[r] = k;
+        }
+        m += __popc(bal);
+    }
+    if (max_frag <= 0 || m <= max_frag) {
+        if (max_frag > 0)   // every candidate, in row order
+            for (int b = 0, r = 0; b < n; b += 32) {
+                const int k = b + lane;
+                const bool c = k < n && rows[(size_t)k * NS + 1] >= z_cut;
+                const unsigned bal = __ballot_sync(0xffffffffu, c);
+                if (c && r + __popc(bal & ((1u << lane) - 1u)) < cap) out[r + __popc(bal & ((1u << lane) - 1u))] = k;
+                r += __popc(bal);
+            }
+        if (lane == 0) cnt[wg] = m;
+        return;
+    }
+    // the max_frag largest Z (ties: the earlier row), one warp argmax at a time
+    int taken[32];
+    for (int t = 0; t < max_frag && t < 32; ++t) {
+        double bz = -1.0;
+        int bk = INT_MAX;
+        for (int k = lane; k < n; k += 32) {
+            const double z = rows[(size_t)k * NS + 1];
+            bool used = false;
+            for (int u = 0; u < t; ++u) used |= (taken[u] == k);
+            if (!used && z >= z_cut && (z > bz || (z == bz && k < bk))) { bz = z; bk = k; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double oz = __shfl_xor_sync(0xffffffffu, bz, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (oz > bz || (oz == bz && ok < bk)) { bz = oz; bk = ok; }
+        }
+        taken[t] = bk;
+    }
+    if (lane == 0) {
+        const int k = max_frag < 32 ? max_frag : 32;
+        for (int a = 1; a < k; ++a)   // back to row order (descending W, as add_qp / add_qh store them)
+            for (int b = a; b > 0 && taken[b - 1] > taken[b]; --b) { const int t = taken[b]; taken[b] = taken[b - 1]; taken[b - 1] = t; }
+        for (int r = 0; r < k && r < cap; ++r) out[r] = taken[r];
+        cnt[wg] = k;
+    }
+}
+
+// The selected solutions written over the propagator in place (the fragment counts are
+// the current ones): energies, amplitudes x_0..x_{D-1}, zeros up to nspb.
+__global__ void k_dressed_write(const double *sol, const long long *sol_off, const int *nq, const int *D_of,
+                                const int *p_start, const int *h_start, int ns, int nspb, int cap, const int *cnt,
+                                const int *sel, double *ep, double *eh, double *fqp, double *fqh) {
+    const int wg = blockIdx.x;   // (subshell, side)
+    if (wg >= 2 * ns) return;
+    const int I = wg >> 1, side = wg & 1, D = D_of[I], NS = 2 + D;
+    const double *rows = sol + sol_off[I] + (side ? (size_t)nq[2 * I] * NS : 0);
+    const int m = cnt[wg];
+    const int base = side ? h_start[I] : p_start[I];
+    double *E = side ? eh : ep;
+    double *F = side ? fqh : fqp;
+    for (int t = threadIdx.x; t < m * nspb; t += blockDim.x) {
+        const int r = t / nspb, q = t - r * nspb;
+        const double *row = rows + (size_t)sel[(size_t)wg * cap + r] * NS;
+        F[(size_t)(base + r) * nspb + q] = q < D ? row[2 + q] : 0.0;
+        if (q == 0) E[base + r] = row[0];
+    }
+}
+
 // Finiteness of n doubles: bad receives 1 + the index of a non-finite one (any, when
 // there are several), and stays as it was when all are finite.
 __global__ void k_nonfinite(const double *x, long long n, int *bad) {

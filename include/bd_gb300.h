@@ -49,8 +49,9 @@ extern "C" {
 #define BD_RUN_LANCZOS   1   /* Lanczos-reduce Sigma(2) before Dyson (else full Dyson)  */
 #define BD_RUN_MIXED     2   /* FP32 Lanczos vectors / reorthogonalisation              */
 #define BD_RUN_PER_CHANNEL 4 /* launch channel by channel (the drop-in call pattern)   */
-#define BD_RUN_STABLE_SORT 8 /* FP64: equal pole energies in their build order instead of
-                                the reference's heap-sort order (the FP32 form always is) */
+#define BD_RUN_REF_ORDER   8 /* FP64: the reduction visits equal pole energies in the
+                                reference's heap-sort order (k_heap_order, a serial chain
+                                per channel: slower) instead of their build order */
 #define BD_RUN_GRAPH     16  /* batched: capture the step in a CUDA graph on first use (per
                                 flag combination) and replay it; any change of the problem,
                                 the pivots or the tuning captures it again */
@@ -124,21 +125,21 @@ int bd_sigma2_build(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, int *n_fw,
  * the pole count (as the reference does).  Output rows have (n_pvt + 1) + D
  * doubles [alpha, beta, g_0 .., m_0 .. m_{D-1}]; ipiv_* receive
  * [n_used_pivots, 1, start_1, ...] and must hold n_pvt + 1 + D ints.
- * flags: 0 = FP64 (poles sorted as the reference sorts them, bd_sigma2_sorted),
- * BD_RUN_MIXED = FP32 vectors, BD_RUN_STABLE_SORT = FP64 with the build order kept
- * among equal energies. */
+ * flags: 0 = FP64, BD_RUN_MIXED = FP32 vectors, BD_RUN_REF_ORDER = FP64 visiting
+ * equal energies in the reference's heap-sort order (the order of equal energies
+ * changes only rounding: the Krylov space does not depend on it). */
 int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_itr_fw, int *n_itr_bk,
                       double *lz_fw, int cap_fw, int *L_fw, int *ipiv_fw,
                       double *lz_bk, int cap_bk, int *L_bk, int *ipiv_bk, int flags);
 
-/* Rows [E, sum_d M_d^2, M_0 .. M_{D-1}] of channel ish's resident Sigma(2) in the order
- * the last Lanczos reduction visited them: the reference sorts the self-energy's poles
- * in place before reducing them (Reduce_SelfEn_Lncz, source/BcDor-Self_energy_ext_Op_e.cpp:
- * 116-130; forward ascending, backward descending, by the heap sorts of
- * source/BcDor-Utilities.cpp:25-94).  The FP64 form reproduces that order, equal
- * energies included, for channels of up to 49 152 poles; the FP32 form (and longer
- * channels) keeps equal energies in their build order.  Capacities in rows; either
- * buffer may be NULL.  BD_ERR_STATE before any reduction of the channel. */
+/* Rows [E, sum_d M_d^2, M_0 .. M_{D-1}] of channel ish's resident Sigma(2) as the
+ * reference leaves them sorted in place before reducing them (Reduce_SelfEn_Lncz,
+ * source/BcDor-Self_energy_ext_Op_e.cpp:116-130; forward ascending, backward descending,
+ * by the heap sorts of source/BcDor-Utilities.cpp:25-94), equal energies in the heap
+ * sort's order, for channels of up to 49 152 poles (longer ones: in their build order).
+ * The order is formed on the device on demand (unless the last reduction of the channel
+ * already visited it, BD_RUN_REF_ORDER).  Capacities in rows; either buffer may be
+ * NULL.  BD_ERR_STATE before any reduction of the channel. */
 int bd_sigma2_sorted(bd_ctx *ctx, int ish, double *sig_fw, int cap_fw, double *sig_bk, int cap_bk);
 
 /* Dyson eigensolve of channel ish with the most recent resident self-energy
@@ -204,6 +205,11 @@ int bd_upload_propagator(bd_ctx *ctx, const bd_propagator *prop);
 int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_current, int *np_out, int *nh_out,
                           double *ep_out, int cap_p, double *eh_out, int cap_h, double *fqp_out, double *fqh_out,
                           double *diff);
+/* 1 when the last bd_dressed_propagator updated the resident propagator on the device:
+ * with 0 < max_frag <= 32 and the truncated propagator keeping the current fragment counts
+ * of every subshell, the fragments are selected and written in place and the block
+ * plan, pole counts and chain schedules stay (no host planning); otherwise 0. */
+int bd_dressed_on_device(bd_ctx *ctx);
 /* Device time of the phases of the last bd_run_all in ms: sigma2, sort, lanczos, dyson, total. */
 int bd_last_timings(bd_ctx *ctx, double *ms5);
 /* Diagnostics: extra reorthogonalisation sweeps of the last bd_run_all; device time of

@@ -199,9 +199,11 @@ def test_graph_replay_equals_stream_launches(bdmod, problems, mixed):
     assert ctx.launch_count() - l0 >= 3 * 20          # every replay counts its kernels
     ctx.set_tuning(lz_cluster=4)                      # a new tuning: captured again
     ctx.run_all(lanczos=True, mixed=mixed, graph=True)
+    # four CTAs per chain sum the FP32 partials in another order: the energies move by
+    # up to ~1e-7 relative, so strength is compared over the mixed form's energy window
     for a, b in zip(want, ctx.results_all()):
         for tag in ("qp", "qh"):
-            e, z = strong_diffs(a[tag], b[tag], zmin=1e-4)
+            e, z = strong_diffs(a[tag], b[tag], zmin=1e-4, etol=1e-5 if mixed else 1e-7)
             assert e < (1e-5 if mixed else 1e-10) and z < (1e-5 if mixed else 1e-10)
     ctx.close()
 

@@ -165,3 +165,32 @@ def test_second_iteration_n_max_6_long_chains(problems, bdmod):
             assert np.isfinite(res[True][ish][tag]).all() and np.isfinite(res[False][ish][tag]).all()
             e, z = strong_diffs(res[False][ish][tag], res[True][ish][tag], zmin=1e-2, etol=1e-5)
             assert e * 300.0 < 1e-3 and z < 1e-4, (ish, tag, e, z)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_device_update_equals_host_update(problems, bdmod, graph):
+    """The propagator update on the device (fragment counts unchanged: selection and write
+    in place, the Fermi energies in device memory, nothing planned again) gives the host
+    update's propagator and the same next iterations, bit for bit -- also when every
+    iteration replays the one captured step graph."""
+    p = problems(4, 20.0, 0, 20)
+    host = bdmod.Context().upload(p)
+    dev = bdmod.Context().upload(p)
+    on_device = 0
+    for it in range(4):
+        host.run_all(lanczos=True, mixed=True)
+        dev.run_all(lanczos=True, mixed=True, graph=graph)
+        assert np.array_equal(host.koltun_all(), dev.koltun_all()), it
+        for ish in range(p.ms.nsubsh):
+            a, b = host.result(ish), dev.result(ish)
+            for tag in ("qp", "qh"):
+                assert np.array_equal(a[tag], b[tag]), (it, ish, tag)
+        ph, dh = host.dressed_propagator(1e-3, 2, keep_current=True)
+        host.upload_propagator(ph)
+        pd, dd = dev.dressed_propagator(1e-3, 2)
+        on_device += dev.dressed_on_device()
+        assert dd == dh, it
+        for k in ("np_", "nh", "ep", "eh", "fqp", "fqh"):
+            assert np.array_equal(getattr(ph, k), getattr(pd, k)), (it, k)
+    assert on_device >= 2
+    host.close(); dev.close()

@@ -10,9 +10,12 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def _poles(rows):
-    """Energies [N] and couplings [D][N] of rows already in the order the chain visits."""
-    return np.ascontiguousarray(rows[:, 0]), np.ascontiguousarray(rows[:, 2:].T)
+def _sorted_poles(rows, descending):
+    """The order bd_lanczos_reduce visits by default: stable by energy, ascending (forward)
+    or descending (backward)."""
+    E = rows[:, 0]
+    order = np.argsort(-E if descending else E, kind="stable")
+    return E[order].copy(), np.ascontiguousarray(rows[order, 2:].T)
 
 
 @pytest.mark.parametrize("mixed,tol", [(False, 1e-10), (True, 1e-5)])
@@ -23,14 +26,13 @@ def test_noalloc_matches_lanczos_reduce(bdmod, problems, mixed, tol):
     pv = p.piv
     cases = []
     for ish in (0, 12, 0):
-        ctx.sigma2_build(ish, copy=False)
+        fw, bk = ctx.sigma2_build(ish)
         want = ctx.lanczos_reduce(ish, pv.vec[ish], pv.n_fw[ish], pv.n_bk[ish], mixed=mixed)
-        fw, bk = ctx.sigma2_sorted(ish)     # the poles in the order that reduction visited them
         for d, rows, tag, ip, nit in ((0, fw, "lz_fw", "ipiv_fw", pv.n_fw[ish]),
                                       (1, bk, "lz_bk", "ipiv_bk", pv.n_bk[ish])):
             cases.append((ish, d, rows, want[tag], want[ip], nit))
     for ish, d, rows, ref, ref_ipiv, nit in cases:
-        E, M = _poles(rows)
+        E, M = _sorted_poles(rows, descending=(d == 1))
         D = M.shape[0]
         N = len(E)
         tE = torch.from_numpy(E).to(dev)
