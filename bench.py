@@ -60,6 +60,10 @@ def parse():
                     help="skip the N_max=12 precision run and the dressed second iteration")
     ap.add_argument("--profile", choices=["mixed", "fp64", "fp64-per-channel"], default=None,
                     help="run only this form's warm-up and timed steps (for ncu); prints its timings, not a bench line")
+    ap.add_argument("--many", action="store_true",
+                    help="the batched many-instance run (independent problems, iterated); prints its own line")
+    ap.add_argument("--problems", type=int, default=256)
+    ap.add_argument("--iterations", type=int, default=10)
     return ap.parse_args()
 
 
@@ -569,10 +573,106 @@ def gpu_arm(args):
     return 0
 
 
+def many_problems(args):
+    """The batched many-instance run: independent synthetic problems from seeds 100 on,
+    each with N_max drawn from {4, 6, 8, 10}, hw uniform in [10, 30] MeV and interaction
+    scale sigma uniform in [1, 3] MeV (8p+8n closed shells, 50 Lanczos iterations per
+    pivot), each iterated `iterations` times: run the whole chain, then the next
+    propagator from the Dyson solutions (z_cut 1e-3, at most one fragment per subshell
+    and side: the truncation that keeps the dressed pole spaces of N_max = 10 inside
+    minutes), Sigma(2) rebuilt from it.  Every step replays the context's captured graph;
+    from the second update on the propagator is updated on the device when the fragment
+    counts stay.  Problem generation (host numpy) is outside the timed region; the upload
+    of each problem is inside it.
+
+    Accuracy against FP64: the first iteration (both forms on the same input) measures
+    the mixed form's precision; the last iteration compares two trajectories, and the
+    truncated update (the strongest solution of each subshell and side) is a discontinuous
+    choice between nearly equal strengths, so small differences can send the trajectories
+    apart.  A second FP64 run with another reduction order (Lanczos clusters of 16 CTAs)
+    measures that sensitivity of the iteration itself."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    bd = importlib.import_module("boccadorata-public_gb300.bd")
+    synth = importlib.import_module("boccadorata-public_gb300.synth")
+    z_cut, max_frag, n_itr = 1e-3, 1, 50
+    times = {"mixed": [], "fp64": []}
+    acc = {k: ([], [], []) for k in ("first_mixed_vs_fp64", "last_mixed_vs_fp64", "last_fp64_vs_fp64_cl16")}
+    device_updates, sizes = 0, []
+    for i in range(args.problems):
+        seed = 100 + i
+        r = np.random.default_rng(seed)
+        nmax = int(r.choice([4, 6, 8, 10]))
+        hw = float(r.uniform(10.0, 30.0))
+        sigma = float(r.uniform(1.0, 3.0))
+        prob = synth.make_problem(nmax, hw, seed, n_itr, sigma)
+        res = {}
+        for form, mixed, cl in (("fp64", False, 8), ("mixed", True, 8), ("fp64_cl16", False, 16)):
+            t0 = time.perf_counter()
+            ctx = bd.Context(local).upload(prob)
+            if cl != 8:
+                ctx.set_tuning(lz_cluster=cl)
+            dev_ms = 0.0
+            first = None
+            for it in range(args.iterations):
+                ctx.run_all(lanczos=True, mixed=mixed, graph=True)
+                dev_ms += ctx.timings()["total"]
+                if it == 0:
+                    first = (ctx.results_all(), ctx.koltun_all())
+                if it + 1 < args.iterations:
+                    ctx.dressed_propagator(z_cut, max_frag)
+                    if mixed:
+                        device_updates += int(ctx.dressed_on_device())
+            last = (ctx.results_all(), ctx.koltun_all())
+            ctx.close()
+            if form in times:
+                times[form].append((time.perf_counter() - t0, dev_ms))
+            res[form] = (first, last)
+        for key, (a, b) in (("first_mixed_vs_fp64", (res["fp64"][0], res["mixed"][0])),
+                            ("last_mixed_vs_fp64", (res["fp64"][1], res["mixed"][1])),
+                            ("last_fp64_vs_fp64_cl16", (res["fp64"][1], res["fp64_cl16"][1]))):
+            (ra, ka), (rb, kb) = a, b
+            for x, y in zip(ra, rb):
+                w, z = solution_errors(x, y, 1e-2)
+                acc[key][0].extend(w)
+                acc[key][1].extend(z)
+            ea = float(((ka[:, 0] + ka[:, 1]) / 2).sum())
+            eb = float(((kb[:, 0] + kb[:, 1]) / 2).sum())
+            acc[key][2].append(abs(eb - ea) / max(abs(ea), 1e-30))
+        sizes.append(nmax)
+        sys.stderr.write(f"problem {i} seed {seed} N_max {nmax}: fp64 {times['fp64'][-1][0]:.2f} s, "
+                         f"mixed {times['mixed'][-1][0]:.2f} s\n")
+    st = lambda q: {"max": float(np.max(q)) if len(q) else 0.0, "p99": float(np.percentile(q, 99)) if len(q) else 0.0,
+                    "median": float(np.median(q)) if len(q) else 0.0}
+    errors = {k: {"solutions_z_above_0.01": len(w), "qp_energy_keV": st(np.array(w) * 1e3),
+                  "spectroscopic_factor": st(np.array(z)), "koltun_rel": st(np.array(kr))}
+              for k, (w, z, kr) in acc.items()}
+    wall32 = sum(t for t, _ in times["mixed"])
+    wall64 = sum(t for t, _ in times["fp64"])
+    dev32 = sum(d for _, d in times["mixed"]) / 1e3
+    dev64 = sum(d for _, d in times["fp64"]) / 1e3
+    line = {"metric": "problems/s, batched many-instance run (iterated, mixed precision)", "impl": "gpu",
+            "value": args.problems / wall32, "unit": "problems/s", "n_gpus": 1, "higher_is_better": True,
+            "config": {"workload": "many_problems", "problems": args.problems, "seeds": [100, 100 + args.problems - 1],
+                       "nmax_choices": [4, 6, 8, 10], "nmax_counts": {str(k): sizes.count(k) for k in (4, 6, 8, 10)},
+                       "hw_MeV": [10, 30], "sigma_MeV": [1, 3], "lanczos_iterations_per_pivot": n_itr,
+                       "iterations": args.iterations, "z_cut": z_cut, "max_fragments_per_subshell_side": max_frag,
+                       "timed": "per problem: upload + every iteration (chain, next propagator); generation excluded"},
+            "mixed": {"problems_per_s": args.problems / wall32, "wall_s": wall32, "device_s": dev32},
+            "fp64": {"problems_per_s": args.problems / wall64, "wall_s": wall64, "device_s": dev64},
+            "speedup_mixed_vs_fp64_wall": wall64 / wall32, "speedup_mixed_vs_fp64_device": dev64 / dev32,
+            "device_propagator_updates": device_updates, "errors": errors}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.many:
+        return many_problems(args)
     return gpu_arm(args)
 
 

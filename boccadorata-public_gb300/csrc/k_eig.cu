@@ -22,6 +22,7 @@
 //             Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
 #include <climits>
 #include "bd_common.cuh"
+#include "df64.cuh"
 #include "bd_kernels.h"
 #include "eig_sturm.cuh"
 
@@ -239,18 +240,6 @@ struct InvitGlobal {   // the job's work area and matrix region, column k at str
 };
 
 constexpr int kIvThreads = 16;   // eigenvectors per CTA of the shared-memory variant
-struct InvitShared {   // shared memory, element i of this thread at i * kIvThreads + lane
-    double *U1, *U2, *DD, *LL, *Y;
-    unsigned char *PV;
-    int lane;
-    __device__ double &u1(int i) { return U1[i * kIvThreads + lane]; }
-    __device__ double &u2(int i) { return U2[i * kIvThreads + lane]; }
-    __device__ double &dd(int i) { return DD[i * kIvThreads + lane]; }
-    __device__ double &ll(int i) { return LL[i * kIvThreads + lane]; }
-    __device__ double &y(int i) { return Y[i * kIvThreads + lane]; }
-    __device__ bool pv(int i) { return PV[i * kIvThreads + lane] != 0; }
-    __device__ void set_pv(int i, bool b) { PV[i * kIvThreads + lane] = b ? 1 : 0; }
-};
 
 // Eigenvector k of block [b0, b1] (b1 > b0) into a.y(b0 .. b1).
 template <class S>
@@ -329,6 +318,106 @@ __device__ void invit_vector(const DyJob &J, int k, int b0, int b1, S &a) {
     }
 }
 
+// The same in double-float (df64.cuh: FP32 hi + lo pairs, ~48 bits) for the shared-memory
+// variant: every step of the factorisation and of the solves is a dependent chain, and
+// an FP64 instruction holds an SM sub-partition's FP64 unit for ~64 cycles on this GPU
+// (a reciprocal by Newton's iteration is four of them), while the double-float forms
+// run on the FP32 pipe at a few cycles per operation.  The shifts, the tolerances and
+// the start vectors are those of invit_vector; the pivot choice compares the high parts
+// (any choice that keeps the multipliers bounded serves), and the result goes to y in
+// FP64.  The tridiagonal is read from J in FP64 and converted off the dependent chain.
+struct InvitSharedDF {   // shared memory, element i of this thread at i * kIvThreads + lane
+    dfm::df *U1, *U2, *DD, *LL, *Y;
+    unsigned char *PV;
+    int lane;
+    __device__ dfm::df &u1(int i) { return U1[i * kIvThreads + lane]; }
+    __device__ dfm::df &u2(int i) { return U2[i * kIvThreads + lane]; }
+    __device__ dfm::df &dd(int i) { return DD[i * kIvThreads + lane]; }
+    __device__ dfm::df &ll(int i) { return LL[i * kIvThreads + lane]; }
+    __device__ dfm::df &y(int i) { return Y[i * kIvThreads + lane]; }
+    __device__ bool pv(int i) { return PV[i * kIvThreads + lane] != 0; }
+    __device__ void set_pv(int i, bool b) { PV[i * kIvThreads + lane] = b ? 1 : 0; }
+};
+
+__device__ inline dfm::df df_abs(dfm::df a) { return a.h < 0.0f ? dfm::neg(a) : a; }
+__device__ inline dfm::df df_sub(dfm::df a, dfm::df b) { return dfm::add(a, dfm::neg(b)); }
+
+__device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, InvitSharedDF &a) {
+    using dfm::df;
+    const int NS = 2 + J.D;
+    const double *d = J.d, *e = J.e;
+    const EigTol tl = eig_tol(J.tau[k]);
+    auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
+    int k0 = k;
+    while (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) --k0;
+    double xs = W(k0);
+    for (int q = k0 + 1; q <= k; ++q) xs = fmax(W(q), xs + tl.pertol);
+    const df x = dfm::from_double(xs);
+    const df zero{0.0f, 0.0f};
+    for (int i = b0; i <= b1; ++i) {
+        a.dd(i) = df_sub(dfm::from_double(d[i]), x);
+        const df ei = (i < b1) ? dfm::from_double(e[i]) : zero;
+        a.u1(i) = ei;
+        a.ll(i) = ei;
+        a.u2(i) = zero;
+    }
+    for (int i = b0; i < b1; ++i) {
+        const df di = a.dd(i), li = a.ll(i);
+        if (fabsf(di.h) >= fabsf(li.h)) {
+            a.set_pv(i, false);
+            const df f = (di.h != 0.0f) ? dfm::mul(li, dfm::rcp(di)) : zero;
+            a.ll(i) = f;
+            a.dd(i + 1) = dfm::fma(dfm::neg(f), a.u1(i), a.dd(i + 1));
+        } else {
+            a.set_pv(i, true);
+            const df f = dfm::mul(di, dfm::rcp(li));
+            a.dd(i) = li;
+            a.ll(i) = f;
+            const df tt = a.u1(i);
+            a.u1(i) = a.dd(i + 1);
+            a.dd(i + 1) = dfm::fma(dfm::neg(f), a.dd(i + 1), tt);
+            if (i + 1 < b1) {
+                a.u2(i) = a.u1(i + 1);
+                a.u1(i + 1) = dfm::mul(dfm::neg(f), a.u1(i + 1));
+            }
+        }
+    }
+    // pivots no smaller than pertol, kept as reciprocals for the solves
+    const float pt = (float)tl.pertol;
+    for (int i = b0; i <= b1; ++i) {
+        df p = a.dd(i);
+        if (fabsf(p.h) < pt) p = df{p.h < 0.0f ? -pt : pt, 0.0f};
+        a.dd(i) = dfm::rcp(p);
+    }
+    for (int i = b0; i <= b1; ++i)
+        a.y(i) = df{0.5f + (float)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0f, 0.0f};
+    for (int it = 0; it < 2; ++it) {
+        for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges
+            df bi = a.y(i), bi1 = a.y(i + 1);
+            const df f = a.ll(i);
+            if (!a.pv(i)) bi1 = dfm::fma(dfm::neg(f), bi, bi1);
+            else { const df tt = bi; bi = bi1; bi1 = dfm::fma(dfm::neg(f), bi1, tt); }
+            a.y(i) = bi; a.y(i + 1) = bi1;
+        }
+        df y1 = zero, y2 = zero;
+        float nrm = 0.0f;
+        for (int i = b1; i >= b0; --i) {   // U y = b, two superdiagonals
+            df v = a.y(i);
+            if (i + 1 <= b1) v = dfm::fma(dfm::neg(a.u1(i)), y1, v);
+            if (i + 2 <= b1) v = dfm::fma(dfm::neg(a.u2(i)), y2, v);
+            v = dfm::mul(v, a.dd(i));
+            a.y(i) = v;
+            y2 = y1; y1 = v;
+            nrm = fmaxf(nrm, fabsf(v.h));
+        }
+        const df sc = (nrm > 0.0f) ? dfm::rcp(df{nrm, 0.0f}) : df{1.0f, 0.0f};
+        df s2 = zero;
+        for (int i = b0; i <= b1; ++i) { const df v = dfm::mul(a.y(i), sc); a.y(i) = v; s2 = dfm::fma(v, v, s2); }
+        const df inv = (s2.h > 0.0f) ? dfm::rsqrt(s2) : zero;
+        for (int i = b0; i <= b1; ++i) a.y(i) = dfm::mul(a.y(i), inv);
+    }
+}
+
 // Matrices of order > kTsMax: one thread per position, factors in the job's work area.
 __global__ void k_invit(const DyJob *jobs, int njobs, const long long *row_first, long long total, double *work,
                         const long long *work_first) {
@@ -359,13 +448,14 @@ __global__ void __launch_bounds__(kIvThreads) k_invit_small(const DyJob *jobs, i
     if (n > kTsMax || k >= n) return;
     extern __shared__ double smi[];
     const int cap = kTsMax * kIvThreads;
-    InvitShared a{smi, smi + cap, smi + 2 * cap, smi + 3 * cap, smi + 4 * cap,
-                  reinterpret_cast<unsigned char *>(smi + 5 * cap), lane};
+    dfm::df *sd = reinterpret_cast<dfm::df *>(smi);
+    InvitSharedDF a{sd, sd + cap, sd + 2 * cap, sd + 3 * cap, sd + 4 * cap,
+                    reinterpret_cast<unsigned char *>(sd + 5 * cap), lane};
     const int b0 = J.blk[k], b1 = J.blk[n + k];
     double *Y = J.A;
     if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
-    invit_vector(J, k, b0, b1, a);
-    for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] = a.y(i);
+    invit_vector_df(J, k, b0, b1, a);
+    for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] = dfm::to_double(a.y(i));
 }
 
 // One CTA per position; the CTA of a cluster's first member (cluster of two or more,

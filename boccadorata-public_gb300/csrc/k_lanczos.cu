@@ -63,6 +63,40 @@ __device__ inline T warp_sum_ct(T v) {
     return v;
 }
 
+// Warp sums of NV values at once (NV a power of two <= 32): each level of the xor
+// butterfly (offsets 16, 8, ..., 1, the order of warp_sum_ct) sends the half of the
+// values a lane does not keep and adds the partner's half to the kept one, so NV - 1
+// shuffles (plus one per level left once a single value remains) replace 5 NV; every
+// total is associated exactly as warp_sum_ct associates it.  Lane L ends with the total
+// of value L >> (5 - log2 NV).
+__device__ __forceinline__ float shfl_xor_t(float x, int o) { return __shfl_xor_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ double shfl_xor_t(double x, int o) { return __shfl_xor_sync(0xffffffffu, x, o); }
+__device__ __forceinline__ dfm::df shfl_xor_t(dfm::df x, int o) { return dfm::shfl_xor(x, o); }
+__device__ __forceinline__ float add_t(float a, float b) { return a + b; }
+__device__ __forceinline__ double add_t(double a, double b) { return a + b; }
+__device__ __forceinline__ dfm::df add_t(dfm::df a, dfm::df b) { return dfm::add(a, b); }
+template <int NV, typename T>
+__device__ __forceinline__ T warp_sums(T *v, int lane) {
+#pragma unroll
+    for (int lev = 0; lev < 5; ++lev) {
+        const int o = 16 >> lev;
+        const int n = NV >> (lev + 1);   // values a lane keeps after this level
+        if (n >= 1) {
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int i = 0; i < (NV >> 1); ++i)
+                if (i < n) {
+                    const T send = up ? v[i] : v[i + n];
+                    const T keep = up ? v[i + n] : v[i];
+                    v[i] = add_t(keep, shfl_xor_t(send, o));
+                }
+        } else {
+            v[0] = add_t(v[0], shfl_xor_t(v[0], o));
+        }
+    }
+    return v[0];
+}
+
 // Sums across warps and CTAs.  FP64 vectors: FP64 adds.  FP32 vectors: the partials
 // are FP32 values, summed in double-float (df64.cuh) on the FP32 pipe -- an FP64 add
 // holds the SM sub-partition's FP64 unit for about 64 cycles, and the trees below are
@@ -151,6 +185,14 @@ template <> __device__ inline void load16<double>(const double *p, double *o) {
 // the same through a generic address (shared or global memory)
 template <typename VT>
 __device__ inline void load16g(const VT *p, VT *out);
+template <typename VT>
+__device__ inline void store16g(VT *p, const VT *v);
+template <> __device__ inline void store16g<float>(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <> __device__ inline void store16g<double>(double *p, const double *v) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+}
 template <> __device__ inline void load16g<float>(const float *p, float *o) {
     const float4 v = *reinterpret_cast<const float4 *>(p);
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
@@ -164,7 +206,7 @@ template <> __device__ inline void load16g<double>(const double *p, double *o) {
 // zero in every vector (E, w, V), so the vector loads need no tail handling.
 //
 // Shared-memory layout: doubles A[2][rmax] (dot partials of alternate passes) |
-// c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | red[kLzWarps * kMaxScal],
+// c[rmax] (totals) | Bs[kMaxScal] (scalar partials) | red[kLzWarps * kMaxScal] (per warp),
 // then CT (the vectors' arithmetic type) cf[rmax rounded up to 4] (totals in CT) |
 // Es[S] | w[S], then touched[S] bytes, then the basis cache up to smem_bytes.
 //
@@ -250,6 +292,9 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int s_nl;
     __shared__ int lslot[8];     // slots of the earlier chains' last vectors (-1: deflated)
     __shared__ int s_start[10], s_last[10];   // the chain schedule (read every step: kept on chip)
+    __shared__ int s_flag;       // thread 0's decision after a full sweep (0 keep, 1 sweep again, 2 exhausted, 3 restart)
+    __shared__ CT s_ixbf;        // 1/|w| in the arithmetic type
+    __shared__ CT lcf[16];       // lc in the arithmetic type
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
@@ -298,93 +343,96 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
     // Sum over the cluster of one value per CTA held at buf[t], a fixed pairwise tree
     // over the ranks (the loads first, then four levels of adds: one DSMEM round trip
-    // and a short FP64 chain instead of CL of each).
-    auto cluster_sum = [&](const double *buf, int t) -> double {
+    // and a short chain instead of CL of each).
+    auto cluster_sum_st = [&](const double *buf, int t) -> ST {
         ST x[16];
 #pragma unroll
         for (int r = 0; r < 16; ++r)
             x[r] = (r < CL) ? Sum::get(cluster.map_shared_rank(const_cast<double *>(buf), r) + t) : Sum::zero();
-        return Sum::value(Sum::add(tree_sum8<Sum>(x), tree_sum8<Sum>(x + 8)));
+        return Sum::add(tree_sum8<Sum>(x), tree_sum8<Sum>(x + 8));
     };
-
     // (b1) dots pass: <v_t, w> for the pass's vectors t < nl and |w|^2, summed over
-    // the cluster into c[0..nl] (c[nl] = |w|^2) and cf[0..nl).  The per-CTA partials
-    // alternate between two buffers: a peer may still gather the previous pass's
-    // while this CTA writes the next (no cluster barrier between a local update and
-    // the full sweep's dot products).
+    // the cluster into cf[0..nl) and c[nl] = |w|^2.  One warp forms each dot product,
+    // w itself counting as the pass's vector nl (its square norm), eight vectors per
+    // warp at a time: eight independent 16-byte loads in flight per lane (one vector's
+    // slice is only a few loads per lane, so a warp that took its vectors one after
+    // another would wait out the L2 latency per vector), and no CTA barrier before the
+    // cluster's.  The per-CTA partials alternate between two buffers: a peer may still
+    // gather the previous pass's while this CTA writes the next (no cluster barrier
+    // between a local update and the full sweep's dot products).
     int dpar = 0;
     auto dots_pass = [&](bool loc, int nl) {
         double *Ap = A + (size_t)dpar * rmax2;
         dpar ^= 1;
-        // four vectors per warp at a time: four independent 16-byte loads in flight per
-        // lane (one vector's slice is only a few loads per lane, so a warp that took
-        // its vectors one after another would wait out the L2 latency per vector)
-        for (int t0 = warp; t0 < nl; t0 += 4 * kLzWarps) {
-            const VT *vp[4];
+        const VT *wv = reinterpret_cast<const VT *>(w);
+        // FP32 vectors: eight per warp at a time; FP64: four, two groups per lane in flight
+        // (the FP64 products bound that pass, not the loads)
+        constexpr int NU = sizeof(CT) == 4 ? 8 : 4;
+        constexpr int LS = sizeof(CT) == 4 ? 2 : 3;   // lane L holds the total of vector L >> LS
+        constexpr int UNR = sizeof(CT) == 4 ? 1 : 2;
+        for (int t0 = warp; t0 <= nl; t0 += NU * kLzWarps) {
+            const VT *vp[NU];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < NU; ++u) {
                 const int t = t0 + u * kLzWarps;
-                vp[u] = vslice(t < nl ? (loc ? lt[t] : t) : (loc ? lt[t0] : t0));
+                vp[u] = (t < nl) ? vslice(loc ? lt[t] : t) : wv;
             }
+            const int nu = min(NU, (nl - t0) / kLzWarps + 1);   // vectors of this warp in this round (warp-uniform)
             if constexpr (kComp) {   // each 16-byte group's four products, then exactly into the pair
-                PA acc[4] = {PS::zero(), PS::zero(), PS::zero(), PS::zero()};
-#pragma unroll 2
+                PA acc[NU];
+#pragma unroll
+                for (int u = 0; u < NU; ++u) acc[u] = PS::zero();
+#pragma unroll UNR
                 for (int q = lane; q < nv; q += 32) {
-                    VT x[4][VW];
+                    VT wq[VW];
+                    load16g<VT>(wv + q * VW, wq);
+                    VT x[NU][VW];   // all loads first (vectors beyond the pass read w: valid, unused)
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
+                    for (int u = 0; u < NU; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        CT g = (CT)0;
+                    for (int u = 0; u < NU; ++u)
+                        if (u < nu) {
+                            CT g = (CT)0;
 #pragma unroll
-                        for (int e = 0; e < VW; ++e) g += x[u][e] * w[q * VW + e];
-                        PS::add(acc[u], g);
-                    }
+                            for (int e = 0; e < VW; ++e) g += x[u][e] * wq[e];
+                            PS::add(acc[u], g);
+                        }
                 }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const ST r = PS::finish(acc[u]);
-                    const int t = t0 + u * kLzWarps;
-                    if (lane == 0 && t < nl) Sum::put(Ap + t, r);
-                }
+                const PA r = warp_sums<NU>(acc, lane);
+                const int u = lane >> LS;
+                if ((lane & ((1 << LS) - 1)) == 0 && u < nu) Sum::put(Ap + t0 + u * kLzWarps, r);
             } else {
-                CT acc[4] = {0, 0, 0, 0};
-#pragma unroll 2
+                CT acc[NU];
+#pragma unroll
+                for (int u = 0; u < NU; ++u) acc[u] = (CT)0;
+#pragma unroll UNR
                 for (int q = lane; q < nv; q += 32) {
-                    VT x[4][VW];
+                    VT wq[VW];
+                    load16g<VT>(wv + q * VW, wq);
+                    VT x[NU][VW];   // all loads first (vectors beyond the pass read w: valid, unused)
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
+                    for (int u = 0; u < NU; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
+                    for (int u = 0; u < NU; ++u)
+                        if (u < nu)
 #pragma unroll
-                        for (int e = 0; e < VW; ++e) acc[u] += x[u][e] * w[q * VW + e];
+                            for (int e = 0; e < VW; ++e) acc[u] += x[u][e] * wq[e];
                 }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    acc[u] = warp_sum_ct(acc[u]);   // lane partials combined in CT: FP32 shuffles for FP32 vectors
-                    const int t = t0 + u * kLzWarps;
-                    if (lane == 0 && t < nl) Sum::put(Ap + t, Sum::from_ct(acc[u]));
-                }
+                const CT r = warp_sums<NU>(acc, lane);   // lane partials combined in CT
+                const int u = lane >> LS;
+                if ((lane & ((1 << LS) - 1)) == 0 && u < nu) Sum::put(Ap + t0 + u * kLzWarps, Sum::from_ct(r));
             }
         }
-        PA nwp = PS::zero();
-        for (int i = tid; i < S; i += kLzThreads) PS::add(nwp, w[i] * w[i]);
-        {
-            const ST r = PS::finish(nwp);
-            if (lane == 0) Sum::put(red + warp * kMaxScal, r);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            ST x[kLzWarps];
-#pragma unroll
-            for (int q = 0; q < kLzWarps; ++q) x[q] = Sum::get(red + q * kMaxScal);
-            Sum::put(Ap + nl, tree_sum8<Sum>(x));
-        }
-        cluster.sync();
+        cluster.sync();   // the partials of every CTA (also a barrier of this CTA's threads)
         for (int t = tid; t <= nl; t += kLzThreads) {   // (b2) totals over the cluster
-            const double s = cluster_sum(Ap, t);
-            c[t] = s;
-            cf[t] = (CT)s;
+            const ST s = cluster_sum_st(Ap, t);
+            if constexpr (sizeof(CT) == 4) {
+                cf[t] = s.h + s.l;   // the pair rounded once, as through FP64; no FP64 instruction
+                if (t == nl) c[t] = Sum::value(s);
+            } else {
+                c[t] = s;
+                cf[t] = (CT)s;
+            }
         }
         __syncthreads();
     };
@@ -427,61 +475,79 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
             }
 #pragma unroll
-            for (int u = 0; u < VW; ++u) w[q * VW + u] -= acc[u];
+            for (int u = 0; u < VW; ++u) w[qo + u] -= acc[u];
         }
     };
 
-    // After a full sweep's update: |w|^2 and the scalars of step (c) of the updated w
-    // (source/BcDor-Lanczos.cpp:180-214), alpha = <w|E|w>, m_d = <M_d|w> and, for each
-    // earlier pivot q, g_q = <v_last(q)|E|w>, summed over the cluster into tot[0] =
-    // |w|^2, tot[1] = alpha, tot[2 + d] = m_d, tot[2 + D + q] = g_q.  Each thread reads
-    // back only the groups it updated, so no barrier separates this from the update.
-    // When another sweep follows, these sums are simply recomputed.
-    auto scalar_pass = [&](int nq) {
+    // After a full sweep's update: the scalars of step (c) of the updated w
+    // (source/BcDor-Lanczos.cpp:180-214): |w|^2, alpha = <w|E|w>, m_d = <M_d|w> and, for
+    // each earlier pivot q, g_q = <v_last(q)|E|w>, and |E w|^2, as partials in
+    // red[warp][slot], slots [|w|^2, alpha, m_0.., g_0.., |E w|^2].  Each thread reads back
+    // only the groups it updated, so no barrier separates this from the update.
+    auto scalar_partials = [&](int nq) {
         PA pn = PS::zero(), sa = PS::zero(), se = PS::zero(), sm_[8], sg[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { sm_[q] = PS::zero(); sg[q] = PS::zero(); }
+        for (int q = 0; q < 8; ++q) {
+            sm_[q] = PS::zero();
+            sg[q] = PS::zero();
+        }
         for (int q = tid; q < nv; q += kLzThreads) {
+            const int qo = q * VW;
+            {
+                // the groups of the first four earlier chains' last vectors, loaded together
+                // (more earlier chains read theirs element by element)
+                VT lv[4][VW];
+                bool lok[8];
 #pragma unroll
-            for (int u = 0; u < VW; ++u) {
-                const int i = q * VW + u;
-                const CT wi = w[i];
-                PS::add(pn, wi * wi);
-                if (i < ns) {
-                    const CT e = Es[i];
-                    PS::add(sa, e * wi * wi);
-                    PS::add(se, e * e * wi * wi);
+                for (int g = 0; g < 8; ++g) {
+                    lok[g] = g < nq && lslot[g] >= 0;
+                    if (g < 4 && lok[g]) load16g<VT>(vslice(lslot[g]) + qo, lv[g]);
+                }
 #pragma unroll
-                    for (int d = 0; d < 8; ++d)
-                        if (d < D) PS::add(sm_[d], (Msl ? Msl[d * S + i] : Mc[(size_t)d * N + i0 + i]) * wi);
+                for (int u = 0; u < VW; ++u) {
+                    const int i = qo + u;
+                    const CT wi = w[i];
+                    PS::add(pn, wi * wi);
+                    if (i < ns) {
+                        const CT e = Es[i];
+                        PS::add(sa, e * wi * wi);
+                        PS::add(se, e * e * wi * wi);
 #pragma unroll
-                    for (int g = 0; g < 8; ++g)
-                        if (g < nq && lslot[g] >= 0) PS::add(sg[g], e * (CT)vslice(lslot[g])[i] * wi);
+                        for (int d = 0; d < 8; ++d)
+                            if (d < D) PS::add(sm_[d], (Msl ? Msl[d * S + i] : Mc[(size_t)d * N + i0 + i]) * wi);
+#pragma unroll
+                        for (int g = 0; g < 8; ++g)
+                            if (lok[g]) PS::add(sg[g], e * (CT)(g < 4 ? lv[g & 3][u] : vslice(lslot[g])[i]) * wi);
+                    }
                 }
             }
         }
-        {
-            const ST a = PS::finish(pn), b = PS::finish(sa), c2 = PS::finish(se);
-            if (lane == 0) {
-                Sum::put(red + warp * kMaxScal, a);
-                Sum::put(red + warp * kMaxScal + 1, b);
-                Sum::put(red + warp * kMaxScal + 2 + D + nq, c2);
-            }
+        // the 19 sums of the warp at once (values 0 |w|^2, 1 alpha, 2 |E w|^2, 3 + d m_d,
+        // 11 + q g_q, the rest zero); lane L stores value L into its slot when in use
+        PA v[32];
+        v[0] = pn; v[1] = sa; v[2] = se;
+#pragma unroll
+        for (int d = 0; d < 8; ++d) { v[3 + d] = sm_[d]; v[11 + d] = sg[d]; }
+#pragma unroll
+        for (int q = 19; q < 32; ++q) v[q] = PS::zero();
+        const PA x = warp_sums<32>(v, lane);
+        int slot = -1;
+        if (lane == 0) slot = 0;
+        else if (lane == 1) slot = 1;
+        else if (lane == 2) slot = 2 + D + nq;
+        else if (lane < 11) slot = (lane - 3 < D) ? 2 + (lane - 3) : -1;
+        else if (lane < 19) slot = (lane - 11 < nq) ? 2 + D + (lane - 11) : -1;
+        if (slot >= 0) {
+            if constexpr (kComp) Sum::put(red + warp * kMaxScal + slot, x);
+            else Sum::put(red + warp * kMaxScal + slot, Sum::from_ct(x));
         }
-#pragma unroll
-        for (int d = 0; d < 8; ++d)
-            if (d < D) {
-                const ST x = PS::finish(sm_[d]);
-                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + d, x);
-            }
-#pragma unroll
-        for (int g = 0; g < 8; ++g)
-            if (g < nq) {
-                const ST x = PS::finish(sg[g]);
-                if (lane == 0) Sum::put(red + warp * kMaxScal + 2 + D + g, x);
-            }
-        __syncthreads();
+    };
+    // The cluster totals of the scalars into tot[0 .. 3 + D + nq): the warps' partials
+    // summed per CTA into Bs, then over the cluster (no barrier after: the caller's
+    // decision follows).
+    auto scalar_reduce = [&](int nq) {
         const int nsc = 3 + D + nq;   // |w|^2, <w|E|w>, m_d, g_q, |E w|^2
+        __syncthreads();
         if (tid < nsc) {
             ST x[kLzWarps];
 #pragma unroll
@@ -489,8 +555,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             Sum::put(Bs + tid, tree_sum8<Sum>(x));
         }
         cluster.sync();
-        if (tid < nsc) tot[tid] = cluster_sum(Bs, tid);
-        __syncthreads();
+        if (tid < nsc) tot[tid] = Sum::value(cluster_sum_st(Bs, tid));
     };
 
     int k = -1;           // current pivot chain
@@ -548,25 +613,46 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (j >= 2 && rowslot[j - 2] >= 0) { lt[n] = rowslot[j - 2]; lc[n++] = prow[1]; }
                 for (int q = 0; q < k; ++q)
                     if (s_last[q] < j - 2 && rowslot[s_last[q]] >= 0) { lt[n] = rowslot[s_last[q]]; lc[n++] = prow[2 + q]; }
+                for (int q = 0; q < n; ++q) lcf[q] = (CT)lc[q];
                 s_nl = n;
             }
             __syncthreads();
             const int nl0 = s_nl;
-            const VT *vp = vslice(lt[0]);
-            for (int i = tid; i < S; i += kLzThreads) {
-                CT x = (CT)vp[i] * Es[i];
-                for (int t = 0; t < nl0; ++t) x -= (CT)lc[t] * (CT)vslice(lt[t])[i];
-                w[i] = x;
+            const VT *vp0 = vslice(lt[0]);
+            for (int q = tid; q < nv; q += kLzThreads) {
+                const int qo = q * VW;
+                VT x0[VW];
+                load16g<VT>(vp0 + qo, x0);
+                CT x[VW];
+#pragma unroll
+                for (int u = 0; u < VW; ++u) x[u] = (CT)x0[u] * Es[qo + u];
+#pragma unroll 4
+                for (int t = 0; t < nl0; ++t) {
+                    VT y[VW];
+                    load16g<VT>(vslice(lt[t]) + qo, y);
+                    const CT ct = lcf[t];
+#pragma unroll
+                    for (int u = 0; u < VW; ++u) x[u] -= ct * (CT)y[u];
+                }
+#pragma unroll
+                for (int u = 0; u < VW; ++u) w[qo + u] = x[u];
             }
         } else {
             const VT *vp = vslice(rowslot[j - 1]);
-            for (int i = tid; i < S; i += kLzThreads) w[i] = (CT)vp[i] * Es[i];
+            for (int q = tid; q < nv; q += kLzThreads) {
+                const int qo = q * VW;
+                VT x0[VW];
+                load16g<VT>(vp + qo, x0);
+#pragma unroll
+                for (int u = 0; u < VW; ++u) w[qo + u] = (CT)x0[u] * Es[qo + u];
+            }
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
         bool done = false;         // step finished by an untouched-pole unit vector
         double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
             int nfull = 0;
+            int fl = 0;            // thread 0's decision after the last sweep (s_flag)
             // A continuing chain's w = E v_{j-1} has large components only on v_{j-1}, v_{j-2}
             // and the last vector of every earlier chain (the fishbone couplings); everything
             // else is rounding.  The first pass projects out just those few vectors, then
@@ -596,25 +682,48 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     wn2_before = c[nl];
                     continue;
                 }
-                scalar_pass(nq);
+                scalar_partials(nq);
+                scalar_reduce(nq);
+                // Thread 0 holds |w|^2 (tot[0]) and takes the step's decision alone (FP64
+                // comparisons in one thread instead of every warp), with 1/|w| when the
+                // vector is kept; the barrier below publishes it with the totals.
+                if (tid == 0) {
+                    const double x2 = tot[0];
+                    int f;
+                    if (nvec > 0 && nfull + 1 < 4 && x2 < eta2 * wn2_before) f = 1;   // another full sweep
+                    else if (attempt == 0 && !contaminated && (x2 <= thr_exh * wn2_first || x2 == 0.0) && next_slot())
+                        f = 2;   // this chain's Krylov space is exhausted
+                    else if (attempt > 0 || !(x2 <= tau * wn2_first || x2 == 0.0)) {
+                        f = 0;   // keep: normalise
+                        const double r = rsqrt_newton(x2);   // 1/sqrt(n2) to a few ulp
+                        s_xb = x2 * r;
+                        s_ixb = r;
+                        s_ixbf = (CT)r;
+                    } else {
+                        f = 3;   // the reachable subspace is exhausted: restart
+                    }
+                    s_flag = f;
+                }
+                __syncthreads();
                 n2 = tot[0];
+                fl = s_flag;
                 // another full sweep while this one removed more than half of the squared norm
                 if (nfull++ > 0) ++extra;
-                if (nvec > 0 && nfull < 4 && n2 < eta2 * wn2_before) {
+                if (fl == 1) {
                     dots_pass(false, nl);
                     wn2_before = c[nl];
                     continue;
                 }
                 break;
             }
-            if (attempt == 0 && !contaminated && (n2 <= thr_exh * wn2_first || n2 == 0.0) && next_slot()) {
+            if (fl == 2) {
                 deflated_row(j);   // this chain's Krylov space is exhausted
                 tail = true;
                 done = true;
                 prow_ok = false;
                 break;
             }
-            if (attempt > 0 || !(n2 <= tau * wn2_first || n2 == 0.0)) break;
+            if (fl == 0) break;
             contaminated = true;
             // (c0) exhausted reachable subspace: an untouched pole's unit vector if one is left,
             // else a pseudo-random vector swept orthogonal to the basis in the second attempt
@@ -660,24 +769,23 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         if (done) continue;
         // (d) normalise, store, write the output row (source/BcDor-Lanczos.cpp:198-216);
-        // the scalars are formed once, by Newton's iteration instead of FP64 division and
-        // square root (long FP64 chains)
-        if (tid == 0) {
-            const double r = rsqrt_newton(n2);   // 1/sqrt(n2) to a few ulp
-            s_xb = n2 * r;
-            s_ixb = r;
-        }
-        __syncthreads();
+        // the scalars were formed once, with the decision, by Newton's iteration instead
+        // of FP64 division and square root (long FP64 chains)
         const double xb = s_xb, ixb = s_ixb;
         VT *vj = V + (size_t)nvec * C.ld + i0;
         {
             VT *vc = nvec < ccap ? cache + (size_t)nvec * S : nullptr;
-            const CT inv = (CT)ixb;
-            for (int i = tid; i < S; i += kLzThreads) {
-                const VT v = (VT)(w[i] * inv);
-                vj[i] = v;
-                if (vc) vc[i] = v;
-                touched[i] |= (v != (VT)0);
+            const CT inv = s_ixbf;
+            for (int q = tid; q < nv; q += kLzThreads) {
+                const int qo = q * VW;
+                VT v[VW];
+#pragma unroll
+                for (int u = 0; u < VW; ++u) {
+                    v[u] = (VT)(w[qo + u] * inv);
+                    touched[qo + u] |= (v[u] != (VT)0);
+                }
+                store16g<VT>(vj + qo, v);
+                if (vc) store16g<VT>(vc + qo, v);
             }
         }
         if (tid < NT) {   // one output element per thread; every CTA keeps the row for the next step
@@ -697,7 +805,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         prow_ok = !injected;
         ++nvec;
-        __syncthreads();
+        // (the barrier at the top of the next step orders these writes before their reads)
     }
     if (rank == 0 && tid == 0) { atomicAdd(&C.stat[0], extra); atomicAdd(&C.stat[2], ndefl); }
     __syncthreads();
