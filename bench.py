@@ -38,10 +38,16 @@ sys.path.insert(0, ROOT)
 METRIC = "channels solved/s at N_max=10: mixed vs FP64 GPU at <=1 keV qp-energy error"
 WORKLOAD = "nmax10_lanczos100"
 CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2, 3, 5, 6
-# Per-launch DRAM traffic of the FP32 Lanczos kernel on this workload, from one ncu
-# capture of that kernel (dram__bytes_read.sum 22 365 184 + dram__bytes_write.sum
-# 9 821 952).
-LANCZOS_TRAFFIC_BYTES = 32_187_136
+# Per-launch traffic of the FP32 Lanczos kernel on this workload, from one ncu capture
+# of that kernel at the current source (dram__bytes_read.sum 22.303744 MB +
+# dram__bytes_write.sum 8.416256 MB; lts__t_bytes.sum 1.365502 GB; issue active 32.7 %
+# of active cycles, barrier stalls 4.26 per issue).
+LANCZOS_TRAFFIC_BYTES = 30_720_000
+LANCZOS_L2_BYTES = 1_365_502_000
+LANCZOS_ISSUE_ACTIVE = 0.327
+# GB300's nominal FP64 rate (no measured FP64 peak exists for this machine): the
+# denominator of the Dyson phase's FP64-class fraction.
+FP64_NOMINAL_TFLOPS = 1.25
 # Accuracy the metric is quoted at: mixed against FP64 on every solution with Z > 1e-4.
 MAX_QP_ERROR_KEV = 1.0
 MAX_Z_ERROR = 1e-5
@@ -474,6 +480,7 @@ def gpu_arm(args):
     # ---- the headline: mixed-precision batched form
     clocks = Clocks(local) if rank == 0 else None
     dev_ms, wall_ms, lz_ms, launches = timed(dict(mixed=True), args.steps, args.warmup)
+    dev_phases = ctx.timings()
     clk = clocks.stop() if clocks else None
     step_s = max_over_ranks(dev_ms / 1e3)
     value = whole_job_rate(world, nch, step_s)
@@ -530,7 +537,24 @@ def gpu_arm(args):
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else "fallback 6.8 TB/s",
             "traffic": LANCZOS_TRAFFIC_BYTES, "algorithmic_bytes": alg, "kernel_ms": lz_mean,
-            "lanczos_rows": int(sum(c[1] for c in chains)), "lanczos_vectors_built": int(sum(stored))}
+            "lanczos_rows": int(sum(c[1] for c in chains)), "lanczos_vectors_built": int(sum(stored)),
+            "l2_bytes": LANCZOS_L2_BYTES, "issue_active": LANCZOS_ISSUE_ACTIVE,
+            "note": "the built basis stays in L2 (traffic is 1.1 % of the algorithmic bytes): the launch is "
+                    "bound by the longest chain's step latency, so the HBM fraction is nominal"}
+    # The Dyson phase against FP64: Householder (4/3 n^3) and the first D rows of Q
+    # (2 n^2 D) over the deflated orders n = D + the chain's built rows (the deflated
+    # tails leave the matrix), divided by the phase's CUDA-event time.
+    dflops = 0.0
+    for ish in range(nch):
+        D = int(prob.ms.no[ish])
+        n = D + int(st[ish, 0]) + int(st[ish, 1])
+        dflops += 4.0 / 3.0 * n ** 3 + 2.0 * n * n * D
+    dy_ms = dev_phases["dyson"]
+    dyson = {"kernels": "k_dyson_deflate .. k_place (Householder, bisection, inverse iteration, placement)",
+             "algorithmic_flops": dflops, "phase_ms": dy_ms, "achieved_tflops": dflops / (dy_ms / 1e3) / 1e12,
+             "fp64_nominal_tflops": FP64_NOMINAL_TFLOPS,
+             "frac_of_fp64_nominal": dflops / (dy_ms / 1e3) / 1e12 / FP64_NOMINAL_TFLOPS,
+             "note": "latency-bound: the largest matrix's serial Householder columns (one CTA per matrix)"}
     extra = {}
     if world == 1 and not args.no_extra:
         extra["precision_nmax12"] = precision_run(bd, synth, local)
@@ -547,11 +571,13 @@ def gpu_arm(args):
                    "l2": "inputs larger than L2 (293 MB interaction, ~0.9 GB Lanczos basis); no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": roof,
+        "dyson_fp64": dyson,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": launches,
         "forms": {"mixed_batched_ms": dev_ms, "mixed_batched_wall_ms": wall_ms,
+                  "mixed_batched_phases_ms": dev_phases,
                   "fp64_batched_ms": f64_ms, "fp64_batched_channels_per_s": nch / (f64_ms / 1e3),
                   "fp64_batched_phases_ms": f64_phases,
                   "fp64_batched_reference_order_ms": f64r_ms, "fp64_batched_reference_order_phases_ms": f64r_phases,

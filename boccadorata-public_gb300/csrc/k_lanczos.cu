@@ -284,7 +284,6 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     }
     __shared__ double tot[kMaxScal];
     __shared__ double prow[kMaxScal];   // the last built row, [alpha, beta, g..., m...] (every CTA)
-    __shared__ double lc[16];           // coefficients of a recurrence step's local vectors
     __shared__ double s_e2v;            // |E v|^2 of the last built vector
     __shared__ double s_xb, s_ixb;
     __shared__ int s_kmin;
@@ -294,7 +293,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int s_start[10], s_last[10];   // the chain schedule (read every step: kept on chip)
     __shared__ int s_flag;       // thread 0's decision after a full sweep (0 keep, 1 sweep again, 2 exhausted, 3 restart)
     __shared__ CT s_ixbf;        // 1/|w| in the arithmetic type
-    __shared__ CT lcf[16];       // lc in the arithmetic type
+    __shared__ CT lcf[16];       // coefficients of a recurrence step's local vectors
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
@@ -607,16 +606,8 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 w[i] = (CT)s;
             }
         } else if (rec) {
-            if (tid == 0) {   // v_{j-1}, v_{j-2} and the earlier chains' last vectors, with their coefficients
-                int n = 0;
-                lt[n] = rowslot[j - 1]; lc[n++] = prow[0];
-                if (j >= 2 && rowslot[j - 2] >= 0) { lt[n] = rowslot[j - 2]; lc[n++] = prow[1]; }
-                for (int q = 0; q < k; ++q)
-                    if (s_last[q] < j - 2 && rowslot[s_last[q]] >= 0) { lt[n] = rowslot[s_last[q]]; lc[n++] = prow[2 + q]; }
-                for (int q = 0; q < n; ++q) lcf[q] = (CT)lc[q];
-                s_nl = n;
-            }
-            __syncthreads();
+            // v_{j-1}, v_{j-2} and the earlier chains' last vectors with their coefficients
+            // (lt, lcf, s_nl), listed by warp 0 when it wrote row j - 1
             const int nl0 = s_nl;
             const VT *vp0 = vslice(lt[0]);
             for (int q = tid; q < nv; q += kLzThreads) {
@@ -802,6 +793,25 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         if (tid == 0) {
             rowslot[j] = nvec;
             s_e2v = tot[2 + D + k] * ixb * ixb;   // |E v_j|^2
+        }
+        // The next step's recurrence, when it continues this chain from this row: its
+        // vectors v_j, v_{j-1} and the earlier chains' last vectors with the row's alpha,
+        // beta and g as coefficients, listed here by warp 0 (which wrote the row), so the
+        // next step needs no barrier of its own before it forms w.
+        if (warp == 0) {
+            __syncwarp();
+            const bool next_newv = (k + 1 < C.n_used) && (j + 1 == s_start[k + 1]);
+            if (tid == 0 && !injected && !next_newv) {
+                int n = 0;
+                lt[n] = nvec; lcf[n++] = (CT)prow[0];
+                if (j >= 1 && rowslot[j - 1] >= 0) { lt[n] = rowslot[j - 1]; lcf[n++] = (CT)prow[1]; }
+                for (int q = 0; q < k; ++q)
+                    if (s_last[q] < j - 1 && rowslot[s_last[q]] >= 0) {
+                        lt[n] = rowslot[s_last[q]];
+                        lcf[n++] = (CT)prow[2 + q];
+                    }
+                s_nl = n;
+            }
         }
         prow_ok = !injected;
         ++nvec;
