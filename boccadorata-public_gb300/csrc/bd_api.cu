@@ -849,7 +849,7 @@ int launch_lanczos_range(bd_ctx *ctx, int ch_lo, int ch_hi, bool fp32) {
                 z.rowslot = ctx->d_lzslot + ctx->lz_slot_off[dir][I];
             }
             z.slice = ctx->d_lzslice + ctx->lz_slice_off[dir][I];
-            z.slice_stride = ((long long)z.S * 17 + 255) / 256 * 256;
+            z.slice_stride = ((long long)z.S * kLzSliceBytesPerPole + 255) / 256 * 256;
             if (reinterpret_cast<uintptr_t>(z.slice) % 256 != 0 ||
                 z.slice_stride * CL > lz_slice_bytes(P.N))
                 return fail(ctx, BD_ERR_STATE, "channel %d: Lanczos slice scratch misplaced", I);

@@ -117,11 +117,18 @@ __host__ __device__ inline GrpScratch lz_grp_scratch(const double *gE, long long
 }
 
 // Global scratch of one chain's slices: enough for any cluster size up to 16 with FP64
-// slices (17 bytes per pole, each CTA's share rounded up to 256 bytes); a multiple of
-// 256 bytes, so consecutive chains' slices stay aligned.
+// slices (E, w and E w as doubles and a touched byte: 25 bytes per pole, each CTA's share
+// rounded up to 256 bytes); a multiple of 256 bytes, so consecutive chains' slices stay
+// aligned.
+constexpr int kLzSliceBytesPerPole = 25;
 __host__ __device__ inline long long lz_slice_bytes(long long N) {
-    return (17 * N + 16 * (17 * 4 + 256) + 255) / 256 * 256;
+    return (kLzSliceBytesPerPole * N + 16 * (kLzSliceBytesPerPole * 4 + 256) + 255) / 256 * 256;
 }
+
+// Doubles of one pass's partial sums in the Lanczos kernel: a recurrence step's pass
+// sums two products per vector (with w and with E w) over the stored vectors, w and
+// E w, and one per coupling vector M_d.
+__host__ __device__ inline int lz_partials_per_pass(int rmax) { return 2 * ((rmax + 1) & ~1) + 32; }
 
 // One Dyson eigenproblem.
 struct DyJob {

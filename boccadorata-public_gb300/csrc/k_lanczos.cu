@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     using Sum = LzSum<CT>;
     using ST = typename Sum::T;
     constexpr bool kComp = kGlobalSlices && sizeof(VT) == 4;   // compensated partial sums
+    constexpr bool kFused = sizeof(VT) == 4;                     // one-reduction recurrence steps
     using PS = PSum<CT, kComp>;
     using PA = typename PS::A;
     constexpr int VW = Vec16<VT>::n;
@@ -247,22 +248,28 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
     extern __shared__ double sm[];
     const int rmax2 = (rmax + 1) & ~1;   // even: keeps the arrays behind 16-byte aligned
-    double *A = sm;                      // [2][rmax2] dot partials, alternating by pass
-    double *c = A + 2 * rmax2;
-    double *Bs = c + rmax2;
+    const int rq = (rmax + 3) / 4 * 4;
+    const int apn = lz_partials_per_pass(rmax);
+    double *A = sm;                      // [2][apn] dot partials, alternating by pass
+    double *c = A + 2 * apn;             // [rmax2] totals
+    double *dt = c + rmax2;              // [rmax2] <v_t|E w> of a recurrence step's pass
+    double *Bs = dt + rmax2;
     double *red = Bs + kMaxScal;
     int *rowslot = reinterpret_cast<int *>(red + kLzWarps * kMaxScal);   // vector slot of every row, -1: deflated
-    CT *cf = reinterpret_cast<CT *>(rowslot + (rmax + 3) / 4 * 4);     // 16-byte aligned
-    CT *Es, *w;
+    int *slotrow = rowslot + rq;                                        // row of every vector slot
+    CT *cf = reinterpret_cast<CT *>(slotrow + rq);                      // 16-byte aligned
+    CT *Es, *w, *ew;
     unsigned char *touched;
     if constexpr (kGlobalSlices) {   // chains too long for shared memory: this CTA's slices in global scratch
         Es = reinterpret_cast<CT *>(C.slice + (size_t)rank * C.slice_stride);
         w = Es + S;
-        touched = reinterpret_cast<unsigned char *>(w + S);
+        ew = w + S;
+        touched = reinterpret_cast<unsigned char *>(ew + S);
     } else {
-        Es = cf + (rmax + 3) / 4 * 4;
+        Es = cf + rq;
         w = Es + S;
-        touched = reinterpret_cast<unsigned char *>(w + S);
+        ew = w + S;
+        touched = reinterpret_cast<unsigned char *>(ew + S);
     }
     // this CTA's slice of the couplings M (CT, [d][S]) behind the slices, then the basis cache
     CT *Msl = nullptr;
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     VT *cache;
     int ccap;
     {
-        const char *end = kGlobalSlices ? reinterpret_cast<const char *>(cf + (rmax + 3) / 4 * 4)
+        const char *end = kGlobalSlices ? reinterpret_cast<const char *>(cf + rq)
                                         : (Msl ? reinterpret_cast<const char *>(Msl + (size_t)D * S)
                                                : reinterpret_cast<const char *>(touched + S));
         const uintptr_t e = (reinterpret_cast<uintptr_t>(end) + 15) & ~static_cast<uintptr_t>(15);
@@ -294,6 +301,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ int s_flag;       // thread 0's decision after a full sweep (0 keep, 1 sweep again, 2 exhausted, 3 restart)
     __shared__ CT s_ixbf;        // 1/|w| in the arithmetic type
     __shared__ CT lcf[16];       // coefficients of a recurrence step's local vectors
+    __shared__ double fsc[12];   // a recurrence step's sums of w: |w|^2, <w|E|w>, |E w|^2, <M_d|w>
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
@@ -361,7 +369,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // between a local update and the full sweep's dot products).
     int dpar = 0;
     auto dots_pass = [&](bool loc, int nl) {
-        double *Ap = A + (size_t)dpar * rmax2;
+        double *Ap = A + (size_t)dpar * apn;
         dpar ^= 1;
         const VT *wv = reinterpret_cast<const VT *>(w);
         // FP32 vectors: eight per warp at a time; FP64: four, two groups per lane in flight
@@ -434,6 +442,171 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             }
         }
         __syncthreads();
+    };
+
+    // (b1') The pass of a recurrence step: w = E v_{j-1} minus its known components, so
+    // the full sweep's coefficients c_t = <v_t|w> are rounding-sized and the scalars of
+    // the swept vector w' = w - sum_t c_t v_t follow from sums over w to first order in c
+    // (the neglected terms are O(|c|^2)):
+    //   |w'|^2 = |w|^2 - sum c_t^2,   <w'|E|w'> = <w|E|w> - 2 sum c_t d_t   (d_t = <v_t|E w>),
+    //   <M_d|w'> = <M_d|w> - sum c_t <M_d|v_t>,   <v_s|E|w'> = d_s - sum c_t <v_s|E|v_t>,
+    // with <M_d|v_t> and <v_s|E|v_t> the stored rows' m and (alpha, beta, g).  One cluster
+    // reduction then serves the step: this pass sums, per CTA, <v_t|w> and <v_t|E w> for
+    // every stored vector, the same for w and E w (|w|^2, <w|E|w>, |E w|^2) and <M_d|w>,
+    // eight vectors per warp at a time as in dots_pass.
+    auto dots_fused = [&](int nl) {
+        double *Ap = A + (size_t)dpar * apn;
+        dpar ^= 1;
+        const VT *wv = reinterpret_cast<const VT *>(w);
+        const VT *ev = reinterpret_cast<const VT *>(ew);
+        constexpr int NU = sizeof(CT) == 4 ? 8 : 4;
+        constexpr int LS2 = sizeof(CT) == 4 ? 1 : 2;   // lane L holds the total of value L >> LS2 of 2 NU
+        constexpr int UNR = sizeof(CT) == 4 ? 1 : 2;
+        const int nit = nl + 2;   // stored vectors, w, E w
+        for (int t0 = warp; t0 < nit; t0 += NU * kLzWarps) {
+            const VT *vp[NU];
+#pragma unroll
+            for (int u = 0; u < NU; ++u) {
+                const int t = t0 + u * kLzWarps;
+                vp[u] = (t < nl) ? vslice(t) : (t == nl ? wv : ev);
+            }
+            const int nu = min(NU, (nit - 1 - t0) / kLzWarps + 1);
+            PA acc[2 * NU];
+#pragma unroll
+            for (int u = 0; u < 2 * NU; ++u) acc[u] = PS::zero();
+#pragma unroll UNR
+            for (int q = lane; q < nv; q += 32) {
+                VT wq[VW], eq[VW];
+                load16g<VT>(wv + q * VW, wq);
+                load16g<VT>(ev + q * VW, eq);
+                VT x[NU][VW];   // all loads first (items beyond the pass read E w: valid, unused)
+#pragma unroll
+                for (int u = 0; u < NU; ++u) load16g<VT>(vp[u] + q * VW, x[u]);
+#pragma unroll
+                for (int u = 0; u < NU; ++u)
+                    if (u < nu) {
+                        if constexpr (kComp) {
+                            CT g = (CT)0, h = (CT)0;
+#pragma unroll
+                            for (int e = 0; e < VW; ++e) { g += x[u][e] * wq[e]; h += x[u][e] * eq[e]; }
+                            PS::add(acc[u], g);
+                            PS::add(acc[NU + u], h);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < VW; ++e) {
+                                acc[u] += x[u][e] * wq[e];
+                                acc[NU + u] += x[u][e] * eq[e];
+                            }
+                        }
+                    }
+            }
+            const PA r = warp_sums<2 * NU>(acc, lane);
+            const int vi = lane >> LS2, u = vi % NU, kind = vi / NU;
+            if ((lane & ((1 << LS2) - 1)) == 0 && u < nu) {
+                if constexpr (kComp) Sum::put(Ap + 2 * (t0 + u * kLzWarps) + kind, r);
+                else Sum::put(Ap + 2 * (t0 + u * kLzWarps) + kind, Sum::from_ct(r));
+            }
+        }
+        if (warp < D) {   // <M_d|w>, a warp per coupling vector (this CTA's slice: in Msl, or read from M)
+            const int d = warp;
+            PA a = PS::zero();
+            for (int q = lane; q < nv; q += 32) {
+                VT wq[VW], m[VW];
+                load16g<VT>(wv + q * VW, wq);
+                if (Msl) {
+                    load16g<VT>(reinterpret_cast<const VT *>(Msl + (size_t)d * S) + q * VW, m);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) {
+                        const int i = q * VW + e;
+                        m[e] = (i < ns) ? (VT)Mc[(size_t)d * N + i0 + i] : (VT)0;
+                    }
+                }
+                if constexpr (kComp) {
+                    CT g = (CT)0;
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) g += m[e] * wq[e];
+                    PS::add(a, g);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < VW; ++e) a += m[e] * wq[e];
+                }
+            }
+            const ST r = PS::finish(a);
+            if (lane == 0) Sum::put(Ap + 2 * nit + d, r);
+        }
+        cluster.sync();   // the partials of every CTA (also a barrier of this CTA's threads)
+        const int nval = 2 * nit + D;
+        for (int t = tid; t < nval; t += kLzThreads) {
+            const ST x = cluster_sum_st(Ap, t);
+            if (t < 2 * nl) {
+                if ((t & 1) == 0) {
+                    if constexpr (sizeof(CT) == 4) cf[t >> 1] = x.h + x.l;
+                    else cf[t >> 1] = (CT)x;
+                } else {
+                    dt[t >> 1] = Sum::value(x);
+                }
+            } else if (t == 2 * nl) {
+                fsc[0] = Sum::value(x);   // |w|^2
+            } else if (t == 2 * nl + 1) {
+                fsc[1] = Sum::value(x);   // <w|E|w>
+            } else if (t == 2 * nl + 3) {
+                fsc[2] = Sum::value(x);   // |E w|^2
+            } else if (t >= 2 * nit) {
+                fsc[3 + (t - 2 * nit)] = Sum::value(x);   // <M_d|w>
+            }
+        }
+        __syncthreads();
+    };
+
+    // <v_s|E|v_t> for s the last vector of earlier chain q, from the stored rows: alpha of
+    // row(s) at t = s, its beta for the chain's previous vector, its g for the earlier
+    // chains' last vectors, and each later row's g_q (read through L2: rank 0 wrote the
+    // rows, the cluster barriers since make them visible).
+    auto t_entry = [&](int sl, int q, int t) -> double {
+        const int srow = s_last[q];
+        const double *rs = C.out + (size_t)srow * NT;
+        if (t == sl) return __ldcg(rs);
+        if (t < sl) {
+            if (slotrow[t] == srow - 1 && srow - 1 >= s_start[q]) return __ldcg(rs + 1);
+            for (int p = 0; p < q; ++p)
+                if (t == lslot[p]) return __ldcg(rs + 2 + p);
+            return 0.0;
+        }
+        return __ldcg(C.out + (size_t)slotrow[t] * NT + 2 + q);
+    };
+    // The scalars of w' into tot[] by the corrections above: quantity 0 sum c_t^2, 1
+    // sum c_t d_t, 2 + d sum c_t <M_d|v_t>, 2 + D + q sum c_t <v_s(q)|E|v_t>, a warp each
+    // (warp 0 takes quantity 0, so thread 0 holds |w'|^2 when it decides).
+    auto fused_scalars = [&](int nl, int nq) {
+        const int nqty = 2 + D + nq;
+        for (int qi = warp; qi < nqty; qi += kLzWarps) {
+            CT a = (CT)0;
+            for (int t = lane; t < nl; t += 32) {
+                const CT ct = cf[t];
+                CT term = (CT)0;
+                if (qi == 0) term = ct * ct;
+                else if (qi == 1) term = ct * (CT)dt[t];
+                else if (qi < 2 + D) term = ct * (CT)__ldcg(C.out + (size_t)slotrow[t] * NT + C.nden_out + (qi - 2));
+                else {
+                    const int q = qi - 2 - D, sl = lslot[q];
+                    if (sl >= 0) term = ct * (CT)t_entry(sl, q, t);
+                }
+                a += term;
+            }
+            a = warp_sum_ct(a);
+            if (lane == 0) {
+                const double x = (double)a;
+                if (qi == 0) tot[0] = fsc[0] - x;
+                else if (qi == 1) tot[1] = fsc[1] - 2.0 * x;
+                else if (qi < 2 + D) tot[qi] = fsc[3 + (qi - 2)] - x;
+                else {
+                    const int q = qi - 2 - D, sl = lslot[q];
+                    tot[2 + D + q] = (sl >= 0) ? dt[sl] - x : 0.0;
+                }
+            }
+        }
+        if (tid == 0) tot[2 + D + nq] = fsc[2];   // |E w'|^2 ~ |E w|^2: only a threshold's scale
     };
 
     // (b3) w -= sum_t cf_t v_t over the pass's vectors: 16-byte vectors, eight rows in
@@ -626,7 +799,10 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     for (int u = 0; u < VW; ++u) x[u] -= ct * (CT)y[u];
                 }
 #pragma unroll
-                for (int u = 0; u < VW; ++u) w[qo + u] = x[u];
+                for (int u = 0; u < VW; ++u) {
+                    w[qo + u] = x[u];
+                    if constexpr (kFused) ew[qo + u] = Es[qo + u] * x[u];
+                }
             }
         } else {
             const VT *vp = vslice(rowslot[j - 1]);
@@ -659,10 +835,17 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             }
             __syncthreads();
             int nl = local ? s_nl : nvec;
-            dots_pass(local, nl);
+            // With FP32 vectors a recurrence step's first sweep takes the one-reduction pass
+            // (dots_fused); its scalars fall back to the exact pass when the sweep removed
+            // more than 1 % of |w|^2 or the step is not kept (the corrections are first order
+            // in the sweep).  With FP64 vectors the pass's second product per element would
+            // cost more FP64-pipe time than the reduction it saves.
+            bool fused = kFused && rec && attempt == 0;
+            if (fused) dots_fused(nl);
+            else dots_pass(local, nl);
             // |w|^2 before any projection: E v_{j-1}'s, from row j - 1's sums, after the recurrence
             const double wn2_first = (rec && attempt == 0) ? s_e2v : c[nl];
-            double wn2_before = c[nl];
+            double wn2_before = fused ? fsc[0] : c[nl];
             for (;;) {
                 update_pass(local, nl);
                 if (local) {   // the full sweep's dot products follow the local update directly
@@ -672,6 +855,30 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     dots_pass(false, nl);
                     wn2_before = c[nl];
                     continue;
+                }
+                if (fused) {
+                    fused = false;
+                    fused_scalars(nl, nq);
+                    if (tid == 0) {
+                        const double x2 = tot[0];
+                        int f = 4;   // the exact scalars of w'
+                        if (x2 >= 0.99 * wn2_before && !(x2 < eta2 * wn2_before) &&
+                            !(x2 <= thr_exh * wn2_first || x2 == 0.0) && !(x2 <= tau * wn2_first)) {
+                            f = 0;   // keep: normalise
+                            const double r = rsqrt_newton(x2);
+                            s_xb = x2 * r;
+                            s_ixb = r;
+                            s_ixbf = (CT)r;
+                        }
+                        s_flag = f;
+                    }
+                    __syncthreads();
+                    if (s_flag == 0) {
+                        n2 = tot[0];
+                        fl = 0;
+                        ++nfull;
+                        break;
+                    }
                 }
                 scalar_partials(nq);
                 scalar_reduce(nq);
@@ -748,7 +955,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     row[0] = C.E[kmin];
                     for (int d = 0; d < D; ++d) row[C.nden_out + d] = C.M[(size_t)d * N + kmin];
                 }
-                if (tid == 0) rowslot[j] = nvec;
+                if (tid == 0) { rowslot[j] = nvec; slotrow[nvec] = j; }
                 ++nvec;
                 done = true;
                 prow_ok = false;
@@ -792,6 +999,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         }
         if (tid == 0) {
             rowslot[j] = nvec;
+            slotrow[nvec] = j;
             s_e2v = tot[2 + D + k] * ixb * ixb;   // |E v_j|^2
         }
         // The next step's recurrence, when it continues this chain from this row: its
@@ -825,12 +1033,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 }
 
 size_t lanczos_smem_bytes(int S, int rmax, bool global_slices) {
-    // sized for FP64 vectors (E and w as doubles); FP32 vectors use less
+    // sized for FP64 vectors (E, w and E w as doubles); FP32 vectors use less
     const size_t rmax2 = ((size_t)rmax + 1) & ~(size_t)1;
-    const size_t fixed = sizeof(double) * (3 * rmax2 + (size_t)(rmax + 3) / 4 * 4 + kMaxScal +
+    const size_t rq = (size_t)(rmax + 3) / 4 * 4;
+    const size_t fixed = sizeof(double) * (2 * (size_t)lz_partials_per_pass(rmax) + 2 * rmax2 + rq + kMaxScal +
                                            (size_t)kLzWarps * kMaxScal) +
-                         sizeof(int) * (size_t)(rmax + 3) / 4 * 4 + 16;
-    return global_slices ? fixed : fixed + sizeof(double) * 2 * (size_t)S + (size_t)S;
+                         sizeof(int) * 2 * rq + 16;
+    return global_slices ? fixed : fixed + sizeof(double) * 3 * (size_t)S + (size_t)S;
 }
 
 template <typename VT, bool G>
