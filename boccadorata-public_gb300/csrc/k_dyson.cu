@@ -397,7 +397,6 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     df *R = w + n;                           // [D][n]
     __shared__ df s_dfs[2][4];               // tau, scal, -, beta of the step, by parity
     __shared__ int s_flag[2];                // the column has a reflector, by parity
-    __shared__ df s_rx[8];                   // R_d[b0+1:] . x[1:]
     __shared__ df s_coef[8];                 // tau s_d, s_d = R_d[b0:] . v
     for (int q = tid; q < n * n; q += kTsThreads) {
         const int i = q / n, j = q - i * n;
@@ -410,64 +409,75 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     for (int q = tid; q < D * n; q += kTsThreads) R[q] = df{((q % n) == (q / n)) ? 1.0f : 0.0f, 0.0f};
     __syncthreads();
     const df zero{0.0f, 0.0f};
+    // The reflector of column k by warp 0: sigma = |x_{1:}|^2, then lane 0 forms beta, tau
+    // and scal into the column's parity slot and writes the column's d, e, tau (FP64).
+    auto reflector = [&](int k) {
+        const int b0 = k + 1, m = n - b0;
+        const df *col = A + k;
+        df *sdf = s_dfs[k & 1];
+        df s2 = zero;
+        for (int t = 1 + lane; t < m; t += 32) { const df x = col[(size_t)(b0 + t) * ld]; s2 = dfm::fma(x, x, s2); }
+        s2 = dfm::warp_sum(s2);
+        if (lane == 0) {
+            // beta = -sign(alpha) |x|, tau = (beta - alpha) / beta = 1 + |alpha| / |x|,
+            // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|), in double-float
+            // with Newton's reciprocal and square root (FP64 only outside the FP32 range)
+            const df al = col[(size_t)b0 * ld];
+            const bool nz = (s2.h != 0.0f || s2.l != 0.0f);
+            const bool ng = signbit(al.h);
+            const df aa = ng ? dfm::neg(al) : al;
+            df tau = zero, scal = zero, beta = al;
+            if (nz) {
+                const df x2 = dfm::fma(al, al, s2);
+                if (x2.h > 1e-30f && x2.h < 1e30f) {
+                    const df r = dfm::rsqrt(x2, 1), nx = dfm::mul(x2, r);
+                    beta = ng ? nx : dfm::neg(nx);
+                    tau = dfm::fma(aa, r, df{1.0f, 0.0f});
+                    scal = dfm::rcp(dfm::add(aa, nx), 1);
+                    if (ng) scal = dfm::neg(scal);
+                } else {
+                    const double a = dfm::to_double(al), x2d = dfm::to_double(x2);
+                    const double r = 1.0 / sqrt(x2d), nx = x2d * r;
+                    beta = dfm::from_double(-copysign(nx, a));
+                    tau = dfm::from_double(fma(fabs(a), r, 1.0));
+                    scal = dfm::from_double(copysign(1.0 / (fabs(a) + nx), a));
+                }
+            }
+            sdf[0] = tau; sdf[1] = scal; sdf[3] = beta;
+            s_flag[k & 1] = nz;
+            J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);   // the step's d, e, tau in FP64
+            J.e[k] = dfm::to_double(beta);
+            J.tau[k] = dfm::to_double(tau);
+        }
+    };
+    // Look-ahead: the rank-2 update of column k leaves column k + 1 to warp 0, which updates
+    // it first and forms column k + 1's reflector while the other warps update the rest of
+    // the trailing block, so a column takes three barriers and the reflector's serial
+    // chain runs beside the update instead of before the next column's product.
+    if (n >= 3 && warp == 0) reflector(0);
+    __syncthreads();
     for (int k = 0; k + 2 < n; ++k) {
         const int b0 = k + 1, m = n - b0;
         const df *col = A + k;               // A(b0 + t, k) = col[(b0 + t) * ld]
-        // the step's scalars alternate between two slots: a warp that skips a step
-        // (H_k = I) may write step k+1's while another still reads step k's
-        df *sdf = s_dfs[k & 1];
-        // 1. warp 0: sigma = |x_{1:}|^2 and the reflector; warps 1..D: rx_d = R_d[b0+1:] . x[1:]
-        if (warp == 0) {
-            df s2 = zero;
-            for (int t = 1 + lane; t < m; t += 32) { const df x = col[(size_t)(b0 + t) * ld]; s2 = dfm::fma(x, x, s2); }
-            s2 = dfm::warp_sum(s2);
-            if (lane == 0) {
-                // beta = -sign(alpha) |x|, tau = (beta - alpha) / beta = 1 + |alpha| / |x|,
-                // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|), in double-float
-                // with Newton's reciprocal and square root (FP64 only outside the FP32 range)
-                const df al = col[(size_t)b0 * ld];
-                const bool nz = (s2.h != 0.0f || s2.l != 0.0f);
-                const bool ng = signbit(al.h);
-                const df aa = ng ? dfm::neg(al) : al;
-                df tau = zero, scal = zero, beta = al;
-                if (nz) {
-                    const df x2 = dfm::fma(al, al, s2);
-                    if (x2.h > 1e-30f && x2.h < 1e30f) {
-                        const df r = dfm::rsqrt(x2, 1), nx = dfm::mul(x2, r);
-                        beta = ng ? nx : dfm::neg(nx);
-                        tau = dfm::fma(aa, r, df{1.0f, 0.0f});
-                        scal = dfm::rcp(dfm::add(aa, nx), 1);
-                        if (ng) scal = dfm::neg(scal);
-                    } else {
-                        const double a = dfm::to_double(al), x2d = dfm::to_double(x2);
-                        const double r = 1.0 / sqrt(x2d), nx = x2d * r;
-                        beta = dfm::from_double(-copysign(nx, a));
-                        tau = dfm::from_double(fma(fabs(a), r, 1.0));
-                        scal = dfm::from_double(copysign(1.0 / (fabs(a) + nx), a));
-                    }
-                }
-                sdf[0] = tau; sdf[1] = scal; sdf[3] = beta;
-                s_flag[k & 1] = nz;
-            }
-        } else {
-            for (int d = warp - 1; d < D; d += kTsThreads / 32 - 1) {
-                df s = zero;
-                for (int t = 1 + lane; t < m; t += 32) s = dfm::fma(R[(size_t)d * n + b0 + t], col[(size_t)(b0 + t) * ld], s);
-                s = dfm::warp_sum(s);
-                if (lane == 0) s_rx[d] = s;
-            }
+        // the step's scalars alternate between two slots (written one column ahead)
+        const df *sdf = s_dfs[k & 1];
+        if (!s_flag[k & 1]) {                // column already reduced: H_k = I
+            if (k + 3 < n && warp == 0) reflector(k + 1);
+            __syncthreads();
+            continue;
         }
-        __syncthreads();
-        if (tid == kTsThreads - 1) {   // the step's d, e, tau in FP64, off the critical path
-            J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
-            J.e[k] = dfm::to_double(sdf[3]);
-            J.tau[k] = dfm::to_double(sdf[0]);
-        }
-        if (!s_flag[k & 1]) continue;        // column already reduced: H_k = I
         const df taud = sdf[0], scald = sdf[1];
-        // 2. parts of A v (trailing block, local indices) with v = (1, scal x[1:]), the
-        //    column read in place, eight parts per row so all sixteen warps are busy; v
-        //    itself, and the R update's coefficients tau s_d, s_d = R_d[b0:] . v
+        // 2. the last D warps first: rx_d = R_d[b0+1:] . x[1:] and the R update's
+        //    coefficients tau s_d, s_d = R_d[b0:] . v; then every warp: parts of A v
+        //    (trailing block, local indices) with v = (1, scal x[1:]), the column read in
+        //    place, eight parts per row so all sixteen warps are busy; and v itself
+        if (warp >= kTsThreads / 32 - D) {
+            const int d = kTsThreads / 32 - 1 - warp;
+            df sx = zero;
+            for (int t = 1 + lane; t < m; t += 32) sx = dfm::fma(R[(size_t)d * n + b0 + t], col[(size_t)(b0 + t) * ld], sx);
+            sx = dfm::warp_sum(sx);
+            if (lane == 0) s_coef[d] = dfm::mul(taud, dfm::fma(scald, sx, R[(size_t)d * n + b0]));
+        }
         for (int u = tid; u < kTsParts * m; u += kTsThreads) {
             const int i = u / kTsParts, h = u - i * kTsParts;
             const int q0 = (int)(((long long)m * h) / kTsParts), q1 = (int)(((long long)m * (h + 1)) / kTsParts);
@@ -484,7 +494,6 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             ph[h * n + i] = r;
         }
         for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(col[(size_t)(b0 + t) * ld], scald);
-        if (tid < D) s_coef[tid] = dfm::mul(taud, dfm::fma(scald, s_rx[tid], R[(size_t)tid * n + b0]));
         __syncthreads();
         // 3. warp 0: p = tau A v, K = (tau / 2) p . v and w = p - K v (each lane its own
         //    entries); the other warps: R <- R H_k
@@ -509,17 +518,32 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             }
         }
         __syncthreads();
-        // 4. A -= v w^T + w v^T on the trailing lower triangle, rows i and m-1-i per warp
-        for (int i1 = warp; i1 < (m + 1) / 2; i1 += kTsThreads / 32) {
-            const int i2 = m - 1 - i1;
-            const int len = (i1 == i2) ? (i1 + 1) : (m + 1);
-            for (int u = lane; u < len; u += 32) {
-                const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
-                df *a = A + (size_t)(b0 + r) * ld + b0 + c;
-                const df t2 = dfm::fma(w[r], v[c], dfm::mul(v[r], w[c]));
+        // 4. A -= v w^T + w v^T on the trailing lower triangle: warp 0 takes column k + 1
+        //    (local column 0) and then that column's reflector; warps 1..15 the rest, rows i
+        //    and m-1-i per warp so the triangle's rows balance, each result also at its mirror
+        if (warp == 0) {
+            for (int r = lane; r < m; r += 32) {
+                df *a = A + (size_t)(b0 + r) * ld + b0;
+                const df t2 = dfm::fma(w[r], v[0], dfm::mul(v[r], w[0]));
                 const df x = dfm::add(*a, dfm::neg(t2));
                 *a = x;
-                A[(size_t)(b0 + c) * ld + b0 + r] = x;   // the mirror, read by the next product
+                A[(size_t)b0 * ld + b0 + r] = x;
+            }
+            __syncwarp();
+            if (k + 3 < n) reflector(k + 1);
+        } else {
+            for (int i1 = warp - 1; i1 < (m + 1) / 2; i1 += kTsThreads / 32 - 1) {
+                const int i2 = m - 1 - i1;
+                const int len = (i1 == i2) ? (i1 + 1) : (m + 1);
+                for (int u = lane; u < len; u += 32) {
+                    const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
+                    if (c == 0) continue;   // column k + 1: warp 0's
+                    df *a = A + (size_t)(b0 + r) * ld + b0 + c;
+                    const df t2 = dfm::fma(w[r], v[c], dfm::mul(v[r], w[c]));
+                    const df x = dfm::add(*a, dfm::neg(t2));
+                    *a = x;
+                    A[(size_t)(b0 + c) * ld + b0 + r] = x;   // the mirror, read by the next product
+                }
             }
         }
         __syncthreads();

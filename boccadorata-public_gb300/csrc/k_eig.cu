@@ -354,51 +354,57 @@ __device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, InvitShar
     for (int q = k0 + 1; q <= k; ++q) xs = fmax(W(q), xs + tl.pertol);
     const df x = dfm::from_double(xs);
     const df zero{0.0f, 0.0f};
-    for (int i = b0; i <= b1; ++i) {
-        a.dd(i) = df_sub(dfm::from_double(d[i]), x);
-        const df ei = (i < b1) ? dfm::from_double(e[i]) : zero;
-        a.u1(i) = ei;
-        a.ll(i) = ei;
-        a.u2(i) = zero;
-    }
+    const float pt = (float)tl.pertol;
+    auto pivot_rcp = [&](df p) {   // pivots no smaller than pertol, kept as reciprocals for the solves
+        if (fabsf(p.h) < pt) p = df{p.h < 0.0f ? -pt : pt, 0.0f};
+        return dfm::rcp(p);
+    };
+    // LU with partial pivoting of T_b - x I (rows i and i+1 may swap).  The running
+    // diagonal and superdiagonal entries of the next row stay in registers, so the
+    // dependent chain is the arithmetic alone; each row's factors go to shared memory
+    // for the solves as soon as they are final.
+    df cur_d = df_sub(dfm::from_double(d[b0]), x);        // dd(i) as updated so far
+    df cur_u = (b0 < b1) ? dfm::from_double(e[b0]) : zero;   // u1(i) as updated so far
     for (int i = b0; i < b1; ++i) {
-        const df di = a.dd(i), li = a.ll(i);
+        const df di = cur_d, li = dfm::from_double(e[i]), ui = cur_u;
+        const df nd = df_sub(dfm::from_double(d[i + 1]), x);              // dd(i+1) before this row
+        const df nu = (i + 1 < b1) ? dfm::from_double(e[i + 1]) : zero;   // u1(i+1) before this row
         if (fabsf(di.h) >= fabsf(li.h)) {
             a.set_pv(i, false);
             const df f = (di.h != 0.0f) ? dfm::mul(li, dfm::rcp(di)) : zero;
             a.ll(i) = f;
-            a.dd(i + 1) = dfm::fma(dfm::neg(f), a.u1(i), a.dd(i + 1));
+            a.u1(i) = ui;
+            a.u2(i) = zero;
+            a.dd(i) = pivot_rcp(di);
+            cur_d = dfm::fma(dfm::neg(f), ui, nd);
+            cur_u = nu;
         } else {
             a.set_pv(i, true);
             const df f = dfm::mul(di, dfm::rcp(li));
-            a.dd(i) = li;
             a.ll(i) = f;
-            const df tt = a.u1(i);
-            a.u1(i) = a.dd(i + 1);
-            a.dd(i + 1) = dfm::fma(dfm::neg(f), a.dd(i + 1), tt);
-            if (i + 1 < b1) {
-                a.u2(i) = a.u1(i + 1);
-                a.u1(i + 1) = dfm::mul(dfm::neg(f), a.u1(i + 1));
-            }
+            a.u1(i) = nd;
+            a.u2(i) = nu;
+            a.dd(i) = pivot_rcp(li);
+            cur_d = dfm::fma(dfm::neg(f), nd, ui);
+            cur_u = dfm::mul(dfm::neg(f), nu);
         }
     }
-    // pivots no smaller than pertol, kept as reciprocals for the solves
-    const float pt = (float)tl.pertol;
-    for (int i = b0; i <= b1; ++i) {
-        df p = a.dd(i);
-        if (fabsf(p.h) < pt) p = df{p.h < 0.0f ? -pt : pt, 0.0f};
-        a.dd(i) = dfm::rcp(p);
-    }
+    a.u1(b1) = zero;
+    a.u2(b1) = zero;
+    a.dd(b1) = pivot_rcp(cur_d);
     for (int i = b0; i <= b1; ++i)
         a.y(i) = df{0.5f + (float)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0f, 0.0f};
     for (int it = 0; it < 2; ++it) {
-        for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges
-            df bi = a.y(i), bi1 = a.y(i + 1);
+        df cur = a.y(b0);
+        for (int i = b0; i < b1; ++i) {   // L^-1 with the interchanges, y(i) carried in a register
+            df bi = cur, bi1 = a.y(i + 1);
             const df f = a.ll(i);
             if (!a.pv(i)) bi1 = dfm::fma(dfm::neg(f), bi, bi1);
             else { const df tt = bi; bi = bi1; bi1 = dfm::fma(dfm::neg(f), bi1, tt); }
-            a.y(i) = bi; a.y(i + 1) = bi1;
+            a.y(i) = bi;
+            cur = bi1;
         }
+        a.y(b1) = cur;
         df y1 = zero, y2 = zero;
         float nrm = 0.0f;
         for (int i = b1; i >= b0; --i) {   // U y = b, two superdiagonals
