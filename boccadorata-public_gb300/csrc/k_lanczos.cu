@@ -611,43 +611,46 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
     // (b3) w -= sum_t cf_t v_t over the pass's vectors: 16-byte vectors, eight rows in
     // flight.  Each thread updates the 16-byte groups q = tid, tid + kLzThreads, ...
+    // sum_t cf_t v_t over the pass's vectors for the 16-byte group at qo
+    auto group_sum = [&](bool loc, int nl, int qo, CT *acc) {
+#pragma unroll
+        for (int u = 0; u < VW; ++u) acc[u] = 0;
+        int t = 0;
+        for (; t + 7 < nl; t += 8) {
+            VT x[8][VW];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) load16g<VT>(vslice(loc ? lt[t + r] : t + r) + qo, x[r]);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const CT cr = cf[t + r];
+#pragma unroll
+                for (int u = 0; u < VW; ++u) acc[u] += cr * x[r][u];
+            }
+        }
+        for (; t + 3 < nl; t += 4) {
+            VT x0[VW], x1[VW], x2[VW], x3[VW];
+            load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
+            load16g<VT>(vslice(loc ? lt[t + 1] : t + 1) + qo, x1);
+            load16g<VT>(vslice(loc ? lt[t + 2] : t + 2) + qo, x2);
+            load16g<VT>(vslice(loc ? lt[t + 3] : t + 3) + qo, x3);
+            const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
+#pragma unroll
+            for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
+        }
+        for (; t < nl; ++t) {
+            VT x0[VW];
+            load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
+            const CT c0 = cf[t];
+#pragma unroll
+            for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
+        }
+    };
     auto update_pass = [&](bool loc, int nl) {
         for (int q = tid; q < nv; q += kLzThreads) {
             CT acc[VW];
+            group_sum(loc, nl, q * VW, acc);
 #pragma unroll
-            for (int u = 0; u < VW; ++u) acc[u] = 0;
-            const int qo = q * VW;
-            int t = 0;
-            for (; t + 7 < nl; t += 8) {
-                VT x[8][VW];
-#pragma unroll
-                for (int r = 0; r < 8; ++r) load16g<VT>(vslice(loc ? lt[t + r] : t + r) + qo, x[r]);
-#pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const CT cr = cf[t + r];
-#pragma unroll
-                    for (int u = 0; u < VW; ++u) acc[u] += cr * x[r][u];
-                }
-            }
-            for (; t + 3 < nl; t += 4) {
-                VT x0[VW], x1[VW], x2[VW], x3[VW];
-                load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
-                load16g<VT>(vslice(loc ? lt[t + 1] : t + 1) + qo, x1);
-                load16g<VT>(vslice(loc ? lt[t + 2] : t + 2) + qo, x2);
-                load16g<VT>(vslice(loc ? lt[t + 3] : t + 3) + qo, x3);
-                const CT c0 = cf[t], c1 = cf[t + 1], c2 = cf[t + 2], c3 = cf[t + 3];
-#pragma unroll
-                for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u] + c1 * x1[u] + c2 * x2[u] + c3 * x3[u];
-            }
-            for (; t < nl; ++t) {
-                VT x0[VW];
-                load16g<VT>(vslice(loc ? lt[t] : t) + qo, x0);
-                const CT c0 = cf[t];
-#pragma unroll
-                for (int u = 0; u < VW; ++u) acc[u] += c0 * x0[u];
-            }
-#pragma unroll
-            for (int u = 0; u < VW; ++u) w[qo + u] -= acc[u];
+            for (int u = 0; u < VW; ++u) w[q * VW + u] -= acc[u];
         }
     };
 
@@ -815,11 +818,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             }
         }
         bool injected = false;     // w replaced by a pseudo-random restart vector
+        bool upd = false;          // the kept sweep's update is still to be applied (with the normalisation)
         bool done = false;         // step finished by an untouched-pole unit vector
         double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
             int nfull = 0;
             int fl = 0;            // thread 0's decision after the last sweep (s_flag)
+            upd = false;
             // A continuing chain's w = E v_{j-1} has large components only on v_{j-1}, v_{j-2}
             // and the last vector of every earlier chain (the fishbone couplings); everything
             // else is rounding.  The first pass projects out just those few vectors, then
@@ -847,16 +852,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             const double wn2_first = (rec && attempt == 0) ? s_e2v : c[nl];
             double wn2_before = fused ? fsc[0] : c[nl];
             for (;;) {
-                update_pass(local, nl);
-                if (local) {   // the full sweep's dot products follow the local update directly
-                    local = false;
-                    nl = nvec;
-                    __syncthreads();
-                    dots_pass(false, nl);
-                    wn2_before = c[nl];
-                    continue;
-                }
-                if (fused) {
+                if (fused) {   // the scalars from the pass, before the sweep's update
                     fused = false;
                     fused_scalars(nl, nq);
                     if (tid == 0) {
@@ -873,11 +869,24 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                         s_flag = f;
                     }
                     __syncthreads();
-                    if (s_flag == 0) {
+                    if (s_flag == 0) {   // kept: the sweep's update is applied with the normalisation
                         n2 = tot[0];
                         fl = 0;
                         ++nfull;
+                        upd = true;
                         break;
+                    }
+                    update_pass(false, nl);   // the exact scalars of the swept vector follow
+                }
+                else {
+                    update_pass(local, nl);
+                    if (local) {   // the full sweep's dot products follow the local update directly
+                        local = false;
+                        nl = nvec;
+                        __syncthreads();
+                        dots_pass(false, nl);
+                        wn2_before = c[nl];
+                        continue;
                     }
                 }
                 scalar_partials(nq);
@@ -976,10 +985,12 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             const CT inv = s_ixbf;
             for (int q = tid; q < nv; q += kLzThreads) {
                 const int qo = q * VW;
+                CT acc[VW] = {};
+                if (upd) group_sum(false, nvec, qo, acc);
                 VT v[VW];
 #pragma unroll
                 for (int u = 0; u < VW; ++u) {
-                    v[u] = (VT)(w[qo + u] * inv);
+                    v[u] = (VT)((w[qo + u] - acc[u]) * inv);
                     touched[qo + u] |= (v[u] != (VT)0);
                 }
                 store16g<VT>(vj + qo, v);
