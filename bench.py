@@ -477,18 +477,22 @@ def gpu_arm(args):
         wall = time.perf_counter() - t0
         return statistics.mean(dev), wall / steps * 1e3, lz, ctx.launch_count() - l0
 
-    # ---- the headline: mixed-precision batched form
+    # ---- the headline: mixed-precision batched form, the step replayed as one captured CUDA
+    # graph (BD_RUN_GRAPH: the same 27 kernels, captured once, replayed every step)
     clocks = Clocks(local) if rank == 0 else None
-    dev_ms, wall_ms, lz_ms, launches = timed(dict(mixed=True), args.steps, args.warmup)
+    dev_ms, wall_ms, lz_ms, launches = timed(dict(mixed=True, graph=True), args.steps, args.warmup)
     dev_phases = ctx.timings()
     clk = clocks.stop() if clocks else None
+    # the same form launched kernel by kernel on the stream
+    stream_ms, stream_wall_ms, _, _ = timed(dict(mixed=True), max(3, min(args.steps, 5)), 1)
     step_s = max_over_ranks(dev_ms / 1e3)
     value = whole_job_rate(world, nch, step_s)
 
     # ---- the plain FP64 forms (the stable pole order the mixed form uses), and the FP64 form
     # whose reduction visits equal energies in the reference's heap-sort order
-    f64_ms, _, f64_lz, _ = timed(dict(mixed=False), max(2, min(args.steps, 3)), 1)
+    f64_ms, _, f64_lz, _ = timed(dict(mixed=False, graph=True), max(2, min(args.steps, 3)), 1)
     f64_phases = ctx.timings()
+    f64s_ms, _, _, _ = timed(dict(mixed=False), max(2, min(args.steps, 3)), 1)
     f64r_ms, _, _, _ = timed(dict(mixed=False, ref_order=True), max(2, min(args.steps, 3)), 1)
     f64r_phases = ctx.timings()
     pc_ms, _, _, _ = timed(dict(mixed=False, per_channel=True), 1, 1)
@@ -567,7 +571,7 @@ def gpu_arm(args):
         "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator in the reference's formats)",
         "config": {"workload": args.workload, "nmax": 10, "hw": 16.0, "seed": 2, "lanczos_iterations_per_pivot": 100,
-                   "channels": nch, "form": "mixed precision (FP32 Lanczos vectors), all channels batched",
+                   "channels": nch, "form": "mixed precision (FP32 Lanczos vectors), all channels batched, the step replayed as a captured CUDA graph",
                    "l2": "inputs larger than L2 (293 MB interaction, ~0.9 GB Lanczos basis); no flush",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "roofline": roof,
@@ -577,8 +581,10 @@ def gpu_arm(args):
         "clocks": clk,
         "gpu_launches": launches,
         "forms": {"mixed_batched_ms": dev_ms, "mixed_batched_wall_ms": wall_ms,
+                  "mixed_batched_stream_launches_ms": stream_ms, "mixed_batched_stream_launches_wall_ms": stream_wall_ms,
                   "mixed_batched_phases_ms": dev_phases,
                   "fp64_batched_ms": f64_ms, "fp64_batched_channels_per_s": nch / (f64_ms / 1e3),
+                  "fp64_batched_stream_launches_ms": f64s_ms,
                   "fp64_batched_phases_ms": f64_phases,
                   "fp64_batched_reference_order_ms": f64r_ms, "fp64_batched_reference_order_phases_ms": f64r_phases,
                   "fp64_per_channel_ms": pc_ms, "fp64_per_channel_channels_per_s": nch / (pc_ms / 1e3),

@@ -289,6 +289,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         cache = reinterpret_cast<VT *>(e);
         ccap = (e < lim && S > 0) ? (int)((lim - e) / ((uintptr_t)S * sizeof(VT))) : 0;
     }
+    // FP64 vectors: the two most recent vectors (read by every recurrence step) keep their
+    // slices in two ring slots behind the cache once they are beyond it.  (With FP32
+    // vectors the cache holds four times as many, and the ring's extra select in every
+    // vector access cost more than it saved.)
+    const bool hasring = sizeof(VT) == 8 && ccap >= 3;
+    if (hasring) ccap -= 2;
+    VT *ring = cache + (size_t)ccap * S;
     __shared__ double tot[kMaxScal];
     __shared__ double prow[kMaxScal];   // the last built row, [alpha, beta, g..., m...] (every CTA)
     __shared__ double s_e2v;            // |E v|^2 of the last built vector
@@ -305,7 +312,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
-    auto vslice = [&](int t) -> VT * { return t < ccap ? cache + (size_t)t * S : V + (size_t)t * C.ld + i0; };
+    int nvec = 0;                // vectors stored so far
+    auto vslice = [&](int t) -> VT * {
+        return t < ccap ? cache + (size_t)t * S
+                        : (hasring && t >= nvec - 2 ? ring + (size_t)(t & 1) * S : V + (size_t)t * C.ld + i0);
+    };
     const CT *Mc = reinterpret_cast<const CT *>(sizeof(CT) == 4 ? static_cast<const void *>(C.Mf)
                                                                   : static_cast<const void *>(C.M));
     for (int i = tid; i < S; i += kLzThreads) { Es[i] = (i < ns) ? (CT)C.E[i0 + i] : (CT)0; touched[i] = 0; }
@@ -331,7 +342,6 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         while (lo < hi) { const int mid = (lo + hi) >> 1; if (C.gInfo[1 + mid] > d) hi = mid; else lo = mid + 1; }
         return lo;
     };
-    int nvec = 0;                // vectors stored so far
     bool tail = false;           // rest of the current pivot chain deflated
     bool contaminated = false;   // a restart vector was stored: no deflation from here on
     int ndefl = 0;
@@ -544,7 +554,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     if constexpr (sizeof(CT) == 4) cf[t >> 1] = x.h + x.l;
                     else cf[t >> 1] = (CT)x;
                 } else {
-                    dt[t >> 1] = Sum::value(x);
+                    Sum::put(dt + (t >> 1), x);   // kept as the sum's pair: no FP64 instruction here
                 }
             } else if (t == 2 * nl) {
                 fsc[0] = Sum::value(x);   // |w|^2
@@ -586,7 +596,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 const CT ct = cf[t];
                 CT term = (CT)0;
                 if (qi == 0) term = ct * ct;
-                else if (qi == 1) term = ct * (CT)dt[t];
+                else if (qi == 1) {
+                    const ST x = Sum::get(dt + t);
+                    if constexpr (sizeof(CT) == 4) term = ct * (x.h + x.l);
+                    else term = ct * (CT)x;
+                }
                 else if (qi < 2 + D) term = ct * (CT)__ldcg(C.out + (size_t)slotrow[t] * NT + C.nden_out + (qi - 2));
                 else {
                     const int q = qi - 2 - D, sl = lslot[q];
@@ -602,7 +616,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 else if (qi < 2 + D) tot[qi] = fsc[3 + (qi - 2)] - x;
                 else {
                     const int q = qi - 2 - D, sl = lslot[q];
-                    tot[2 + D + q] = (sl >= 0) ? dt[sl] - x : 0.0;
+                    tot[2 + D + q] = (sl >= 0) ? Sum::value(Sum::get(dt + sl)) - x : 0.0;
                 }
             }
         }
@@ -951,7 +965,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             if (rank == 0 && tid == 0) atomicAdd(&C.stat[1], 1);
             if (kmin != INT_MAX) {
                 VT *vj = V + (size_t)nvec * C.ld + i0;
-                VT *vc = nvec < ccap ? cache + (size_t)nvec * S : nullptr;
+                VT *vc = nvec < ccap ? cache + (size_t)nvec * S : (hasring ? ring + (size_t)(nvec & 1) * S : nullptr);
                 for (int i = tid; i < S; i += kLzThreads) {
                     const bool hit = (i0 + i == kmin);
                     vj[i] = hit ? (VT)1 : (VT)0;
@@ -981,7 +995,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         const double xb = s_xb, ixb = s_ixb;
         VT *vj = V + (size_t)nvec * C.ld + i0;
         {
-            VT *vc = nvec < ccap ? cache + (size_t)nvec * S : nullptr;
+            VT *vc = nvec < ccap ? cache + (size_t)nvec * S : (hasring ? ring + (size_t)(nvec & 1) * S : nullptr);
             const CT inv = s_ixbf;
             for (int q = tid; q < nv; q += kLzThreads) {
                 const int qo = q * VW;
