@@ -231,6 +231,8 @@ struct bd_ctx {
     // lists, so the segment scan and the plan's uploads overlap their transfer
     cudaStream_t st_aux = nullptr;
     cudaEvent_t ev_up[2] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // the step's auxiliary branch (EHF)
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr; // and its backward poles
     bool v_pending = false;
     bool v_checked = false;   // h_vcheck holds the check of the last interaction upload
     long long vpp_repeated = 0;   // repeated pairs left out of the last interaction read from a file
@@ -696,10 +698,19 @@ int check_chan(bd_ctx *ctx, int ish) {
 }
 
 // ---------------------------------------------------------------- Sigma(2)
-int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
+// aux != nullptr: the backward poles go to that stream once the V' gather is done (their
+// rows are independent of the forward ones); the caller joins it before the sort.
+int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t aux = nullptr) {
     const Chan &A = ctx->chans[ch_lo], &Z = ctx->chans[ch_hi - 1];
     const int b0 = A.blk_first, nb = Z.blk_first + Z.nblk - b0;
-    if (nb <= 0) return BD_OK;
+    if (nb <= 0) {
+        if (aux) {   // the join the caller waits for
+            CU(cudaEventRecord(ctx->ev_fork2, ctx->st));
+            CU(cudaStreamWaitEvent(aux, ctx->ev_fork2, 0));
+            CU(cudaEventRecord(ctx->ev_join2, aux));
+        }
+        return BD_OK;
+    }
     const long long vp0 = A.vp_first, nvp = Z.vp_first + Z.nvp - vp0;
     if (nvp > 0) {
         const int w0 = ctx->vchunk_first[b0], nw = ctx->vchunk_first[b0 + nb] - w0;
@@ -708,6 +719,19 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
+    const long long k0 = A.bk_off, nk = Z.bk_off + Z.nbk - k0;
+    if (aux) {   // (launched before the forward poles so the two run side by side)
+        CU(cudaEventRecord(ctx->ev_fork2, ctx->st));
+        CU(cudaStreamWaitEvent(aux, ctx->ev_fork2, 0));
+    }
+    if (nk > 0) {
+        k_poles<<<(unsigned)((nk + 127) / 128), 128, 0, aux ? aux : ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
+                                                                     ctx->d_blk_bk_first + b0, nb, k0, nk, ctx->d_cs,
+                                                                     1, ctx->d_vp, ctx->d_Ebk, ctx->d_S2bk, ctx->d_Mbk);
+        CU(cudaGetLastError());
+        ctx->launches += 1;
+    }
+    if (aux) CU(cudaEventRecord(ctx->ev_join2, aux));
     const long long f0 = A.fw_off, nf = Z.fw_off + Z.nfw - f0;
     if (nf > 0) {
         k_poles<<<(unsigned)((nf + 127) / 128), 128, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
@@ -716,18 +740,11 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi) {
         CU(cudaGetLastError());
         ctx->launches += 1;
     }
-    const long long k0 = A.bk_off, nk = Z.bk_off + Z.nbk - k0;
-    if (nk > 0) {
-        k_poles<<<(unsigned)((nk + 127) / 128), 128, 0, ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
-                                                                     ctx->d_blk_bk_first + b0, nb, k0, nk, ctx->d_cs,
-                                                                     1, ctx->d_vp, ctx->d_Ebk, ctx->d_S2bk, ctx->d_Mbk);
-        CU(cudaGetLastError());
-        ctx->launches += 1;
-    }
     return BD_OK;
 }
 
-int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
+int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t st = nullptr) {
+    if (!st) st = ctx->st;
     // entries of channels [ch_lo, ch_hi) are contiguous in d_ehf_entries
     int e0 = 0, e1 = 0, acc = 0;
     for (int I = 0; I < ctx->nsubsh; ++I) {
@@ -739,10 +756,10 @@ int launch_ehf(bd_ctx *ctx, int ch_lo, int ch_hi) {
     if (e1 > e0) {
         const long long nt = ctx->ehf_term_first[e1] - ctx->ehf_term_first[e0];
         if (nt > 0)
-            k_ehf_terms<<<(unsigned)((nt + 255) / 256), 256, 0, ctx->st>>>(
+            k_ehf_terms<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(
                 ctx->dp, ctx->d_ehf_entries, ctx->d_ehf_term_first, e0, e1, ctx->d_ehf_cmb, ctx->d_ehf_toff,
                 ctx->d_ehf_coff, ctx->d_ehf_ncomb, ctx->d_ehf_terms);
-        k_ehf_sum<<<e1 - e0, 256, 0, ctx->st>>>(ctx->dp, ctx->d_ehf_entries, ctx->d_ehf_term_first, e0, ctx->d_ehf_cmb,
+        k_ehf_sum<<<e1 - e0, 256, 0, st>>>(ctx->dp, ctx->d_ehf_entries, ctx->d_ehf_term_first, e0, ctx->d_ehf_cmb,
                                                 ctx->d_ehf_toff, ctx->d_ehf_coff, ctx->d_ehf_ncomb, ctx->d_ehf_terms,
                                                 ctx->d_dd_off, ctx->d_sighf);
         CU(cudaGetLastError());
@@ -1547,6 +1564,10 @@ int bd_create(bd_ctx **out, int device) {
     for (auto &e : ctx->ev) cudaEventCreate(&e);
     for (auto &e : ctx->ev_lz) cudaEventCreate(&e);
     for (auto &e : ctx->ev_up) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->ev_fork2, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ctx->ev_join2, cudaEventDisableTiming);
     if (cudaStreamCreateWithFlags(&ctx->st_aux, cudaStreamNonBlocking) != cudaSuccess) {
         bd_destroy(ctx);
         return BD_ERR_CUDA;
@@ -1570,6 +1591,10 @@ void bd_destroy(bd_ctx *ctx) {
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
     for (auto &e : ctx->ev_lz) if (e) cudaEventDestroy(e);
     for (auto &e : ctx->ev_up) if (e) cudaEventDestroy(e);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->ev_fork2) cudaEventDestroy(ctx->ev_fork2);
+    if (ctx->ev_join2) cudaEventDestroy(ctx->ev_join2);
     if (ctx->h_segcheck) cudaFreeHost(ctx->h_segcheck);
     if (ctx->h_vcheck) cudaFreeHost(ctx->h_vcheck);
     if (ctx->st_aux) cudaStreamDestroy(ctx->st_aux);
@@ -2018,13 +2043,22 @@ int enqueue_step(bd_ctx *ctx, int flags) {
         CU(record(ctx, ctx->ev[3]));
         for (int I = 0; I < ns; ++I) if ((rc = launch_dyson_range(ctx, I, I + 1, lanczos))) return rc;
     } else {
-        if ((rc = launch_ehf(ctx, 0, ns))) return rc;
-        if ((rc = launch_sigma2(ctx, 0, ns))) return rc;
+        // The static self-energy (EHF) depends only on the propagator and is read only by
+        // the Dyson solve: it runs on the auxiliary stream beside Sigma(2), the sort and
+        // the Lanczos reduction, joined before the Dyson solve (a branch of the graph when
+        // the step is captured).
+        CU(cudaEventRecord(ctx->ev_fork, ctx->st));
+        CU(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_fork, 0));
+        if ((rc = launch_ehf(ctx, 0, ns, ctx->st_aux))) return rc;
+        CU(cudaEventRecord(ctx->ev_join, ctx->st_aux));
+        if ((rc = launch_sigma2(ctx, 0, ns, ctx->st_aux))) return rc;
+        CU(cudaStreamWaitEvent(ctx->st, ctx->ev_join2, 0));
         CU(record(ctx, ctx->ev[1]));
         if (lanczos && (rc = launch_sort(ctx, 0, ns, ref_order))) return rc;
         CU(record(ctx, ctx->ev[2]));
         if (lanczos && (rc = launch_lanczos_range(ctx, 0, ns, fp32))) return rc;
         CU(record(ctx, ctx->ev[3]));
+        CU(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
         if ((rc = launch_dyson_range(ctx, 0, ns, lanczos))) return rc;
     }
     CU(record(ctx, ctx->ev[4]));
