@@ -15,7 +15,13 @@
 // v_{j-1}, v_{j-2} and the last vector of each earlier chain, the only vectors on
 // which E v_{j-1} has more than rounding-size components; the full sweep that
 // follows then removes little, so one full sweep per step is the common case
-// instead of two.  On the degenerate unperturbed spectra the
+// instead of two.  With FP32 vectors such a continuing step takes one cluster
+// reduction: the sweep's dot products are summed together with the sums over w that
+// the step's scalars need, the scalars of the swept vector follow from those and the
+// stored rows to first order in the sweep's rounding-sized coefficients (dots_fused,
+// fused_scalars), and the update is applied in the pass that writes the vector; the
+// exact scalar pass remains for every step where that does not hold.  On the
+// degenerate unperturbed spectra the
 // chains break down every few steps and, with few distinct pole energies, the
 // reachable subspace (E is diagonal, so the support of M.p never grows) can be
 // spanned completely; a single sweep then leaves the new vectors far from
