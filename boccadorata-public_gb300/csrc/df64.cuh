@@ -18,7 +18,7 @@
 namespace bd {
 namespace dfm {
 
-struct df {
+struct alignas(8) df {   // 8-byte aligned: one 64-bit load or store per value
     float h, l;
 };
 

@@ -354,31 +354,43 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
 
 // ---------------------------------------------------------------- K4a' small matrices
 // Matrices of order nc <= kTsMax (after deflation nearly all: the N_max = 10 channels
-// reduce to 11..94) are reduced by one CTA with the lower triangle resident in shared
-// memory, and the first D rows of Q = H_0 ... H_{n-3} (what k_qrows forms for the
-// cluster path) are updated in the same pass.  The element arithmetic is double-float
-// (df64.cuh: hi + lo FP32 pairs, ~48 bits): on this GPU an FP64 FMA issues at 1/64 of
-// the FP32 rate.  The reflector's scalars are formed by one thread per column, also in
-// double-float (Newton's reciprocal and square root), since that thread's dependent
-// chain is the serial part of every column.
-//   - A -= v w^T + w v^T on the lower triangle, each result also stored at its mirror
-//     position: a warp takes rows i and m-1-i together, m+1 elements, so the
-//     triangle's rows balance;
-//   - p = A v over full rows (contiguous, the same trip count in every lane), each row
-//     split in eight parts of q over eight threads, no atomics and no shuffles, with v
-//     read as the scaled column in place (so no barrier between the reflector and it);
-//   - sums (column norm, R x, p.v) are single-warp reductions, and the warp that forms
-//     p.v also forms w = p - K v.
-// Step k (trailing order m = n-k-1) has four barriers.  The reflector's square root and
-// reciprocal take one Newton step each from their FP32 seeds (about 2^-43, far inside
-// the eigenvalue tolerance).
+// reduce to 11..94) are reduced by one CTA with the matrix resident in shared memory
+// (both triangles), and the first D rows of Q = H_0 ... H_{n-3} (what k_qrows forms
+// for the cluster path) are updated in the same pass.  The element arithmetic is
+// double-float (df64.cuh: hi + lo FP32 pairs, ~48 bits): on this GPU an FP64 FMA
+// issues at 1/64 of the FP32 rate.
+//
+// Step k reduces column k (x = rows k+1 .. n-1, alpha = x_0) with H = I - tau v v^T,
+// v = (1, s x_1 ..), s = 1 / (alpha - beta), beta = -sign(alpha) |x|.  The column is
+// carried scaled by a power of two, xs = 2^-e x with max(|alpha|, |x_1:|) in [1, 2)
+// (exact), so the reflector's scalars need no range checks.  Every sum the step needs
+// is formed from xs without the scalars, which lets one thread form them beside the
+// product instead of before it:
+//   S_i = sum_{t>=1} A_{b0+i, b0+t} xs_t   (eight parts per row, over fifteen warps),
+//   Q = sum_{i>=1} xs_i S_i                 (per-warp partials of the same pass),
+//   A v = A_{:,0} + s S,  v^T A v = A_00 + 2 s S_0 + s^2 Q,  p = tau A v,
+//   w = p - (tau^2 / 2) (v^T A v) v,  A <- A - v w^T - w v^T,  R <- R - tau (R v) v^T.
+// One step, three barriers:
+//   2. warp 0, lane 0: beta, tau and s from (alpha, |x_1:|^2) in double-float (Newton's
+//      reciprocal and square root); warps 1..15: the parts of S and Q; the last D
+//      warps also R_d[b0+1:] . xs[1:];
+//   3. every thread of a trailing row t: v_t and w_t from the parts (each thread sums
+//      the warp partials of Q itself, in one fixed order), and the R update;
+//   4. the rank-2 update of the trailing block, each result also at its mirror
+//      position; warp 0 takes column k + 1 and scales it for the next step.
 constexpr int kTsThreads = 512;
-constexpr int kTsParts = 8;   // threads per row of the symmetric product
+constexpr int kTsParts = 8;                   // threads per row of the symmetric product
+constexpr int kTsIt = kTsMax / 32;            // column entries per lane of warp 0
+static_assert(kTsMax % 32 == 0, "warp 0 holds a column in kTsIt entries per lane");
 
 __device__ inline double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+// Binary exponent of a non-zero float (denormals give -127), and 2^e for -126 <= e <= 127.
+__device__ inline int f32_exp(float x) { return (int)((__float_as_uint(x) >> 23) & 255u) - 127; }
+__device__ inline float f32_pow2(int e) { return __uint_as_float((unsigned)(e + 127) << 23); }
 
 __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs, int njobs) {
     using dfm::df;
@@ -392,12 +404,16 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     extern __shared__ double sm[];
     df *A = reinterpret_cast<df *>(sm);      // [n][ld], both triangles
     df *v = A + (size_t)n * ld;              // [n]
-    df *ph = v + n;                          // [kTsParts][n] parts of A v
+    df *ph = v + n;                          // [kTsParts][n] parts of S
     df *w = ph + kTsParts * n;               // [n]
-    df *R = w + n;                           // [D][n]
-    __shared__ df s_dfs[2][4];               // tau, scal, -, beta of the step, by parity
-    __shared__ int s_flag[2];                // the column has a reflector, by parity
-    __shared__ df s_coef[8];                 // tau s_d, s_d = R_d[b0:] . v
+    df *xs = w + n;                          // [n] the step's scaled column
+    df *R = xs + n;                          // [D][n]
+    __shared__ df s_col[2][2];               // alpha and |x_1:|^2 of a column, scaled, by parity
+    __shared__ int s_nz[2], s_exp[2];        // the column has a reflector; e, by parity
+    __shared__ df s_al[2];                   // alpha unscaled (a column left as it is), by parity
+    __shared__ df s_sc[2];                   // tau, s of the step
+    __shared__ df s_q[kTsThreads / 32];      // per-warp partials of Q
+    __shared__ df s_rx[8][2];                // R_d[b0+1:] . xs[1:], R_d[b0] before the update
     for (int q = tid; q < n * n; q += kTsThreads) {
         const int i = q / n, j = q - i * n;
         if (j <= i) {   // the assembled lower triangle, mirrored
@@ -409,117 +425,140 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     for (int q = tid; q < D * n; q += kTsThreads) R[q] = df{((q % n) == (q / n)) ? 1.0f : 0.0f, 0.0f};
     __syncthreads();
     const df zero{0.0f, 0.0f};
-    // The reflector of column k by warp 0: sigma = |x_{1:}|^2, then lane 0 forms beta, tau
-    // and scal into the column's parity slot and writes the column's d, e, tau (FP64).
-    auto reflector = [&](int k) {
-        const int b0 = k + 1, m = n - b0;
-        const df *col = A + k;
-        df *sdf = s_dfs[k & 1];
+    // Warp 0: column kc's entries below the diagonal (rows kc+1 .. n-1), alpha, the sum of
+    // the other entries' squares, the power of two 2^-e that brings the larger of |alpha|
+    // and that norm into [1, 2), and xs = 2^-e x, into the column's parity slots.
+    auto scale_column = [&](int kc) {
+        const int b = kc + 1, mc = n - b, par = kc & 1;
+        df x[kTsIt];
         df s2 = zero;
-        for (int t = 1 + lane; t < m; t += 32) { const df x = col[(size_t)(b0 + t) * ld]; s2 = dfm::fma(x, x, s2); }
+#pragma unroll
+        for (int it = 0; it < kTsIt; ++it) {
+            const int t = lane + 32 * it;
+            x[it] = (t < mc) ? A[(size_t)(b + t) * ld + kc] : zero;
+            if (t >= 1) s2 = dfm::fma(x[it], x[it], s2);
+        }
         s2 = dfm::warp_sum(s2);
+        const df al{__shfl_sync(0xffffffffu, x[0].h, 0), __shfl_sync(0xffffffffu, x[0].l, 0)};
+        const int ea = (al.h != 0.0f) ? f32_exp(al.h) : -1000;
+        const int es = (s2.h != 0.0f) ? (f32_exp(s2.h) >> 1) : -1000;   // floor(e / 2)
+        int e = max(ea, es);
+        e = (e == -1000) ? 0 : min(max(e, -126), 126);
+        const float sg = f32_pow2(-e);
+#pragma unroll
+        for (int it = 0; it < kTsIt; ++it) {
+            const int t = lane + 32 * it;
+            if (t < mc) xs[t] = df{x[it].h * sg, x[it].l * sg};
+        }
         if (lane == 0) {
-            // beta = -sign(alpha) |x|, tau = (beta - alpha) / beta = 1 + |alpha| / |x|,
-            // scal = 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|), in double-float
-            // with Newton's reciprocal and square root (FP64 only outside the FP32 range)
-            const df al = col[(size_t)b0 * ld];
-            const bool nz = (s2.h != 0.0f || s2.l != 0.0f);
-            const bool ng = signbit(al.h);
-            const df aa = ng ? dfm::neg(al) : al;
-            df tau = zero, scal = zero, beta = al;
-            if (nz) {
-                const df x2 = dfm::fma(al, al, s2);
-                if (x2.h > 1e-30f && x2.h < 1e30f) {
-                    const df r = dfm::rsqrt(x2, 1), nx = dfm::mul(x2, r);
-                    beta = ng ? nx : dfm::neg(nx);
-                    tau = dfm::fma(aa, r, df{1.0f, 0.0f});
-                    scal = dfm::rcp(dfm::add(aa, nx), 1);
-                    if (ng) scal = dfm::neg(scal);
-                } else {
-                    const double a = dfm::to_double(al), x2d = dfm::to_double(x2);
-                    const double r = 1.0 / sqrt(x2d), nx = x2d * r;
-                    beta = dfm::from_double(-copysign(nx, a));
-                    tau = dfm::from_double(fma(fabs(a), r, 1.0));
-                    scal = dfm::from_double(copysign(1.0 / (fabs(a) + nx), a));
-                }
-            }
-            sdf[0] = tau; sdf[1] = scal; sdf[3] = beta;
-            s_flag[k & 1] = nz;
-            J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);   // the step's d, e, tau in FP64
-            J.e[k] = dfm::to_double(beta);
-            J.tau[k] = dfm::to_double(tau);
+            s_nz[par] = (s2.h != 0.0f || s2.l != 0.0f);
+            s_exp[par] = e;
+            s_al[par] = al;
+            s_col[par][0] = df{al.h * sg, al.l * sg};
+            s_col[par][1] = df{(s2.h * sg) * sg, (s2.l * sg) * sg};
         }
     };
-    // Look-ahead: the rank-2 update of column k leaves column k + 1 to warp 0, which updates
-    // it first and forms column k + 1's reflector while the other warps update the rest of
-    // the trailing block, so a column takes three barriers and the reflector's serial
-    // chain runs beside the update instead of before the next column's product.
-    if (n >= 3 && warp == 0) reflector(0);
+    if (n >= 3 && warp == 0) scale_column(0);
     __syncthreads();
     for (int k = 0; k + 2 < n; ++k) {
-        const int b0 = k + 1, m = n - b0;
-        const df *col = A + k;               // A(b0 + t, k) = col[(b0 + t) * ld]
-        // the step's scalars alternate between two slots (written one column ahead)
-        const df *sdf = s_dfs[k & 1];
-        if (!s_flag[k & 1]) {                // column already reduced: H_k = I
-            if (k + 3 < n && warp == 0) reflector(k + 1);
+        const int b0 = k + 1, m = n - b0, par = k & 1;
+        if (!s_nz[par]) {                    // column already reduced: H_k = I
+            if (warp == 0) {
+                if (lane == 0) {
+                    J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
+                    J.e[k] = dfm::to_double(s_al[par]);
+                    J.tau[k] = 0.0;
+                }
+                if (k + 3 < n) scale_column(k + 1);
+            }
             __syncthreads();
             continue;
         }
-        const df taud = sdf[0], scald = sdf[1];
-        // 2. the last D warps first: rx_d = R_d[b0+1:] . x[1:] and the R update's
-        //    coefficients tau s_d, s_d = R_d[b0:] . v; then every warp: parts of A v
-        //    (trailing block, local indices) with v = (1, scal x[1:]), the column read in
-        //    place, eight parts per row so all sixteen warps are busy; and v itself
-        if (warp >= kTsThreads / 32 - D) {
-            const int d = kTsThreads / 32 - 1 - warp;
-            df sx = zero;
-            for (int t = 1 + lane; t < m; t += 32) sx = dfm::fma(R[(size_t)d * n + b0 + t], col[(size_t)(b0 + t) * ld], sx);
-            sx = dfm::warp_sum(sx);
-            if (lane == 0) s_coef[d] = dfm::mul(taud, dfm::fma(scald, sx, R[(size_t)d * n + b0]));
-        }
-        for (int u = tid; u < kTsParts * m; u += kTsThreads) {
-            const int i = u / kTsParts, h = u - i * kTsParts;
-            const int q0 = (int)(((long long)m * h) / kTsParts), q1 = (int)(((long long)m * (h + 1)) / kTsParts);
-            const df *Ai = A + (size_t)(b0 + i) * ld + b0;   // the full row (the update mirrors)
-            df acc0 = zero, acc1 = zero;   // two chains
-            int q = q0 > 0 ? q0 : 1;
-            for (; q + 1 < q1; q += 2) {
-                acc0 = dfm::fma(Ai[q], col[(size_t)(b0 + q) * ld], acc0);
-                acc1 = dfm::fma(Ai[q + 1], col[(size_t)(b0 + q + 1) * ld], acc1);
-            }
-            if (q < q1) acc0 = dfm::fma(Ai[q], col[(size_t)(b0 + q) * ld], acc0);
-            df r = dfm::mul(scald, dfm::add(acc0, acc1));
-            if (q0 == 0 && q1 > 0) r = dfm::add(Ai[0], r);   // the part holding v_0 = 1
-            ph[h * n + i] = r;
-        }
-        for (int t = tid; t < m; t += kTsThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(col[(size_t)(b0 + t) * ld], scald);
-        __syncthreads();
-        // 3. warp 0: p = tau A v, K = (tau / 2) p . v and w = p - K v (each lane its own
-        //    entries); the other warps: R <- R H_k
+        // 2. the reflector's scalars (warp 0, lane 0) beside the parts of S and Q
         if (warp == 0) {
-            df s = zero;
-            for (int t = lane; t < m; t += 32) {
-                df pa = ph[t];
-#pragma unroll
-                for (int h = 1; h < kTsParts; ++h) pa = dfm::add(pa, ph[h * n + t]);
-                const df pt = dfm::mul(taud, pa);
-                w[t] = pt;
-                s = dfm::fma(pt, v[t], s);
+            if (lane == 0) {
+                const df al = s_col[par][0], s2 = s_col[par][1];
+                const df x2 = dfm::fma(al, al, s2);   // in [1, 12)
+                const df r = dfm::rsqrt(x2, 1), nx = dfm::mul(x2, r);
+                const bool ng = signbit(al.h);
+                const df aa = ng ? dfm::neg(al) : al;
+                const df tau = dfm::fma(aa, r, df{1.0f, 0.0f});   // (beta - alpha) / beta = 1 + |alpha| / |x|
+                df s = dfm::rcp(dfm::add(aa, nx), 1);               // 1 / (alpha - beta) = sign(alpha) / (|alpha| + |x|)
+                if (ng) s = dfm::neg(s);
+                s_sc[0] = tau;
+                s_sc[1] = s;
+                s_q[0] = zero;
+                const float un = f32_pow2(s_exp[par]);        // beta = 2^e beta~
+                const df beta = ng ? nx : dfm::neg(nx);
+                J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
+                J.e[k] = dfm::to_double(df{beta.h * un, beta.l * un});
+                J.tau[k] = dfm::to_double(tau);
             }
-            s = dfm::warp_sum(s);
-            const df nK = dfm::neg(dfm::mul(dfm::mul(df{0.5f, 0.0f}, taud), s));
-            for (int t = lane; t < m; t += 32) w[t] = dfm::fma(nK, v[t], w[t]);
         } else {
-            for (int u = tid - 32; u < D * m; u += kTsThreads - 32) {
-                const int d = u / m, t = u - d * m;
-                df &r = R[(size_t)d * n + b0 + t];
-                r = dfm::fma(dfm::neg(s_coef[d]), v[t], r);
+            if (warp >= kTsThreads / 32 - D) {   // R_d[b0+1:] . xs[1:] and R_d[b0]
+                const int d = kTsThreads / 32 - 1 - warp;
+                df sx = zero;
+                for (int t = 1 + lane; t < m; t += 32) sx = dfm::fma(R[(size_t)d * n + b0 + t], xs[t], sx);
+                sx = dfm::warp_sum(sx);
+                if (lane == 0) { s_rx[d][0] = sx; s_rx[d][1] = R[(size_t)d * n + b0]; }
             }
+            df qa = zero;
+            for (int u = tid - 32; u < kTsParts * m; u += kTsThreads - 32) {
+                const int i = u / kTsParts, h = u - i * kTsParts;
+                const int q0 = (m * h) / kTsParts, q1 = (m * (h + 1)) / kTsParts;
+                const df *Ai = A + (size_t)(b0 + i) * ld + b0;   // the full row (the update mirrors)
+                df acc0 = zero, acc1 = zero;   // two chains
+                int q = q0 > 0 ? q0 : 1;
+                for (; q + 1 < q1; q += 2) {
+                    acc0 = dfm::fma(Ai[q], xs[q], acc0);
+                    acc1 = dfm::fma(Ai[q + 1], xs[q + 1], acc1);
+                }
+                if (q < q1) acc0 = dfm::fma(Ai[q], xs[q], acc0);
+                const df r = dfm::add(acc0, acc1);
+                ph[h * n + i] = r;
+                if (i >= 1) qa = dfm::fma(xs[i], r, qa);
+            }
+            qa = dfm::warp_sum(qa);
+            if (lane == 0) s_q[warp] = qa;
         }
         __syncthreads();
-        // 4. A -= v w^T + w v^T on the trailing lower triangle: warp 0 takes column k + 1
-        //    (local column 0) and then that column's reflector; warps 1..15 the rest, rows i
+        // 3. v and w of every trailing row; R <- R - tau (R v) v^T
+        const df tau = s_sc[0], s = s_sc[1];
+        if (tid < m) {
+            const int t = tid;
+            df qv[kTsThreads / 32];
+#pragma unroll
+            for (int q = 0; q < kTsThreads / 32; ++q) qv[q] = s_q[q];
+#pragma unroll
+            for (int o = kTsThreads / 64; o > 0; o >>= 1)
+#pragma unroll
+                for (int q = 0; q < o; ++q) qv[q] = dfm::add(qv[q], qv[q + o]);
+            df p0[kTsParts], pt[kTsParts];
+#pragma unroll
+            for (int h = 0; h < kTsParts; ++h) { p0[h] = ph[h * n]; pt[h] = ph[h * n + t]; }
+#pragma unroll
+            for (int o = kTsParts / 2; o > 0; o >>= 1)
+#pragma unroll
+                for (int h = 0; h < o; ++h) { p0[h] = dfm::add(p0[h], p0[h + o]); pt[h] = dfm::add(pt[h], pt[h + o]); }
+            // v^T A v = A_00 + s (2 S_0 + s Q); K = (tau^2 / 2) v^T A v
+            const df vav = dfm::fma(s, dfm::fma(s, qv[0], dfm::add(p0[0], p0[0])), A[(size_t)b0 * ld + b0]);
+            const df tk = dfm::mul(tau, tau);
+            const df nK = dfm::neg(dfm::mul(df{0.5f * tk.h, 0.5f * tk.l}, vav));
+            const df vt = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(s, xs[t]);
+            const df p = dfm::mul(tau, dfm::fma(s, pt[0], A[(size_t)(b0 + t) * ld + b0]));
+            v[t] = vt;
+            w[t] = dfm::fma(nK, vt, p);
+        }
+        for (int u = tid; u < D * m; u += kTsThreads) {
+            const int d = u / m, t = u - d * m;
+            const df vt = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(s, xs[t]);
+            const df nc = dfm::neg(dfm::mul(tau, dfm::fma(s, s_rx[d][0], s_rx[d][1])));
+            df &r = R[(size_t)d * n + b0 + t];
+            r = dfm::fma(nc, vt, r);
+        }
+        __syncthreads();
+        // 4. A -= v w^T + w v^T on the trailing block: warp 0 takes column k + 1 (local
+        //    column 0) and then scales it for the next step; warps 1..15 the rest, rows i
         //    and m-1-i per warp so the triangle's rows balance, each result also at its mirror
         if (warp == 0) {
             for (int r = lane; r < m; r += 32) {
@@ -530,7 +569,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
                 A[(size_t)b0 * ld + b0 + r] = x;
             }
             __syncwarp();
-            if (k + 3 < n) reflector(k + 1);
+            if (k + 3 < n) scale_column(k + 1);
         } else {
             for (int i1 = warp - 1; i1 < (m + 1) / 2; i1 += kTsThreads / 32 - 1) {
                 const int i2 = m - 1 - i1;
@@ -563,7 +602,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
 
 size_t tridiag_small_smem_bytes(int nmax, int Dmax) {
     const size_t n = (size_t)std::min(nmax, kTsMax);
-    return sizeof(double) * (n * (n | 1) + (size_t)(kTsParts + 2) * n + (size_t)Dmax * n + 32);
+    return sizeof(double) * (n * (n | 1) + (size_t)(kTsParts + 3) * n + (size_t)Dmax * n);
 }
 
 // Per-warp partial vectors that fit next to the other arrays (8 = one per warp).

@@ -325,7 +325,7 @@ __device__ void invit_vector(const DyJob &J, int k, int b0, int b1, S &a) {
 // run on the FP32 pipe at a few cycles per operation.  The shifts, the tolerances and
 // the start vectors are those of invit_vector; the pivot choice compares the high parts
 // (any choice that keeps the multipliers bounded serves), and the result goes to y in
-// FP64.  The tridiagonal is read from J in FP64 and converted off the dependent chain.
+// FP64.  The tridiagonal is converted to double-float once per CTA, into shared memory.
 struct InvitSharedDF {   // shared memory, element i of this thread at i * kIvThreads + lane
     dfm::df *U1, *U2, *DD, *LL, *Y;
     unsigned char *PV;
@@ -342,10 +342,10 @@ struct InvitSharedDF {   // shared memory, element i of this thread at i * kIvTh
 __device__ inline dfm::df df_abs(dfm::df a) { return a.h < 0.0f ? dfm::neg(a) : a; }
 __device__ inline dfm::df df_sub(dfm::df a, dfm::df b) { return dfm::add(a, dfm::neg(b)); }
 
-__device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, InvitSharedDF &a) {
+__device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, const dfm::df *dt, const dfm::df *et,
+                                InvitSharedDF &a) {
     using dfm::df;
     const int NS = 2 + J.D;
-    const double *d = J.d, *e = J.e;
     const EigTol tl = eig_tol(J.tau[k]);
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
     int k0 = k;
@@ -355,43 +355,49 @@ __device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, InvitShar
     const df x = dfm::from_double(xs);
     const df zero{0.0f, 0.0f};
     const float pt = (float)tl.pertol;
-    auto pivot_rcp = [&](df p) {   // pivots no smaller than pertol, kept as reciprocals for the solves
-        if (fabsf(p.h) < pt) p = df{p.h < 0.0f ? -pt : pt, 0.0f};
-        return dfm::rcp(p);
+    // Reciprocals by one Newton step from the FP32 seed (~2^-44): the factors only need
+    // to keep the shifted matrix's direction, far looser than that.
+    auto rcp1 = [&](df p) { return dfm::rcp(p, 1); };
+    auto clamp_piv = [&](df p) {   // pivots no smaller than pertol
+        return (fabsf(p.h) < pt) ? df{p.h < 0.0f ? -pt : pt, 0.0f} : p;
     };
     // LU with partial pivoting of T_b - x I (rows i and i+1 may swap).  The running
     // diagonal and superdiagonal entries of the next row stay in registers, so the
-    // dependent chain is the arithmetic alone; each row's factors go to shared memory
-    // for the solves as soon as they are final.
-    df cur_d = df_sub(dfm::from_double(d[b0]), x);        // dd(i) as updated so far
-    df cur_u = (b0 < b1) ? dfm::from_double(e[b0]) : zero;   // u1(i) as updated so far
+    // dependent chain is the arithmetic alone (one reciprocal per row: the multiplier's
+    // and the kept pivot's are the same unless the pivot is below pertol); each row's
+    // factors go to shared memory for the solves as soon as they are final.  The
+    // tridiagonal comes in double-float from dt, et (shared memory).
+    df cur_d = df_sub(dt[b0], x);                 // dd(i) as updated so far
+    df cur_u = (b0 < b1) ? et[b0] : zero;         // u1(i) as updated so far
     for (int i = b0; i < b1; ++i) {
-        const df di = cur_d, li = dfm::from_double(e[i]), ui = cur_u;
-        const df nd = df_sub(dfm::from_double(d[i + 1]), x);              // dd(i+1) before this row
-        const df nu = (i + 1 < b1) ? dfm::from_double(e[i + 1]) : zero;   // u1(i+1) before this row
+        const df di = cur_d, li = et[i], ui = cur_u;
+        const df nd = df_sub(dt[i + 1], x);                     // dd(i+1) before this row
+        const df nu = (i + 1 < b1) ? et[i + 1] : zero;          // u1(i+1) before this row
         if (fabsf(di.h) >= fabsf(li.h)) {
             a.set_pv(i, false);
-            const df f = (di.h != 0.0f) ? dfm::mul(li, dfm::rcp(di)) : zero;
+            const df cp = clamp_piv(di), r = rcp1(cp);
+            const df f = (di.h != 0.0f) ? dfm::mul(li, (cp.h == di.h) ? r : rcp1(di)) : zero;
             a.ll(i) = f;
             a.u1(i) = ui;
             a.u2(i) = zero;
-            a.dd(i) = pivot_rcp(di);
+            a.dd(i) = r;
             cur_d = dfm::fma(dfm::neg(f), ui, nd);
             cur_u = nu;
         } else {
             a.set_pv(i, true);
-            const df f = dfm::mul(di, dfm::rcp(li));
+            const df cp = clamp_piv(li), r = rcp1(cp);
+            const df f = dfm::mul(di, (cp.h == li.h) ? r : rcp1(li));
             a.ll(i) = f;
             a.u1(i) = nd;
             a.u2(i) = nu;
-            a.dd(i) = pivot_rcp(li);
+            a.dd(i) = r;
             cur_d = dfm::fma(dfm::neg(f), nd, ui);
             cur_u = dfm::mul(dfm::neg(f), nu);
         }
     }
     a.u1(b1) = zero;
     a.u2(b1) = zero;
-    a.dd(b1) = pivot_rcp(cur_d);
+    a.dd(b1) = rcp1(clamp_piv(cur_d));
     for (int i = b0; i <= b1; ++i)
         a.y(i) = df{0.5f + (float)(hash32((unsigned)(i * 2654435761u) ^ (unsigned)(k * 97 + 13)) & 0xffff) / 65536.0f, 0.0f};
     for (int it = 0; it < 2; ++it) {
@@ -405,22 +411,36 @@ __device__ void invit_vector_df(const DyJob &J, int k, int b0, int b1, InvitShar
             cur = bi1;
         }
         a.y(b1) = cur;
+        // U y = b, two superdiagonals: the term of y(i+2) first, off the chain through y(i+1)
         df y1 = zero, y2 = zero;
         float nrm = 0.0f;
-        for (int i = b1; i >= b0; --i) {   // U y = b, two superdiagonals
+        for (int i = b1; i >= b0; --i) {
             df v = a.y(i);
-            if (i + 1 <= b1) v = dfm::fma(dfm::neg(a.u1(i)), y1, v);
             if (i + 2 <= b1) v = dfm::fma(dfm::neg(a.u2(i)), y2, v);
+            if (i + 1 <= b1) v = dfm::fma(dfm::neg(a.u1(i)), y1, v);
             v = dfm::mul(v, a.dd(i));
             a.y(i) = v;
             y2 = y1; y1 = v;
             nrm = fmaxf(nrm, fabsf(v.h));
         }
-        const df sc = (nrm > 0.0f) ? dfm::rcp(df{nrm, 0.0f}) : df{1.0f, 0.0f};
-        df s2 = zero;
-        for (int i = b0; i <= b1; ++i) { const df v = dfm::mul(a.y(i), sc); a.y(i) = v; s2 = dfm::fma(v, v, s2); }
-        const df inv = (s2.h > 0.0f) ? dfm::rsqrt(s2) : zero;
-        for (int i = b0; i <= b1; ++i) a.y(i) = dfm::mul(a.y(i), inv);
+        const df sc = (nrm > 0.0f) ? rcp1(df{nrm, 0.0f}) : df{1.0f, 0.0f};
+        if (it == 0) {   // scaled to a largest entry of about one; the norm matters only at the end
+            for (int i = b0; i <= b1; ++i) a.y(i) = dfm::mul(a.y(i), sc);
+            continue;
+        }
+        df s2a = zero, s2b = zero;   // two chains
+        int i = b0;
+        for (; i + 1 <= b1; i += 2) {
+            const df v0 = dfm::mul(a.y(i), sc), v1 = dfm::mul(a.y(i + 1), sc);
+            a.y(i) = v0;
+            a.y(i + 1) = v1;
+            s2a = dfm::fma(v0, v0, s2a);
+            s2b = dfm::fma(v1, v1, s2b);
+        }
+        if (i <= b1) { const df v0 = dfm::mul(a.y(i), sc); a.y(i) = v0; s2a = dfm::fma(v0, v0, s2a); }
+        const df s2 = dfm::add(s2a, s2b);
+        const df inv = (s2.h > 0.0f) ? dfm::rsqrt(s2, 1) : zero;
+        for (int q = b0; q <= b1; ++q) a.y(q) = dfm::mul(a.y(q), inv);
     }
 }
 
@@ -451,16 +471,24 @@ __global__ void __launch_bounds__(kIvThreads) k_invit_small(const DyJob *jobs, i
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
     const int n = J.nc, lane = threadIdx.x, k = blockIdx.y * kIvThreads + lane;
-    if (n > kTsMax || k >= n) return;
+    if (n > kTsMax || blockIdx.y * kIvThreads >= n) return;   // uniform over the CTA
     extern __shared__ double smi[];
     const int cap = kTsMax * kIvThreads;
     dfm::df *sd = reinterpret_cast<dfm::df *>(smi);
     InvitSharedDF a{sd, sd + cap, sd + 2 * cap, sd + 3 * cap, sd + 4 * cap,
                     reinterpret_cast<unsigned char *>(sd + 5 * cap), lane};
+    // the tridiagonal in double-float, converted once by the CTA's threads
+    dfm::df *dt = sd + 5 * cap + cap / 8, *et = dt + kTsMax;
+    for (int i = lane; i < n; i += kIvThreads) {
+        dt[i] = dfm::from_double(J.d[i]);
+        et[i] = dfm::from_double(J.e[i]);
+    }
+    __syncthreads();
+    if (k >= n) return;
     const int b0 = J.blk[k], b1 = J.blk[n + k];
     double *Y = J.A;
     if (b0 == b1) { Y[(size_t)b0 * n + k] = 1.0; return; }
-    invit_vector_df(J, k, b0, b1, a);
+    invit_vector_df(J, k, b0, b1, dt, et, a);
     for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] = dfm::to_double(a.y(i));
 }
 
@@ -705,7 +733,7 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
     k_invit<<<(unsigned)((total_rows + 31) / 32), 32, 0, st>>>(d_jobs, njobs, d_row_first, total_rows, work,
                                                                d_work_first);
     {
-        const int smem = (int)(sizeof(double) * 5 * kTsMax * kIvThreads + kTsMax * kIvThreads);
+        const int smem = (int)(sizeof(double) * 5 * kTsMax * kIvThreads + kTsMax * kIvThreads + sizeof(double) * 2 * kTsMax);
         cudaError_t e = cudaFuncSetAttribute(k_invit_small, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         k_invit_small<<<dim3(njobs, (kTsMax + kIvThreads - 1) / kIvThreads), kIvThreads, smem, st>>>(d_jobs, njobs);
