@@ -464,11 +464,7 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         const int b0 = k + 1, m = n - b0, par = k & 1;
         if (!s_nz[par]) {                    // column already reduced: H_k = I
             if (warp == 0) {
-                if (lane == 0) {
-                    J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
-                    J.e[k] = dfm::to_double(s_al[par]);
-                    J.tau[k] = 0.0;
-                }
+                if (lane == 0) A[(size_t)k * ld + k + 2] = zero;   // tau (e is alpha, in place)
                 if (k + 3 < n) scale_column(k + 1);
             }
             __syncthreads();
@@ -488,11 +484,12 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
                 s_sc[0] = tau;
                 s_sc[1] = s;
                 s_q[0] = zero;
+                // e and tau of the step into row k, right of the diagonal (never read again),
+                // converted to FP64 with d at the end: FP64 instructions stay off this chain
                 const float un = f32_pow2(s_exp[par]);        // beta = 2^e beta~
                 const df beta = ng ? nx : dfm::neg(nx);
-                J.d[k] = dfm::to_double(A[(size_t)k * ld + k]);
-                J.e[k] = dfm::to_double(df{beta.h * un, beta.l * un});
-                J.tau[k] = dfm::to_double(tau);
+                A[(size_t)k * ld + k + 1] = df{beta.h * un, beta.l * un};
+                A[(size_t)k * ld + k + 2] = tau;
             }
         } else {
             if (warp >= kTsThreads / 32 - D) {   // R_d[b0+1:] . xs[1:] and R_d[b0]
@@ -587,15 +584,11 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         }
         __syncthreads();
     }
-    if (tid == 0) {
-        if (n >= 2) {
-            J.d[n - 2] = dfm::to_double(A[(size_t)(n - 2) * ld + (n - 2)]);
-            J.e[n - 2] = dfm::to_double(A[(size_t)(n - 1) * ld + (n - 2)]);
-            J.tau[n - 2] = 0.0;
-        }
-        J.d[n - 1] = dfm::to_double(A[(size_t)(n - 1) * ld + (n - 1)]);
-        J.e[n - 1] = 0.0;
-        J.tau[n - 1] = 0.0;
+    for (int k = tid; k < n; k += kTsThreads) {   // d, e, tau in FP64 (row k: d_k, e_k, tau_k)
+        const df *Ak = A + (size_t)k * ld + k;
+        J.d[k] = dfm::to_double(Ak[0]);
+        J.e[k] = (k + 1 < n) ? dfm::to_double(Ak[1]) : 0.0;
+        J.tau[k] = (k + 2 < n) ? dfm::to_double(Ak[2]) : 0.0;
     }
     for (int q = tid; q < D * n; q += kTsThreads) J.R[q] = dfm::to_double(R[q]);
 }
