@@ -315,6 +315,12 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     __shared__ CT s_ixbf;        // 1/|w| in the arithmetic type
     __shared__ CT lcf[16];       // coefficients of a recurrence step's local vectors
     __shared__ double fsc[12];   // a recurrence step's sums of w: |w|^2, <w|E|w>, |E w|^2, <M_d|w>
+    // FP32 vectors: the step's scalars in double-float as well, for its serial part (thread
+    // 0's decision, warp 0's row), where each FP64 instruction would hold an SM
+    // sub-partition's FP64 unit for ~64 cycles
+    __shared__ dfm::df fscd[12], totd[kMaxScal];
+    __shared__ dfm::df s_rd, s_xbd, s_e2vd;   // 1/|w|, |w| of the step; |E v|^2 of the last built vector
+    __shared__ float prowf[kMaxScal];         // the last built row in FP32 (the next step's coefficients)
 
     VT *V = reinterpret_cast<VT *>(C.V);
     // this CTA's slice of stored vector t: in the cache, or in V
@@ -340,6 +346,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
     // eigenvectors of E that no coupling reaches (energy groups from k_lz_groups): each
     // such row is (E_q, 0, ..., 0), needs no vector, and deflates out of the Dyson matrix.
     const double thr_exh = (sizeof(VT) == 4) ? 1e-9 : 1e-20;
+    // the decision's factors in double-float (FP32 vectors)
+    const dfm::df c099d = dfm::from_double(0.99), eta2d = dfm::from_double(eta2), thr_exhd = dfm::from_double(thr_exh),
+                  taud = dfm::from_double(tau);
+    auto df_lt = [](dfm::df a, dfm::df b) { return a.h < b.h || (a.h == b.h && a.l < b.l); };
+    auto df_le = [](dfm::df a, dfm::df b) { return a.h < b.h || (a.h == b.h && a.l <= b.l); };
     const int Qg = C.gE ? C.gInfo[0] : 0;
     const int dtot = Qg > 0 ? C.gInfo[Qg] : 0;   // unreached directions of all groups
     int dcur = 0;                // directions used so far (identical in every CTA)
@@ -563,13 +574,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                     Sum::put(dt + (t >> 1), x);   // kept as the sum's pair: no FP64 instruction here
                 }
             } else if (t == 2 * nl) {
-                fsc[0] = Sum::value(x);   // |w|^2
+                if constexpr (kFused) fscd[0] = x; else fsc[0] = Sum::value(x);   // |w|^2
             } else if (t == 2 * nl + 1) {
-                fsc[1] = Sum::value(x);   // <w|E|w>
+                if constexpr (kFused) fscd[1] = x; else fsc[1] = Sum::value(x);   // <w|E|w>
             } else if (t == 2 * nl + 3) {
-                fsc[2] = Sum::value(x);   // |E w|^2
+                if constexpr (kFused) fscd[2] = x; else fsc[2] = Sum::value(x);   // |E w|^2
             } else if (t >= 2 * nit) {
-                fsc[3 + (t - 2 * nit)] = Sum::value(x);   // <M_d|w>
+                if constexpr (kFused) fscd[3 + (t - 2 * nit)] = x; else fsc[3 + (t - 2 * nit)] = Sum::value(x);   // <M_d|w>
             }
         }
         __syncthreads();
@@ -615,7 +626,18 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 a += term;
             }
             a = warp_sum_ct(a);
-            if (lane == 0) {
+            if constexpr (kFused) {   // into totd, in double-float
+                if (lane == 0) {
+                    const dfm::df xa{-(float)a, 0.0f};
+                    if (qi == 0) totd[0] = dfm::add(fscd[0], xa);
+                    else if (qi == 1) totd[1] = dfm::add(fscd[1], dfm::df{-2.0f * (float)a, 0.0f});
+                    else if (qi < 2 + D) totd[qi] = dfm::add(fscd[3 + (qi - 2)], xa);
+                    else {
+                        const int q = qi - 2 - D, sl = lslot[q];
+                        totd[2 + D + q] = (sl >= 0) ? dfm::add(Sum::get(dt + sl), xa) : dfm::df{0.0f, 0.0f};
+                    }
+                }
+            } else if (lane == 0) {
                 const double x = (double)a;
                 if (qi == 0) tot[0] = fsc[0] - x;
                 else if (qi == 1) tot[1] = fsc[1] - 2.0 * x;
@@ -626,7 +648,9 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 }
             }
         }
-        if (tid == 0) tot[2 + D + nq] = fsc[2];   // |E w'|^2 ~ |E w|^2: only a threshold's scale
+        if (tid == 0) {   // |E w'|^2 ~ |E w|^2: only a threshold's scale
+            if constexpr (kFused) totd[2 + D + nq] = fscd[2]; else tot[2 + D + nq] = fsc[2];
+        }
     };
 
     // (b3) w -= sum_t cf_t v_t over the pass's vectors: 16-byte vectors, eight rows in
@@ -750,7 +774,11 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             Sum::put(Bs + tid, tree_sum8<Sum>(x));
         }
         cluster.sync();
-        if (tid < nsc) tot[tid] = Sum::value(cluster_sum_st(Bs, tid));
+        if (tid < nsc) {
+            const ST x = cluster_sum_st(Bs, tid);
+            tot[tid] = Sum::value(x);
+            if constexpr (kFused) totd[tid] = x;
+        }
     };
 
     int k = -1;           // current pivot chain
@@ -840,7 +868,6 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
         bool injected = false;     // w replaced by a pseudo-random restart vector
         bool upd = false;          // the kept sweep's update is still to be applied (with the normalisation)
         bool done = false;         // step finished by an untouched-pole unit vector
-        double n2 = 0.0;           // |w|^2 after the last sweep (identical in every CTA)
         for (int attempt = 0; attempt < 2 && !done; ++attempt) {
             int nfull = 0;
             int fl = 0;            // thread 0's decision after the last sweep (s_flag)
@@ -869,33 +896,37 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             if (fused) dots_fused(nl);
             else dots_pass(local, nl);
             // |w|^2 before any projection: E v_{j-1}'s, from row j - 1's sums, after the recurrence
-            const double wn2_first = (rec && attempt == 0) ? s_e2v : c[nl];
-            double wn2_before = fused ? fsc[0] : c[nl];
+            // (FP32 vectors: a recurrence step's two are read in double-float by the fused
+            // decision, and converted where the exact pass follows it)
+            const bool wf_df = kFused && rec && attempt == 0;
+            const double wn2_first0 = (rec && attempt == 0) ? (kFused ? 0.0 : s_e2v) : c[nl];
+            double wn2_before = fused ? (kFused ? 0.0 : fsc[0]) : c[nl];
             for (;;) {
                 if (fused) {   // the scalars from the pass, before the sweep's update
                     fused = false;
                     fused_scalars(nl, nq);
-                    if (tid == 0) {
-                        const double x2 = tot[0];
+                    if (tid == 0) {   // in double-float: comparisons, 1/|w| by Newton's iteration
+                        const dfm::df x2 = totd[0], wb = fscd[0], wf = s_e2vd;
                         int f = 4;   // the exact scalars of w'
-                        if (x2 >= 0.99 * wn2_before && !(x2 < eta2 * wn2_before) &&
-                            !(x2 <= thr_exh * wn2_first || x2 == 0.0) && !(x2 <= tau * wn2_first)) {
+                        if (x2.h > 1e-36f && x2.h < 1e36f && !df_lt(x2, dfm::mul(c099d, wb)) &&
+                            !df_lt(x2, dfm::mul(eta2d, wb)) && !df_le(x2, dfm::mul(thr_exhd, wf)) &&
+                            !df_le(x2, dfm::mul(taud, wf))) {
                             f = 0;   // keep: normalise
-                            const double r = rsqrt_newton(x2);
-                            s_xb = x2 * r;
-                            s_ixb = r;
-                            s_ixbf = (CT)r;
+                            const dfm::df r = dfm::rsqrt(x2, 2);
+                            s_rd = r;
+                            s_xbd = dfm::mul(x2, r);
+                            s_ixbf = __fadd_rn(r.h, r.l);
                         }
                         s_flag = f;
                     }
                     __syncthreads();
                     if (s_flag == 0) {   // kept: the sweep's update is applied with the normalisation
-                        n2 = tot[0];
                         fl = 0;
                         ++nfull;
                         upd = true;
                         break;
                     }
+                    if constexpr (kFused) wn2_before = dfm::to_double(fscd[0]);
                     update_pass(false, nl);   // the exact scalars of the swept vector follow
                 }
                 else {
@@ -916,6 +947,7 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 // vector is kept; the barrier below publishes it with the totals.
                 if (tid == 0) {
                     const double x2 = tot[0];
+                    const double wn2_first = wf_df ? dfm::to_double(s_e2vd) : wn2_first0;
                     int f;
                     if (nvec > 0 && nfull + 1 < 4 && x2 < eta2 * wn2_before) f = 1;   // another full sweep
                     else if (attempt == 0 && !contaminated && (x2 <= thr_exh * wn2_first || x2 == 0.0) && next_slot())
@@ -926,13 +958,13 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                         s_xb = x2 * r;
                         s_ixb = r;
                         s_ixbf = (CT)r;
+                        if constexpr (kFused) { s_rd = dfm::from_double(r); s_xbd = dfm::from_double(x2 * r); }
                     } else {
                         f = 3;   // the reachable subspace is exhausted: restart
                     }
                     s_flag = f;
                 }
                 __syncthreads();
-                n2 = tot[0];
                 fl = s_flag;
                 // another full sweep while this one removed more than half of the squared norm
                 if (nfull++ > 0) ++extra;
@@ -1017,21 +1049,41 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
                 if (vc) store16g<VT>(vc + qo, v);
             }
         }
-        if (tid < NT) {   // one output element per thread; every CTA keeps the row for the next step
-            double x = 0.0;
-            if (tid == 0) x = tot[1] * ixb * ixb;   // <w|E|w> / |w|^2
-            else if (tid == 1) x = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
-            else if (tid < 2 + k) x = tot[2 + D + (tid - 2)] * ixb;
-            else if (tid >= C.nden_out && tid < C.nden_out + D) x = tot[2 + (tid - C.nden_out)] * ixb;
-            if (newv && tid == 1) x = (k >= 1) ? tot[2 + D + (k - 1)] * ixb : x;
-            if (!(tid < 2 + k || tid >= C.nden_out)) x = 0.0;
-            prow[tid] = x;
-            if (rank == 0) C.out[(size_t)j * NT + tid] = x;
-        }
-        if (tid == 0) {
-            rowslot[j] = nvec;
-            slotrow[nvec] = j;
-            s_e2v = tot[2 + D + k] * ixb * ixb;   // |E v_j|^2
+        if constexpr (kFused) {   // the row in double-float, FP64 only for the stored copy
+            if (tid < NT) {
+                const dfm::df r = s_rd, z{0.0f, 0.0f};
+                dfm::df x = z;
+                if (tid == 0) x = dfm::mul(dfm::mul(totd[1], r), r);   // <w|E|w> / |w|^2
+                else if (tid == 1) x = injected ? z : s_xbd;          // a restart vector has no coupling to v_{j-1}
+                else if (tid < 2 + k) x = dfm::mul(totd[2 + D + (tid - 2)], r);
+                else if (tid >= C.nden_out && tid < C.nden_out + D) x = dfm::mul(totd[2 + (tid - C.nden_out)], r);
+                if (newv && tid == 1) x = (k >= 1) ? dfm::mul(totd[2 + D + (k - 1)], r) : x;
+                if (!(tid < 2 + k || tid >= C.nden_out)) x = z;
+                prowf[tid] = __fadd_rn(x.h, x.l);
+                if (rank == 0) C.out[(size_t)j * NT + tid] = dfm::to_double(x);
+            }
+            if (tid == 0) {
+                rowslot[j] = nvec;
+                slotrow[nvec] = j;
+                s_e2vd = dfm::mul(dfm::mul(totd[2 + D + k], s_rd), s_rd);   // |E v_j|^2
+            }
+        } else {
+            if (tid < NT) {   // one output element per thread; every CTA keeps the row for the next step
+                double x = 0.0;
+                if (tid == 0) x = tot[1] * ixb * ixb;   // <w|E|w> / |w|^2
+                else if (tid == 1) x = injected ? 0.0 : xb;   // a restart vector has no coupling to v_{j-1}
+                else if (tid < 2 + k) x = tot[2 + D + (tid - 2)] * ixb;
+                else if (tid >= C.nden_out && tid < C.nden_out + D) x = tot[2 + (tid - C.nden_out)] * ixb;
+                if (newv && tid == 1) x = (k >= 1) ? tot[2 + D + (k - 1)] * ixb : x;
+                if (!(tid < 2 + k || tid >= C.nden_out)) x = 0.0;
+                prow[tid] = x;
+                if (rank == 0) C.out[(size_t)j * NT + tid] = x;
+            }
+            if (tid == 0) {
+                rowslot[j] = nvec;
+                slotrow[nvec] = j;
+                s_e2v = tot[2 + D + k] * ixb * ixb;   // |E v_j|^2
+            }
         }
         // The next step's recurrence, when it continues this chain from this row: its
         // vectors v_j, v_{j-1} and the earlier chains' last vectors with the row's alpha,
@@ -1041,13 +1093,14 @@ __global__ void __launch_bounds__(kLzThreads, 2) k_lanczos(const LzChain *chains
             __syncwarp();
             const bool next_newv = (k + 1 < C.n_used) && (j + 1 == s_start[k + 1]);
             if (tid == 0 && !injected && !next_newv) {
+                auto pr = [&](int q) -> CT { if constexpr (kFused) return prowf[q]; else return (CT)prow[q]; };
                 int n = 0;
-                lt[n] = nvec; lcf[n++] = (CT)prow[0];
-                if (j >= 1 && rowslot[j - 1] >= 0) { lt[n] = rowslot[j - 1]; lcf[n++] = (CT)prow[1]; }
+                lt[n] = nvec; lcf[n++] = pr(0);
+                if (j >= 1 && rowslot[j - 1] >= 0) { lt[n] = rowslot[j - 1]; lcf[n++] = pr(1); }
                 for (int q = 0; q < k; ++q)
                     if (s_last[q] < j - 1 && rowslot[s_last[q]] >= 0) {
                         lt[n] = rowslot[s_last[q]];
-                        lcf[n++] = (CT)prow[2 + q];
+                        lcf[n++] = pr(2 + q);
                     }
                 s_nl = n;
             }
