@@ -64,8 +64,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the N_max=12 precision run and the dressed second iteration")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64-per-channel"], default=None,
-                    help="run only this form's warm-up and timed steps (for ncu); prints its timings, not a bench line")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "fp64-per-channel", "mixed-dressed", "mixed-dressed-fp64c"],
+                    default=None,
+                    help="run only this form's warm-up and timed steps (for ncu); prints its timings, not a bench line; "
+                         "*-dressed: on the second iteration's propagator (z_cut 1e-3, two fragments), the couplings "
+                         "on the tensor cores (-fp64c: with the FP64 build)")
     ap.add_argument("--many", action="store_true",
                     help="the batched many-instance run (independent problems, iterated); prints its own line")
     ap.add_argument("--problems", type=int, default=256)
@@ -432,7 +435,11 @@ def gpu_arm(args):
 
     if args.profile:
         kw = {"mixed": dict(mixed=True), "fp64": dict(mixed=False),
-              "fp64-per-channel": dict(mixed=False, per_channel=True)}[args.profile]
+              "fp64-per-channel": dict(mixed=False, per_channel=True), "mixed-dressed": dict(mixed=True),
+              "mixed-dressed-fp64c": dict(mixed=True, fp64_couplings=True)}[args.profile]
+        if args.profile.startswith("mixed-dressed"):
+            ctx.run_all(lanczos=True, mixed=False)
+            ctx.dressed_propagator(1e-3, 2)
         for _ in range(args.warmup):
             ctx.run_all(lanczos=True, **kw)
         ms = []
@@ -442,6 +449,7 @@ def gpu_arm(args):
         if rank == 0:
             print(json.dumps({"profile": args.profile, "workload": args.workload, "steps": args.steps,
                               "timings_ms": ms, "lanczos_kernel_ms": ctx.lanczos_kernel_ms(),
+                              "tensor_couplings": ctx.tensor_couplings(),
                               "extra_sweeps": ctx.two_pass_steps(),
                               "lanczos_steps": sum(L for _, L, _, _ in lanczos_sizes(ctx, prob)),
                               "lanczos_vectors_built": int(ctx.lanczos_stored().sum())}), flush=True)

@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(HERE, "libbd_gb300.so")
 
 BD_OK, BD_ERR_ARG, BD_ERR_CUDA, BD_ERR_CAPACITY, BD_ERR_STATE, BD_ERR_NUMERIC, BD_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5, -6
 BD_RUN_LANCZOS, BD_RUN_MIXED, BD_RUN_PER_CHANNEL, BD_RUN_REF_ORDER, BD_RUN_GRAPH = 1, 2, 4, 8, 16
+BD_RUN_FP64_COUPLINGS = 32
 
 _ip = C.POINTER(C.c_int)
 _dp = C.POINTER(C.c_double)
@@ -64,7 +65,7 @@ EXPORTED = ["bd_create", "bd_destroy", "bd_last_error", "bd_version", "bd_upload
             "bd_files_propagator", "bd_files_pivots", "bd_files_interaction_lines", "bd_upload_files",
             "bd_interaction_fetch", "bd_files_write_propagator", "bd_files_write_pivots", "bd_write_interaction_bin",
             "bd_files_save_selfenergy", "bd_files_load_selfenergy", "bd_files_selfenergy_name", "bd_autotune",
-            "bd_dressed_on_device"]
+            "bd_dressed_on_device", "bd_tensor_couplings"]
 
 
 def load_library(path: str = LIB_PATH):
@@ -99,6 +100,7 @@ def load_library(path: str = LIB_PATH):
     lib.bd_last_timings.argtypes = [vp, _dp]
     lib.bd_diag_two_pass.argtypes = [vp]
     lib.bd_dressed_on_device.argtypes = [vp]
+    lib.bd_tensor_couplings.argtypes = [vp]
     lib.bd_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_double]
     lib.bd_autotune.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.bd_set_lanczos_slices.argtypes = [vp, C.c_int]
@@ -362,8 +364,9 @@ class Context:
 
     # ---------------------------------------------------------------- all channels
     @staticmethod
-    def _flags(lanczos=True, mixed=False, per_channel=False, ref_order=False, graph=False):
+    def _flags(lanczos=True, mixed=False, per_channel=False, ref_order=False, graph=False, fp64_couplings=False):
         flags = (BD_RUN_LANCZOS if lanczos else 0) | (BD_RUN_MIXED if mixed else 0) | (BD_RUN_PER_CHANNEL if per_channel else 0)
+        flags |= BD_RUN_FP64_COUPLINGS if fp64_couplings else 0
         return flags | (BD_RUN_REF_ORDER if ref_order else 0) | (BD_RUN_GRAPH if graph else 0)
 
     def autotune(self, reps=3, **kw):
@@ -372,8 +375,11 @@ class Context:
         self._chk(self.lib.bd_autotune(self.h, self._flags(**kw), reps, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True, ref_order=False, graph=False):
-        flags = self._flags(lanczos, mixed, per_channel, ref_order, graph)
+    def run_all(self, lanczos=True, mixed=False, per_channel=False, sync=True, ref_order=False, graph=False,
+                fp64_couplings=False):
+        """bd_run_all.  fp64_couplings: the mixed form on a dressed propagator builds its
+        couplings with the FP64 kernel instead of the tensor cores."""
+        flags = self._flags(lanczos, mixed, per_channel, ref_order, graph, fp64_couplings)
         self._chk(self.lib.bd_run_all(self.h, flags))
         if sync:
             self.sync()
@@ -389,6 +395,10 @@ class Context:
     def dressed_on_device(self):
         """Whether the last dressed_propagator stayed on the device (no re-planning)."""
         return bool(self.lib.bd_dressed_on_device(self.h))
+
+    def tensor_couplings(self):
+        """Whether the last batched run_all built the couplings on the tensor cores."""
+        return bool(self.lib.bd_tensor_couplings(self.h))
 
     def two_pass_steps(self):
         return int(self.lib.bd_diag_two_pass(self.h))

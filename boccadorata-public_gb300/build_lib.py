@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libbd_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["bd_api.cu", "k_sigma2.cu", "k_lanczos.cu", "k_dyson.cu", "k_eig.cu", "k_sort.cu", "bd_files.cu"]
+SOURCES = ["bd_api.cu", "k_sigma2.cu", "k_lanczos.cu", "k_dyson.cu", "k_eig.cu", "k_sort.cu", "bd_files.cu",
+           "k_coupling_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -18,6 +18,7 @@
 #include <limits>
 #include <map>
 #include <thread>
+#include <tuple>
 #include <unistd.h>
 #include <atomic>
 #include <condition_variable>
@@ -254,6 +255,8 @@ struct bd_ctx {
     std::vector<Chan> chans;
     PinnedArray<S2Block> blocks;
     std::vector<std::vector<S2Block>> chan_blocks;   // per channel, before placement (kept for their capacity)
+    std::vector<int> tc_blk;                         // block indices grouped for the tensor-core tiles
+    std::vector<int4> tc_tiles;                      // (first in tc_blk, blocks, rows, -)
     std::vector<int> chan_chunks;
     HostPool pool_threads;
     PinnedArray<long long> blk_fw_first, blk_bk_first;
@@ -278,6 +281,14 @@ struct bd_ctx {
     size_t pool_bytes = 0;
     DevProblem dp{};
     S2Block *d_blocks = nullptr;
+    // tensor-core coupling build (k_coupling_tc.cu): blocks grouped by (ia, ib, ig, nJab)
+    // into tiles of up to 128 rows; usable when every block's pair count fits
+    int *d_tc_blk = nullptr;
+    int4 *d_tc_tiles = nullptr;
+    int ntc_tiles = 0, tc_np_fw = 0, tc_np_bk = 0;
+    bool tc_ok = false;
+    bool prop_dressed = false;   // some fragment has more than one non-zero amplitude
+    bool last_tc = false;        // the last batched step built the couplings on the tensor cores
     int *d_vchunk_first = nullptr, *d_vchunk_blk = nullptr;
     long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr;
     ChanSig *d_cs = nullptr;
@@ -647,6 +658,35 @@ int build_plan(bd_ctx *c) {
     });
     c->vchunk_first[nb] = nchunk;
     c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
+    // tensor-core tiles: the blocks of every channel that share (ia, ib, ig, nJab) share
+    // the contraction's right-hand operand; their D rows are stacked, 128 to a tile
+    c->tc_blk.resize(nb);
+    for (size_t b = 0; b < nb; ++b) c->tc_blk[b] = (int)b;
+    auto key = [&](int b) {
+        const S2Block &B = c->blocks[b];
+        return std::make_tuple(B.ia, B.ib, B.ig, B.nJab);
+    };
+    std::stable_sort(c->tc_blk.begin(), c->tc_blk.end(), [&](int x, int y) { return key(x) < key(y); });
+    c->tc_tiles.clear();
+    c->tc_np_fw = c->tc_np_bk = 0;
+    c->tc_ok = true;
+    for (size_t q = 0; q < nb;) {
+        const int b0 = c->tc_blk[q];
+        const S2Block &B = c->blocks[b0];
+        if ((long long)c->no[B.ia] * c->no[B.ib] > 64 || B.nfw > 256 || B.nbk > 256) c->tc_ok = false;
+        c->tc_np_fw = std::max(c->tc_np_fw, (B.nfw + 15) & ~15);
+        c->tc_np_bk = std::max(c->tc_np_bk, (B.nbk + 15) & ~15);
+        int rows = 0, n = 0;
+        size_t e = q;
+        while (e < nb && key(c->tc_blk[e]) == key(b0) && rows + c->no[c->blocks[c->tc_blk[e]].ch] <= 128) {
+            rows += c->no[c->blocks[c->tc_blk[e]].ch];
+            ++n;
+            ++e;
+        }
+        if (n == 0) { c->tc_ok = false; break; }   // a block of more than 128 rows
+        c->tc_tiles.push_back(int4{(int)q, n, rows, 0});
+        q = e;
+    }
     return BD_OK;
 }
 
@@ -700,7 +740,9 @@ int check_chan(bd_ctx *ctx, int ish) {
 // ---------------------------------------------------------------- Sigma(2)
 // aux != nullptr: the backward poles go to that stream once the V' gather is done (their
 // rows are independent of the forward ones); the caller joins it before the sort.
-int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t aux = nullptr) {
+// tc: the couplings on the tensor cores (k_poles_tc, every channel at once); the energies
+// are formed there too, with k_poles's operations.
+int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t aux = nullptr, bool tc = false) {
     const Chan &A = ctx->chans[ch_lo], &Z = ctx->chans[ch_hi - 1];
     const int b0 = A.blk_first, nb = Z.blk_first + Z.nblk - b0;
     if (nb <= 0) {
@@ -723,6 +765,21 @@ int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t aux = nullptr)
     if (aux) {   // (launched before the forward poles so the two run side by side)
         CU(cudaEventRecord(ctx->ev_fork2, ctx->st));
         CU(cudaStreamWaitEvent(aux, ctx->ev_fork2, 0));
+    }
+    if (tc) {   // (all channels: the tiles mix them)
+        for (int dir = 1; dir >= 0; --dir) {
+            const int np = dir == 0 ? ctx->tc_np_fw : ctx->tc_np_bk;
+            if (np == 0) continue;
+            const size_t smem = tc_smem_bytes(np);
+            cudaStream_t st = (dir == 1 && aux) ? aux : ctx->st;
+            CU(launch_poles_tc(ctx->dp, ctx->d_blocks, ctx->d_tc_blk, ctx->d_tc_tiles, ctx->ntc_tiles, ctx->d_cs, dir,
+                               ctx->d_vp, dir == 0 ? ctx->d_Efw : ctx->d_Ebk, dir == 0 ? ctx->d_S2fw : ctx->d_S2bk,
+                               dir == 0 ? ctx->d_Mfw : ctx->d_Mbk, ctx->d_lzstat + 3, smem, st));
+            ctx->launches += 1;
+            if (dir == 1 && aux) CU(cudaEventRecord(ctx->ev_join2, aux));
+        }
+        if (aux && ctx->tc_np_bk == 0) CU(cudaEventRecord(ctx->ev_join2, aux));
+        return BD_OK;
     }
     if (nk > 0) {
         k_poles<<<(unsigned)((nk + 127) / 128), 128, 0, aux ? aux : ctx->st>>>(ctx->dp, ctx->d_blocks + b0,
@@ -1388,6 +1445,16 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if (long long k = first_nonfinite(prop->fqh, (long long)nqh * prop->nspb); k >= 0)
         return fail(ctx, BD_ERR_NUMERIC, "propagator: quasihole amplitude %lld is not finite", k);
     ctx->ep.assign(prop->ep, prop->ep + nqp); ctx->eh.assign(prop->eh, prop->eh + nqh);
+    ctx->prop_dressed = false;
+    for (int side = 0; side < 2 && !ctx->prop_dressed; ++side) {
+        const double *f = side == 0 ? prop->fqp : prop->fqh;
+        const int nq = side == 0 ? nqp : nqh;
+        for (int q = 0; q < nq && !ctx->prop_dressed; ++q) {
+            int nz = 0;
+            for (int o = 0; o < prop->nspb; ++o) nz += f[(size_t)q * prop->nspb + o] != 0.0;
+            ctx->prop_dressed = nz > 1;
+        }
+    }
     std::vector<double> fqp(prop->fqp, prop->fqp + (size_t)nqp * prop->nspb);
     std::vector<double> fqh(prop->fqh, prop->fqh + (size_t)nqh * prop->nspb);
     int rc;
@@ -1410,6 +1477,11 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &ctx->d_vchunk_blk, ctx->vchunk_blk))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
+    ctx->ntc_tiles = (int)ctx->tc_tiles.size();
+    if (ctx->ntc_tiles > 0) {
+        if ((rc = dupload(ctx, &ctx->d_tc_blk, ctx->tc_blk))) return rc;
+        if ((rc = dupload(ctx, &ctx->d_tc_tiles, ctx->tc_tiles))) return rc;
+    }
     std::vector<ChanSig> cs(ns);
     std::vector<int> segoff_fw(ns + 1), segoff_bk(ns + 1);
     for (int I = 0; I < ns; ++I) {
@@ -2051,7 +2123,10 @@ int enqueue_step(bd_ctx *ctx, int flags) {
         CU(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_fork, 0));
         if ((rc = launch_ehf(ctx, 0, ns, ctx->st_aux))) return rc;
         CU(cudaEventRecord(ctx->ev_join, ctx->st_aux));
-        if ((rc = launch_sigma2(ctx, 0, ns, ctx->st_aux))) return rc;
+        const bool tc = fp32 && lanczos && ctx->prop_dressed && ctx->tc_ok && ctx->ntc_tiles > 0 && ctx->d_lzstat &&
+                        !(flags & BD_RUN_FP64_COUPLINGS);
+        ctx->last_tc = tc;
+        if ((rc = launch_sigma2(ctx, 0, ns, ctx->st_aux, tc))) return rc;
         CU(cudaStreamWaitEvent(ctx->st, ctx->ev_join2, 0));
         CU(record(ctx, ctx->ev[1]));
         if (lanczos && (rc = launch_sort(ctx, 0, ns, ref_order))) return rc;
@@ -2109,7 +2184,7 @@ extern "C" {
 int bd_run_all(bd_ctx *ctx, int flags) {
     if (!ctx) return BD_ERR_ARG;
     if (!ctx->uploaded) return fail(ctx, BD_ERR_STATE, "no problem uploaded");
-    if (flags & ~(BD_RUN_LANCZOS | BD_RUN_MIXED | BD_RUN_PER_CHANNEL | BD_RUN_REF_ORDER | BD_RUN_GRAPH))
+    if (flags & ~(BD_RUN_LANCZOS | BD_RUN_MIXED | BD_RUN_PER_CHANNEL | BD_RUN_REF_ORDER | BD_RUN_GRAPH | BD_RUN_FP64_COUPLINGS))
         return fail(ctx, BD_ERR_ARG, "flags 0x%x", flags);
     const bool lanczos = (flags & BD_RUN_LANCZOS) != 0;
     if (lanczos && !ctx->have_pivots) return fail(ctx, BD_ERR_STATE, "no pivots uploaded");
@@ -2181,7 +2256,14 @@ int bd_sync(bd_ctx *ctx) {
         for (int q = 0; q < 4; ++q) ctx->timings[q] = ms[q];
         ctx->timings[4] = ms[0] + ms[1] + ms[2] + ms[3];
         ctx->lz_two_pass = 0;
-        if (ctx->d_lzstat) CU(cudaMemcpy(&ctx->lz_two_pass, ctx->d_lzstat, sizeof(int), cudaMemcpyDeviceToHost));
+        int lzs[4] = {0, 0, 0, 0};
+        if (ctx->d_lzstat) CU(cudaMemcpy(lzs, ctx->d_lzstat, sizeof(lzs), cudaMemcpyDeviceToHost));
+        ctx->lz_two_pass = lzs[0];
+        if (lzs[3]) {
+            ctx->results_valid = false;
+            CU(cudaMemset(ctx->d_lzstat, 0, sizeof(lzs)));
+            return fail(ctx, BD_ERR_TIMEOUT, "tensor-core coupling build: a bounded wait for the MMAs gave up");
+        }
         ctx->lz_kernel_ms = 0.0;
         if (ctx->lz_timed) {
             float m = 0.f;
@@ -2323,6 +2405,10 @@ int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_curr
             ctx->results_valid = false;
             for (int I = 0; I < ns; ++I) ctx->chans[I].state = ST_NONE;
             ctx->last_update_on_device = true;
+            if (!ctx->prop_dressed) {   // the solutions' amplitudes are general: the mixed form's
+                ctx->prop_dressed = true;   // captured steps switch to the tensor-core couplings
+                graph_invalidate(ctx);
+            }
             return rc;
         }
         for (void *q : {(void *)dcnt, (void *)dsel, (void *)ddof, (void *)doff}) CU(cudaFreeAsync(q, ctx->st));
@@ -2393,6 +2479,7 @@ int bd_last_timings(bd_ctx *ctx, double *ms5) {
  * reorthogonalisation sweep in the last bd_run_all, and tuning knobs. */
 int bd_diag_two_pass(bd_ctx *ctx) { return ctx ? ctx->lz_two_pass : -1; }
 int bd_dressed_on_device(bd_ctx *ctx) { return ctx ? (ctx->last_update_on_device ? 1 : 0) : -1; }
+int bd_tensor_couplings(bd_ctx *ctx) { return ctx ? (ctx->last_tc ? 1 : 0) : -1; }
 double bd_lanczos_kernel_ms(bd_ctx *ctx) { return ctx ? ctx->lz_kernel_ms : -1.0; }
 long long bd_launch_count(bd_ctx *ctx) { return ctx ? ctx->launches : -1; }
 int bd_lanczos_stored(bd_ctx *ctx, int *stored) {

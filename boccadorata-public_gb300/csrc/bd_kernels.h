@@ -27,6 +27,12 @@ __global__ void k_permute_soa(const int *perm, long long n0, long long n, const 
 __global__ void k_rows_aos(const double *E, const double *S2, const double *M, int N, int D, double *rows);
 __global__ void k_rows_aos_perm(const int *perm, long long off, const double *E, const double *S2, const double *M,
                                 int N, int D, double *rows);
+// Tensor-core coupling build of the mixed form (k_coupling_tc.cu): M, E and S2 of every
+// pole of direction dir from the tiles of blocks sharing (ia, ib, ig, nJab).
+size_t tc_smem_bytes(int np);
+cudaError_t launch_poles_tc(const DevProblem &P, const S2Block *blk, const int *tile_blk, const int4 *tiles,
+                            int ntiles, const ChanSig *cs, int dir, const double *vp, double *E, double *S2, double *M,
+                            int *err, size_t smem, cudaStream_t st);
 constexpr int kSortThreads = 512;
 constexpr int kSortChunk = 2048;  // poles per chunk of the shared-memory sort
 constexpr int kSortMax = 16384;   // longest channel sorted by chunks (longer: radix sort)

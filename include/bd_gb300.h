@@ -55,6 +55,8 @@ extern "C" {
 #define BD_RUN_GRAPH     16  /* batched: capture the step in a CUDA graph on first use (per
                                 flag combination) and replay it; any change of the problem,
                                 the pivots or the tuning captures it again */
+#define BD_RUN_FP64_COUPLINGS 32 /* batched BD_RUN_MIXED on a dressed propagator: build the
+                                couplings with the FP64 kernel instead of the tensor cores */
 
 typedef struct bd_ctx bd_ctx;
 
@@ -210,6 +212,12 @@ int bd_dressed_propagator(bd_ctx *ctx, double z_cut, int max_frag, int keep_curr
  * of every subshell, the fragments are selected and written in place and the block
  * plan, pole counts and chain schedules stay (no host planning); otherwise 0. */
 int bd_dressed_on_device(bd_ctx *ctx);
+/* 1 when the last batched bd_run_all built the couplings M on the tensor cores: the
+ * BD_RUN_MIXED form (with BD_RUN_LANCZOS) on a propagator with some fragment of more than
+ * one non-zero amplitude, unless BD_RUN_FP64_COUPLINGS (tcgen05, TF32 in three products
+ * hi*hi + hi*lo + lo*hi with FP32 accumulation, about 2^-21 relative; the FP64 form and
+ * the per-channel calls always use the FP64 build, bit for bit the reference's). */
+int bd_tensor_couplings(bd_ctx *ctx);
 /* Device time of the phases of the last bd_run_all in ms: sigma2, sort, lanczos, dyson, total. */
 int bd_last_timings(bd_ctx *ctx, double *ms5);
 /* Diagnostics: extra reorthogonalisation sweeps of the last bd_run_all; device time of
