@@ -349,11 +349,17 @@ def dressed_run(bd, prob, device, z_cut=1e-3, max_frag=2):
     ns = prob.ms.nsubsh
     cnt = [ctx.count_poles(i) for i in range(ns)]
     res = {}
+    tc = {}
     for form, mixed, cl in (("fp64", False, 8), ("fp64_cl16", False, 16), ("mixed", True, 8)):
         ctx.set_tuning(lz_cluster=cl)
         ctx.run_all(lanczos=True, mixed=mixed)
         ctx.run_all(lanczos=True, mixed=mixed)
         res[form] = (ctx.timings(), ctx.results_all(), ctx.koltun_all(), ctx.lanczos_kernel_ms())
+        if mixed:   # the couplings on the tensor cores; the FP64 build beside it for its Sigma(2) time
+            tc["tensor_couplings"] = ctx.tensor_couplings()
+            tc["sigma2_ms_tensor"] = ctx.timings()["sigma2"]
+            ctx.run_all(lanczos=True, mixed=True, fp64_couplings=True)
+            tc["sigma2_ms_fp64_couplings"] = ctx.timings()["sigma2"]
     ctx.set_tuning(lz_cluster=8)
     st = ctx.lanczos_stored()
     chi = lanczos_sizes(ctx, ctx.prob, with_index=True)
@@ -388,7 +394,7 @@ def dressed_run(bd, prob, device, z_cut=1e-3, max_frag=2):
             "backward_poles": int(sum(c[1] for c in cnt)), "lanczos_vectors_built": int(sum(stored)),
             "lanczos_rows": int(sum(c[1] for c in chains)),
             "fp64_ms": t64["total"], "mixed_ms": t32["total"], "fp64_phases_ms": t64, "mixed_phases_ms": t32,
-            "speedup_mixed_vs_fp64": t64["total"] / t32["total"],
+            "speedup_mixed_vs_fp64": t64["total"] / t32["total"], "mixed_couplings": tc,
             "mixed_lanczos": {"kernel": "k_lanczos<float> (global slices)", "kernel_ms": l32, "algorithmic_bytes": alg32,
                               "achieved_gbs": alg32 / (l32 / 1e3) / 1e9, "peak_gbs": peak,
                               "frac": alg32 / (l32 / 1e3) / 1e9 / peak, "peak_source": src},
