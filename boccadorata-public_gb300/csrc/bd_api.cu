@@ -18,7 +18,6 @@
 #include <limits>
 #include <map>
 #include <thread>
-#include <tuple>
 #include <unistd.h>
 #include <atomic>
 #include <condition_variable>
@@ -289,6 +288,7 @@ struct bd_ctx {
     bool tc_ok = false;
     bool prop_dressed = false;   // some fragment has more than one non-zero amplitude
     bool last_tc = false;        // the last batched step built the couplings on the tensor cores
+    bool tc_built = false;       // tensor-core tiles of the current plan uploaded
     int *d_vchunk_first = nullptr, *d_vchunk_blk = nullptr;
     long long *d_blk_fw_first = nullptr, *d_blk_bk_first = nullptr;
     ChanSig *d_cs = nullptr;
@@ -658,35 +658,8 @@ int build_plan(bd_ctx *c) {
     });
     c->vchunk_first[nb] = nchunk;
     c->tot_fw = fw; c->tot_bk = bk; c->tot_mfw = mfw; c->tot_mbk = mbk; c->tot_vp = vp;
-    // tensor-core tiles: the blocks of every channel that share (ia, ib, ig, nJab) share
-    // the contraction's right-hand operand; their D rows are stacked, 128 to a tile
-    c->tc_blk.resize(nb);
-    for (size_t b = 0; b < nb; ++b) c->tc_blk[b] = (int)b;
-    auto key = [&](int b) {
-        const S2Block &B = c->blocks[b];
-        return std::make_tuple(B.ia, B.ib, B.ig, B.nJab);
-    };
-    std::stable_sort(c->tc_blk.begin(), c->tc_blk.end(), [&](int x, int y) { return key(x) < key(y); });
-    c->tc_tiles.clear();
-    c->tc_np_fw = c->tc_np_bk = 0;
-    c->tc_ok = true;
-    for (size_t q = 0; q < nb;) {
-        const int b0 = c->tc_blk[q];
-        const S2Block &B = c->blocks[b0];
-        if ((long long)c->no[B.ia] * c->no[B.ib] > 64 || B.nfw > 256 || B.nbk > 256) c->tc_ok = false;
-        c->tc_np_fw = std::max(c->tc_np_fw, (B.nfw + 15) & ~15);
-        c->tc_np_bk = std::max(c->tc_np_bk, (B.nbk + 15) & ~15);
-        int rows = 0, n = 0;
-        size_t e = q;
-        while (e < nb && key(c->tc_blk[e]) == key(b0) && rows + c->no[c->blocks[c->tc_blk[e]].ch] <= 128) {
-            rows += c->no[c->blocks[c->tc_blk[e]].ch];
-            ++n;
-            ++e;
-        }
-        if (n == 0) { c->tc_ok = false; break; }   // a block of more than 128 rows
-        c->tc_tiles.push_back(int4{(int)q, n, rows, 0});
-        q = e;
-    }
+    c->tc_built = false;   // the tensor-core tiles follow on demand (build_tc_tiles)
+    c->ntc_tiles = 0;
     return BD_OK;
 }
 
@@ -740,6 +713,52 @@ int check_chan(bd_ctx *ctx, int ish) {
 // ---------------------------------------------------------------- Sigma(2)
 // aux != nullptr: the backward poles go to that stream once the V' gather is done (their
 // rows are independent of the forward ones); the caller joins it before the sort.
+// Tensor-core tiles of the current plan (host grouping, then upload), built when a dressed
+// propagator first asks for them: the blocks of every channel that share (ia, ib, ig,
+// nJab) share the contraction's right-hand operand; their D rows are stacked, 128 to a tile.
+int build_tc_tiles(bd_ctx *c) {
+    const size_t nb = c->blocks.size();
+    const long long ns = c->nsubsh;
+    auto key = [&](int b) {
+        const S2Block &B = c->blocks[b];
+        return (size_t)((((long long)B.ia * ns + B.ib) * ns + B.ig) * 2 + (B.nJab ? 1 : 0));
+    };
+    // counting sort by key, stable (the plan's block order inside a group)
+    std::vector<int> first((size_t)(ns * ns * ns * 2) + 1, 0);
+    for (size_t b = 0; b < nb; ++b) ++first[key((int)b) + 1];
+    for (size_t q = 1; q < first.size(); ++q) first[q] += first[q - 1];
+    c->tc_blk.resize(nb);
+    for (size_t b = 0; b < nb; ++b) c->tc_blk[first[key((int)b)]++] = (int)b;
+    c->tc_tiles.clear();
+    c->tc_np_fw = c->tc_np_bk = 0;
+    c->tc_ok = true;
+    for (size_t q = 0; q < nb;) {
+        const int b0 = c->tc_blk[q];
+        const S2Block &B = c->blocks[b0];
+        if ((long long)c->no[B.ia] * c->no[B.ib] > 64 || B.nfw > 256 || B.nbk > 256) c->tc_ok = false;
+        c->tc_np_fw = std::max(c->tc_np_fw, (B.nfw + 15) & ~15);
+        c->tc_np_bk = std::max(c->tc_np_bk, (B.nbk + 15) & ~15);
+        int rows = 0, n = 0;
+        size_t e = q;
+        while (e < nb && key(c->tc_blk[e]) == key(b0) && rows + c->no[c->blocks[c->tc_blk[e]].ch] <= 128) {
+            rows += c->no[c->blocks[c->tc_blk[e]].ch];
+            ++n;
+            ++e;
+        }
+        if (n == 0) { c->tc_ok = false; break; }   // a block of more than 128 rows
+        c->tc_tiles.push_back(int4{(int)q, n, rows, 0});
+        q = e;
+    }
+    c->ntc_tiles = (int)c->tc_tiles.size();
+    if (c->ntc_tiles > 0) {
+        int rc;
+        if ((rc = dupload(c, &c->d_tc_blk, c->tc_blk))) return rc;
+        if ((rc = dupload(c, &c->d_tc_tiles, c->tc_tiles))) return rc;
+    }
+    c->tc_built = true;
+    return BD_OK;
+}
+
 // tc: the couplings on the tensor cores (k_poles_tc, every channel at once); the energies
 // are formed there too, with k_poles's operations.
 int launch_sigma2(bd_ctx *ctx, int ch_lo, int ch_hi, cudaStream_t aux = nullptr, bool tc = false) {
@@ -1477,11 +1496,6 @@ int upload_propagator(bd_ctx *ctx, const bd_propagator *prop) {
     if ((rc = dupload(ctx, &ctx->d_vchunk_blk, ctx->vchunk_blk))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_fw_first, ctx->blk_fw_first))) return rc;
     if ((rc = dupload(ctx, &ctx->d_blk_bk_first, ctx->blk_bk_first))) return rc;
-    ctx->ntc_tiles = (int)ctx->tc_tiles.size();
-    if (ctx->ntc_tiles > 0) {
-        if ((rc = dupload(ctx, &ctx->d_tc_blk, ctx->tc_blk))) return rc;
-        if ((rc = dupload(ctx, &ctx->d_tc_tiles, ctx->tc_tiles))) return rc;
-    }
     std::vector<ChanSig> cs(ns);
     std::vector<int> segoff_fw(ns + 1), segoff_bk(ns + 1);
     for (int I = 0; I < ns; ++I) {
@@ -2123,7 +2137,7 @@ int enqueue_step(bd_ctx *ctx, int flags) {
         CU(cudaStreamWaitEvent(ctx->st_aux, ctx->ev_fork, 0));
         if ((rc = launch_ehf(ctx, 0, ns, ctx->st_aux))) return rc;
         CU(cudaEventRecord(ctx->ev_join, ctx->st_aux));
-        const bool tc = fp32 && lanczos && ctx->prop_dressed && ctx->tc_ok && ctx->ntc_tiles > 0 && ctx->d_lzstat &&
+        const bool tc = fp32 && lanczos && ctx->prop_dressed && ctx->tc_built && ctx->tc_ok && ctx->ntc_tiles > 0 && ctx->d_lzstat &&
                         !(flags & BD_RUN_FP64_COUPLINGS);
         ctx->last_tc = tc;
         if ((rc = launch_sigma2(ctx, 0, ns, ctx->st_aux, tc))) return rc;
@@ -2195,6 +2209,10 @@ int bd_run_all(bd_ctx *ctx, int flags) {
     ctx->lz_timed = false;
     if ((rc = ensure_dyson(ctx, lanczos))) return rc;
     const bool graph = (flags & BD_RUN_GRAPH) && !(flags & BD_RUN_PER_CHANNEL);
+    // the tensor-core tiles, when this step will use them (built here, before any capture)
+    if (lanczos && (flags & BD_RUN_MIXED) && !(flags & (BD_RUN_FP64_COUPLINGS | BD_RUN_PER_CHANNEL)) &&
+        ctx->prop_dressed && !ctx->tc_built && (rc = build_tc_tiles(ctx)))
+        return rc;
     rc = graph ? graph_step(ctx, flags & ~BD_RUN_GRAPH) : enqueue_step(ctx, flags & ~BD_RUN_GRAPH);
     if (rc) return rc;
     if (graph && lanczos) ctx->lz_timed = true;

@@ -352,6 +352,194 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     cluster.sync();
 }
 
+// ---------------------------------------------------------------- K4a'' double-float clusters
+// The cluster reduction above in double-float (df64.cuh) where every warp keeps its own
+// partial vector (npriv = 8): k_tridiag's steps, rows and sums unchanged, the matrix's
+// lower triangle turned into (hi, lo) FP32 pairs in place first (each CTA its own rows,
+// from the doubles' bits), the reflector's scalars from the column scaled by a power of
+// two (as k_tridiag_small forms them), and the reflectors stored for k_qrows in FP64 as
+// before.  An FP64 multiply-add holds an SM sub-partition's FP64 unit for ~64 cycles;
+// the double-float one is ~14 FP32 instructions.
+namespace {
+
+__device__ inline dfm::df ld_df(const double *p) {
+    const float2 f = __ldcg(reinterpret_cast<const float2 *>(p));
+    return dfm::df{f.x, f.y};
+}
+__device__ inline void st_df(double *p, dfm::df x) { *reinterpret_cast<float2 *>(p) = make_float2(x.h, x.l); }
+
+// x as hi + lo from its bits: hi the double truncated to FP32, lo the next bits of the
+// significand (rounded to FP32), then renormalised; no FP64 instruction (values inside
+// the FP32 range; below it, zero)
+__device__ inline dfm::df df_from_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF) - 1023;
+    if (E < -126) return dfm::df{0.0f, 0.0f};
+    const unsigned s = (unsigned)(b >> 63) << 31;
+    const float hi = __uint_as_float(s | ((unsigned)(E + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+    // remainder (b & (2^29 - 1)) 2^(E - 52); below 2^-126 the factor goes in two steps
+    float lo = __uint2float_rn((unsigned)(b & 0x1FFFFFFFull));
+    if (E - 52 >= -126) {
+        lo = __fmul_rn(lo, __uint_as_float((unsigned)(E - 52 + 127) << 23));
+    } else {
+        lo = __fmul_rn(lo, __uint_as_float((unsigned)(E - 52 + 64 + 127) << 23));
+        lo = __fmul_rn(lo, 5.42101086242752217e-20f);   // 2^-64
+    }
+    if (s) lo = -lo;
+    return dfm::renorm(hi, lo);
+}
+
+__device__ inline dfm::df block_sum_df(dfm::df v, dfm::df *scratch) {
+    v = dfm::warp_sum(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    dfm::df s{0.0f, 0.0f};
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s = dfm::add(s, scratch[q]);
+    return s;
+}
+
+__device__ inline int f32_exponent(float x) { return (int)((__float_as_uint(x) >> 23) & 255u) - 127; }
+__device__ inline float pow2_f32(int e) { return __uint_as_float((unsigned)(e + 127) << 23); }
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTdThreads) k_tridiag_df(const DyJob *jobs, int njobs, int nmax, int npriv) {
+    using dfm::df;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CL = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int jid = blockIdx.x / CL;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.nc;
+    if (n <= kTsMax) return;   // k_tridiag_small's (the whole cluster leaves together)
+    extern __shared__ double sm[];
+    df *v = reinterpret_cast<df *>(sm);
+    df *p = v + nmax;
+    df *pc = p + nmax;
+    df *pt = pc + nmax;
+    df *pr = pt + (size_t)npriv * nmax;
+    df *scratch = pr + (nmax / CL + 1);
+    double *A = J.A;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kWarps = kTdThreads / 32;
+    df *ptw = pt + (size_t)warp * nmax;   // npriv == kWarps: a partial vector per warp
+    const df zero{0.0f, 0.0f};
+    // this CTA's rows (i = rank, rank + CL, ...), lower triangle, to double-float in place
+    for (int i = rank; i < n; i += CL)
+        for (int j = tid; j <= i; j += kTdThreads) {
+            double *a = A + (size_t)i * n + j;
+            st_df(a, df_from_bits(__ldcg(a)));
+        }
+    cluster.sync();
+    for (int k = 0; k + 2 < n; ++k) {
+        const int b0 = k + 1, m = n - b0;
+        // 1. reflector from column k (rows > k), every CTA alike: alpha, |x_1:|^2, the
+        //    power of two that scales them into [1, 2), then beta, tau and 1/(alpha - beta)
+        df s2 = zero;
+        for (int t = 1 + tid; t < m; t += kTdThreads) { const df x = ld_df(A + (size_t)(b0 + t) * n + k); s2 = dfm::fma(x, x, s2); }
+        s2 = block_sum_df(s2, scratch);
+        const df al = ld_df(A + (size_t)b0 * n + k);
+        const bool nz = (s2.h != 0.0f || s2.l != 0.0f);
+        df tau = zero, scal = zero, beta = al;
+        if (nz) {
+            const int ea = (al.h != 0.0f) ? f32_exponent(al.h) : -1000;
+            int e = max(ea, f32_exponent(s2.h) >> 1);
+            e = min(max(e, -126), 126);
+            const float sg = pow2_f32(-e);
+            const df alt{al.h * sg, al.l * sg}, s2t{(s2.h * sg) * sg, (s2.l * sg) * sg};
+            const df x2 = dfm::fma(alt, alt, s2t);   // in [1, 12)
+            const df r = dfm::rsqrt(x2, 2), nx = dfm::mul(x2, r);
+            const bool ng = signbit(alt.h);
+            const df aa = ng ? dfm::neg(alt) : alt;
+            tau = dfm::fma(aa, r, df{1.0f, 0.0f});
+            df st = dfm::rcp(dfm::add(aa, nx), 2);   // 1 / (alpha~ - beta~)
+            if (ng) st = dfm::neg(st);
+            scal = df{st.h * sg, st.l * sg};         // 1 / (alpha - beta)
+            const df bt = ng ? nx : dfm::neg(nx);
+            const float un = pow2_f32(e);
+            beta = df{bt.h * un, bt.l * un};
+            for (int t = tid; t < m; t += kTdThreads) v[t] = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(ld_df(A + (size_t)(b0 + t) * n + k), scal);
+        }
+        if (rank == 0 && tid == 0) { J.e[k] = dfm::to_double(beta); J.tau[k] = dfm::to_double(tau); J.d[k] = dfm::to_double(ld_df(A + (size_t)k * n + k)); }
+        if (nz) {
+            for (int t = tid; t < kWarps * m; t += kTdThreads) pt[(size_t)(t / m) * nmax + t % m] = zero;
+            __syncthreads();
+            // 2. own rows: row part and transposed part of A v (two chains per lane)
+            const int first = b0 + ((rank - b0 % CL) % CL + CL) % CL;
+            for (int i = first + warp * CL; i < n; i += CL * kWarps) {
+                const double *Ai = A + (size_t)i * n;
+                const df vi = v[i - b0];
+                df rs0 = zero, rs1 = zero;
+                int j = b0 + lane;
+                for (; j + 32 < i; j += 64) {
+                    const int t = j - b0;
+                    const df a0 = ld_df(Ai + j), a1 = ld_df(Ai + j + 32);
+                    rs0 = dfm::fma(a0, v[t], rs0);
+                    rs1 = dfm::fma(a1, v[t + 32], rs1);
+                    ptw[t] = dfm::fma(a0, vi, ptw[t]);
+                    ptw[t + 32] = dfm::fma(a1, vi, ptw[t + 32]);
+                }
+                for (; j <= i; j += 32) {
+                    const df a = ld_df(Ai + j);
+                    rs0 = dfm::fma(a, v[j - b0], rs0);
+                    if (j < i) ptw[j - b0] = dfm::fma(a, vi, ptw[j - b0]);
+                }
+                const df rs = dfm::warp_sum(dfm::add(rs0, rs1));
+                if (lane == 0) pr[(i - first) / CL] = rs;
+            }
+            __syncthreads();
+            for (int t = tid; t < m; t += kTdThreads) {
+                df s = zero;
+                for (int q = 0; q < kWarps; ++q) s = dfm::add(s, pt[(size_t)q * nmax + t]);
+                const int i = b0 + t;
+                if (i >= first && (i - first) % CL == 0) s = dfm::add(s, pr[(i - first) / CL]);
+                pc[t] = s;
+            }
+            cluster.sync();
+            // 3. p = tau A v over the cluster in rank order; w = p - (tau/2)(p.v) v
+            df kv = zero;
+            for (int t = tid; t < m; t += kTdThreads) {
+                df s = zero;
+                for (int r = 0; r < CL; ++r) s = dfm::add(s, cluster.map_shared_rank(pc, r)[t]);
+                s = dfm::mul(s, tau);
+                p[t] = s;
+                kv = dfm::fma(s, v[t], kv);
+            }
+            const df K = block_sum_df(kv, scratch);
+            const df nK = dfm::neg(dfm::mul(df{0.5f * tau.h, 0.5f * tau.l}, K));
+            for (int t = tid; t < m; t += kTdThreads) p[t] = dfm::fma(nK, v[t], p[t]);
+            __syncthreads();
+            // 4. A_ij -= v_i w_j + w_i v_j on the own rows, j <= i
+            for (int i = first + warp * CL; i < n; i += CL * kWarps) {
+                double *Ai = A + (size_t)i * n;
+                const df vi = v[i - b0], wi = p[i - b0];
+                for (int j = b0 + lane; j <= i; j += 32) {
+                    const int t = j - b0;
+                    const df t2 = dfm::fma(vi, p[t], dfm::mul(wi, v[t]));
+                    st_df(Ai + j, dfm::add(ld_df(Ai + j), dfm::neg(t2)));
+                }
+            }
+            if (rank == 0)   // the reflector for k_qrows, in FP64, in row k right of the diagonal
+                for (int t = tid; t < m; t += kTdThreads) A[(size_t)k * n + b0 + t] = dfm::to_double(v[t]);
+        }
+        cluster.sync();
+    }
+    if (rank == 0 && tid == 0) {
+        if (n >= 2) {
+            J.d[n - 2] = dfm::to_double(ld_df(A + (size_t)(n - 2) * n + (n - 2)));
+            J.e[n - 2] = dfm::to_double(ld_df(A + (size_t)(n - 1) * n + (n - 2)));
+            J.tau[n - 2] = 0.0;
+        }
+        J.d[n - 1] = dfm::to_double(ld_df(A + (size_t)(n - 1) * n + (n - 1)));
+        J.e[n - 1] = 0.0;
+        J.tau[n - 1] = 0.0;
+    }
+    cluster.sync();
+}
+
 // ---------------------------------------------------------------- K4a' small matrices
 // Matrices of order nc <= kTsMax (after deflation nearly all: the N_max = 10 channels
 // reduce to 11..94) are reduced by one CTA with the matrix resident in shared memory
@@ -643,10 +831,12 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    const int npriv = tridiag_npriv(nmax, cluster);
+    auto kern = (npriv == kTdThreads / 32) ? k_tridiag_df : k_tridiag;   // double-float with a partial per warp
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
-    e = cudaLaunchKernelEx(&cfg, k_tridiag, d_jobs, njobs, nmax, tridiag_npriv(nmax, cluster));
+    e = cudaLaunchKernelEx(&cfg, kern, d_jobs, njobs, nmax, npriv);
     if (e != cudaSuccess) return e;
     return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);
 }
