@@ -175,7 +175,10 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
         int ishc = P.orb_sh[ic], ishd = P.orb_sh[id];
         icd = ind_i1i2J(id, ic, J); iph += (P.j2[ishc] + P.j2[ishd]) / 2 - J + 1;
     }
-    double xph = (double)(1 - 2 * (abs(iph) % 2));
+    // the phase (-1)^iph as a sign flip on the integer pipe: V * (+-1) exactly, without an
+    // FP64 multiply (one FP64 instruction holds the sub-partition's FP64 unit ~64 cycles)
+    const unsigned long long xph = (abs(iph) % 2) ? 0x8000000000000000ull : 0ull;
+    auto phased = [xph](double x) { return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ xph)); };
     if (icd < iab) { int t = iab; iab = icd; icd = t; }
     int key = ind_chipJ(ch, ip, J);
     int lo = P.seg_str[key], hi = P.seg_end[key];
@@ -194,14 +197,14 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
             const int r1 = P.prank[((size_t)c * P.norb + d) * P.nJ + J], r0 = P.prank[pa];
             if (r1 >= 0 && r0 >= 0) {
                 const int pos = rw.x + (r1 - r0);
-                if (pos >= rw.x && pos <= rw.y && P.icdJ[pos] == icd) return __dmul_rn(P.V[pos], xph);
+                if (pos >= rw.x && pos <= rw.y && P.icdJ[pos] == icd) return phased(P.V[pos]);
             }
         }
         int f = rw.x, l = rw.y;
         while (f <= l) {
             const int mid = (f + l) >> 1;
             const int cm = P.icdJ[mid];
-            if (cm == icd) return __dmul_rn(P.V[mid], xph);
+            if (cm == icd) return phased(P.V[mid]);
             if (cm < icd) f = mid + 1; else l = mid - 1;
         }
         return 0.0;
@@ -212,7 +215,7 @@ __device__ inline double vget(const DevProblem &P, int ia, int ib, int ic, int i
         int test = (iab < am);
         if (am == iab) {
             int cm = P.icdJ[mid];
-            if (cm == icd) return __dmul_rn(P.V[mid], xph);
+            if (cm == icd) return phased(P.V[mid]);
             test = (icd < cm);
         }
         if (test) hi = mid;
