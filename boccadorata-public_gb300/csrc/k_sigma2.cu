@@ -100,9 +100,11 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
     const double *fb = fA + (size_t)(sA[B.ib] + nbf) * NS;
     const double *fg = fG + (size_t)(sG[B.ig] + ngf) * NS;
     const double e = __dsub_rn(__dadd_rn(eA[sA[B.ia] + na], eA[sA[B.ib] + nbf]), eG[sG[B.ig] + ngf]);
-    const double xJab = (double)(1 - 2 * B.nJab);
-    double x4 = 1.0;
-    if (B.ia == B.ib && na == nbf) x4 = __ddiv_rn(x4, kSqr2);
+    // (1 - 2 nJab) x as a sign flip and 1 / sqrt2 as the constant the IEEE division gives
+    // (0x3FE6A09E667F3BCC): the same bits without their FP64 instructions
+    const unsigned long long jflip = B.nJab ? 0x8000000000000000ull : 0ull;
+    auto xj = [jflip](double x) { return __longlong_as_double((long long)((unsigned long long)__double_as_longlong(x) ^ jflip)); };
+    const double x4 = (B.ia == B.ib && na == nbf) ? __longlong_as_double(0x3FE6A09E667F3BCCll) : 1.0;
     const int noa = P.no[B.ia], nob = P.no[B.ib], nog = P.no[B.ig], D = C.D;
     const int iid0 = P.orb_start[I], iig0 = P.orb_start[B.ig];
     const double *V = vp + B.vp_first;
@@ -128,7 +130,7 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
             if (z1 && z2) continue;
             double x2 = __dmul_rn(fa[nas], fb[nbs]);
             if (B.ia == B.ib) {
-                x2 = __dadd_rn(x2, __dmul_rn(__dmul_rn(xJab, fa[nbs]), fb[nas]));
+                x2 = __dadd_rn(x2, __dmul_rn(xj(fa[nbs]), fb[nas]));
                 if (nas == nbs) x2 = __ddiv_rn(x2, kSqr2);
             }
             if (x2 == 0.0) continue;
@@ -167,7 +169,7 @@ __global__ void k_poles(DevProblem P, const S2Block *blk, const long long *pole_
             for (int nbs = nst2; nbs < nob; ++nbs) {
                 double x2 = __dmul_rn(fa[nas], fb[nbs]);
                 if (B.ia == B.ib) {
-                    x2 = __dadd_rn(x2, __dmul_rn(__dmul_rn(xJab, fa[nbs]), fb[nas]));
+                    x2 = __dadd_rn(x2, __dmul_rn(xj(fa[nbs]), fb[nas]));
                     if (nas == nbs) x2 = __ddiv_rn(x2, kSqr2);
                 }
                 // Terms with a zero amplitude factor add an exact zero to x1, which starts
