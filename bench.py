@@ -42,8 +42,8 @@ CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2,
 # of that kernel at the current source (dram__bytes_read.sum 22.402816 MB +
 # dram__bytes_write.sum 8.712448 MB; lts__t_bytes.sum 1.810563 GB; issue active 32.3 %
 # of active cycles, barrier stalls 3.89 per issue).
-LANCZOS_TRAFFIC_BYTES = 31_115_264
-LANCZOS_L2_BYTES = 1_810_563_000
+LANCZOS_TRAFFIC_BYTES = 31_053_056
+LANCZOS_L2_BYTES = 1_810_338_000
 LANCZOS_ISSUE_ACTIVE = 0.323
 # GB300's nominal FP64 rate (no measured FP64 peak exists for this machine): the
 # denominator of the Dyson phase's FP64-class fraction.

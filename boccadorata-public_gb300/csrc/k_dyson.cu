@@ -570,6 +570,7 @@ constexpr int kTsThreads = 512;
 constexpr int kTsParts = 8;                   // threads per row of the symmetric product
 constexpr int kTsIt = kTsMax / 32;            // column entries per lane of warp 0
 static_assert(kTsMax % 32 == 0, "warp 0 holds a column in kTsIt entries per lane");
+static_assert(2 * kTsMax <= kTsThreads, "the R update keeps at least half the threads");
 
 __device__ inline double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -598,7 +599,6 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
     df *R = xs + n;                          // [D][n]
     __shared__ df s_col[2][2];               // alpha and |x_1:|^2 of a column, scaled, by parity
     __shared__ int s_nz[2], s_exp[2];        // the column has a reflector; e, by parity
-    __shared__ df s_al[2];                   // alpha unscaled (a column left as it is), by parity
     __shared__ df s_sc[2];                   // tau, s of the step
     __shared__ df s_q[kTsThreads / 32];      // per-warp partials of Q
     __shared__ df s_rx[8][2];                // R_d[b0+1:] . xs[1:], R_d[b0] before the update
@@ -641,7 +641,6 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
         if (lane == 0) {
             s_nz[par] = (s2.h != 0.0f || s2.l != 0.0f);
             s_exp[par] = e;
-            s_al[par] = al;
             s_col[par][0] = df{al.h * sg, al.l * sg};
             s_col[par][1] = df{(s2.h * sg) * sg, (s2.l * sg) * sg};
         }
@@ -734,7 +733,9 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             v[t] = vt;
             w[t] = dfm::fma(nK, vt, p);
         }
-        for (int u = tid; u < D * m; u += kTsThreads) {
+        // the R update on the warps that form no v and w
+        const int rb = (m + 31) & ~31;
+        for (int u = tid - rb; u >= 0 && u < D * m; u += kTsThreads - rb) {
             const int d = u / m, t = u - d * m;
             const df vt = (t == 0) ? df{1.0f, 0.0f} : dfm::mul(s, xs[t]);
             const df nc = dfm::neg(dfm::mul(tau, dfm::fma(s, s_rx[d][0], s_rx[d][1])));
@@ -759,14 +760,29 @@ __global__ void __launch_bounds__(kTsThreads) k_tridiag_small(const DyJob *jobs,
             for (int i1 = warp - 1; i1 < (m + 1) / 2; i1 += kTsThreads / 32 - 1) {
                 const int i2 = m - 1 - i1;
                 const int len = (i1 == i2) ? (i1 + 1) : (m + 1);
-                for (int u = lane; u < len; u += 32) {
-                    const int r = (u <= i1) ? i1 : i2, c = (u <= i1) ? u : u - i1 - 1;
-                    if (c == 0) continue;   // column k + 1: warp 0's
-                    df *a = A + (size_t)(b0 + r) * ld + b0 + c;
-                    const df t2 = dfm::fma(w[r], v[c], dfm::mul(v[r], w[c]));
-                    const df x = dfm::add(*a, dfm::neg(t2));
-                    *a = x;
-                    A[(size_t)(b0 + c) * ld + b0 + r] = x;   // the mirror, read by the next product
+                // two entries per pass, both read before either is written: the entries
+                // are distinct lower-triangle ones, so no write meets the other's reads
+                for (int u = lane; u < len; u += 64) {
+                    int r[2], c[2];
+                    df x[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int uu = u + 32 * h;
+                        r[h] = (uu <= i1) ? i1 : i2;
+                        c[h] = (uu <= i1) ? uu : uu - i1 - 1;
+                        if (uu < len && c[h] != 0) {   // column k + 1: warp 0's
+                            const df t2 = dfm::fma(w[r[h]], v[c[h]], dfm::mul(v[r[h]], w[c[h]]));
+                            x[h] = dfm::add(A[(size_t)(b0 + r[h]) * ld + b0 + c[h]], dfm::neg(t2));
+                        } else {
+                            c[h] = 0;
+                        }
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if (c[h] != 0) {
+                            A[(size_t)(b0 + r[h]) * ld + b0 + c[h]] = x[h];
+                            A[(size_t)(b0 + c[h]) * ld + b0 + r[h]] = x[h];   // the mirror, read by the next product
+                        }
                 }
             }
         }
@@ -800,8 +816,8 @@ size_t tridiag_smem_bytes(int nmax, int cluster) {
 }
 
 // Kernels launch_dyson starts for matrices of order up to nmax: deflate, assemble, the
-// small-matrix reduction (and the cluster one beyond kTsMax), then launch_eig's eight.
-int dyson_launch_count(int nmax) { return (nmax <= kTsMax ? 3 : 4) + 8; }
+// small-matrix reduction (and the cluster one beyond kTsMax), then launch_eig's nine.
+int dyson_launch_count(int nmax) { return (nmax <= kTsMax ? 3 : 4) + 9; }
 
 cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                          int nmax, int Dmax, int cluster, double *work, const long long *d_work_first, cudaStream_t st) {

@@ -18,8 +18,8 @@
 //             groups of tens to hundreds of zero-strength solutions in the Dyson
 //             spectra fall into different blocks and need nothing)
 //   k_post    x_k[0:D] = R y_k, Z_k = sum_d x_k[d]^2
-//   k_place   quasiparticle / quasihole split by E_F with both lists by descending W,
-//             Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
+//   k_place   quasiparticle / quasihole split by E_F with both lists by descending W
+//   k_koltun  Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594)
 #include <climits>
 #include "bd_common.cuh"
 #include "df64.cuh"
@@ -492,62 +492,76 @@ __global__ void __launch_bounds__(kIvThreads) k_invit_small(const DyJob *jobs, i
     for (int i = b0; i <= b1; ++i) Y[(size_t)i * n + k] = dfm::to_double(a.y(i));
 }
 
-// One CTA per position; the CTA of a cluster's first member (cluster of two or more,
-// inside one block) orthonormalises the members with two classical Gram-Schmidt
-// sweeps over the block's rows.
-__global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs, int njobs, const long long *row_first,
-                                                               long long total) {
-    const long long g = blockIdx.x;
-    if (g >= total) return;
-    const int lo = job_of(row_first, njobs, g);
-    const DyJob J = jobs[lo];
-    const int k0 = (int)(g - row_first[lo]), n = J.nc, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31,
-              warp = tid >> 5;
-    if (k0 >= n) return;
-    const int b0 = J.blk[k0], b1 = J.blk[n + k0];
-    if (b0 == b1) return;
-    __shared__ EigTol tl;
+// kOrthCtas CTAs per matrix.  Each takes 256 positions at a time, a thread per
+// position marks the first members of clusters (two or more members, inside one
+// block), then the CTA orthonormalises each marked cluster's members with two
+// classical Gram-Schmidt sweeps over the block's rows.  Clusters are disjoint sets of
+// columns, so the order the CTA takes them in changes nothing.
+constexpr int kOrthCtas = 8;
+
+__global__ void __launch_bounds__(kEigThreads) k_cluster_orth(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x / kOrthCtas;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int n = J.nc, NS = 2 + J.D, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ double cbuf[1024];
     __shared__ double red[kEigThreads / 32];
-    if (tid == 0) tl = eig_tol(J.tau[k0]);
-    __syncthreads();
+    __shared__ int s_first[kEigThreads], s_last[kEigThreads], s_nc;
     auto W = [&](int q) { return J.sol[(size_t)q * NS]; };
-    if (k0 > b0 && W(k0) - W(k0 - 1) <= tl.ortol) return;
-    int k1 = k0 + 1;
-    while (k1 <= b1 && W(k1) - W(k1 - 1) <= tl.ortol) ++k1;
-    if (k1 - k0 < 2) return;
     double *Y = J.A;   // y_p is column p: element (i, p) at i * n + p
-    for (int q = k0; q < k1; ++q) {
-        for (int sweep = 0; sweep < 2; ++sweep) {
-            // c_p = <y_p, y_q> for the earlier members, blocks of 1024: a warp per member
-            for (int p0 = k0; p0 < q; p0 += 1024) {
-                const int p1 = min(q, p0 + 1024);
-                for (int p = p0 + warp; p < p1; p += kEigThreads / 32) {
-                    double s = 0.0;
-                    for (int i = b0 + lane; i <= b1; i += 32) s += Y[(size_t)i * n + p] * Y[(size_t)i * n + q];
-                    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                    if (lane == 0) cbuf[p - p0] = s;
+    for (int base = (blockIdx.x % kOrthCtas) * kEigThreads; base < n; base += kOrthCtas * kEigThreads) {
+        __syncthreads();   // the previous pass's list is read
+        if (tid == 0) s_nc = 0;
+        __syncthreads();
+        if (base + tid < n) {
+            const int k0 = base + tid, b0 = J.blk[k0], b1 = J.blk[n + k0];
+            if (b0 != b1) {
+                const double ortol = eig_tol(J.tau[k0]).ortol;
+                if (!(k0 > b0 && W(k0) - W(k0 - 1) <= ortol) && k0 < b1 && W(k0 + 1) - W(k0) <= ortol) {
+                    int k1 = k0 + 2;
+                    while (k1 <= b1 && W(k1) - W(k1 - 1) <= ortol) ++k1;
+                    const int slot = atomicAdd(&s_nc, 1);
+                    s_first[slot] = k0;
+                    s_last[slot] = k1;
                 }
+            }
+        }
+        __syncthreads();
+        for (int c = 0; c < s_nc; ++c) {
+            const int k0 = s_first[c], k1 = s_last[c], b0 = J.blk[k0], b1 = J.blk[n + k0];
+            for (int q = k0; q < k1; ++q) {
+                for (int sweep = 0; sweep < 2; ++sweep) {
+                    // c_p = <y_p, y_q> for the earlier members, blocks of 1024: a warp per member
+                    for (int p0 = k0; p0 < q; p0 += 1024) {
+                        const int p1 = min(q, p0 + 1024);
+                        for (int p = p0 + warp; p < p1; p += kEigThreads / 32) {
+                            double s = 0.0;
+                            for (int i = b0 + lane; i <= b1; i += 32) s += Y[(size_t)i * n + p] * Y[(size_t)i * n + q];
+                            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                            if (lane == 0) cbuf[p - p0] = s;
+                        }
+                        __syncthreads();
+                        // y_q -= sum_p c_p y_p: a thread per row, running along the row's members
+                        for (int i = b0 + tid; i <= b1; i += kEigThreads) {
+                            double acc = 0.0;
+                            for (int p = p0; p < p1; ++p) acc += cbuf[p - p0] * Y[(size_t)i * n + p];
+                            Y[(size_t)i * n + q] -= acc;
+                        }
+                        __syncthreads();
+                    }
+                }
+                double s = 0.0;
+                for (int i = b0 + tid; i <= b1; i += kEigThreads) s += Y[(size_t)i * n + q] * Y[(size_t)i * n + q];
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) red[warp] = s;
                 __syncthreads();
-                // y_q -= sum_p c_p y_p: a thread per row, running along the row's members
-                for (int i = b0 + tid; i <= b1; i += kEigThreads) {
-                    double acc = 0.0;
-                    for (int p = p0; p < p1; ++p) acc += cbuf[p - p0] * Y[(size_t)i * n + p];
-                    Y[(size_t)i * n + q] -= acc;
-                }
+                double tot = 0.0;
+                for (int w = 0; w < kEigThreads / 32; ++w) tot += red[w];
+                const double inv = (tot > 0.0) ? 1.0 / sqrt(tot) : 0.0;
+                for (int i = b0 + tid; i <= b1; i += kEigThreads) Y[(size_t)i * n + q] *= inv;
                 __syncthreads();
             }
         }
-        double s = 0.0;
-        for (int i = b0 + tid; i <= b1; i += kEigThreads) s += Y[(size_t)i * n + q] * Y[(size_t)i * n + q];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) red[warp] = s;
-        __syncthreads();
-        double tot = 0.0;
-        for (int w = 0; w < kEigThreads / 32; ++w) tot += red[w];
-        const double inv = (tot > 0.0) ? 1.0 / sqrt(tot) : 0.0;
-        for (int i = b0 + tid; i <= b1; i += kEigThreads) Y[(size_t)i * n + q] *= inv;
-        __syncthreads();
     }
 }
 
@@ -589,100 +603,85 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
 }
 
 // Places the staged rows: quasiparticles (W > E_F) then quasiholes, each by
-// descending W (ties by position), and forms the Koltun partial sums.  One CTA per
-// matrix; the staged rows are block-major, so each finds its rank among all of them.
-__global__ void k_place(const DyJob *jobs, int njobs) {
-    const int jid = blockIdx.x;
+// descending W (ties by position).  kPlaceCtas CTAs per matrix; each thread takes up
+// to kPlacePer rows and finds each one's rank among all staged rows (the staged rows
+// are block-major, not sorted).  The energies are compared as order-preserving 64-bit
+// integer keys (negative values bit-inverted, others with the sign bit set): FP64
+// compares would issue on the FP64 pipe, 1/64 of the integer rate here.  The keys go
+// through shared memory kPlaceChunk at a time.
+constexpr int kPlaceCtas = 8, kPlacePer = 4, kPlaceChunk = 2048, kPlaceThreads = 256;
+
+__global__ void __launch_bounds__(kPlaceThreads) k_place(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x, tid = threadIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    const int n = J.n, D = J.D, NS = 2 + D;
+    const int n = J.n, D = J.D, NS = 2 + D, first = (int)blockIdx.y * kPlaceThreads;
+    if (first >= n) {   // the whole CTA; an empty matrix still reports its counts
+        if (n == 0 && blockIdx.y == 0 && tid == 0) { J.nq[0] = 0; J.nq[1] = 0; }
+        return;
+    }
     const double *st = J.R + (size_t)D * n;
-    __shared__ int nbelow;
-    if (threadIdx.x == 0) nbelow = 0;
-    __syncthreads();
-    int c = 0;
     const double ef = J.efp ? *J.efp : J.efermi;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) c += !(st[(size_t)k * NS] > ef);
-    atomicAdd(&nbelow, c);
-    __syncthreads();
-    const int nqh = nbelow, nqp = n - nbelow;
-    // ascending rank of every staged row (ties by position).  The energies are compared
-    // as order-preserving 64-bit integer keys (negative values bit-inverted, others with
-    // the sign bit set): FP64 compares would issue on the FP64 pipe, 1/64 of the
-    // integer rate here.  Up to kPlaceSort rows: a bitonic sort of (key, position) in
-    // shared memory gives every rank; beyond, each row counts the rows below it.
     auto key = [](double x) -> unsigned long long {
         const unsigned long long b = (unsigned long long)__double_as_longlong(x);
         return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
     };
-    auto put = [&](int k, int rank) {   // quasiparticles descending, then quasiholes descending
-        const int row = (rank >= nqh) ? (n - 1 - rank) : (nqp + (nqh - 1 - rank));
-        for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
-    };
-    constexpr int kPlaceSort = 2048;
-    __shared__ unsigned long long pkey[kPlaceSort];
-    __shared__ int pidx[kPlaceSort];
-    if (n <= kPlaceSort) {
-        int P = 32;
-        while (P < n) P <<= 1;
-        for (int t = threadIdx.x; t < P; t += blockDim.x) {
-            pkey[t] = (t < n) ? key(st[(size_t)t * NS]) : ~0ull;
-            pidx[t] = (t < n) ? t : INT_MAX;
+    __shared__ unsigned long long wbuf[kPlaceChunk];
+    __shared__ int nbelow;
+    if (tid == 0) nbelow = 0;
+    constexpr int span = kPlaceCtas * kPlaceThreads;
+    for (int g0 = first; g0 < n; g0 += kPlacePer * span) {
+        int r[kPlacePer];
+        unsigned long long w[kPlacePer];
+#pragma unroll
+        for (int u = 0; u < kPlacePer; ++u) {
+            const int k = g0 + tid + u * span;
+            r[u] = 0;
+            w[u] = key((k < n) ? st[(size_t)k * NS] : 0.0);
         }
+        int c = 0;
+        for (int q0 = 0; q0 < n; q0 += kPlaceChunk) {
+            const int qn = min(kPlaceChunk, n - q0);
+            __syncthreads();
+            for (int q = tid; q < qn; q += kPlaceThreads) {
+                const double x = st[(size_t)(q0 + q) * NS];
+                wbuf[q] = key(x);
+                c += !(x > ef);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < kPlacePer; ++u) {
+                const int k = g0 + tid + u * span;
+                if (k >= n) continue;
+                int c2 = 0;
+                for (int q = 0; q < qn; ++q) {
+                    const unsigned long long wq = wbuf[q];
+                    c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
+                }
+                r[u] += c2;
+            }
+        }
+        if (g0 == first) atomicAdd(&nbelow, c);
         __syncthreads();
-        for (int kk = 2; kk <= P; kk <<= 1)
-            for (int j = kk >> 1; j > 0; j >>= 1) {
-                for (int t = threadIdx.x; t < P; t += blockDim.x) {
-                    const int u = t ^ j;
-                    if (u <= t) continue;
-                    const unsigned long long ka = pkey[t], kb = pkey[u];
-                    const int ia = pidx[t], ib = pidx[u];
-                    const bool gt = (ka > kb) || (ka == kb && ia > ib);
-                    if (((t & kk) == 0) ? gt : !gt) { pkey[t] = kb; pkey[u] = ka; pidx[t] = ib; pidx[u] = ia; }
-                }
-                __syncthreads();
-            }
-        for (int r = threadIdx.x; r < n; r += blockDim.x) put(pidx[r], r);
-    } else {
-        // rows in tiles of eight per thread, compared against the energies staged in
-        // shared memory kPlaceSort at a time
-        constexpr int kPer = 8;
-        unsigned long long *wbuf = pkey;
-        const int tile = kPer * blockDim.x;
-        for (int k0 = 0; k0 < n; k0 += tile) {
-            int r[kPer];
-            unsigned long long w[kPer];
+        const int nqh = nbelow, nqp = n - nqh;
+        if (g0 == first && blockIdx.y == 0 && tid == 0) { J.nq[0] = nqp; J.nq[1] = nqh; }
 #pragma unroll
-            for (int u = 0; u < kPer; ++u) {
-                const int k = k0 + threadIdx.x + u * blockDim.x;
-                r[u] = 0;
-                w[u] = key((k < n) ? st[(size_t)k * NS] : 0.0);
-            }
-            for (int q0 = 0; q0 < n; q0 += kPlaceSort) {
-                const int qn = min(kPlaceSort, n - q0);
-                __syncthreads();
-                for (int q = threadIdx.x; q < qn; q += blockDim.x) wbuf[q] = key(st[(size_t)(q0 + q) * NS]);
-                __syncthreads();
-#pragma unroll
-                for (int u = 0; u < kPer; ++u) {
-                    const int k = k0 + threadIdx.x + u * blockDim.x;
-                    if (k >= n) continue;
-                    int c2 = 0;
-                    for (int q = 0; q < qn; ++q) {
-                        const unsigned long long wq = wbuf[q];
-                        c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
-                    }
-                    r[u] += c2;
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kPer; ++u) {
-                const int k = k0 + threadIdx.x + u * blockDim.x;
-                if (k < n) put(k, r[u]);
-            }
+        for (int u = 0; u < kPlacePer; ++u) {
+            const int k = g0 + tid + u * span;
+            if (k >= n) continue;
+            // quasiparticles descending, then quasiholes descending
+            const int row = (r[u] >= nqh) ? (n - 1 - r[u]) : (nqp + (nqh - 1 - r[u]));
+            for (int q = 0; q < NS; ++q) J.sol[(size_t)row * NS + q] = st[(size_t)k * NS + q];
         }
     }
-    __syncthreads();
+}
+
+// The Koltun partial sums over the placed quasiholes, one CTA per matrix.
+__global__ void __launch_bounds__(kPlaceThreads) k_koltun(const DyJob *jobs, int njobs) {
+    const int jid = blockIdx.x;
+    if (jid >= njobs) return;
+    const DyJob J = jobs[jid];
+    const int D = J.D, NS = 2 + D, nqp = J.nq[0], nqh = J.nq[1];
     // Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594): each thread
     // takes quasiholes ne = tid, tid + blockDim, ... into its own three buckets by |x|^2
     // (> 0.01, > 1e-5, the rest); the partials meet in a fixed order, so the sums are
@@ -710,7 +709,6 @@ __global__ void k_place(const DyJob *jobs, int njobs) {
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        J.nq[0] = nqp; J.nq[1] = nqh;
         double t[9];
         for (int q = 0; q < 9; ++q) {
             t[q] = 0.0;
@@ -738,9 +736,10 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
         if (e != cudaSuccess) return e;
         k_invit_small<<<dim3(njobs, (kTsMax + kIvThreads - 1) / kIvThreads), kIvThreads, smem, st>>>(d_jobs, njobs);
     }
-    k_cluster_orth<<<(unsigned)total_rows, kEigThreads, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
+    k_cluster_orth<<<(unsigned)(njobs * kOrthCtas), kEigThreads, 0, st>>>(d_jobs, njobs);
     k_post<<<(unsigned)((total_rows * 4 + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
-    k_place<<<njobs, 256, 0, st>>>(d_jobs, njobs);
+    k_place<<<dim3(njobs, kPlaceCtas), kPlaceThreads, 0, st>>>(d_jobs, njobs);
+    k_koltun<<<njobs, kPlaceThreads, 0, st>>>(d_jobs, njobs);
     return cudaGetLastError();
 }
 
