@@ -611,7 +611,10 @@ __global__ void k_post(const DyJob *jobs, int njobs, const long long *row_first,
 // through shared memory kPlaceChunk at a time.
 constexpr int kPlaceCtas = 8, kPlacePer = 4, kPlaceChunk = 2048, kPlaceThreads = 256;
 
-__global__ void __launch_bounds__(kPlaceThreads) k_place(const DyJob *jobs, int njobs) {
+constexpr int kKtVirt = 256;   // k_koltun's virtual threads
+
+__global__ void __launch_bounds__(kPlaceThreads) k_place(const DyJob *jobs, int njobs, double *work,
+                                                         const long long *work_first) {
     const int jid = blockIdx.x, tid = threadIdx.x;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
@@ -653,18 +656,22 @@ __global__ void __launch_bounds__(kPlaceThreads) k_place(const DyJob *jobs, int 
             for (int u = 0; u < kPlacePer; ++u) {
                 const int k = g0 + tid + u * span;
                 if (k >= n) continue;
+                // rows before k in this chunk count when not above it, the rest when below
+                const int split = min(max(k - q0, 0), qn);
                 int c2 = 0;
-                for (int q = 0; q < qn; ++q) {
-                    const unsigned long long wq = wbuf[q];
-                    c2 += (wq < w[u]) || (wq == w[u] && q0 + q < k);
-                }
+                for (int q = 0; q < split; ++q) c2 += (wbuf[q] <= w[u]);
+                for (int q = split; q < qn; ++q) c2 += (wbuf[q] < w[u]);
                 r[u] += c2;
             }
         }
         if (g0 == first) atomicAdd(&nbelow, c);
         __syncthreads();
         const int nqh = nbelow, nqp = n - nqh;
-        if (g0 == first && blockIdx.y == 0 && tid == 0) { J.nq[0] = nqp; J.nq[1] = nqh; }
+        if (g0 == first && blockIdx.y == 0 && tid == 0) {
+            J.nq[0] = nqp; J.nq[1] = nqh;
+            if (nqh > kKtVirt)   // k_koltun's ticket, behind its partials in the work area
+                *reinterpret_cast<unsigned *>(work + work_first[jid] + kPlaceCtas * 9) = 0u;
+        }
 #pragma unroll
         for (int u = 0; u < kPlacePer; ++u) {
             const int k = g0 + tid + u * span;
@@ -676,48 +683,110 @@ __global__ void __launch_bounds__(kPlaceThreads) k_place(const DyJob *jobs, int 
     }
 }
 
-// The Koltun partial sums over the placed quasiholes, one CTA per matrix.
-__global__ void __launch_bounds__(kPlaceThreads) k_koltun(const DyJob *jobs, int njobs) {
-    const int jid = blockIdx.x;
+// The Koltun partial sums over the placed quasiholes (Calc_En,
+// source/BcDor-DysonMatrix.cpp:542-594).  Virtual thread vt = 0..255 takes quasiholes
+// ne = vt, vt + 256, ... in that order into its own three buckets by |x|^2 (> 0.01,
+// > 1e-5, the rest); the 32 virtual threads of a virtual warp meet in a shuffle tree and
+// the eight virtual warps in order, so the sums are deterministic (the reference adds
+// the rows one by one, ne from nqh - 1 down).  Up to 256 quasiholes one CTA runs the
+// virtual threads as its own threads.  Beyond, CTA y of the matrix's kPlaceCtas is
+// virtual warp y: its eight warps form the rows' |x|^2 and x^T S1 x (the FP64 work)
+// side by side, its first warp adds them up in each virtual thread's order, and the
+// eight partials meet in the matrix's work area, summed by the CTA that finishes last.
+static_assert(kPlaceCtas * 32 == kKtVirt && kPlaceThreads == kKtVirt, "one CTA per virtual warp");
+
+__device__ inline void koltun_row(const DyJob &J, const double *x, double &x1, double &x2) {
+    const int D = J.D;
+    x1 = 0.0;
+    x2 = 0.0;
+    for (int r = 0; r < D; ++r) {
+        x1 += x[r] * x[r];
+        for (int cc = 0; cc < D; ++cc) x2 += J.sig1b[r * D + cc] * x[r] * x[cc];
+    }
+}
+
+__device__ inline void koltun_add(double *acc, double x1, double x2, double w) {
+    const int b = (x1 > 0.01) ? 0 : (x1 > 1.e-5) ? 1 : 2;
+    acc[b] += x2; acc[3 + b] += x1 * w; acc[6 + b] += x1;
+}
+
+__device__ inline void koltun_store(const DyJob &J, const double *t) {
+    const double xj = (double)J.j2 + 1.0;
+    J.koltun[0] = (t[0] + t[1] + t[2]) * xj;
+    J.koltun[1] = (t[3] + t[4] + t[5]) * xj;
+    J.koltun[2] = (t[6] + t[7] + t[8]) * xj;
+}
+
+__global__ void __launch_bounds__(kPlaceThreads) k_koltun(const DyJob *jobs, int njobs, double *work,
+                                                          const long long *work_first) {
+    const int jid = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (jid >= njobs) return;
     const DyJob J = jobs[jid];
-    const int D = J.D, NS = 2 + D, nqp = J.nq[0], nqh = J.nq[1];
-    // Koltun partial sums (Calc_En, source/BcDor-DysonMatrix.cpp:542-594): each thread
-    // takes quasiholes ne = tid, tid + blockDim, ... into its own three buckets by |x|^2
-    // (> 0.01, > 1e-5, the rest); the partials meet in a fixed order, so the sums are
-    // deterministic (the reference adds the rows one by one, ne from nqh - 1 down)
+    const int NS = 2 + J.D, nqp = J.nq[0], nqh = J.nq[1];
+    const bool multi = nqh > kKtVirt;
+    if (!multi && blockIdx.y != 0) return;
     double acc[9];
 #pragma unroll
     for (int q = 0; q < 9; ++q) acc[q] = 0.0;
-    for (int ne = threadIdx.x; ne < nqh; ne += blockDim.x) {
-        const double *p1 = J.sol + (size_t)(nqp + ne) * NS, *x = p1 + 2;
-        double x1 = 0.0, x2 = 0.0;
-        for (int r = 0; r < D; ++r) {
-            x1 += x[r] * x[r];
-            for (int cc = 0; cc < D; ++cc) x2 += J.sig1b[r * D + cc] * x[r] * x[cc];
+    if (!multi) {
+        for (int ne = tid; ne < nqh; ne += kKtVirt) {
+            const double *p1 = J.sol + (size_t)(nqp + ne) * NS;
+            double x1, x2;
+            koltun_row(J, p1 + 2, x1, x2);
+            koltun_add(acc, x1, x2, p1[0]);
         }
-        const int b = (x1 > 0.01) ? 0 : (x1 > 1.e-5) ? 1 : 2;
-        acc[b] += x2; acc[3 + b] += x1 * p1[0]; acc[6 + b] += x1;
+        __shared__ double kred[9][32];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            double v = acc[q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) kred[q][warp] = v;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double t[9];
+            for (int q = 0; q < 9; ++q) {
+                t[q] = 0.0;
+                for (int w = 0; w < kKtVirt / 32; ++w) t[q] += kred[q][w];
+            }
+            koltun_store(J, t);
+        }
+        return;
     }
-    __shared__ double kred[9][32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ double s_x1[8][32], s_x2[8][32];
+    const int vt = (int)blockIdx.y * 32 + lane;         // warp 0's lane: its virtual thread
+    const int nj = (nqh + kKtVirt - 1) / kKtVirt;       // rows of a virtual thread, at most
+    for (int j0 = 0; j0 < nj; j0 += 8) {
+        const int ne = vt + kKtVirt * (j0 + warp);      // warp w: row j0 + w of each virtual thread
+        if (ne < nqh) koltun_row(J, J.sol + (size_t)(nqp + ne) * NS + 2, s_x1[warp][lane], s_x2[warp][lane]);
+        __syncthreads();
+        if (warp == 0)
+            for (int h = 0; h < 8; ++h) {
+                const int nh = vt + kKtVirt * (j0 + h);
+                if (nh < nqh) koltun_add(acc, s_x1[h][lane], s_x2[h][lane], J.sol[(size_t)(nqp + nh) * NS]);
+            }
+        __syncthreads();
+    }
+    if (warp != 0) return;
+    double *part = work + work_first[jid];              // [kPlaceCtas][9], then the ticket
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
         double v = acc[q];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) kred[q][warp] = v;
+        if (lane == 0) part[blockIdx.y * 9 + q] = v;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t[9];
-        for (int q = 0; q < 9; ++q) {
-            t[q] = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t[q] += kred[q][w];
+    if (lane == 0) {
+        __threadfence();
+        unsigned *ticket = reinterpret_cast<unsigned *>(part + kPlaceCtas * 9);
+        if (atomicAdd(ticket, 1u) == kPlaceCtas - 1) {   // every other partial is visible
+            __threadfence();
+            double t[9];
+            for (int q = 0; q < 9; ++q) {
+                t[q] = 0.0;
+                for (int w = 0; w < kPlaceCtas; ++w) t[q] += __ldcg(part + w * 9 + q);
+            }
+            koltun_store(J, t);
         }
-        const double xj = (double)J.j2 + 1.0;
-        J.koltun[0] = (t[0] + t[1] + t[2]) * xj;
-        J.koltun[1] = (t[3] + t[4] + t[5]) * xj;
-        J.koltun[2] = (t[6] + t[7] + t[8]) * xj;
     }
 }
 
@@ -738,8 +807,8 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
     }
     k_cluster_orth<<<(unsigned)(njobs * kOrthCtas), kEigThreads, 0, st>>>(d_jobs, njobs);
     k_post<<<(unsigned)((total_rows * 4 + 127) / 128), 128, 0, st>>>(d_jobs, njobs, d_row_first, total_rows);
-    k_place<<<dim3(njobs, kPlaceCtas), kPlaceThreads, 0, st>>>(d_jobs, njobs);
-    k_koltun<<<njobs, kPlaceThreads, 0, st>>>(d_jobs, njobs);
+    k_place<<<dim3(njobs, kPlaceCtas), kPlaceThreads, 0, st>>>(d_jobs, njobs, work, d_work_first);
+    k_koltun<<<dim3(njobs, kPlaceCtas), kPlaceThreads, 0, st>>>(d_jobs, njobs, work, d_work_first);
     return cudaGetLastError();
 }
 
