@@ -1658,6 +1658,7 @@ int bd_create(bd_ctx **out, int device) {
         bd_destroy(ctx);
         return BD_ERR_CUDA;
     }
+    tridiag_fit_warm();   // attribute queries now, not inside a later stream capture
     *out = ctx;
     return BD_OK;
 }
@@ -1944,6 +1945,14 @@ int bd_lanczos_reduce(bd_ctx *ctx, int ish, int n_pvt, double *pivots, int *n_it
     return BD_OK;
 }
 
+// A Dyson job's device status as the call's error.
+static int dyson_status_error(bd_ctx *ctx, int ish, int st) {
+    if (st == kDyStatCapacity)
+        return fail(ctx, BD_ERR_CAPACITY,
+                    "channel %d: the deflated Dyson matrix is larger than the cluster reduction's shared memory holds", ish);
+    return fail(ctx, BD_ERR_NUMERIC, "channel %d: the eigensolver did not converge", ish);
+}
+
 int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_hf, double e_fermi, double *sol_qp,
                    int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh, double *koltun) {
     int rc = check_chan(ctx, ish);
@@ -1977,7 +1986,7 @@ int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_
     CU(cudaStreamSynchronize(ctx->st));
     if (st) {
         CU(cudaMemsetAsync(ctx->d_dystat + ish, 0, sizeof(int), ctx->st));
-        return fail(ctx, BD_ERR_NUMERIC, "channel %d: the eigensolver did not converge", ish);
+        return dyson_status_error(ctx, ish, st);
     }
     if (n_qp) *n_qp = nq[0];
     if (n_qh) *n_qh = nq[1];
@@ -2050,18 +2059,24 @@ int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_row
     CU(cudaMemcpyAsync(drf, zero, sizeof zero, cudaMemcpyHostToDevice, ctx->st));
     CU(launch_dyson(dj, 1, drf, n, n, D, dy_cluster_for(ctx, 1), dwork, dwf, ctx->st));
     ctx->launches += dyson_launch_count(n);
-    int nq[2] = {0, 0};
+    int nq[2] = {0, 0}, dst = 0;
     double kol[3];
     CU(cudaMemcpyAsync(nq, ctx->d_dynq + 2 * ish, sizeof nq, cudaMemcpyDeviceToHost, ctx->st));
     CU(cudaMemcpyAsync(kol, ctx->d_dykol + 3 * ish, sizeof kol, cudaMemcpyDeviceToHost, ctx->st));
+    CU(cudaMemcpyAsync(&dst, ctx->d_dystat + ish, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CU(cudaStreamSynchronize(ctx->st));
-    if (n_qp) *n_qp = nq[0];
-    if (n_qh) *n_qh = nq[1];
-    if (koltun) std::memcpy(koltun, kol, sizeof kol);
     rc = BD_OK;
-    if ((sol_qp && cap_qp < nq[0]) || (sol_qh && cap_qh < nq[1]))
+    if (dst) {
+        CU(cudaMemsetAsync(ctx->d_dystat + ish, 0, sizeof(int), ctx->st));
+        rc = dyson_status_error(ctx, ish, dst);
+    } else {
+        if (n_qp) *n_qp = nq[0];
+        if (n_qh) *n_qh = nq[1];
+        if (koltun) std::memcpy(koltun, kol, sizeof kol);
+    }
+    if (!rc && ((sol_qp && cap_qp < nq[0]) || (sol_qh && cap_qh < nq[1])))
         rc = fail(ctx, BD_ERR_CAPACITY, "solution buffers too small (%d, %d needed)", nq[0], nq[1]);
-    else {
+    else if (!rc) {
         if (sol_qp && nq[0]) CU(cudaMemcpyAsync(sol_qp, dsol, sizeof(double) * (size_t)nq[0] * (2 + D), cudaMemcpyDeviceToHost, ctx->st));
         if (sol_qh && nq[1])
             CU(cudaMemcpyAsync(sol_qh, dsol + (size_t)nq[0] * (2 + D), sizeof(double) * (size_t)nq[1] * (2 + D),
@@ -2292,7 +2307,7 @@ int bd_sync(bd_ctx *ctx) {
             if (st[I]) {
                 ctx->results_valid = false;
                 CU(cudaMemset(ctx->d_dystat, 0, sizeof(int) * ctx->nsubsh));
-                return fail(ctx, BD_ERR_NUMERIC, "channel %d: the eigensolver did not converge", I);
+                return dyson_status_error(ctx, I, st[I]);
             }
     }
     return BD_OK;

@@ -87,5 +87,10 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
 cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_first, long long total_rows,
                        double *work, const long long *d_work_first, cudaStream_t st);
 size_t tridiag_smem_bytes(int nmax, int cluster);
+int tridiag_fit_order(int cluster);   // the largest order the cluster reduction's layout holds
+void tridiag_fit_warm();              // fills tridiag_fit_order's cache (cluster sizes 1..16)
+// DyJob::stat values: the eigensolver did not converge; the deflated matrix is larger
+// than the cluster reduction's shared-memory layout holds (nothing solved)
+constexpr int kDyStatNumeric = 1, kDyStatCapacity = 2;
 
 }  // namespace bd

@@ -12,6 +12,7 @@
 //   K4b..K5 (k_eig.cu)    eigenvalues and the first D eigenvector components of T,
 //                         back-transformed, split by E_F, Koltun sums.
 #include <algorithm>
+#include <atomic>
 #include <cooperative_groups.h>
 #include "bd_common.cuh"
 #include "bd_kernels.h"
@@ -227,6 +228,16 @@ __device__ inline double block_sum(double v, double *scratch) {
 //
 // Shared layout (doubles): v[nmax] | p[nmax] | pc[nmax] | pt[npriv][nmax] |
 // pr[nmax / CL + 1] | scratch[32]
+// A deflated matrix of order beyond the launch's shared-memory layout (sized for at
+// most the largest order that layout can hold): the cluster leaves together before its
+// first barrier, the job reports kDyStatCapacity, and a zero tridiagonal with no
+// reflectors lets the eigen kernels after it finish on it at once.
+__device__ inline void tridiag_beyond_layout(const DyJob &J, int rank) {
+    if (rank != 0) return;
+    for (int i = threadIdx.x; i < J.nc; i += blockDim.x) { J.d[i] = 0.0; J.e[i] = 0.0; J.tau[i] = 0.0; }
+    if (threadIdx.x == 0) *J.stat = kDyStatCapacity;
+}
+
 __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int njobs, int nmax, int npriv) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
@@ -236,6 +247,7 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag(const DyJob *jobs, int n
     const DyJob J = jobs[jid];
     const int n = J.nc;   // order after deflation
     if (n <= kTsMax) return;   // k_tridiag_small's (the whole cluster leaves together)
+    if (n > nmax) { tridiag_beyond_layout(J, rank); return; }
     extern __shared__ double sm[];
     double *v = sm;
     double *p = v + nmax;
@@ -415,6 +427,7 @@ __global__ void __launch_bounds__(kTdThreads) k_tridiag_df(const DyJob *jobs, in
     const DyJob J = jobs[jid];
     const int n = J.nc;
     if (n <= kTsMax) return;   // k_tridiag_small's (the whole cluster leaves together)
+    if (n > nmax) { tridiag_beyond_layout(J, rank); return; }
     extern __shared__ double sm[];
     df *v = reinterpret_cast<df *>(sm);
     df *p = v + nmax;
@@ -815,6 +828,39 @@ size_t tridiag_smem_bytes(int nmax, int cluster) {
     return sizeof(double) * ((size_t)(3 + tridiag_npriv(nmax, cluster)) * nmax + (size_t)(nmax / cluster + 1) + 32);
 }
 
+// The largest order whose layout fits the dynamic shared memory a CTA may opt into.
+// Up to the orders that leave room for two partial vectors the layout stays within
+// 200 KB; beyond, it grows with the order, so the orders that fit are a prefix.
+// Cached per cluster size (bd_create fills the cache, so no attribute query falls inside
+// a stream capture); the GPUs a process drives are of one kind.
+static std::atomic<int> g_fit_order[17];
+
+int tridiag_fit_order(int cluster) {
+    const bool cached = cluster >= 1 && cluster <= 16;
+    if (cached) {
+        const int v = g_fit_order[cluster].load(std::memory_order_relaxed);
+        if (v) return v;
+    }
+    int dev = 0, optin = 0;
+    cudaFuncAttributes a{}, b{};
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&a, k_tridiag) != cudaSuccess || cudaFuncGetAttributes(&b, k_tridiag_df) != cudaSuccess)
+        return kTsMax + 1;   // the launch that follows reports the error
+    const size_t limit = (size_t)optin - std::max(a.sharedSizeBytes, b.sharedSizeBytes);
+    int lo = kTsMax + 1, hi = 1 << 22;
+    while (lo < hi) {
+        const int mid = lo + (hi - lo + 1) / 2;
+        if (tridiag_smem_bytes(mid, cluster) <= limit) lo = mid; else hi = mid - 1;
+    }
+    if (cached) g_fit_order[cluster].store(lo, std::memory_order_relaxed);
+    return lo;
+}
+
+void tridiag_fit_warm() {
+    for (int c = 1; c <= 16; c <<= 1) tridiag_fit_order(c);
+}
+
 // Kernels launch_dyson starts for matrices of order up to nmax: deflate, assemble, the
 // small-matrix reduction (and the cluster one beyond kTsMax), then launch_eig's nine.
 int dyson_launch_count(int nmax) { return (nmax <= kTsMax ? 3 : 4) + 9; }
@@ -834,6 +880,9 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (nmax <= kTsMax) return launch_eig(d_jobs, njobs, d_row_first, total_rows, work, d_work_first, st);
+    // the full orders bound the deflated ones; the layout is sized for at most the
+    // largest order shared memory holds, and larger deflated orders report it
+    nmax = std::min(nmax, tridiag_fit_order(cluster));
     size_t smem = tridiag_smem_bytes(nmax, cluster);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(njobs * cluster, 1, 1);

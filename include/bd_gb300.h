@@ -160,7 +160,10 @@ int bd_dyson_solve(bd_ctx *ctx, int ish, const double *sig1b, const double *sig_
  * Wide_self_energy_t::load_SelfEn_bin, the ExtSE path of source/BcDor-Main.cpp:350-356).
  * Rows have nden + D doubles: nden = 2 for a plain Sigma(2) [E, *, M_0 ..], or
  * n_pvt + 1 for Lanczos rows [alpha, beta, g_0 .., m_0 ..] with their i_piv array
- * (ipiv_* = NULL marks plain rows).  Outputs as bd_dyson_solve. */
+ * (ipiv_* = NULL marks plain rows).  Outputs as bd_dyson_solve.  Rows with no coupling
+ * leave the matrix first; a remaining (deflated) order above what the cluster
+ * reduction's shared memory holds (about 7 000 on GB300) gives BD_ERR_CAPACITY, as it
+ * does in bd_dyson_solve and bd_sync. */
 int bd_dyson_rows(bd_ctx *ctx, int ish, int nden, int n_fw, const double *fw_rows, const int *ipiv_fw,
                   int n_bk, const double *bk_rows, const int *ipiv_bk, const double *sig1b, const double *sig_hf,
                   double e_fermi, double *sol_qp, int cap_qp, int *n_qp, double *sol_qh, int cap_qh, int *n_qh,

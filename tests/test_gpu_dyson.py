@@ -123,3 +123,72 @@ def test_dressed_orders_near_1000_against_lapack(bdmod, problems, oracle):
         np.testing.assert_allclose(got["koltun"], ref["koltun"], rtol=1e-7, atol=1e-9)
     assert max(orders) > 800, orders
     ctx.close()
+
+
+def test_dyson_rows_beyond_eight_thousand_deflated_poles(bdmod, problems, oracle):
+    """Plain Sigma(2) rows of one channel with 9 000 uncoupled poles appended (every M
+    zero, distinct energies above the forward and below the backward poles): the
+    uncoupled poles deflate, so the compact eigenproblem is the oracle's, while the
+    placement ranks more than 8 192 rows (k_place's several row groups) and the Koltun
+    sums run over more than 256 quasiholes (k_koltun's eight CTAs).  Every appended pole
+    comes back once as [E, 0, 0 ..], both lists descend, the rest and the Koltun sums
+    are the oracle's."""
+    p = problems(4, 20.0, 0, 20)
+    orc = oracle(4, 20.0, 0, 20)
+    ctx = bdmod.Context().upload(p)
+    ish = 0
+    o2 = orc.run_channel(ish, True, passes=2)
+    fw, bk = orc.sigma2(ish)
+    full = orc.dyson(ish, o2["sig_1b"], o2["sig_hf"], 2, fw, bk)
+    D = fw.shape[1] - 2
+    rng = np.random.default_rng(7)
+    nfx, nbx = 4000, 5000
+    efx = fw[:, 0].max() + 1.0 + np.sort(rng.uniform(0.0, 300.0, nfx))
+    ebx = bk[:, 0].min() - 1.0 - np.sort(rng.uniform(0.0, 300.0, nbx))
+    assert len(np.unique(efx)) == nfx and len(np.unique(ebx)) == nbx
+    fwx = np.zeros((nfx, 2 + D)); fwx[:, 0] = efx
+    bkx = np.zeros((nbx, 2 + D)); bkx[:, 0] = ebx
+    big_fw, big_bk = np.vstack([fw, fwx[::-1]]), np.vstack([bk, bkx[rng.permutation(nbx)]])
+    assert D + len(big_fw) + len(big_bk) > 8192
+    r = ctx.dyson_rows(ish, 2, big_fw, big_bk, None, None, o2["sig_1b"], o2["sig_hf"])
+    assert len(r["qp"]) == len(full["qp"]) + nfx and len(r["qh"]) == len(full["qh"]) + nbx
+    assert len(r["qh"]) > 256
+    for tag, extra in (("qp", efx), ("qh", ebx)):
+        got = r[tag]
+        assert np.all(np.diff(got[:, 0]) <= 0), tag            # descending W
+        hit = np.isin(got[:, 0], extra)
+        assert hit.sum() == len(extra), tag                     # each appended pole once
+        assert np.all(got[hit, 1:] == 0.0), tag                 # with Z = 0 and x = 0
+        e, z = strong_diffs(full[tag], got[~hit])
+        assert e < 1e-10 and z < 1e-9, (tag, e, z)
+    np.testing.assert_allclose(r["koltun"], full["koltun"], rtol=1e-10, atol=1e-10)
+    ctx.close()
+
+
+def test_dyson_rows_beyond_the_cluster_layout_report_capacity(bdmod, problems, oracle):
+    """A deflated Dyson matrix larger than the cluster reduction's shared-memory layout
+    (the channel's plain Sigma(2) rows thirty times over, energies spread apart, so
+    about 9 000 coupled poles): BD_ERR_CAPACITY with a message, and the context then
+    solves the channel's own rows as the oracle does."""
+    p = problems(4, 20.0, 0, 20)
+    orc = oracle(4, 20.0, 0, 20)
+    ctx = bdmod.Context().upload(p)
+    ish = 0
+    o2 = orc.run_channel(ish, True, passes=2)
+    fw, bk = orc.sigma2(ish)
+    reps = []
+    for q in range(30):
+        r = fw.copy()
+        r[:, 0] += 1e-3 * q
+        reps.append(r)
+    big_fw = np.vstack(reps)
+    with pytest.raises(bdmod.BDError) as ei:
+        ctx.dyson_rows(ish, 2, big_fw, bk, None, None, o2["sig_1b"], o2["sig_hf"])
+    assert ei.value.code == bdmod.BD_ERR_CAPACITY and "shared memory" in str(ei.value)
+    full = orc.dyson(ish, o2["sig_1b"], o2["sig_hf"], 2, fw, bk)
+    r2 = ctx.dyson_rows(ish, 2, fw, bk, None, None, o2["sig_1b"], o2["sig_hf"])
+    for tag in ("qp", "qh"):
+        e, z = strong_diffs(full[tag], r2[tag])
+        assert e < 1e-10 and z < 1e-9, (tag, e, z)
+    np.testing.assert_allclose(r2["koltun"], full["koltun"], rtol=1e-10, atol=1e-10)
+    ctx.close()
