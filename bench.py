@@ -42,8 +42,8 @@ CPU_SAMPLE = [20, 16, 13, 9, 4, 0]          # neutron channels with D = 1, 2, 2,
 # of that kernel at the current source (dram__bytes_read.sum 22.402816 MB +
 # dram__bytes_write.sum 8.712448 MB; lts__t_bytes.sum 1.810563 GB; issue active 32.3 %
 # of active cycles, barrier stalls 3.89 per issue).
-LANCZOS_TRAFFIC_BYTES = 31_930_880
-LANCZOS_L2_BYTES = 1_812_559_000
+LANCZOS_TRAFFIC_BYTES = 31_193_600
+LANCZOS_L2_BYTES = 1_811_236_000
 LANCZOS_ISSUE_ACTIVE = 0.323
 # GB300's nominal FP64 rate (no measured FP64 peak exists for this machine): the
 # denominator of the Dyson phase's FP64-class fraction.
@@ -601,7 +601,7 @@ def gpu_arm(args):
             "traffic": LANCZOS_TRAFFIC_BYTES, "algorithmic_bytes": alg, "kernel_ms": lz_mean,
             "lanczos_rows": int(sum(c[1] for c in chains)), "lanczos_vectors_built": int(sum(stored)),
             "l2_bytes": LANCZOS_L2_BYTES, "issue_active": LANCZOS_ISSUE_ACTIVE,
-            "note": "the built basis stays in L2 (traffic is 1.2 % of the algorithmic bytes): the launch is "
+            "note": "the built basis stays in L2 (traffic is 1.1 % of the algorithmic bytes): the launch is "
                     "bound by the longest chain's step latency, so the HBM fraction is nominal"}
     # The Dyson phase against FP64: Householder (4/3 n^3) and the first D rows of Q
     # (2 n^2 D) over the deflated orders n = D + the chain's built rows (the deflated
