@@ -73,6 +73,8 @@ def parse():
                     help="the batched many-instance run (independent problems, iterated); prints its own line")
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--iterations", type=int, default=10)
+    ap.add_argument("--concurrent", type=int, default=3,
+                    help="--many: problems run side by side, each on its own context and host thread")
     return ap.parse_args()
 
 
@@ -672,8 +674,10 @@ def many_problems(args):
     and side: the truncation that keeps the dressed pole spaces of N_max = 10 inside
     minutes), Sigma(2) rebuilt from it.  Every step replays the context's captured graph;
     from the second update on the propagator is updated on the device when the fragment
-    counts stay.  Problem generation (host numpy) is outside the timed region; the upload
-    of each problem is inside it.
+    counts stay.  Problems go in batches of `concurrent` (default 3), side by side, each
+    on its own context and host thread (one chain leaves most of the GPU idle); each form
+    times its batches.  Problem generation (host numpy) is outside the timed region; the
+    upload of each problem is inside it.
 
     Accuracy against FP64: the first iteration (both forms on the same input) measures
     the mixed form's precision; the last iteration compares two trajectories, and the
@@ -690,49 +694,74 @@ def many_problems(args):
     times = {"mixed": [], "fp64": []}
     acc = {k: ([], [], []) for k in ("first_mixed_vs_fp64", "last_mixed_vs_fp64", "last_fp64_vs_fp64_cl16")}
     device_updates, sizes = 0, []
-    for i in range(args.problems):
-        seed = 100 + i
-        r = np.random.default_rng(seed)
-        nmax = int(r.choice([4, 6, 8, 10]))
-        hw = float(r.uniform(10.0, 30.0))
-        sigma = float(r.uniform(1.0, 3.0))
-        prob = synth.make_problem(nmax, hw, seed, n_itr, sigma)
-        res = {}
+    import threading
+    nconc = max(1, args.concurrent)
+
+    def solve(prob, mixed, cl, out, j):
+        """One problem in one form on its own context: upload, every iteration."""
+        ctx = bd.Context(local).upload(prob)
+        if cl != 8:
+            ctx.set_tuning(lz_cluster=cl)
+        dev_ms, first, upd = 0.0, None, 0
+        for it in range(args.iterations):
+            ctx.run_all(lanczos=True, mixed=mixed, graph=True)
+            dev_ms += ctx.timings()["total"]
+            if it == 0:
+                first = (ctx.results_all(), ctx.koltun_all())
+            if it + 1 < args.iterations:
+                ctx.dressed_propagator(z_cut, max_frag)
+                upd += int(mixed and ctx.dressed_on_device())
+        out[j] = (first, (ctx.results_all(), ctx.koltun_all()), dev_ms, upd)
+        ctx.close()
+
+    for b0 in range(0, args.problems, nconc):
+        batch = []
+        for i in range(b0, min(b0 + nconc, args.problems)):
+            seed = 100 + i
+            r = np.random.default_rng(seed)
+            nmax = int(r.choice([4, 6, 8, 10]))
+            hw = float(r.uniform(10.0, 30.0))
+            sigma = float(r.uniform(1.0, 3.0))
+            batch.append((i, seed, nmax, synth.make_problem(nmax, hw, seed, n_itr, sigma)))
+        res = [dict() for _ in batch]
         for form, mixed, cl in (("fp64", False, 8), ("mixed", True, 8), ("fp64_cl16", False, 16)):
+            # the batch's problems side by side, each on its own context and host thread
+            out, errs = [None] * len(batch), []
+
+            def run(j):
+                try:
+                    solve(batch[j][3], mixed, cl, out, j)
+                except Exception as ex:
+                    errs.append(repr(ex))
             t0 = time.perf_counter()
-            ctx = bd.Context(local).upload(prob)
-            if cl != 8:
-                ctx.set_tuning(lz_cluster=cl)
-            dev_ms = 0.0
-            first = None
-            for it in range(args.iterations):
-                ctx.run_all(lanczos=True, mixed=mixed, graph=True)
-                dev_ms += ctx.timings()["total"]
-                if it == 0:
-                    first = (ctx.results_all(), ctx.koltun_all())
-                if it + 1 < args.iterations:
-                    ctx.dressed_propagator(z_cut, max_frag)
-                    if mixed:
-                        device_updates += int(ctx.dressed_on_device())
-            last = (ctx.results_all(), ctx.koltun_all())
-            ctx.close()
+            ths = [threading.Thread(target=run, args=(j,)) for j in range(len(batch))]
+            for t in ths:
+                t.start()
+            for t in ths:
+                t.join()
+            wall = time.perf_counter() - t0
+            if errs:
+                raise RuntimeError(f"problems {b0}..: " + "; ".join(errs))
             if form in times:
-                times[form].append((time.perf_counter() - t0, dev_ms))
-            res[form] = (first, last)
-        for key, (a, b) in (("first_mixed_vs_fp64", (res["fp64"][0], res["mixed"][0])),
-                            ("last_mixed_vs_fp64", (res["fp64"][1], res["mixed"][1])),
-                            ("last_fp64_vs_fp64_cl16", (res["fp64"][1], res["fp64_cl16"][1]))):
-            (ra, ka), (rb, kb) = a, b
-            for x, y in zip(ra, rb):
-                w, z = solution_errors(x, y, 1e-2)
-                acc[key][0].extend(w)
-                acc[key][1].extend(z)
-            ea = float(((ka[:, 0] + ka[:, 1]) / 2).sum())
-            eb = float(((kb[:, 0] + kb[:, 1]) / 2).sum())
-            acc[key][2].append(abs(eb - ea) / max(abs(ea), 1e-30))
-        sizes.append(nmax)
-        sys.stderr.write(f"problem {i} seed {seed} N_max {nmax}: fp64 {times['fp64'][-1][0]:.2f} s, "
-                         f"mixed {times['mixed'][-1][0]:.2f} s\n")
+                times[form].append((wall, sum(o[2] for o in out)))
+            device_updates += sum(o[3] for o in out)
+            for j, o in enumerate(out):
+                res[j][form] = (o[0], o[1])
+        for (i, seed, nmax, _), rj in zip(batch, res):
+            for key, (a, b) in (("first_mixed_vs_fp64", (rj["fp64"][0], rj["mixed"][0])),
+                                ("last_mixed_vs_fp64", (rj["fp64"][1], rj["mixed"][1])),
+                                ("last_fp64_vs_fp64_cl16", (rj["fp64"][1], rj["fp64_cl16"][1]))):
+                (ra, ka), (rb, kb) = a, b
+                for x, y in zip(ra, rb):
+                    w, z = solution_errors(x, y, 1e-2)
+                    acc[key][0].extend(w)
+                    acc[key][1].extend(z)
+                ea = float(((ka[:, 0] + ka[:, 1]) / 2).sum())
+                eb = float(((kb[:, 0] + kb[:, 1]) / 2).sum())
+                acc[key][2].append(abs(eb - ea) / max(abs(ea), 1e-30))
+            sizes.append(nmax)
+        sys.stderr.write(f"problems {b0}..{b0 + len(batch) - 1} (N_max {[x[2] for x in batch]}): "
+                         f"fp64 {times['fp64'][-1][0]:.2f} s, mixed {times['mixed'][-1][0]:.2f} s\n")
     st = lambda q: {"max": float(np.max(q)) if len(q) else 0.0, "p99": float(np.percentile(q, 99)) if len(q) else 0.0,
                     "median": float(np.median(q)) if len(q) else 0.0}
     errors = {k: {"solutions_z_above_0.01": len(w), "qp_energy_keV": st(np.array(w) * 1e3),
@@ -748,7 +777,9 @@ def many_problems(args):
                        "nmax_choices": [4, 6, 8, 10], "nmax_counts": {str(k): sizes.count(k) for k in (4, 6, 8, 10)},
                        "hw_MeV": [10, 30], "sigma_MeV": [1, 3], "lanczos_iterations_per_pivot": n_itr,
                        "iterations": args.iterations, "z_cut": z_cut, "max_fragments_per_subshell_side": max_frag,
-                       "timed": "per problem: upload + every iteration (chain, next propagator); generation excluded"},
+                       "concurrent_problems": nconc,
+                       "timed": "per batch of concurrent problems, per form: upload + every iteration (chain, next "
+                                "propagator) of each, on its own context and host thread; generation excluded"},
             "mixed": {"problems_per_s": args.problems / wall32, "wall_s": wall32, "device_s": dev32},
             "fp64": {"problems_per_s": args.problems / wall64, "wall_s": wall64, "device_s": dev64},
             "speedup_mixed_vs_fp64_wall": wall64 / wall32, "speedup_mixed_vs_fp64_device": dev64 / dev32,

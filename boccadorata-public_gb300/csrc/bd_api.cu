@@ -1658,7 +1658,12 @@ int bd_create(bd_ctx **out, int device) {
         bd_destroy(ctx);
         return BD_ERR_CUDA;
     }
-    tridiag_fit_warm();   // attribute queries now, not inside a later stream capture
+    // attribute queries and settings now, not inside a later stream capture
+    tridiag_fit_warm();
+    tc_smem_init();
+    eig_smem_init();
+    sigma2_smem_init();
+    lanczos_smem_init();
     *out = ctx;
     return BD_OK;
 }

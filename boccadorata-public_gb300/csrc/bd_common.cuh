@@ -2,9 +2,32 @@
 // Sigma(2) -> Lanczos -> Dyson chain (sm_103a).
 #pragma once
 #include <cstdint>
+#include <mutex>
+#include <unordered_set>
 #include <cuda_runtime.h>
 
 namespace bd {
+
+// Lets a kernel take all the dynamic shared memory a CTA may opt into, once per kernel
+// in the process.  The limit is a property of the function, not of a launch: set to a
+// launch's own size, contexts on other host threads (other problem sizes) could lower
+// it between that setting and the launch.  bd_create registers every kernel that needs
+// it, so no first setting falls inside a stream capture.
+inline cudaError_t allow_dynamic_smem(const void *kernel) {
+    static std::mutex mu;
+    static std::unordered_set<const void *> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(kernel)) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, kernel);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert(kernel);
+    return e;
+}
 
 constexpr double kSqr2 = 1.4142135623730950488016887;
 constexpr int kChOff = -2, kJMult = 128, kABMult = 1024, kChMult = 5;

@@ -88,7 +88,13 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
                        double *work, const long long *d_work_first, cudaStream_t st);
 size_t tridiag_smem_bytes(int nmax, int cluster);
 int tridiag_fit_order(int cluster);   // the largest order the cluster reduction's layout holds
-void tridiag_fit_warm();              // fills tridiag_fit_order's cache (cluster sizes 1..16)
+void tridiag_fit_warm();              // fills tridiag_fit_order's cache (cluster sizes 1..16) and
+                                      // registers the Dyson kernels' shared-memory limits
+// each translation unit's kernels with large dynamic shared memory (allow_dynamic_smem)
+void tc_smem_init();
+void eig_smem_init();
+void sigma2_smem_init();
+void lanczos_smem_init();
 // DyJob::stat values: the eigensolver did not converge; the deflated matrix is larger
 // than the cluster reduction's shared-memory layout holds (nothing solved)
 constexpr int kDyStatNumeric = 1, kDyStatCapacity = 2;

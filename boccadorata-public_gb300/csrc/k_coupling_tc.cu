@@ -311,10 +311,12 @@ cudaError_t launch_poles_tc(const DevProblem &P, const S2Block *blk, const int *
                             int ntiles, const ChanSig *cs, int dir, const double *vp, double *E, double *S2, double *M,
                             int *err, size_t smem, cudaStream_t st) {
     if (ntiles <= 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_poles_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem((const void *)k_poles_tc);
     if (e != cudaSuccess) return e;
     k_poles_tc<<<ntiles, kTcThreads, smem, st>>>(P, blk, tile_blk, tiles, ntiles, cs, dir, vp, E, S2, M, err);
     return cudaGetLastError();
 }
+
+void tc_smem_init() { allow_dynamic_smem((const void *)k_poles_tc); }
 
 }  // namespace bd

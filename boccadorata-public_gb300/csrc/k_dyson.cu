@@ -859,6 +859,9 @@ int tridiag_fit_order(int cluster) {
 
 void tridiag_fit_warm() {
     for (int c = 1; c <= 16; c <<= 1) tridiag_fit_order(c);
+    allow_dynamic_smem((const void *)k_tridiag_small);
+    allow_dynamic_smem((const void *)k_tridiag);
+    allow_dynamic_smem((const void *)k_tridiag_df);
 }
 
 // Kernels launch_dyson starts for matrices of order up to nmax: deflate, assemble, the
@@ -874,7 +877,7 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t ssmem = tridiag_small_smem_bytes(nmax, Dmax);
-    e = cudaFuncSetAttribute(k_tridiag_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem);
+    e = allow_dynamic_smem((const void *)k_tridiag_small);
     if (e != cudaSuccess) return e;
     k_tridiag_small<<<njobs, kTsThreads, ssmem, st>>>(d_jobs, njobs);
     e = cudaGetLastError();
@@ -898,7 +901,7 @@ cudaError_t launch_dyson(const DyJob *d_jobs, int njobs, const long long *d_row_
     cfg.numAttrs = 1;
     const int npriv = tridiag_npriv(nmax, cluster);
     auto kern = (npriv == kTdThreads / 32) ? k_tridiag_df : k_tridiag;   // double-float with a partial per warp
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = allow_dynamic_smem((const void *)kern);
     if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernelEx(&cfg, kern, d_jobs, njobs, nmax, npriv);

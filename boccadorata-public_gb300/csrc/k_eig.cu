@@ -801,7 +801,7 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
                                                                d_work_first);
     {
         const int smem = (int)(sizeof(double) * 5 * kTsMax * kIvThreads + kTsMax * kIvThreads + sizeof(double) * 2 * kTsMax);
-        cudaError_t e = cudaFuncSetAttribute(k_invit_small, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = allow_dynamic_smem((const void *)k_invit_small);
         if (e != cudaSuccess) return e;
         k_invit_small<<<dim3(njobs, (kTsMax + kIvThreads - 1) / kIvThreads), kIvThreads, smem, st>>>(d_jobs, njobs);
     }
@@ -811,5 +811,7 @@ cudaError_t launch_eig(const DyJob *d_jobs, int njobs, const long long *d_row_fi
     k_koltun<<<dim3(njobs, kPlaceCtas), kPlaceThreads, 0, st>>>(d_jobs, njobs, work, d_work_first);
     return cudaGetLastError();
 }
+
+void eig_smem_init() { allow_dynamic_smem((const void *)k_invit_small); }
 
 }  // namespace bd

@@ -1130,8 +1130,7 @@ template <typename VT, bool G>
 static cudaError_t launch_lz(const cudaLaunchConfig_t &cfg, int cluster, const LzChain *d_chains, int nchains, int rmax,
                              double eta2) {
     const int smem_bytes = (int)cfg.dynamicSmemBytes;
-    cudaError_t e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)cfg.dynamicSmemBytes);
+    cudaError_t e = allow_dynamic_smem((const void *)k_lanczos<VT, G>);
     if (e == cudaSuccess && cluster > 8)
         e = cudaFuncSetAttribute(k_lanczos<VT, G>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return e;
@@ -1547,4 +1546,12 @@ cudaError_t launch_lz_groups(const LzChain *d_chains, int nchains, long long gra
     k_lz_groups<<<nchains, kGrpThreads, 0, st>>>(d_chains, nchains);
     return cudaGetLastError();
 }
+
+void lanczos_smem_init() {
+    allow_dynamic_smem((const void *)k_lanczos<float, false>);
+    allow_dynamic_smem((const void *)k_lanczos<float, true>);
+    allow_dynamic_smem((const void *)k_lanczos<double, false>);
+    allow_dynamic_smem((const void *)k_lanczos<double, true>);
+}
+
 }  // namespace bd

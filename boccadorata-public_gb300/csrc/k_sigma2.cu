@@ -778,10 +778,12 @@ cudaError_t launch_heap_order(const double *E, const int *d_off, int nseg, int m
                               cudaStream_t st) {
     if (nseg <= 0 || max_len < 2) return cudaSuccess;
     const size_t smem = sizeof(unsigned) * (size_t)(std::min(max_len, kHeapMax) + 4);
-    cudaError_t e = cudaFuncSetAttribute(k_heap_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_dynamic_smem((const void *)k_heap_order);
     if (e != cudaSuccess) return e;
     k_heap_order<<<nseg, kHeapThreads, smem, st>>>(E, d_off, n0, perm);
     return cudaGetLastError();
 }
+
+void sigma2_smem_init() { allow_dynamic_smem((const void *)k_heap_order); }
 
 }  // namespace bd

@@ -216,3 +216,42 @@ def test_autotune_picks_a_cluster_size(bdmod, problems):
     ctx.run_all(lanczos=True, mixed=True, graph=True)
     assert np.isfinite(ctx.koltun_all()).all()
     ctx.close()
+
+
+def test_contexts_of_different_sizes_on_host_threads(bdmod, problems):
+    """Two contexts with problems of different sizes driven from two host threads at
+    once (kernel attributes are per process): every step gives the results the context
+    gives alone, bit for bit, in both forms."""
+    import threading
+    probs = [problems(4, 20.0, 0, 20), problems(6, 20.0, 1, 50)]
+    want = []
+    for p in probs:
+        c = bdmod.Context().upload(p)
+        w = {}
+        for mixed in (False, True):
+            c.run_all(lanczos=True, mixed=mixed)
+            w[mixed] = c.results_all()
+        c.close()
+        want.append(w)
+    ctxs = [bdmod.Context().upload(p) for p in probs]
+    errs = []
+
+    def drive(j):
+        try:
+            for step in range(6):
+                mixed = bool(step & 1)
+                ctxs[j].run_all(lanczos=True, mixed=mixed, graph=(step >= 2))
+                for a, b in zip(want[j][mixed], ctxs[j].results_all()):
+                    for k in ("qp", "qh", "koltun"):
+                        if not np.array_equal(a[k], b[k]):
+                            errs.append((j, step, k))
+        except Exception as ex:
+            errs.append(repr(ex))
+    ths = [threading.Thread(target=drive, args=(j,)) for j in range(len(ctxs))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    for c in ctxs:
+        c.close()
+    assert not errs, errs[:5]
